@@ -1,0 +1,336 @@
+"""Benchmark of the FreeFEM assemble-and-solve path on one GB300.
+
+Workload (default): 3D linear elasticity on the unit cube, cube(64,64,64) split into 6 tets per
+hexahedron (1,572,864 tets), [P2,P2,P2] (6,440,067 DOFs), E=1, nu=0.3, clamped on the face x=0
+(label 4), body force (0,0,-1), FP64, Jacobi-PCG to FreeFEM's eps=1e-10.  A step is one full
+pass of the path from the mesh + DOF table to the solution:
+    space setup (node->element incidence) + matrix A = a(Vh,Vh) (pattern, values, tgv)
+    + b = a(0,Vh) (same pass) + u[] = A^-1*b (CG)
+value: inputs (coordinates, elements, DOF table) resident in HBM before the timed region.
+e2e:   the same through the public API from host (numpy) arrays, host<->device copies timed.
+The matrix (~6 GB) is larger than L2 (129 MB), so no flush is needed between steps.
+
+--impl reference times the oracle port of FreeFEM's CPU path (oracle/ffo.c) on the host cores,
+one single-threaded instance per core (FreeFEM's core is single-threaded), on a bounded sample
+of the same workload family.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "freefem-sources_gb300"))
+
+METRIC = "assemble+solve DOFs/s: FP64 plain vs mixed/adjoint/batched, at 1e-8 rel err"
+UNIT = "DOFs/s"
+
+CONFIGS = {
+    # name: (builder, kind, varf kwargs)
+    "elasticity_p2_cube64": dict(mesh=("cube", 64), kind="P2vec", form="elasticity", on=(4,),
+                                 eps=1e-10),
+    "poisson_p1_square256": dict(mesh=("square", 256), kind="P1", form="diffusion",
+                                 on=(1, 2, 3, 4), eps=1e-10),
+}
+SAMPLE = {"elasticity_p2_cube64": ("cube", 12), "poisson_p1_square256": ("square", 256)}
+
+
+def build_problem(cfg, size=None):
+    import numpy as np
+    import ffgpu
+    from ffgpu.fespace import FESpace
+    kind_mesh, n = cfg["mesh"] if size is None else size
+    Th = ffgpu.cube(n) if kind_mesh == "cube" else ffgpu.square(n)
+    Vh = FESpace(Th, cfg["kind"])
+    if cfg["form"] == "elasticity":
+        a = ffgpu.varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=cfg["on"])
+    else:
+        a = ffgpu.varf_diffusion(f=1.0, on=cfg["on"])
+    return Th, Vh, a, np
+
+
+# ------------------------------------------------------------------ CPU: the oracle port
+def _oracle_run(args):
+    cfgname, size = args
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ffo
+    cfg = CONFIGS[cfgname]
+    Th, Vh, a, np = build_problem(cfg, size)
+    t0 = time.perf_counter()
+    quad = None if cfg["kind"] != "P1" or Th.dim == 3 else "qf2pT"
+    A = ffo.assemble(Th, Vh, form=cfg["form"], quad=quad)
+    b = ffo.rhs(Th, Vh, f=(0.0, 0.0, -1.0) if cfg["form"] == "elasticity" else 1.0, quad=quad)
+    ffo.setbc(A, b, Vh.on(cfg["on"]))
+    u, it, r, _ = ffo.cg(A, b, eps=cfg["eps"])
+    dt = time.perf_counter() - t0
+    return Vh.ndof, dt, it
+
+
+def cpu_baseline(cfgname, procs=1, reps=1):
+    """DOFs/s of the oracle on the sample problem, `procs` concurrent single-core instances."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ffo
+    ffo.build()
+    size = SAMPLE[cfgname]
+    jobs = [(cfgname, size)] * (procs * reps)
+    t0 = time.perf_counter()
+    if procs == 1:
+        res = [_oracle_run(j) for j in jobs]
+    else:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_oracle_run, jobs)
+    wall = time.perf_counter() - t0
+    ndof = res[0][0]
+    per = statistics.median(r[1] for r in res)
+    value = ndof * len(res) / wall if procs > 1 else ndof / per
+    return dict(value=value, unit=UNIT, cores=procs, kind="port",
+                sample=f"{size[0]}({size[1]}) same varf, full assemble+rhs+CG(eps={CONFIGS[cfgname]['eps']}), "
+                       f"{len(res)} run(s), {res[0][2]} CG iterations, single-threaded oracle "
+                       f"(oracle/ffo.c) per core"), wall
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1])); mx.append(float(t[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, t[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, rank, world):
+    import numpy as np
+    import torch
+    import ffgpu
+    from ffgpu.build import build
+    build()
+    cfgname = args.config
+    cfg = CONFIGS[cfgname]
+    dev = 0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(dev)
+    Th, Vh, a, _ = build_problem(cfg)
+    ctx = ffgpu.context(dev)
+    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(dev), device=dev)
+    X = torch.from_numpy(Th.coords).cuda(dev)
+    E = torch.from_numpy(np.ascontiguousarray(Th.elems)).cuda(dev)
+    D = torch.from_numpy(np.ascontiguousarray(Vh.dof)).cuda(dev)
+    onbc = Vh.on(cfg["on"])
+    a.on = cfg["on"]
+    b = torch.empty(Vh.ndof, dtype=torch.float64, device=dev)
+
+    def step_device():
+        S = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D)
+        A = ffgpu.matrix(a, S, eps=cfg["eps"], rhs_out=b, device=dev)
+        u = A.solve(b)
+        return S, A, u
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up
+    for _ in range(args.warmup):
+        S, A, u = step_device()
+        it_warm = A.stats.iterations
+        del A, S
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    l0 = ffgpu.kernel_launches(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    times, iters, asm_ms = [], [], []
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier()
+    ev0.record(stream)
+    evs[0].record(stream)
+    for k in range(args.steps):
+        S, A, u = step_device()
+        evs[k + 1].record(stream)
+        evs[k + 1].synchronize()
+        times.append(evs[k].elapsed_time(evs[k + 1]))
+        iters.append(A.stats.iterations)
+        asm_ms.append(times[-1] - A.stats.elapsed_ms)
+        keep = (S, A, u)
+    ev1.record(stream)
+    barrier()
+    total_ms = ev0.elapsed_time(ev1)
+    launches = ffgpu.kernel_launches(dev) - l0
+    clk = clocks.stop()
+    S, A, u = keep
+    # accuracy: relative residual of the solution on non-tgv rows
+    ub = u
+    r = A.mult(ub)
+    rh = (b - r).cpu().numpy()
+    mask = onbc.astype(bool)
+    rel_res = float(np.linalg.norm(rh[~mask]) / np.linalg.norm(b.cpu().numpy()[~mask]))
+    # dominant kernel: the SpMV of the CG (K_a); timed alone on the library stream
+    nrep = 20
+    y = torch.empty_like(b)
+    A.mult(ub, out=y)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    spmv_ms = []
+    for _ in range(nrep):
+        e0.record(stream)
+        A.mult(ub, out=y)
+        e1.record(stream)
+        e1.synchronize()
+        spmv_ms.append(e0.elapsed_time(e1))
+    spmv_avg = statistics.median(spmv_ms)
+    n, nnz, bs = A.n, A.nnz, A.block_size
+    nnzb = nnz // (bs * bs)
+    nb = n // bs
+    spmv_bytes = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
+    achieved = spmv_bytes / (spmv_avg * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(REPO, "profiles", "traffic.json")))
+        traffic = tr.get(cfgname, {}).get("spmv_bytes_per_launch")
+    except Exception:
+        pass
+    # e2e: public API from host arrays (H2D of mesh/DOF table/BC mask, D2H of b and u)
+    e2e_times = []
+    bh = np.empty(Vh.ndof)
+    for s in range(max(1, args.warmup // 3) + args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        Ah = ffgpu.matrix(a, Vh, eps=cfg["eps"], rhs_out=bh, device=dev)
+        uh = Ah.solve(bh)
+        t1 = time.perf_counter()
+        if s >= max(1, args.warmup // 3):
+            e2e_times.append((t1 - t0) * 1e3)
+        del Ah
+    h2d = Th.coords.nbytes + Th.elems.nbytes + Vh.dof.nbytes + onbc.nbytes + bh.nbytes
+    d2h = bh.nbytes + uh.nbytes
+    # max over ranks
+    t_step = total_ms / args.steps
+    t_e2e = sum(e2e_times) / len(e2e_times)
+    if world > 1:
+        tt = torch.tensor([t_step, t_e2e], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step, t_e2e = tt.tolist()
+    value = world * Vh.ndof / (t_step * 1e-3)
+    e2e_value = world * Vh.ndof / (t_e2e * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfgname, "mesh": f"{cfg['mesh'][0]}({cfg['mesh'][1]})",
+                   "fe": cfg["kind"], "ndof": Vh.ndof, "nnz": nnz, "nt": Th.nt,
+                   "solver": "Jacobi-PCG", "eps": cfg["eps"], "cg_iterations": iters[-1],
+                   "l2": "inputs larger than L2 (matrix %.1f GB)" % (nnz * 8 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "assembly_ms": statistics.median(asm_ms), "rel_residual": rel_res},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "spmv BSR3 FP64 (cg_ka body)", "bytes_per_launch": spmv_bytes,
+                     "ms_per_launch": spmv_avg, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "clocks": clk,
+    }
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="elasticity_p2_cube64", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        procs = os.cpu_count() or 1
+        vals = []
+        for _ in range(args.warmup + args.steps):
+            cb, wall = cpu_baseline(args.config, procs=procs)
+            vals.append((cb, wall))
+        timed = vals[args.warmup:]
+        value = statistics.median(v[0]["value"] for v in timed)
+        cb = timed[-1][0]
+        cb["value"] = value
+        print(json.dumps({
+            "metric": METRIC, "impl": "reference", "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.median(v[1] for v in timed) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.config}, "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            cb, _ = cpu_baseline(args.config, procs=1)
+            out["cpu_baseline"] = cb
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

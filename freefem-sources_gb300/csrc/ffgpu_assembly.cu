@@ -1,0 +1,794 @@
+// ffgpu_assembly.cu -- mesh/FE-space upload, symbolic pattern and numeric assembly.
+//
+// Design (GB300): FreeFEM walks elements and scatters each element matrix into a hash
+// matrix (problem.cpp:1096-1103, HashMatrix.cpp:1295-1332).  Here every matrix row is
+// owned by one warp, which gathers the contributions of the elements incident to its node:
+//   pass 1 (count):  gather the nodes of the incident elements, sort, unique -> row degree;
+//   scan:            row pointer;
+//   pass 2 (fill):   same gather -> sorted column list, then add the element-matrix rows of
+//                    the incident elements in ascending element order (the reference's
+//                    summation order), apply tgv, write the row once, coalesced.
+// No atomics and no colouring are needed on the value path: each value is written once and
+// no read-modify-write of the matrix happens.  The element geometry (barycentric gradients
+// and measure) is computed once per element and cached (16 doubles per element).
+// For [P2]^3 the pattern is stored as 3x3 blocks (DOF = 3*node + c, FESpacen.hpp:582),
+// which is the same (i,j) set as FreeFEM's MatriceMorse and 2/3 of the index traffic.
+#include <string.h>
+
+#include "ffgpu_internal.cuh"
+
+namespace ffgpu {
+
+constexpr int kGeoStride = 16;   // doubles per element: meas, kappa, -, -, G[4][3]
+
+// ------------------------------------------------------------------ small device utils
+template <typename T>
+__device__ void warp_bitonic_sort(T *s, int P) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < P; i += 32) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    bool up = (i & k) == 0;
+                    T a = s[i], b = s[ixj];
+                    if ((a > b) == up) { s[i] = b; s[ixj] = a; }
+                }
+            }
+            __syncwarp();
+        }
+}
+
+__device__ __forceinline__ int pow2_ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// binary search of v in the sorted list s[0..n)
+__device__ __forceinline__ int find_sorted(const int *s, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        int w = s[mid];
+        if (w == v) return mid;
+        if (w < v) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+// ------------------------------------------------------------------ space construction
+__global__ void build_nodes_kernel(const int32_t *dof, int nt, int ndofK, int nn, int bs,
+                                   int ndof, int32_t *nodes, int *status) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nt * nn) return;
+    int k = (int)(t / nn), i = (int)(t % nn);
+    const int32_t *d = dof + (int64_t)k * ndofK;
+    int v0 = d[i];
+    if (v0 < 0 || v0 >= ndof) { dev_fail(status, kDevBadIndex); nodes[t] = 0; return; }
+    if (bs == 1) { nodes[t] = v0; return; }
+    int node = v0 / bs;
+    bool ok = (v0 % bs) == 0;
+    for (int c = 1; c < bs; ++c) ok = ok && d[c * nn + i] == bs * node + c;
+    if (!ok) dev_fail(status, kDevBadDofLayout);
+    nodes[t] = node;
+}
+
+__global__ void check_elems_kernel(const int32_t *elems, int64_t m, int nv, int *status) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < m && (elems[t] < 0 || elems[t] >= nv)) dev_fail(status, kDevBadIndex);
+}
+
+__global__ void inc_count_kernel(const int32_t *nodes, int64_t m, int32_t *cnt) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < m) atomicAdd(&cnt[nodes[t]], 1);
+}
+
+__global__ void inc_fill_kernel(const int32_t *nodes, int64_t m, int nn, const int32_t *ptr,
+                                int32_t *cursor, int32_t *inc_elem, uint8_t *inc_loc) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    int a = nodes[t];
+    int pos = ptr[a] + atomicAdd(&cursor[a], 1);
+    inc_elem[pos] = (int32_t)(t / nn);
+    inc_loc[pos] = (uint8_t)(t % nn);
+}
+
+// sort each node's incidence list by element number (the reference's element order)
+__global__ void inc_sort_kernel(const int32_t *ptr, int nnodes, int max_inc, int32_t *inc_elem,
+                                uint8_t *inc_loc) {
+    extern __shared__ long long sh_inc[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int P = pow2_ceil(max_inc);
+    long long *s = sh_inc + (int64_t)w * P;
+    for (int a = blockIdx.x * (blockDim.x >> 5) + w; a < nnodes; a += gridDim.x * (blockDim.x >> 5)) {
+        int b = ptr[a], e = ptr[a + 1], n = e - b;
+        for (int i = lane; i < P; i += 32)
+            s[i] = i < n ? (((long long)inc_elem[b + i]) << 8) | inc_loc[b + i] : 0x7fffffffffffffffLL;
+        __syncwarp();
+        warp_bitonic_sort(s, P);
+        for (int i = lane; i < n; i += 32) {
+            inc_elem[b + i] = (int32_t)(s[i] >> 8);
+            inc_loc[b + i] = (uint8_t)(s[i] & 0xff);
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ geometry
+// meas and barycentric gradients: Triangle::H (fem.hpp:321-324), Tet::Gradlambda
+// (Mesh3dn.hpp:126-136), tet volume det(AB,AC,AD)/6 (Mesh3dn.hpp:70)
+__global__ void geometry_kernel(const double *X, const int32_t *elems, int nt, int dim,
+                                const double *kappa, double c_stiff, double *geo) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    double *g = geo + (int64_t)k * kGeoStride;
+    double G[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double meas;
+    if (dim == 2) {
+        const int32_t *v = elems + 3 * (int64_t)k;
+        double P[3][2];
+        for (int i = 0; i < 3; ++i) { P[i][0] = X[2 * (int64_t)v[i]]; P[i][1] = X[2 * (int64_t)v[i] + 1]; }
+        double area = ((P[1][0] - P[0][0]) * (P[2][1] - P[0][1]) - (P[1][1] - P[0][1]) * (P[2][0] - P[0][0])) * 0.5;
+        for (int i = 0; i < 3; ++i) {
+            int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+            double ex = P[i2][0] - P[i1][0], ey = P[i2][1] - P[i1][1];
+            G[i][0] = -ey / (2 * area);
+            G[i][1] = ex / (2 * area);
+        }
+        meas = area;
+    } else {
+        const int32_t *v = elems + 4 * (int64_t)k;
+        double A[3], V[3][3];
+        for (int d = 0; d < 3; ++d) A[d] = X[3 * (int64_t)v[0] + d];
+        for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) V[i][d] = X[3 * (int64_t)v[i + 1] + d] - A[d];
+        double c23[3] = {V[1][1] * V[2][2] - V[1][2] * V[2][1], V[1][2] * V[2][0] - V[1][0] * V[2][2],
+                         V[1][0] * V[2][1] - V[1][1] * V[2][0]};
+        double c31[3] = {V[2][1] * V[0][2] - V[2][2] * V[0][1], V[2][2] * V[0][0] - V[2][0] * V[0][2],
+                         V[2][0] * V[0][1] - V[2][1] * V[0][0]};
+        double c12[3] = {V[0][1] * V[1][2] - V[0][2] * V[1][1], V[0][2] * V[1][0] - V[0][0] * V[1][2],
+                         V[0][0] * V[1][1] - V[0][1] * V[1][0]};
+        double vol = (V[0][0] * c23[0] + V[0][1] * c23[1] + V[0][2] * c23[2]) / 6.;
+        double det1 = 1. / (6. * vol);
+        for (int d = 0; d < 3; ++d) {
+            G[1][d] = c23[d] * det1;
+            G[2][d] = c31[d] * det1;
+            G[3][d] = c12[d] * det1;
+            G[0][d] = -G[1][d] - G[2][d] - G[3][d];
+        }
+        meas = vol;
+    }
+    g[0] = meas;
+    g[1] = (kappa ? kappa[k] : 1.0) * c_stiff;
+    g[2] = 0; g[3] = 0;
+    for (int i = 0; i < 4; ++i)
+        for (int d = 0; d < 3; ++d) g[4 + 3 * i + d] = G[i][d];
+}
+
+// ------------------------------------------------------------------ element entries
+// P2 gradients are linear: grad(phi_i) = sum_a lambda_a C_i[a], with
+//   vertex i: C_i[i] = 3 g_i, C_i[a != i] = -g_i            (grad = (4 lambda_i - 1) g_i)
+//   edge (p,q): C_i[p] = 4 g_q, C_i[q] = 4 g_p, else 0      (grad = 4(lambda_p g_q + lambda_q g_p))
+// (P012_3d.cpp:199-277; 2D: FESpace.cpp:1219-1300 with edge i opposite vertex i), and
+//   int_K lambda_a lambda_b = |K| (1 + delta_ab) / ((d+1)(d+2)),
+// so int_K d_alpha(phi_i) d_beta(phi_j) = m (sum_a C_i[a].al C_j[a].be + S_i.al S_j.be),
+// m = |K|/((d+1)(d+2)), S_i = sum_a C_i[a].  This integrates the degree-2 integrand
+// exactly, as FreeFEM's default rules (T_5, Tet_5) do.
+__constant__ int c_tet_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+__constant__ int c_tri_edge[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+
+template <int DIM>
+struct P2Grad {
+    double C[DIM + 1][3];
+    double S[3];
+    __device__ void make(const double *G /* [4][3] */, int i) {
+        constexpr int nvk = DIM + 1;
+        for (int a = 0; a < nvk; ++a)
+            for (int d = 0; d < 3; ++d) C[a][d] = 0.0;
+        if (i < nvk) {
+            for (int a = 0; a < nvk; ++a)
+                for (int d = 0; d < 3; ++d) C[a][d] = (a == i ? 3.0 : -1.0) * G[3 * i + d];
+        } else {
+            int e = i - nvk;
+            int p = DIM == 3 ? c_tet_edge[e][0] : c_tri_edge[e][0];
+            int q = DIM == 3 ? c_tet_edge[e][1] : c_tri_edge[e][1];
+            for (int d = 0; d < 3; ++d) { C[p][d] = 4.0 * G[3 * q + d]; C[q][d] = 4.0 * G[3 * p + d]; }
+        }
+        for (int d = 0; d < 3; ++d) {
+            double s = 0;
+            for (int a = 0; a < nvk; ++a) s += C[a][d];
+            S[d] = s;
+        }
+    }
+};
+
+template <int DIM>
+__device__ __forceinline__ double p2_gab(const P2Grad<DIM> &I, const P2Grad<DIM> &J, int al, int be) {
+    double s = I.S[al] * J.S[be];
+#pragma unroll
+    for (int a = 0; a < DIM + 1; ++a) s += I.C[a][al] * J.C[a][be];
+    return s;
+}
+
+// int_K phi_i for the linear form with a constant source on the element
+template <int DIM, int ORDER>
+__device__ __forceinline__ double basis_integral(double meas, int i) {
+    if (ORDER == 1) return meas / (DIM + 1);
+    if (DIM == 3) return i < 4 ? -meas / 20.0 : meas / 5.0;
+    return i < 3 ? 0.0 : meas / 3.0;
+}
+
+// ------------------------------------------------------------------ row gather (both passes)
+// Gathers the candidate neighbour nodes of node a into s, sorts and compacts them in
+// place; returns the row degree (or -1 on overflow).
+__device__ int gather_row(int a, const int32_t *inc_ptr, const int32_t *inc_elem,
+                          const int32_t *nodes, int nn, int *s, int *status) {
+    const int lane = threadIdx.x & 31;
+    int b = inc_ptr[a], e = inc_ptr[a + 1];
+    int m = (e - b) * nn;
+    if (m > kCandMax) { if (lane == 0) dev_fail(status, kDevCandOverflow); return -1; }
+    int P = pow2_ceil(max(m, 32));
+    for (int p = lane; p < P; p += 32) {
+        int v = 0x7fffffff;
+        if (p < m) {
+            int t = p / nn, i = p - t * nn;
+            v = nodes[(int64_t)inc_elem[b + t] * nn + i];
+        }
+        s[p] = v;
+    }
+    __syncwarp();
+    warp_bitonic_sort(s, P);
+    int count = 0, prev = (int)0x80000000;
+    for (int c = 0; c < P; c += 32) {
+        int v = s[c + lane];
+        int vp = __shfl_up_sync(0xffffffffu, v, 1);
+        if (lane == 0) vp = prev;
+        bool f = (v != 0x7fffffff) && (v != vp);
+        unsigned bal = __ballot_sync(0xffffffffu, f);
+        prev = __shfl_sync(0xffffffffu, v, 31);
+        __syncwarp();
+        if (f) s[count + __popc(bal & ((1u << lane) - 1u))] = v;
+        count += __popc(bal);
+        __syncwarp();
+    }
+    return count;
+}
+
+__global__ void row_count_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *inc_elem,
+                                 const int32_t *nodes, int nn, int32_t *deg, int *status) {
+    __shared__ int sh[4][kCandMax];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int a = blockIdx.x * 4 + w; a < nnodes; a += gridDim.x * 4) {
+        int d = gather_row(a, inc_ptr, inc_elem, nodes, nn, sh[w], status);
+        if (lane == 0) deg[a] = d < 0 ? 0 : d;
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ fill + numeric pass
+struct FillArgs {
+    int nnodes, nt;
+    const int32_t *inc_ptr, *inc_elem;
+    const uint8_t *inc_loc;
+    const int32_t *nodes;
+    const double *geo;
+    const int32_t *browptr;
+    int32_t *bcol;            // NULL: numeric only (pattern already built)
+    double *val;              // NULL: no matrix (linear form only)
+    double *rhs;              // NULL: no linear form
+    const double *fP0;        // nt*bs or NULL
+    double f0, f1, f2;
+    double c_mass;
+    double lam, mu;           // elasticity
+    const uint8_t *onbc;
+    const double *g;
+    double tgv;
+    int max_deg;
+    int *status;
+};
+
+// FE: 1 = P1 scalar, 2 = P2 scalar, 3 = [P2]^3 elasticity
+template <int DIM, int FE>
+__global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
+    constexpr int nvk = DIM + 1;
+    constexpr int NN = FE == 1 ? nvk : (DIM == 3 ? 10 : 6);
+    constexpr int BS = FE == 3 ? 3 : 1;
+    constexpr int BS2 = BS * BS;
+    // lanes: FE 1/2 -> slot*NN + lb (several elements per step); FE 3 -> lb*3 + c
+    constexpr int SLOTS = FE == 3 ? 1 : 32 / NN;
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warps = blockDim.x >> 5;
+    int *cols = (int *)sh_raw + w * kCandMax;
+    double *acc = (double *)((int *)sh_raw + warps * kCandMax) + (int64_t)w * A.max_deg * BS2;
+    const double mfac = DIM == 3 ? 1.0 / 20.0 : 1.0 / 12.0;
+
+    for (int a = blockIdx.x * warps + w; a < A.nnodes; a += gridDim.x * warps) {
+        int deg = gather_row(a, A.inc_ptr, A.inc_elem, A.nodes, NN, cols, A.status);
+        if (deg < 0) continue;
+        if (deg > A.max_deg) { if (lane == 0) dev_fail(A.status, kDevDegOverflow); continue; }
+        const int64_t rb = A.browptr[a];
+        if (A.bcol)
+            for (int r = lane; r < deg; r += 32) A.bcol[rb + r] = cols[r];
+        for (int q = lane; q < deg * BS2; q += 32) acc[q] = 0.0;
+        double racc = 0.0;   // rhs of component `lane` (lanes < BS)
+        __syncwarp();
+        const int ib = A.inc_ptr[a], ie = A.inc_ptr[a + 1];
+        for (int t0 = ib; t0 < ie; t0 += SLOTS) {
+            // ---- element contributions of this step
+            int slot = FE == 3 ? 0 : lane / NN;
+            int lb = FE == 3 ? lane / 3 : lane - slot * NN;
+            int t = t0 + slot;
+            bool act = (FE == 3 ? lane < 30 : slot < SLOTS) && t < ie;
+            int rank = -1;
+            double v[BS];
+#pragma unroll
+            for (int c = 0; c < BS; ++c) v[c] = 0.0;
+            int e = 0, la = 0;
+            if (act) {
+                e = A.inc_elem[t];
+                la = A.inc_loc[t];
+                const double *ge = A.geo + (int64_t)e * kGeoStride;
+                const double meas = ge[0], kap = ge[1];
+                const double *G = ge + 4;
+                int nb = A.nodes[(int64_t)e * NN + lb];
+                rank = find_sorted(cols, deg, nb);
+                if (FE == 1) {
+                    double s = 0;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) s += G[3 * la + d] * G[3 * lb + d];
+                    double val = kap * meas * s;
+                    if (A.c_mass != 0.0) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
+                    v[0] = val;
+                } else {
+                    P2Grad<DIM> I, J;
+                    I.make(G, la);
+                    J.make(G, lb);
+                    double m = meas * mfac;
+                    if (FE == 2) {
+                        double s = 0;
+#pragma unroll
+                        for (int d = 0; d < DIM; ++d) s += p2_gab<DIM>(I, J, d, d);
+                        v[0] = kap * m * s;
+                    } else {
+                        int c = lane - 3 * lb;
+                        double tr = p2_gab<DIM>(I, J, 0, 0) + p2_gab<DIM>(I, J, 1, 1) + p2_gab<DIM>(I, J, 2, 2);
+#pragma unroll
+                        for (int cp = 0; cp < 3; ++cp) {
+                            double x = A.lam * p2_gab<DIM>(I, J, c, cp) + A.mu * p2_gab<DIM>(I, J, cp, c);
+                            if (cp == c) x += A.mu * tr;
+                            v[cp] = m * x;
+                        }
+                    }
+                }
+                if (rank < 0) dev_fail(A.status, kDevNotFound);
+            }
+            // ---- accumulate in element order
+            if (FE == 3) {
+                if (act && rank >= 0) {
+                    int c = lane - 3 * lb;
+#pragma unroll
+                    for (int cp = 0; cp < 3; ++cp) acc[rank * 9 + 3 * c + cp] += v[cp];
+                }
+                __syncwarp();
+            } else {
+                for (int sl = 0; sl < SLOTS; ++sl) {
+                    if (act && slot == sl && rank >= 0) acc[rank] += v[0];
+                    __syncwarp();
+                }
+            }
+            // ---- linear form: lanes < BS accumulate component `lane`, element order
+            if (A.rhs) {
+                for (int sl = 0; sl < SLOTS; ++sl) {
+                    int tt = t0 + sl;
+                    if (tt < ie && lane < BS) {
+                        int ee = A.inc_elem[tt], ll = A.inc_loc[tt];
+                        double meas = A.geo[(int64_t)ee * kGeoStride];
+                        double f = A.fP0 ? A.fP0[(int64_t)ee * BS + lane]
+                                         : (lane == 0 ? A.f0 : (lane == 1 ? A.f1 : A.f2));
+                        racc += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // ---- Dirichlet rows (tgv > 0): diagonal := tgv, rhs := tgv * g
+        int self = find_sorted(cols, deg, a);
+        if (self < 0) { if (lane == 0) dev_fail(A.status, kDevNotFound); continue; }
+        if (lane < BS) {
+            int64_t dof = (int64_t)a * BS + lane;
+            bool on = A.onbc && A.onbc[dof];
+            if (on && A.tgv > 0) {
+                if (A.val) acc[self * BS2 + lane * BS + lane] = A.tgv;
+                racc = A.tgv * (A.g ? A.g[dof] : 0.0);
+            }
+            if (A.rhs) A.rhs[dof] = racc;
+        }
+        __syncwarp();
+        if (A.val)
+            for (int q = lane; q < deg * BS2; q += 32) A.val[rb * BS2 + q] = acc[q];
+        __syncwarp();
+    }
+}
+
+// linear form only (real[int] b = a(0,Vh)): per node, sum over incident elements
+template <int DIM, int FE>
+__global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *inc_elem,
+                           const uint8_t *inc_loc, const double *geo, const double *fP0,
+                           double f0, double f1, double f2, const uint8_t *onbc, const double *g,
+                           double tgv, double *rhs) {
+    constexpr int BS = FE == 3 ? 3 : 1;
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nnodes * BS) return;
+    int a = (int)(t / BS), c = (int)(t % BS);
+    double s = 0;
+    for (int p = inc_ptr[a]; p < inc_ptr[a + 1]; ++p) {
+        int e = inc_elem[p], l = inc_loc[p];
+        double meas = geo[(int64_t)e * kGeoStride];
+        double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
+        s += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
+    }
+    if (onbc && onbc[t] && tgv > 0) s = tgv * (g ? g[t] : 0.0);
+    rhs[t] = s;
+}
+
+// ------------------------------------------------------------------ CSR export
+__global__ void export_csr_kernel(int nb, int bs, const int32_t *browptr, const int32_t *bcol,
+                                  const double *val, int32_t *rowptr, int32_t *col, double *out) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nb) return;
+    int64_t b0 = browptr[a], deg = browptr[a + 1] - b0;
+    for (int c = 0; c < bs; ++c) {
+        int64_t r0 = b0 * bs * bs + c * bs * deg;
+        rowptr[(int64_t)a * bs + c] = (int32_t)r0;
+        for (int64_t k = 0; k < deg; ++k)
+            for (int cp = 0; cp < bs; ++cp) {
+                col[r0 + k * bs + cp] = bs * bcol[b0 + k] + cp;
+                out[r0 + k * bs + cp] = val[(b0 + k) * bs * bs + c * bs + cp];
+            }
+    }
+    if (a == nb - 1) rowptr[(int64_t)nb * bs] = (int32_t)((int64_t)browptr[nb] * bs * bs);
+}
+
+static int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+}  // namespace ffgpu
+
+using namespace ffgpu;
+
+// ------------------------------------------------------------------ helpers on the host
+static int fill_launch(ffgpu_space *S, FillArgs &fa) {
+    ffgpu_ctx *ctx = S->ctx;
+    const int warps = 4;
+    int bs2 = S->bs * S->bs;
+    size_t smem = (size_t)warps * kCandMax * sizeof(int) + (size_t)warps * fa.max_deg * bs2 * sizeof(double);
+    int grid = min(kNumSM * 16, max(1, (S->nnodes + warps - 1) / warps));
+    void (*kern)(FillArgs) = nullptr;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P1) kern = row_fill_kernel<2, 1>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P1) kern = row_fill_kernel<3, 1>;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P2) kern = row_fill_kernel<2, 2>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2) kern = row_fill_kernel<3, 2>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) kern = row_fill_kernel<3, 3>;
+    FFGPU_CHECK(kern, FFGPU_EINVAL, "unsupported element (dim %d, fe %d)", S->dim, S->fe);
+    FFGPU_CHECK(smem <= 200 * 1024, FFGPU_EMESH, "row degree %d too large for shared memory", fa.max_deg);
+    FFGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, warps * 32, smem, ctx->stream>>>(fa);
+    return launch_check(ctx, "row_fill_kernel");
+}
+
+static int varf_check(const ffgpu_space *S, const ffgpu_varf *v) {
+    FFGPU_CHECK(v, FFGPU_EINVAL, "varf is NULL");
+    if (v->form == FFGPU_FORM_ELASTICITY)
+        FFGPU_CHECK(S->fe == FFGPU_FE_P2VEC3, FFGPU_EINVAL, "elasticity needs the [P2,P2,P2] space");
+    else
+        FFGPU_CHECK(v->form == FFGPU_FORM_DIFFUSION && S->fe != FFGPU_FE_P2VEC3, FFGPU_EINVAL,
+                    "unsupported form %d for this space", v->form);
+    FFGPU_CHECK(!(S->fe == FFGPU_FE_P2 && v->c_mass != 0.0), FFGPU_EINVAL,
+                "P2 mass term is not supported on the device path");
+    return FFGPU_OK;
+}
+
+static int run_geometry(ffgpu_space *S, const ffgpu_varf *v, double *geo) {
+    ffgpu_ctx *ctx = S->ctx;
+    DevIn<double> kap(v->kappa, v->kappa ? S->nt : 0, ctx->stream);
+    FFGPU_TRY(kap.err);
+    double cs = v->form == FFGPU_FORM_DIFFUSION ? v->c_stiff : 1.0;
+    geometry_kernel<<<grid_for(S->nt, 256), 256, 0, ctx->stream>>>(S->coords, S->elems, S->nt, S->dim,
+                                                                   kap.d, cs, geo);
+    return launch_check(ctx, "geometry_kernel");
+}
+
+static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc, double *rhs,
+                        bool build_cols) {
+    ffgpu_space *S = M->space;
+    ffgpu_ctx *ctx = S->ctx;
+    FFGPU_TRY(varf_check(S, v));
+    FFGPU_TRY(run_geometry(S, v, M->geo));
+    int bs = S->bs;
+    DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * bs : 0, ctx->stream);
+    DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, ctx->stream);
+    DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, ctx->stream);
+    DevOut<double> rh(rhs, rhs ? S->ndof : 0, ctx->stream, false);
+    FFGPU_TRY(fP0.err); FFGPU_TRY(onbc.err); FFGPU_TRY(gv.err); FFGPU_TRY(rh.err);
+    FillArgs fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.nnodes = S->nnodes; fa.nt = S->nt;
+    fa.inc_ptr = S->inc_ptr; fa.inc_elem = S->inc_elem; fa.inc_loc = S->inc_loc;
+    fa.nodes = S->nodes; fa.geo = M->geo; fa.browptr = M->browptr;
+    fa.bcol = build_cols ? M->bcol : nullptr;
+    fa.val = M->val; fa.rhs = rh.d; fa.fP0 = fP0.d;
+    fa.f0 = v->f_const[0]; fa.f1 = v->f_const[1]; fa.f2 = v->f_const[2];
+    fa.c_mass = v->form == FFGPU_FORM_DIFFUSION ? v->c_mass : 0.0;
+    if (v->form == FFGPU_FORM_ELASTICITY) {
+        fa.mu = v->E / (2 * (1 + v->nu));
+        fa.lam = v->E * v->nu / ((1 + v->nu) * (1 - 2 * v->nu));
+    }
+    fa.onbc = onbc.d; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
+    fa.max_deg = M->max_deg; fa.status = ctx->d_status;
+    FFGPU_TRY(fill_launch(S, fa));
+    FFGPU_TRY(check_device_status(ctx, "assembly"));
+    FFGPU_TRY(rh.finish(ctx->stream));
+    // the solver data of a previous numeric state are stale
+    M->ntgv = -1;
+    if (M->val_t) { cudaFree(M->val_t); M->val_t = nullptr; }
+    if (M->val32) { cudaFree(M->val32); M->val32 = nullptr; }
+    return FFGPU_OK;
+}
+
+extern "C" {
+
+int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, int nt,
+                       const int32_t *elems, int fe, int ndofK, const int32_t *dof, int ndof,
+                       ffgpu_space **out) {
+    FFGPU_CHECK(ctx && out && coords && elems && dof, FFGPU_EINVAL, "ffgpu_space_create: NULL argument");
+    FFGPU_CHECK(dim == 2 || dim == 3, FFGPU_EINVAL, "dim must be 2 or 3");
+    FFGPU_CHECK(nv > 0 && nt > 0 && ndof > 0, FFGPU_EINVAL, "empty mesh or space");
+    int nvk = dim + 1, nn, bs;
+    if (fe == FFGPU_FE_P1) { nn = nvk; bs = 1; }
+    else if (fe == FFGPU_FE_P2) { nn = dim == 3 ? 10 : 6; bs = 1; }
+    else if (fe == FFGPU_FE_P2VEC3) { FFGPU_CHECK(dim == 3, FFGPU_EINVAL, "[P2]^3 needs dim 3"); nn = 10; bs = 3; }
+    else { set_error("unknown finite element %d", fe); return FFGPU_EINVAL; }
+    FFGPU_CHECK(ndofK == nn * bs, FFGPU_EINVAL, "ndofK %d does not match the element (%d)", ndofK, nn * bs);
+    FFGPU_CHECK(ndof % bs == 0, FFGPU_EINVAL, "ndof %d not a multiple of %d", ndof, bs);
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    ffgpu_space *S = new ffgpu_space();
+    memset(S, 0, sizeof(*S));
+    S->ctx = ctx; S->dim = dim; S->nvk = nvk; S->nv = nv; S->nt = nt; S->fe = fe; S->nn = nn;
+    S->bs = bs; S->ndofK = ndofK; S->ndof = ndof; S->nnodes = ndof / bs;
+    int64_t m = (int64_t)nt * nn;
+    int rc = FFGPU_OK;
+    int32_t *cnt = nullptr;
+    {
+        DevIn<double> X(coords, (size_t)nv * dim, s);
+        DevIn<int32_t> E(elems, (size_t)nt * nvk, s);
+        DevIn<int32_t> D(dof, (size_t)nt * ndofK, s);
+        if (X.err || E.err || D.err) { rc = X.err ? X.err : (E.err ? E.err : D.err); goto fail; }
+        if (cudaMalloc((void **)&S->coords, sizeof(double) * nv * dim) ||
+            cudaMalloc((void **)&S->elems, sizeof(int32_t) * nt * nvk) ||
+            cudaMalloc((void **)&S->nodes, sizeof(int32_t) * m) ||
+            cudaMalloc((void **)&S->inc_ptr, sizeof(int32_t) * (S->nnodes + 1)) ||
+            cudaMalloc((void **)&S->inc_elem, sizeof(int32_t) * m) ||
+            cudaMalloc((void **)&S->inc_loc, m) ||
+            cudaMalloc((void **)&cnt, sizeof(int32_t) * (S->nnodes + 1))) {
+            set_error("ffgpu_space_create: device allocation failed");
+            rc = FFGPU_ENOMEM; goto fail;
+        }
+        cudaMemcpyAsync(S->coords, X.d, sizeof(double) * nv * dim, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(S->elems, E.d, sizeof(int32_t) * nt * nvk, cudaMemcpyDeviceToDevice, s);
+        check_elems_kernel<<<grid_for((int64_t)nt * nvk, 256), 256, 0, s>>>(S->elems, (int64_t)nt * nvk, nv, ctx->d_status);
+        if ((rc = launch_check(ctx, "check_elems"))) goto fail;
+        build_nodes_kernel<<<grid_for(m, 256), 256, 0, s>>>(D.d, nt, ndofK, nn, bs, ndof, S->nodes, ctx->d_status);
+        if ((rc = launch_check(ctx, "build_nodes"))) goto fail;
+        if ((rc = check_device_status(ctx, "ffgpu_space_create"))) goto fail;
+    }
+    cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (S->nnodes + 1), s);
+    inc_count_kernel<<<grid_for(m, 256), 256, 0, s>>>(S->nodes, m, cnt);
+    if ((rc = launch_check(ctx, "inc_count"))) goto fail;
+    if ((rc = device_max_i32(ctx, cnt, S->nnodes, &S->max_inc))) goto fail;
+    if ((rc = device_scan_i32(ctx, cnt, S->inc_ptr, S->nnodes))) goto fail;
+    cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (S->nnodes + 1), s);
+    inc_fill_kernel<<<grid_for(m, 256), 256, 0, s>>>(S->nodes, m, nn, S->inc_ptr, cnt, S->inc_elem, S->inc_loc);
+    if ((rc = launch_check(ctx, "inc_fill"))) goto fail;
+    {
+        int P = 1;
+        while (P < S->max_inc) P <<= 1;
+        size_t smem = (size_t)4 * P * sizeof(long long);
+        if (smem > 200 * 1024 || (int64_t)S->max_inc * nn > kCandMax) {
+            set_error("node valence %d too high (at most %d candidate neighbours)", S->max_inc, kCandMax);
+            rc = FFGPU_EMESH; goto fail;
+        }
+        cudaFuncSetAttribute(inc_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        inc_sort_kernel<<<min(kNumSM * 8, max(1, (S->nnodes + 3) / 4)), 128, smem, s>>>(
+            S->inc_ptr, S->nnodes, S->max_inc, S->inc_elem, S->inc_loc);
+        if ((rc = launch_check(ctx, "inc_sort"))) goto fail;
+    }
+    cudaFreeAsync(cnt, s);
+    cnt = nullptr;
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error("ffgpu_space_create: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = FFGPU_ECUDA; goto fail;
+    }
+    *out = S;
+    return FFGPU_OK;
+fail:
+    if (cnt) cudaFree(cnt);
+    ffgpu_space_destroy(S);
+    return rc;
+}
+
+int ffgpu_space_destroy(ffgpu_space *S) {
+    if (!S) return FFGPU_OK;
+    cudaStreamSynchronize(S->ctx->stream);
+    cudaFree(S->coords); cudaFree(S->elems); cudaFree(S->nodes);
+    cudaFree(S->inc_ptr); cudaFree(S->inc_elem); cudaFree(S->inc_loc);
+    delete S;
+    return FFGPU_OK;
+}
+
+int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, double *rhs,
+                          ffgpu_matrix **out) {
+    FFGPU_CHECK(S && out, FFGPU_EINVAL, "ffgpu_matrix_assemble: NULL argument");
+    FFGPU_TRY(varf_check(S, v));
+    ffgpu_ctx *ctx = S->ctx;
+    cudaStream_t s = ctx->stream;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    ffgpu_matrix *M = new ffgpu_matrix();
+    memset(M, 0, sizeof(*M));
+    M->ctx = ctx; M->space = S; M->bs = S->bs; M->nb = S->nnodes; M->n = S->ndof;
+    M->ntgv = -1; M->csr_lanes = 0;
+    int rc = FFGPU_OK;
+    int32_t *deg = nullptr;
+    if (cudaMalloc((void **)&M->browptr, sizeof(int32_t) * (M->nb + 1)) ||
+        cudaMalloc((void **)&deg, sizeof(int32_t) * (M->nb + 1)) ||
+        cudaMalloc((void **)&M->geo, sizeof(double) * kGeoStride * S->nt)) {
+        set_error("ffgpu_matrix_assemble: device allocation failed");
+        rc = FFGPU_ENOMEM; goto fail;
+    }
+    // symbolic: row degrees, row pointer
+    row_count_kernel<<<min(kNumSM * 16, max(1, (M->nb + 3) / 4)), 128, 0, s>>>(
+        M->nb, S->inc_ptr, S->inc_elem, S->nodes, S->nn, deg, ctx->d_status);
+    if ((rc = launch_check(ctx, "row_count"))) goto fail;
+    if ((rc = check_device_status(ctx, "pattern"))) goto fail;
+    if ((rc = device_max_i32(ctx, deg, M->nb, &M->max_deg))) goto fail;
+    if ((rc = device_scan_i32(ctx, deg, M->browptr, M->nb))) goto fail;
+    {
+        int32_t nnzb = 0;
+        cudaMemcpyAsync(&nnzb, M->browptr + M->nb, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        M->nnzb = nnzb;
+        M->nnz = M->nnzb * M->bs * M->bs;
+    }
+    cudaFreeAsync(deg, s);
+    deg = nullptr;
+    if (cudaMalloc((void **)&M->bcol, sizeof(int32_t) * M->nnzb) ||
+        cudaMalloc((void **)&M->val, sizeof(double) * M->nnz)) {
+        set_error("ffgpu_matrix_assemble: allocation of %lld values failed", (long long)M->nnz);
+        rc = FFGPU_ENOMEM; goto fail;
+    }
+    if ((rc = numeric_pass(M, v, bc, rhs, true))) goto fail;
+    *out = M;
+    return FFGPU_OK;
+fail:
+    if (deg) cudaFree(deg);
+    ffgpu_matrix_destroy(M);
+    return rc;
+}
+
+int ffgpu_matrix_reassemble(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc, double *rhs) {
+    FFGPU_CHECK(M && M->space, FFGPU_EINVAL, "ffgpu_matrix_reassemble: matrix has no FE space");
+    FFGPU_CUDA(cudaSetDevice(M->ctx->device));
+    return numeric_pass(M, v, bc, rhs, false);
+}
+
+int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, double *rhs) {
+    FFGPU_CHECK(S && v && rhs, FFGPU_EINVAL, "ffgpu_rhs_assemble: NULL argument");
+    FFGPU_TRY(varf_check(S, v));
+    ffgpu_ctx *ctx = S->ctx;
+    cudaStream_t s = ctx->stream;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    double *geo = nullptr;
+    FFGPU_CUDA(cudaMallocAsync((void **)&geo, sizeof(double) * kGeoStride * S->nt, s));
+    int rc = run_geometry(S, v, geo);
+    {
+        DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * S->bs : 0, s);
+        DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, s);
+        DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, s);
+        DevOut<double> rh(rhs, S->ndof, s, false);
+        if (!rc) rc = fP0.err ? fP0.err : (onbc.err ? onbc.err : (gv.err ? gv.err : rh.err));
+        if (!rc) {
+            void (*k)(int, const int32_t *, const int32_t *, const uint8_t *, const double *,
+                      const double *, double, double, double, const uint8_t *, const double *,
+                      double, double *) = nullptr;
+            if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = rhs_kernel<2, 1>;
+            if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = rhs_kernel<3, 1>;
+            if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = rhs_kernel<2, 2>;
+            if (S->dim == 3 && S->fe == FFGPU_FE_P2) k = rhs_kernel<3, 2>;
+            if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) k = rhs_kernel<3, 3>;
+            k<<<grid_for((int64_t)S->ndof, 256), 256, 0, s>>>(
+                S->nnodes, S->inc_ptr, S->inc_elem, S->inc_loc, geo, fP0.d, v->f_const[0],
+                v->f_const[1], v->f_const[2], onbc.d, gv.d, bc ? bc->tgv : 0.0, rh.d);
+            rc = launch_check(ctx, "rhs_kernel");
+        }
+        if (!rc) rc = rh.finish(s);
+    }
+    cudaFreeAsync(geo, s);
+    cudaStreamSynchronize(s);
+    return rc;
+}
+
+int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *rowptr,
+                          const int32_t *col, const double *val, ffgpu_matrix **out) {
+    FFGPU_CHECK(ctx && out && rowptr && col && val && n > 0 && nnz > 0, FFGPU_EINVAL,
+                "ffgpu_matrix_from_csr: bad argument");
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    ffgpu_matrix *M = new ffgpu_matrix();
+    memset(M, 0, sizeof(*M));
+    M->ctx = ctx; M->bs = 1; M->nb = n; M->n = n; M->nnzb = nnz; M->nnz = nnz; M->ntgv = -1;
+    if (cudaMalloc((void **)&M->browptr, sizeof(int32_t) * (n + 1)) ||
+        cudaMalloc((void **)&M->bcol, sizeof(int32_t) * nnz) ||
+        cudaMalloc((void **)&M->val, sizeof(double) * nnz)) {
+        set_error("ffgpu_matrix_from_csr: device allocation failed");
+        ffgpu_matrix_destroy(M);
+        return FFGPU_ENOMEM;
+    }
+    cudaMemcpyAsync(M->browptr, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyDefault, s);
+    cudaMemcpyAsync(M->bcol, col, sizeof(int32_t) * nnz, cudaMemcpyDefault, s);
+    cudaMemcpyAsync(M->val, val, sizeof(double) * nnz, cudaMemcpyDefault, s);
+    {
+        int32_t *deg = nullptr;
+        cudaMallocAsync((void **)&deg, sizeof(int32_t) * n, s);
+        // row degrees from the row pointer, for the max-degree bookkeeping
+        std::vector<int32_t> hp(n + 1);
+        cudaMemcpyAsync(hp.data(), M->browptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        int md = 0;
+        for (int i = 0; i < n; ++i) md = max(md, hp[i + 1] - hp[i]);
+        M->max_deg = md;
+        cudaFreeAsync(deg, s);
+        FFGPU_CHECK(hp[n] == nnz && hp[0] == 0, FFGPU_EINVAL, "rowptr inconsistent with nnz");
+    }
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    *out = M;
+    return FFGPU_OK;
+}
+
+int ffgpu_matrix_destroy(ffgpu_matrix *M) {
+    if (!M) return FFGPU_OK;
+    cudaStreamSynchronize(M->ctx->stream);
+    if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
+    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->val); cudaFree(M->geo);
+    cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
+    cudaFree(M->val32); cudaFree(M->ks);
+    delete M;
+    return FFGPU_OK;
+}
+
+int ffgpu_matrix_info(const ffgpu_matrix *M, int *n, int64_t *nnz, int *bs) {
+    FFGPU_CHECK(M, FFGPU_EINVAL, "ffgpu_matrix_info: NULL matrix");
+    if (n) *n = M->n;
+    if (nnz) *nnz = M->nnz;
+    if (bs) *bs = M->bs;
+    return FFGPU_OK;
+}
+
+int ffgpu_matrix_csr(const ffgpu_matrix *M, int32_t *rowptr, int32_t *col, double *val) {
+    FFGPU_CHECK(M && rowptr && col && val, FFGPU_EINVAL, "ffgpu_matrix_csr: NULL argument");
+    ffgpu_ctx *ctx = M->ctx;
+    cudaStream_t s = ctx->stream;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    DevOut<int32_t> rp(rowptr, M->n + 1, s, false);
+    DevOut<int32_t> cl(col, M->nnz, s, false);
+    DevOut<double> vl(val, M->nnz, s, false);
+    FFGPU_TRY(rp.err); FFGPU_TRY(cl.err); FFGPU_TRY(vl.err);
+    export_csr_kernel<<<grid_for(M->nb, 128), 128, 0, s>>>(M->nb, M->bs, M->browptr, M->bcol, M->val,
+                                                            rp.d, cl.d, vl.d);
+    FFGPU_TRY(launch_check(ctx, "export_csr"));
+    FFGPU_TRY(rp.finish(s)); FFGPU_TRY(cl.finish(s)); FFGPU_TRY(vl.finish(s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    return FFGPU_OK;
+}
+
+}  // extern "C"

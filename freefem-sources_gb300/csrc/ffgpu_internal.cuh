@@ -1,0 +1,202 @@
+// ffgpu_internal.cuh -- shared types and helpers of libffgpu (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+#include <vector>
+
+#include "ffgpu.h"
+
+namespace ffgpu {
+
+constexpr int kWarp = 32;
+constexpr int kNumSM = 152;          // GB300: 2 dies x 76 SMs
+constexpr int kCandMax = 512;        // candidate neighbour nodes gathered per matrix row
+constexpr int kRedBlocks = 4 * kNumSM;  // reduction partials of the fused vector kernels
+
+void set_error(const char *fmt, ...);
+
+#define FFGPU_CUDA(call)                                                               \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            ffgpu::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,                \
+                             cudaGetErrorString(e_));                                  \
+            return FFGPU_ECUDA;                                                        \
+        }                                                                              \
+    } while (0)
+
+#define FFGPU_CHECK(cond, code, ...)                                                   \
+    do {                                                                               \
+        if (!(cond)) {                                                                 \
+            ffgpu::set_error(__VA_ARGS__);                                             \
+            return (code);                                                             \
+        }                                                                              \
+    } while (0)
+
+#define FFGPU_TRY(expr)                                                                \
+    do {                                                                               \
+        int r_ = (expr);                                                               \
+        if (r_ != FFGPU_OK) return r_;                                                 \
+    } while (0)
+
+// Device-side status word: kernels record the first failure here instead of trapping.
+enum DevStatus : int {
+    kDevOk = 0,
+    kDevCandOverflow = 1,   // more candidate neighbours than kCandMax
+    kDevDegOverflow = 2,    // row degree above the smem capacity the launch was sized for
+    kDevBadDofLayout = 3,   // [P2]^3 DOF table not of the form 3*node+c
+    kDevBadIndex = 4,       // index out of range in an input table
+    kDevNotFound = 5,       // column missing from a row (pattern inconsistency)
+};
+
+// Scalars of a running Krylov solve, kept in device memory so the iteration loop runs
+// inside one CUDA graph without host round trips.
+struct KrylovScalars {
+    double gcg, gcgp, eps2, rho, gamma, s_gh, s_hq;
+    double gcg0;
+    int iter, itmax, done, converged;
+    unsigned int ticket;   // last-block counter of the fused reductions
+    int pad;
+};
+
+struct ffgpu_ctx_impl;
+}  // namespace ffgpu
+
+struct ffgpu_ctx {
+    int device;
+    cudaStream_t stream;
+    int64_t launches;
+    double *d_part;             // reduction partials [kRedBlocks * 4]
+    int *d_status;              // DevStatus word
+    unsigned int *d_ticket;     // last-block counters
+    int *d_iscratch;            // small integer scratch (max reductions)
+};
+
+struct ffgpu_space {
+    ffgpu_ctx *ctx;
+    int dim, nvk, nv, nt, fe, nn, bs, ndofK, ndof, nnodes;
+    double *coords;      // nv*dim
+    int32_t *elems;      // nt*nvk
+    int32_t *nodes;      // nt*nn  (scalar node of each local basis function)
+    int32_t *inc_ptr;    // nnodes+1
+    int32_t *inc_elem;   // node -> incident elements, ascending
+    uint8_t *inc_loc;    // local index of the node in that element
+    int max_inc;
+};
+
+struct ffgpu_matrix {
+    ffgpu_ctx *ctx;
+    ffgpu_space *space;   // NULL for matrices uploaded from CSR
+    int n, bs, nb;        // DOFs, block size, block rows
+    int64_t nnzb, nnz;
+    int max_deg;
+    int32_t *browptr;     // nb+1
+    int32_t *bcol;        // nnzb
+    double *val;          // nnzb*bs*bs, each block row-major
+    double *geo;          // per-element geometry cache (16 doubles per element)
+    // solver state (lazily allocated)
+    double *diag_inv;     // Jacobi 1/A_ii (1 if tiny)
+    uint8_t *wcl;         // tgv rows found by gettgv
+    int ntgv;
+    double tgv_found;
+    double *vec;          // work vectors (8*n)
+    double *val_t;        // transpose values (same pattern), built on demand
+    float *val32;         // FP32 copy for the mixed-precision inner solve
+    ffgpu::KrylovScalars *ks;
+    // cached CG graph
+    cudaGraphExec_t cg_exec;
+    int cg_unroll, cg_trans;
+    int cg_kernels_init, cg_kernels_body;
+    // tuning
+    int csr_lanes;        // lanes per row of the bs=1 SpMV
+};
+
+namespace ffgpu {
+
+// -------------------------------------------------------------------- host helpers
+bool is_device_ptr(const void *p);
+
+// A view of a caller array on the device: copies host data in on construction when needed.
+template <typename T>
+struct DevIn {
+    const T *d = nullptr;
+    T *owned = nullptr;
+    int err = FFGPU_OK;
+    cudaStream_t st;
+    DevIn(const T *p, size_t n, cudaStream_t s) : st(s) {
+        if (!p || n == 0) { d = nullptr; return; }
+        if (is_device_ptr(p)) { d = p; return; }
+        if (cudaMallocAsync((void **)&owned, n * sizeof(T), s) != cudaSuccess) {
+            set_error("device allocation of %zu bytes failed", n * sizeof(T));
+            err = FFGPU_ENOMEM; return;
+        }
+        if (cudaMemcpyAsync(owned, p, n * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            set_error("host to device copy failed"); err = FFGPU_ECUDA; return;
+        }
+        d = owned;
+    }
+    ~DevIn() { if (owned) cudaFreeAsync(owned, st); }
+};
+
+// A device buffer standing in for a caller output array; copied back by finish().
+template <typename T>
+struct DevOut {
+    T *user = nullptr, *d = nullptr;
+    bool owned = false;
+    size_t n = 0;
+    int err = FFGPU_OK;
+    cudaStream_t st;
+    DevOut(T *p, size_t nn, cudaStream_t s, bool copy_in) : user(p), n(nn), st(s) {
+        if (!p || n == 0) return;
+        if (is_device_ptr(p)) { d = p; return; }
+        owned = true;
+        if (cudaMallocAsync((void **)&d, n * sizeof(T), s) != cudaSuccess) {
+            set_error("device allocation of %zu bytes failed", n * sizeof(T));
+            err = FFGPU_ENOMEM; d = nullptr; return;
+        }
+        if (copy_in &&
+            cudaMemcpyAsync(d, p, n * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            set_error("host to device copy failed"); err = FFGPU_ECUDA;
+        }
+    }
+    int finish(cudaStream_t s) {
+        if (owned && d) {
+            if (cudaMemcpyAsync(user, d, n * sizeof(T), cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+                set_error("device to host copy failed"); return FFGPU_ECUDA;
+            }
+            if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("stream sync failed"); return FFGPU_ECUDA; }
+        }
+        return FFGPU_OK;
+    }
+    ~DevOut() { if (owned && d) cudaFreeAsync(d, st); }
+};
+
+int check_device_status(ffgpu_ctx *ctx, const char *where);
+int launch_check(ffgpu_ctx *ctx, const char *what);
+int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n);  // exclusive, out[n]=total
+int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
+
+// matrix-level operations shared by the solvers
+int matrix_prepare_solver(ffgpu_matrix *A);
+int matrix_prepare_transpose(ffgpu_matrix *A);
+int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t s);
+
+// -------------------------------------------------------------------- device helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void dev_fail(int *status, int code) {
+    atomicCAS(status, 0, code);
+}
+
+}  // namespace ffgpu

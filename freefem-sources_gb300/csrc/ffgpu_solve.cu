@@ -1,0 +1,788 @@
+// ffgpu_solve.cu -- SpMV, Jacobi PCG (CUDA-graph loop) and FGMRES on the device.
+//
+// The PCG is FreeFEM's ConjugueGradient (src/femlib/CG.cpp:196-265) step for step:
+//   G = Ax - b; gCg = (G, CG); H = -CG; eps2 = eps^2 gCg (eps > 0)
+//   loop: rho = -(G,H)/(H,AH); x += rho H; G += rho AH; gCg' = (G,CG); gamma = gCg'/gCg;
+//         H = gamma H - CG; stop when gCg' < eps2
+// with C = Jacobi (1/A_ii, 1 if |A_ii|^2 < 1e-60) and x_i = b_i/tgv on tgv rows
+// (VirtualSolverCG.hpp:27-99).  One iteration = three fused kernels:
+//   K_a  AH = A H (SpMV) with (H,AH) -> rho                     [last block]
+//   K_b  x += rho H, G += rho AH, (G, C G) -> gamma, stop test  [last block]
+//   K_c  H = gamma H - C G with (G,H)                            [last block]
+// CG = C G is recomputed where it is used instead of being stored.  The iteration loop is
+// a CUDA graph `while` node whose condition K_b clears on convergence or at itmax, so a
+// whole solve is one graph launch with no host round trip.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ffgpu_internal.cuh"
+
+namespace ffgpu {
+
+constexpr int kSpmvWarps = 8;                 // warps per SpMV block
+constexpr int kSpmvBlocks = 16 * kNumSM;      // persistent grid of the fused SpMV
+constexpr int kVecBlocks = 4 * kNumSM;        // grid of the fused vector kernels
+constexpr int kVecThreads = 256;
+
+// ------------------------------------------------------------------ reductions
+// Block sum of one double; returns the block total in thread 0.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (w == 0) {
+        t = lane < nw ? sh[lane] : 0.0;
+        t = warp_sum(t);
+    }
+    __syncthreads();
+    return t;
+}
+
+// Stores this block's partial, returns true in exactly one thread of the last block to
+// finish; that thread's `tot` receives the deterministic sum of all partials (fixed order).
+__device__ __forceinline__ bool last_block_total(double partial, double *part, unsigned *ticket,
+                                                  double *tot, double *sh) {
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = partial;
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double s = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(part + i);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) {
+        *tot = s;
+        *ticket = 0u;
+        return true;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ SpMV rows
+// CSR (block size 1): T lanes per row, lanes stride the row.
+template <int T>
+__device__ __forceinline__ double csr_row(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                          const double *__restrict__ val, const double *__restrict__ x,
+                                          int r, int sub) {
+    int b = __ldg(rp + r), e = __ldg(rp + r + 1);
+    double s = 0;
+    for (int k = b + sub; k < e; k += T) s = fma(__ldg(val + k), __ldg(x + __ldg(col + k)), s);
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+// BSR 3x3: T lanes per block row, each lane whole blocks (9 values, 3 outputs).
+template <int T>
+__device__ __forceinline__ void bsr3_row(const int32_t *__restrict__ brp, const int32_t *__restrict__ bcol,
+                                         const double *__restrict__ val, const double *__restrict__ x,
+                                         int a, int sub, double y[3]) {
+    int b = __ldg(brp + a), e = __ldg(brp + a + 1);
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int k = b + sub; k < e; k += T) {
+        int c = __ldg(bcol + k);
+        const double *v = val + (int64_t)k * 9;
+        double x0 = __ldg(x + 3 * (int64_t)c), x1 = __ldg(x + 3 * (int64_t)c + 1), x2 = __ldg(x + 3 * (int64_t)c + 2);
+        s0 = fma(__ldg(v + 0), x0, s0); s0 = fma(__ldg(v + 1), x1, s0); s0 = fma(__ldg(v + 2), x2, s0);
+        s1 = fma(__ldg(v + 3), x0, s1); s1 = fma(__ldg(v + 4), x1, s1); s1 = fma(__ldg(v + 5), x2, s1);
+        s2 = fma(__ldg(v + 6), x0, s2); s2 = fma(__ldg(v + 7), x1, s2); s2 = fma(__ldg(v + 8), x2, s2);
+    }
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    y[0] = s0; y[1] = s1; y[2] = s2;
+}
+
+struct SpmvArgs {
+    int nb, bs;
+    const int32_t *rp, *col;
+    const double *val;
+};
+
+// y = A x, optionally with the partial of (w, y) (w may alias x); persistent grid.
+template <int BS, int T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) spmv_kernel(SpmvArgs A, const double *__restrict__ x,
+                                                               double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int gsub = lane / T, sub = lane % T;
+    const int groups = (blockDim.x / 32) * (32 / T);
+    int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
+    for (int base = 0; base < A.nb; base += gridDim.x * groups) {
+        int a = base + g;
+        if (BS == 1) {
+            double s = 0;
+            if (a < A.nb) s = csr_row<T>(A.rp, A.col, A.val, x, a, sub);
+            else s = csr_row<T>(A.rp, A.col, A.val, x, 0, T);   // keep the warp converged
+            if (a < A.nb && sub == 0) y[a] = s;
+        } else {
+            double v[3];
+            bsr3_row<T>(A.rp, A.col, A.val, x, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
+            if (a < A.nb && sub < 3) y[3 * (int64_t)a + sub] = sub == 0 ? v[0] : (sub == 1 ? v[1] : v[2]);
+        }
+    }
+}
+
+// K_a: AH = A H and (H, AH) -> rho = -(G,H)/(H,AH)
+template <int BS, int T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const double *__restrict__ h,
+                                                         double *__restrict__ q, KrylovScalars *ks,
+                                                         double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const int lane = threadIdx.x & 31;
+    const int gsub = lane / T, sub = lane % T;
+    const int groups = (blockDim.x / 32) * (32 / T);
+    int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
+    double hq = 0;
+    for (int base = 0; base < A.nb; base += gridDim.x * groups) {
+        int a = base + g;
+        if (BS == 1) {
+            double s = csr_row<T>(A.rp, A.col, A.val, h, a < A.nb ? a : 0, a < A.nb ? sub : T);
+            if (a < A.nb && sub == 0) { q[a] = s; hq = fma(h[a], s, hq); }
+        } else {
+            double v[3];
+            bsr3_row<T>(A.rp, A.col, A.val, h, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
+            if (a < A.nb && sub < 3) {
+                int64_t i = 3 * (int64_t)a + sub;
+                double vs = sub == 0 ? v[0] : (sub == 1 ? v[1] : v[2]);
+                q[i] = vs;
+                hq = fma(h[i], vs, hq);
+            }
+        }
+    }
+    double tot;
+    double p = block_sum(hq, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
+        ks->s_hq = tot;
+        ks->rho = -ks->s_gh / tot;
+    }
+}
+
+// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence
+__global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
+                                                     const double *__restrict__ h, const double *__restrict__ q,
+                                                     const double *__restrict__ dinv, KrylovScalars *ks,
+                                                     double *part, cudaGraphConditionalHandle cond) {
+    __shared__ double sh[32];
+    if (ks->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0);
+        return;
+    }
+    const double rho = ks->rho;
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double hi = h[i];
+        x[i] = fma(rho, hi, x[i]);
+        double gi = fma(rho, q[i], g[i]);
+        g[i] = gi;
+        s = fma(gi, dinv[i] * gi, s);
+    }
+    double tot;
+    double p = block_sum(s, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
+        ks->gcgp = ks->gcg;
+        ks->gcg = tot;
+        ks->gamma = tot / ks->gcgp;
+        ks->iter += 1;
+        if (tot < ks->eps2) { ks->converged = 1; ks->done = 1; }
+        else if (ks->iter >= ks->itmax) ks->done = 1;
+        if (ks->done) cudaGraphSetConditional(cond, 0);
+    }
+}
+
+// K_c: H = gamma H - C G and (G, H)
+__global__ void __launch_bounds__(kVecThreads) cg_kc(int n, const double *__restrict__ g, double *__restrict__ h,
+                                                     const double *__restrict__ dinv, KrylovScalars *ks,
+                                                     double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const double gamma = ks->gamma;
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double gi = g[i];
+        double hi = gamma * h[i] - dinv[i] * gi;
+        h[i] = hi;
+        s = fma(gi, hi, s);
+    }
+    double tot;
+    double p = block_sum(s, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
+}
+
+// init: x_i = b_i/tgv on tgv rows (done before the SpMV), then with G = A x:
+//   G -= b; gCg = (G, CG); H = -CG; (G,H); eps2; done if gCg < 1e-30
+__global__ void cg_x0_kernel(int n, double *x, const double *b, const uint8_t *wcl, double tgv) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n && wcl[i]) x[i] = b[i] / tgv;
+}
+
+__global__ void __launch_bounds__(kVecThreads) cg_init(int n, double *__restrict__ g, const double *__restrict__ b,
+                                                       double *__restrict__ h, const double *__restrict__ dinv,
+                                                       KrylovScalars *ks, double eps, int itmax, double *part) {
+    __shared__ double sh[32];
+    double s1 = 0, s2 = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double gi = g[i] - b[i];
+        g[i] = gi;
+        double ci = dinv[i] * gi;
+        h[i] = -ci;
+        s1 = fma(gi, ci, s1);
+        s2 = fma(gi, -ci, s2);
+    }
+    double p1 = block_sum(s1, sh);
+    double p2 = block_sum(s2, sh);
+    // two totals: use two passes of the last-block protocol on separate partial slots
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = p1;
+        part[gridDim.x + blockIdx.x] = p2;
+        __threadfence();
+        unsigned t = atomicAdd(&ks->ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double a = 0, c = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        a += __ldcg(part + i);
+        c += __ldcg(part + gridDim.x + i);
+    }
+    a = block_sum(a, sh);
+    c = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+        ks->gcg = a;
+        ks->gcg0 = a;
+        ks->gcgp = a;
+        ks->s_gh = c;
+        ks->eps2 = eps > 0 ? eps * eps * a : eps * eps;
+        ks->iter = 0;
+        ks->itmax = itmax;
+        ks->converged = 0;
+        ks->done = 0;
+        if (a < 1e-30) { ks->done = 1; ks->converged = 2; }
+        ks->ticket = 0u;
+    }
+}
+
+// ------------------------------------------------------------------ Jacobi + gettgv
+__global__ void diag_kernel(int nb, int bs, const int32_t *brp, const int32_t *bcol, const double *val,
+                            double *diag, unsigned long long *maxbits) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nb * bs) return;
+    int a = (int)(t / bs), c = (int)(t % bs);
+    double d = 0;
+    bool found = false;
+    for (int k = brp[a]; k < brp[a + 1]; ++k)
+        if (bcol[k] == a) { d = val[(int64_t)k * bs * bs + c * bs + c]; found = true; break; }
+    diag[t] = d;
+    if (found && d > 0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
+}
+
+__global__ void diag_second_kernel(int64_t n, const double *diag, double top, unsigned long long *max1bits,
+                                   int *count) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = diag[i];
+    if (d == top) atomicAdd(count, 1);
+    else if (d > 0 && d < top) atomicMax(max1bits, (unsigned long long)__double_as_longlong(d));
+}
+
+__global__ void jacobi_kernel(int64_t n, double *diag, uint8_t *wcl, double tgve, int ntgv) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = diag[i];
+    wcl[i] = ntgv ? (d == tgve) : 0;
+    diag[i] = (d * d < 1e-60) ? 1.0 : 1.0 / d;
+}
+
+// transpose values on the (structurally symmetric) pattern: At(a,b) = A(b,a)^T blockwise
+__global__ void transpose_kernel(int nb, int bs, const int32_t *brp, const int32_t *bcol, const double *val,
+                                 double *valt, int *status) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nb) return;
+    for (int k = brp[a]; k < brp[a + 1]; ++k) {
+        int b = bcol[k];
+        int lo = brp[b], hi = brp[b + 1] - 1, pos = -1;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            int c = bcol[mid];
+            if (c == a) { pos = mid; break; }
+            if (c < a) lo = mid + 1; else hi = mid - 1;
+        }
+        if (pos < 0) { dev_fail(status, kDevNotFound); return; }
+        for (int r = 0; r < bs; ++r)
+            for (int c = 0; c < bs; ++c)
+                valt[(int64_t)k * bs * bs + r * bs + c] = val[(int64_t)pos * bs * bs + c * bs + r];
+    }
+}
+
+// ------------------------------------------------------------------ host side
+static int pick_lanes(const ffgpu_matrix *A) {
+    if (A->csr_lanes > 0) return A->csr_lanes;
+    double avg = (double)A->nnzb / (double)max(1, A->nb);
+    if (A->bs == 3) return avg >= 24 ? 4 : 2;
+    if (avg >= 24) return 8;
+    if (avg >= 10) return 4;
+    return 2;
+}
+
+template <int BS>
+static void *spmv_fn(int T) {
+    switch (T) {
+        case 1: return (void *)spmv_kernel<BS, 1>;
+        case 2: return (void *)spmv_kernel<BS, 2>;
+        case 4: return (void *)spmv_kernel<BS, 4>;
+        case 8: return (void *)spmv_kernel<BS, 8>;
+        case 16: return (void *)spmv_kernel<BS, 16>;
+        default: return (void *)spmv_kernel<BS, 32>;
+    }
+}
+template <int BS>
+static void *ka_fn(int T) {
+    switch (T) {
+        case 1: return (void *)cg_ka<BS, 1>;
+        case 2: return (void *)cg_ka<BS, 2>;
+        case 4: return (void *)cg_ka<BS, 4>;
+        case 8: return (void *)cg_ka<BS, 8>;
+        case 16: return (void *)cg_ka<BS, 16>;
+        default: return (void *)cg_ka<BS, 32>;
+    }
+}
+
+static int spmv_grid(const ffgpu_matrix *A, int T) {
+    int groups = kSpmvWarps * (32 / T);
+    int need = (A->nb + groups - 1) / groups;
+    return max(1, min(kSpmvBlocks, need));
+}
+
+static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
+    SpmvArgs s;
+    s.nb = A->nb; s.bs = A->bs; s.rp = A->browptr; s.col = A->bcol;
+    s.val = trans ? A->val_t : A->val;
+    return s;
+}
+
+int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st) {
+    if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
+    int T = pick_lanes(A);
+    SpmvArgs s = spmv_args(A, trans);
+    void *fn = A->bs == 3 ? spmv_fn<3>(T) : spmv_fn<1>(T);
+    void *args[] = {&s, &x, &y};
+    FFGPU_CUDA(cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, st));
+    return launch_check(A->ctx, "spmv");
+}
+
+int matrix_prepare_transpose(ffgpu_matrix *A) {
+    if (A->val_t) return FFGPU_OK;
+    ffgpu_ctx *ctx = A->ctx;
+    FFGPU_CUDA(cudaMalloc((void **)&A->val_t, sizeof(double) * A->nnz));
+    transpose_kernel<<<(A->nb + 127) / 128, 128, 0, ctx->stream>>>(A->nb, A->bs, A->browptr, A->bcol, A->val,
+                                                                   A->val_t, ctx->d_status);
+    FFGPU_TRY(launch_check(ctx, "transpose"));
+    return check_device_status(ctx, "transpose (pattern not structurally symmetric)");
+}
+
+int matrix_prepare_solver(ffgpu_matrix *A) {
+    ffgpu_ctx *ctx = A->ctx;
+    cudaStream_t s = ctx->stream;
+    int64_t n = A->n;
+    if (!A->vec) {
+        FFGPU_CUDA(cudaMalloc((void **)&A->vec, sizeof(double) * n * 8));
+        FFGPU_CUDA(cudaMalloc((void **)&A->diag_inv, sizeof(double) * n));
+        FFGPU_CUDA(cudaMalloc((void **)&A->wcl, n));
+        FFGPU_CUDA(cudaMalloc((void **)&A->ks, sizeof(KrylovScalars)));
+        FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
+    }
+    if (A->ntgv >= 0) return FFGPU_OK;
+    unsigned long long *bits = (unsigned long long *)ctx->d_iscratch;   // [0] max, [1] max1
+    int *cnt = ctx->d_iscratch + 4;
+    FFGPU_CUDA(cudaMemsetAsync(ctx->d_iscratch, 0, sizeof(int) * 8, s));
+    diag_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(A->nb, A->bs, A->browptr, A->bcol, A->val, A->diag_inv, bits);
+    FFGPU_TRY(launch_check(ctx, "diag"));
+    unsigned long long hb[2] = {0, 0};
+    FFGPU_CUDA(cudaMemcpyAsync(hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    double top;
+    memcpy(&top, &hb[0], sizeof(double));
+    diag_second_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A->diag_inv, top, bits + 1, cnt);
+    FFGPU_TRY(launch_check(ctx, "diag_second"));
+    int hc = 0;
+    FFGPU_CUDA(cudaMemcpyAsync(hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    FFGPU_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    double max1;
+    memcpy(&max1, &hb[1], sizeof(double));
+    // HashMatrix::gettgv (HashMatrix.cpp:1341-1371): no tgv when max1*1e6 > ttgv
+    double ttgv = top;
+    int ntgv = hc;
+    if (max1 * 1e6 > ttgv) { ttgv = 0; ntgv = 0; }
+    A->ntgv = ntgv;
+    A->tgv_found = ttgv;
+    jacobi_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A->diag_inv, A->wcl, ttgv > 0 ? ttgv : 1e200, ntgv);
+    return launch_check(ctx, "jacobi");
+}
+
+// Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }].
+static int cg_graph(ffgpu_matrix *A, int trans, int unroll, double *x, double *g, double *h, double *q) {
+    if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans) return FFGPU_OK;
+    if (A->cg_exec) { cudaGraphExecDestroy(A->cg_exec); A->cg_exec = nullptr; }
+    ffgpu_ctx *ctx = A->ctx;
+    cudaStream_t s = ctx->stream;
+    cudaGraph_t graph, body;
+    FFGPU_CUDA(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle cond;
+    FFGPU_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+    // cudaGraphNodeParams has no usable default constructor: build it in zeroed storage
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+    memset(cp_buf, 0, sizeof(cp_buf));
+    cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
+    cp->type = cudaGraphNodeTypeConditional;
+    cp->conditional.handle = cond;
+    cp->conditional.type = cudaGraphCondTypeWhile;
+    cp->conditional.size = 1;
+    cudaGraphNode_t node;
+    FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
+    body = cp->conditional.phGraph_out[0];
+    FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int T = pick_lanes(A);
+    SpmvArgs sa = spmv_args(A, trans);
+    void *ka = A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T);
+    int n = A->n;
+    KrylovScalars *ks = A->ks;
+    double *part = ctx->d_part;
+    const double *dinv = A->diag_inv;
+    for (int u = 0; u < unroll; ++u) {
+        void *aa[] = {&sa, &h, &q, &ks, &part};
+        cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
+        cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond);
+        cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, dinv, ks, part);
+    }
+    cudaError_t e = cudaStreamEndCapture(s, &body);
+    if (e != cudaSuccess) {
+        set_error("CG graph capture failed: %s", cudaGetErrorString(e));
+        cudaGraphDestroy(graph);
+        return FFGPU_ECUDA;
+    }
+    e = cudaGraphInstantiate(&A->cg_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error("CG graph instantiate failed: %s", cudaGetErrorString(e));
+        A->cg_exec = nullptr;
+        return FFGPU_ECUDA;
+    }
+    A->cg_unroll = unroll;
+    A->cg_trans = trans;
+    A->cg_kernels_body = 3 * unroll;
+    return FFGPU_OK;
+}
+
+// one right-hand side; x/b device pointers of length n
+static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
+                  ffgpu_solver_stats *st) {
+    ffgpu_ctx *ctx = A->ctx;
+    cudaStream_t s = ctx->stream;
+    int n = A->n;
+    double *g = A->vec, *h = A->vec + n, *q = A->vec + 2 * (int64_t)n;
+    double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
+    int itmax = prm->itmax > 0 ? prm->itmax : n;
+    int unroll = prm->unroll > 0 ? prm->unroll : 8;
+    FFGPU_TRY(cg_graph(A, trans, unroll, x, g, h, q));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    if (A->ntgv > 0) {
+        cg_x0_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, x, b, A->wcl, tgv);
+        FFGPU_TRY(launch_check(ctx, "cg_x0"));
+    }
+    FFGPU_TRY(spmv(A, x, g, trans, s));
+    cg_init<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, b, h, A->diag_inv, A->ks, prm->eps, itmax, ctx->d_part);
+    FFGPU_TRY(launch_check(ctx, "cg_init"));
+    FFGPU_CUDA(cudaGraphLaunch(A->cg_exec, s));
+    cudaEventRecord(e1, s);
+    KrylovScalars hk;
+    FFGPU_CUDA(cudaMemcpyAsync(&hk, A->ks, sizeof(hk), cudaMemcpyDeviceToHost, s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int bodies = hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll;
+    ctx->launches += (int64_t)bodies * A->cg_kernels_body;
+    if (st) {
+        st->iterations = hk.iter;
+        st->converged = hk.converged != 0;
+        st->gcg = hk.gcg;
+        st->eps2 = hk.eps2;
+        st->elapsed_ms += ms;
+    }
+    return hk.converged ? FFGPU_OK : FFGPU_ENOCONV;
+}
+
+// ------------------------------------------------------------------ FGMRES kernels
+__global__ void vec_dot_kernel(int n, const double *x, const double *y, double *part, unsigned *ticket,
+                               double *out) {
+    __shared__ double sh[32];
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(x[i], y[i], s);
+    double tot;
+    double p = block_sum(s, sh);
+    if (last_block_total(p, part, ticket, &tot, sh)) *out = tot;
+}
+
+// y += alpha * x with alpha = sign * (*palpha)
+__global__ void vec_axpy_dev_kernel(int n, const double *palpha, double sign, const double *x, double *y) {
+    double a = sign * *palpha;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = fma(a, x[i], y[i]);
+}
+
+// y = x * (1/ *pnorm2 ^ 0.5) ... y = (1/sqrt(*pn2)) * x
+__global__ void vec_scale_inv_sqrt_kernel(int n, const double *pn2, const double *x, double *y) {
+    double a = 1.0 / sqrt(*pn2);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = a * x[i];
+}
+
+__global__ void vec_mul_kernel(int n, const double *d, const double *x, double *y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = d[i] * x[i];
+}
+
+// r = b - r ; (r,r)
+__global__ void resid_kernel(int n, const double *b, double *r) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = -(r[i] - b[i]);
+}
+
+__global__ void masked_copy_kernel(int n, const double *b, const uint8_t *wcl, int use, double *w) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = (use && wcl[i]) ? 0.0 : b[i];
+}
+
+// Givens step of fgmres on column `it` of Hn (device resident, single thread).
+__global__ void givens_kernel(int it, int ld, double *Hn, const double *hnext2, double *rot0, double *rot1,
+                              double *g, double *relres) {
+    Hn[(size_t)(it + 1) * ld + it] = sqrt(*hnext2);
+    for (int i = 0; i < it; i++) {
+        double a = Hn[(size_t)i * ld + it], b = Hn[(size_t)(i + 1) * ld + it];
+        Hn[(size_t)i * ld + it] = rot0[i] * a + rot1[i] * b;
+        Hn[(size_t)(i + 1) * ld + it] = -rot1[i] * a + rot0[i] * b;
+    }
+    double a = Hn[(size_t)it * ld + it], b = Hn[(size_t)(it + 1) * ld + it];
+    double sq = sqrt(a * a + b * b);
+    rot0[it] = a / sq;
+    rot1[it] = b / sq;
+    Hn[(size_t)it * ld + it] = rot0[it] * a + rot1[it] * b;
+    Hn[(size_t)(it + 1) * ld + it] = 0.;
+    g[it + 1] = -rot1[it] * g[it];
+    g[it] = rot0[it] * g[it];
+    *relres = fabs(g[it + 1]);
+}
+
+// back substitution y = Hn^-1 g (upper triangular, it+1 unknowns)
+__global__ void backsolve_kernel(int it, int ld, const double *Hn, const double *g, double *y) {
+    for (int i = it; i >= 0; i--) {
+        double s = g[i];
+        for (int j = i + 1; j < it + 1; j++) s -= Hn[(size_t)i * ld + j] * y[j];
+        y[i] = s / Hn[(size_t)i * ld + i];
+    }
+}
+
+__global__ void gmres_update_kernel(int n, int k, const double *y, const double *Vp, const double *x0, double *x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0;
+        for (int j = 0; j < k; ++j) s += y[j] * Vp[(size_t)j * n + i];
+        x[i] = s + x0[i];
+    }
+}
+
+static int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
+                     ffgpu_solver_stats *st) {
+    ffgpu_ctx *ctx = A->ctx;
+    cudaStream_t s = ctx->stream;
+    const int n = A->n;
+    const int m = prm->dim_krylov > 0 ? prm->dim_krylov : 50;
+    const int itmax = prm->itmax > 0 ? prm->itmax : n;
+    const double eps = prm->eps;
+    const double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
+    const int G = kVecBlocks, TB = kVecThreads;
+    double *V = nullptr, *Vp = nullptr, *dev = nullptr;
+    size_t ld = m + 1;
+    FFGPU_CUDA(cudaMallocAsync((void **)&V, sizeof(double) * (size_t)n * (m + 1), s));
+    FFGPU_CUDA(cudaMallocAsync((void **)&Vp, sizeof(double) * (size_t)n * (m + 1), s));
+    // device scalars: Hn[(m+2) x (m+1)], rot0, rot1, g, y, dotv, relres
+    size_t nsc = (size_t)(m + 2) * ld + 4 * (m + 2) + 8;
+    FFGPU_CUDA(cudaMallocAsync((void **)&dev, sizeof(double) * nsc, s));
+    FFGPU_CUDA(cudaMemsetAsync(dev, 0, sizeof(double) * nsc, s));
+    double *Hn = dev, *rot0 = Hn + (size_t)(m + 2) * ld, *rot1 = rot0 + (m + 2), *gv = rot1 + (m + 2);
+    double *y = gv + (m + 2), *dotv = y + (m + 2), *relres_d = dotv + 2;
+    double *wi = A->vec, *ri = A->vec + 2 * (int64_t)n, *x0 = A->vec + 3 * (int64_t)n;
+    unsigned *tk = ctx->d_ticket;
+    double *part = ctx->d_part;
+    int rc = FFGPU_OK;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    if (A->ntgv > 0) cg_x0_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, x, b, A->wcl, tgv);
+    masked_copy_kernel<<<G, TB, 0, s>>>(n, b, A->wcl, A->ntgv > 0, wi);
+    vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, wi, part, tk, dotv);
+    ctx->launches += 3;
+    double hb[2];
+    cudaMemcpyAsync(hb, dotv, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    double normb = sqrt(hb[0]);
+    int iter = 0;
+    bool noconv = true;
+    double relres = 1e100;
+    while (noconv) {
+        cudaMemcpyAsync(x0, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+        if ((rc = spmv(A, x, ri, trans, s))) break;
+        resid_kernel<<<G, TB, 0, s>>>(n, b, ri);
+        vec_dot_kernel<<<G, TB, 0, s>>>(n, ri, ri, part, tk, dotv);
+        ctx->launches += 2;
+        cudaMemcpyAsync(hb, dotv, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        double g0 = sqrt(hb[0]);
+        if (normb < 1.e-20 || eps < 0) normb = 1.;
+        cudaMemcpyAsync(gv, &g0, sizeof(double), cudaMemcpyHostToDevice, s);
+        vec_scale_inv_sqrt_kernel<<<G, TB, 0, s>>>(n, dotv, ri, V);
+        ctx->launches += 1;
+        int it;
+        for (it = 0; it < m; it++, iter++) {
+            double *Vit = V + (size_t)it * n, *Vpit = Vp + (size_t)it * n;
+            vec_mul_kernel<<<G, TB, 0, s>>>(n, A->diag_inv, Vit, Vpit);
+            ctx->launches += 1;
+            if ((rc = spmv(A, Vpit, wi, trans, s))) break;
+            for (int i = 0; i <= it; i++) {   // modified Gram-Schmidt
+                double *hij = Hn + (size_t)i * ld + it;
+                vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, V + (size_t)i * n, part, tk, hij);
+                vec_axpy_dev_kernel<<<G, TB, 0, s>>>(n, hij, -1.0, V + (size_t)i * n, wi);
+                ctx->launches += 2;
+            }
+            vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, wi, part, tk, dotv);
+            vec_scale_inv_sqrt_kernel<<<G, TB, 0, s>>>(n, dotv, wi, V + (size_t)(it + 1) * n);
+            givens_kernel<<<1, 1, 0, s>>>(it, (int)ld, Hn, dotv, rot0, rot1, gv, relres_d);
+            ctx->launches += 3;
+            cudaMemcpyAsync(&relres, relres_d, sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("gmres: %s", cudaGetErrorString(cudaGetLastError())); rc = FFGPU_ECUDA; break; }
+            if (relres / normb < fabs(eps)) { noconv = false; break; }
+            if (it > itmax) break;
+        }
+        if (rc) break;
+        it = min(it, m - 1);
+        backsolve_kernel<<<1, 1, 0, s>>>(it, (int)ld, Hn, gv, y);
+        gmres_update_kernel<<<G, TB, 0, s>>>(n, it + 1, y, Vp, x0, x);
+        ctx->launches += 2;
+        if (!noconv) break;
+        if (iter > itmax) break;
+    }
+    cudaEventRecord(e1, s);
+    cudaStreamSynchronize(s);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(V, s);
+    cudaFreeAsync(Vp, s);
+    cudaFreeAsync(dev, s);
+    cudaStreamSynchronize(s);
+    if (rc) return rc;
+    if (st) {
+        st->iterations = iter;
+        st->converged = !noconv;
+        st->residual = relres / normb;
+        st->elapsed_ms += ms;
+    }
+    return noconv ? FFGPU_ENOCONV : FFGPU_OK;
+}
+
+}  // namespace ffgpu
+
+using namespace ffgpu;
+
+typedef int (*one_solver)(ffgpu_matrix *, const double *, double *, int, const ffgpu_solver_params *,
+                          ffgpu_solver_stats *);
+
+static int solve_many(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                      const ffgpu_solver_params *prm, ffgpu_solver_stats *stats, one_solver fn) {
+    FFGPU_CHECK(A && b && x && prm && nrhs >= 1, FFGPU_EINVAL, "solve: bad argument");
+    ffgpu_ctx *ctx = A->ctx;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    int64_t n = A->n;
+    FFGPU_TRY(matrix_prepare_solver(A));
+    if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
+    DevIn<double> bd(b, (size_t)n * nrhs, s);
+    DevOut<double> xd(x, (size_t)n * nrhs, s, true);
+    FFGPU_TRY(bd.err);
+    FFGPU_TRY(xd.err);
+    ffgpu_solver_stats acc;
+    memset(&acc, 0, sizeof(acc));
+    int err = 0, total_it = 0;
+    ffgpu_solver_stats one;
+    for (int k = 0; k < nrhs; ++k) {
+        memset(&one, 0, sizeof(one));
+        int r = fn(A, bd.d + k * n, xd.d + k * n, trans, prm, &one);
+        if (r == FFGPU_ENOCONV) err++;
+        else if (r != FFGPU_OK) return r;
+        total_it += one.iterations;
+        acc.elapsed_ms += one.elapsed_ms;
+    }
+    FFGPU_TRY(xd.finish(s));
+    if (stats) {
+        *stats = one;
+        stats->iterations = nrhs == 1 ? one.iterations : total_it;
+        stats->elapsed_ms = acc.elapsed_ms;
+        stats->converged = err == 0;
+    }
+    if (err) {
+        set_error("Krylov solver did not converge for %d of %d right-hand sides", err, nrhs);
+        return FFGPU_ENOCONV;
+    }
+    return FFGPU_OK;
+}
+
+extern "C" {
+
+int ffgpu_solve_cg(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                   const ffgpu_solver_params *prm, ffgpu_solver_stats *stats) {
+    return solve_many(A, b, x, nrhs, trans, prm, stats, cg_one);
+}
+
+int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                      const ffgpu_solver_params *prm, ffgpu_solver_stats *stats) {
+    return solve_many(A, b, x, nrhs, trans, prm, stats, gmres_one);
+}
+
+int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans) {
+    FFGPU_CHECK(A && x && y, FFGPU_EINVAL, "ffgpu_matrix_mult: NULL argument");
+    ffgpu_ctx *ctx = A->ctx;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    DevIn<double> xd(x, A->n, s);
+    DevOut<double> yd(y, A->n, s, false);
+    FFGPU_TRY(xd.err);
+    FFGPU_TRY(yd.err);
+    FFGPU_TRY(spmv(A, xd.d, yd.d, trans, s));
+    FFGPU_TRY(yd.finish(s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    return FFGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,299 @@
+"""Host-side mirror of FreeFEM's interface for the assemble-and-solve path.
+
+The names follow the FreeFEM script being replaced::
+
+    mesh Th = square(256,256);             Th = square(256, 256)
+    fespace Vh(Th,P1);                     Vh = fespace(Th, "P1")
+    varf a(u,v) = int2d(Th)(grad u.grad v) a  = varf_diffusion(f=1.0, on=(1,2,3,4))
+               + int2d(Th)(1*v) + on(1,2,3,4,u=0);
+    matrix A = a(Vh,Vh,solver=CG,eps=1e-10);   A = matrix(a, Vh, solver="CG", eps=1e-10)
+    real[int] b = a(0,Vh);                  b = rhs(a, Vh)
+    u[] = A^-1*b;                           u = A.solve(b)          (A'^-1*b: trans=True)
+
+Arrays are numpy (host) or CUDA torch tensors (device, passed by pointer).  Every call goes
+through the C ABI of libffgpu.so; there is no CPU path.  Errors raise ``FFGPUError`` (FreeFEM
+raises ExecError / ffassert at the same points, e.g. CG non-convergence,
+VirtualSolverCG.hpp:188-189).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import BC, SolverParams, SolverStats, Varf, check, lib
+from .fespace import FESpace
+from .mesh import Mesh
+
+_ctx = {}
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array or a torch tensor (host or CUDA), None for None."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data_as(C.c_void_p)
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def context(device: int = 0):
+    """The library context of a GPU (created on first use)."""
+    if device not in _ctx:
+        h = C.c_void_p()
+        check(lib().ffgpu_ctx_create(device, C.byref(h)))
+        _ctx[device] = h
+    return _ctx[device]
+
+
+def kernel_launches(device: int = 0) -> int:
+    return int(lib().ffgpu_ctx_kernel_launches(context(device)))
+
+
+def stream_handle(device: int = 0) -> int:
+    """The CUDA stream (cudaStream_t as int) all library calls of this context run on."""
+    return int(lib().ffgpu_ctx_stream(context(device)) or 0)
+
+
+def fespace(Th: Mesh, kind: str, dof=None) -> FESpace:
+    return FESpace(Th, kind, dof)
+
+
+class DeviceSpace:
+    """Mesh + FE space resident on the GPU (ffgpu_space_create)."""
+
+    def __init__(self, Vh: FESpace, device: int = 0, coords=None, elems=None, dof=None):
+        self.Vh = Vh
+        Th = Vh.Th
+        self.device = device
+        self._keep = []
+        X = coords if coords is not None else np.ascontiguousarray(Th.coords, np.float64)
+        E = elems if elems is not None else np.ascontiguousarray(Th.elems, np.int32)
+        D = dof if dof is not None else np.ascontiguousarray(Vh.dof, np.int32)
+        self._keep += [X, E, D]
+        h = C.c_void_p()
+        check(lib().ffgpu_space_create(context(device), Th.dim, Th.nv, _ptr(X), Th.nt, _ptr(E),
+                                       Vh.fe, Vh.ndofK, _ptr(D), Vh.ndof, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ffgpu_space_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class VarForm:
+    """A varf of the supported family (P0 coefficients, constant or P0 sources)."""
+
+    form: int = _lib.FORM_DIFFUSION
+    kappa: object = None          # P0 coefficient (nt) or None
+    c_stiff: float = 1.0
+    c_mass: float = 0.0
+    E: float = 1.0
+    nu: float = 0.3
+    f: object = 1.0               # scalar, per-component tuple, or P0 array (nt[, ncomp])
+    on: tuple = ()                # boundary labels of on(..., u=g)
+    g: object = None              # Dirichlet values per DOF (None = 0)
+    components: tuple | None = None
+    tgv: float = 1e30
+    _keep: list = field(default_factory=list)
+
+    def c_varf(self, Vh: FESpace) -> Varf:
+        v = Varf()
+        v.form = self.form
+        v.c_stiff = self.c_stiff
+        v.c_mass = self.c_mass
+        v.E = self.E
+        v.nu = self.nu
+        v.kappa = None
+        if self.kappa is not None:
+            k = self.kappa if hasattr(self.kappa, "data_ptr") else np.ascontiguousarray(self.kappa, np.float64)
+            self._keep.append(k)
+            v.kappa = _ptr(k).value
+        v.f = None
+        if np.isscalar(self.f):
+            v.f_const[0] = float(self.f)
+        elif hasattr(self.f, "data_ptr"):
+            v.f = _ptr(self.f).value
+            self._keep.append(self.f)
+        else:
+            fa = np.asarray(self.f, np.float64)
+            nc = 3 if Vh.kind == "P2vec" else 1
+            if fa.ndim == 1 and fa.size == nc and fa.size != Vh.Th.nt:
+                for c in range(nc):
+                    v.f_const[c] = fa[c]
+            else:
+                fa = np.ascontiguousarray(fa.reshape(Vh.Th.nt, nc))
+                self._keep.append(fa)
+                v.f = _ptr(fa).value
+        return v
+
+    def c_bc(self, Vh: FESpace) -> BC:
+        bc = BC()
+        bc.tgv = self.tgv
+        bc.onbc = None
+        bc.g = None
+        if self.on:
+            m = Vh.on(self.on, self.components)
+            self._keep.append(m)
+            bc.onbc = _ptr(m).value
+            if self.g is not None:
+                g = np.ascontiguousarray(self.g, np.float64)
+                self._keep.append(g)
+                bc.g = _ptr(g).value
+        return bc
+
+
+def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tgv=1e30) -> VarForm:
+    """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v) + on(on, u=g)."""
+    return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
+                   c_stiff=c_stiff, tgv=tgv)
+
+
+def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30) -> VarForm:
+    """varf a([u],[v]) = int(lambda div u div v + 2mu eps(u):eps(v)) + int(f.v) + on(on, u=0)."""
+    return VarForm(form=_lib.FORM_ELASTICITY, E=E, nu=nu, f=f, on=tuple(on), components=components,
+                   tgv=tgv)
+
+
+class Matrix:
+    """``matrix A = a(Vh,Vh, solver=..., eps=..., ...)`` with a device-resident pattern/values."""
+
+    def __init__(self, h, space: DeviceSpace | None, solver="CG", eps=1e-6, itmax=0,
+                 dim_krylov=50, tgv=1e30, device=0):
+        self.h = h
+        self.space = space
+        self.solver = solver
+        self.eps = eps
+        self.itmax = itmax
+        self.dim_krylov = dim_krylov
+        self.tgv = tgv
+        self.device = device
+        self.stats = None
+        n = C.c_int()
+        nnz = C.c_int64()
+        bs = C.c_int()
+        check(lib().ffgpu_matrix_info(h, C.byref(n), C.byref(nnz), C.byref(bs)))
+        self.n, self.nnz, self.block_size = n.value, nnz.value, bs.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ffgpu_matrix_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self, eps=None, itmax=None, unroll=8) -> SolverParams:
+        p = SolverParams()
+        p.eps = self.eps if eps is None else eps
+        p.itmax = self.itmax if itmax is None else itmax
+        p.dim_krylov = self.dim_krylov
+        p.tgv = self.tgv
+        p.verb = 0
+        p.unroll = unroll
+        return p
+
+    def solve(self, b, x0=None, trans=False, solver=None, eps=None, itmax=None, out=None, unroll=8):
+        """u[] = A^-1*b (A'^-1*b when trans).  x0 is the initial guess (FreeFEM: u[] before)."""
+        solver = (solver or self.solver).upper()
+        dev_in = hasattr(b, "data_ptr")
+        if out is None:
+            if dev_in:
+                import torch
+                out = torch.zeros_like(b) if x0 is None else x0.clone()
+            else:
+                out = np.zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
+        elif x0 is not None:
+            out[...] = x0
+        bb = b if dev_in else np.ascontiguousarray(b, np.float64)
+        nrhs = int(np.prod(np.shape(b))) // self.n
+        st = SolverStats()
+        p = self.params(eps, itmax, unroll)
+        fn = lib().ffgpu_solve_cg if solver == "CG" else lib().ffgpu_solve_gmres
+        if solver not in ("CG", "GMRES"):
+            raise ValueError(f"solver {solver!r}: the device path provides CG and GMRES")
+        code = fn(self.h, _ptr(bb), _ptr(out), nrhs, int(trans), C.byref(p), C.byref(st))
+        self.stats = st
+        check(code)
+        return out
+
+    def mult(self, x, trans=False, out=None):
+        if out is None:
+            out = np.empty(self.n) if not hasattr(x, "data_ptr") else x.new_empty(self.n)
+        xx = x if hasattr(x, "data_ptr") else np.ascontiguousarray(x, np.float64)
+        check(lib().ffgpu_matrix_mult(self.h, _ptr(xx), _ptr(out), int(trans)))
+        return out
+
+    def csr(self):
+        """(rowptr, col, val) of the matrix in FreeFEM's sorted (row, column) order."""
+        rp = np.empty(self.n + 1, np.int32)
+        cl = np.empty(self.nnz, np.int32)
+        vl = np.empty(self.nnz, np.float64)
+        check(lib().ffgpu_matrix_csr(self.h, _ptr(rp), _ptr(cl), _ptr(vl)))
+        return rp, cl, vl
+
+    def coo(self):
+        """[I,J,C] = A (row-major sorted COO, as FreeFEM's [I,J,C]=A gives)."""
+        rp, cl, vl = self.csr()
+        return np.repeat(np.arange(self.n, dtype=np.int32), np.diff(rp)), cl, vl
+
+    def reassemble(self, varf: VarForm, rhs_out=None):
+        Vh = self.space.Vh
+        v = varf.c_varf(Vh)
+        bc = varf.c_bc(Vh)
+        check(lib().ffgpu_matrix_reassemble(self.h, C.byref(v), C.byref(bc), _ptr(rhs_out)))
+        return rhs_out
+
+
+def matrix(varf: VarForm, Vh, solver="CG", eps=1e-6, itmax=0, dim_krylov=50, rhs_out=None,
+           device=0) -> Matrix:
+    """matrix A = a(Vh,Vh, solver=..., eps=...).  Vh: FESpace or DeviceSpace.  If rhs_out is
+    given the linear form a(0,Vh) is assembled into it in the same device pass."""
+    space = Vh if isinstance(Vh, DeviceSpace) else DeviceSpace(Vh, device)
+    V = space.Vh
+    v = varf.c_varf(V)
+    bc = varf.c_bc(V)
+    h = C.c_void_p()
+    check(lib().ffgpu_matrix_assemble(space.h, C.byref(v), C.byref(bc), _ptr(rhs_out), C.byref(h)))
+    return Matrix(h, space, solver=solver, eps=eps, itmax=itmax, dim_krylov=dim_krylov,
+                  tgv=varf.tgv, device=device)
+
+
+def rhs(varf: VarForm, Vh, out=None, device=0):
+    """real[int] b = a(0,Vh)."""
+    space = Vh if isinstance(Vh, DeviceSpace) else DeviceSpace(Vh, device)
+    V = space.Vh
+    if out is None:
+        out = np.empty(V.ndof)
+    v = varf.c_varf(V)
+    bc = varf.c_bc(V)
+    check(lib().ffgpu_rhs_assemble(space.h, C.byref(v), C.byref(bc), _ptr(out)))
+    return out
+
+
+def matrix_from_csr(rowptr, col, val, solver="CG", eps=1e-6, tgv=1e30, device=0) -> Matrix:
+    """A FreeFEM-assembled matrix handed to the device solver (the addsolver path)."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    cl = np.ascontiguousarray(col, np.int32)
+    vl = np.ascontiguousarray(val, np.float64)
+    h = C.c_void_p()
+    check(lib().ffgpu_matrix_from_csr(context(device), rp.size - 1, cl.size, _ptr(rp), _ptr(cl),
+                                      _ptr(vl), C.byref(h)))
+    return Matrix(h, None, solver=solver, eps=eps, tgv=tgv, device=device)

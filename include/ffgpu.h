@@ -1,0 +1,153 @@
+/*
+ * ffgpu.h -- C ABI of the GB300-native FreeFEM assemble-and-solve library (libffgpu.so).
+ *
+ * Plain C types only: pointers, sizes and POD structs.  Every array argument may live in
+ * host memory or in device memory of the context's GPU; host arrays are copied in (and
+ * results copied out) inside the call, which is synchronous on return.  Every function
+ * returns FFGPU_OK (0) or a negative FFGPU_E* code; ffgpu_last_error() gives the message.
+ *
+ * Each entry point names the FreeFEM interface it replaces (file:line in FreeFEM-sources).
+ */
+#ifndef FFGPU_H
+#define FFGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define FFGPU_OK 0
+#define FFGPU_EINVAL (-1)    /* bad argument (sizes, layout, unsupported form)       */
+#define FFGPU_ECUDA (-2)     /* CUDA runtime error                                   */
+#define FFGPU_ENOCONV (-3)   /* Krylov solver hit its iteration cap (FreeFEM: ffassert) */
+#define FFGPU_EMESH (-4)     /* mesh/space inconsistency found on the device          */
+#define FFGPU_ENOMEM (-5)    /* device allocation failed                              */
+
+/* finite elements: FreeFEM's P1, P2 and the vector space [P2,P2,P2] on tetrahedra */
+#define FFGPU_FE_P1 1
+#define FFGPU_FE_P2 2
+#define FFGPU_FE_P2VEC3 3
+
+/* bilinear forms (grad/div operators with P0 coefficients) */
+#define FFGPU_FORM_DIFFUSION 0  /* int(c_stiff*kappa*grad(u).grad(v) + c_mass*u*v)      */
+#define FFGPU_FORM_ELASTICITY 1 /* int(lambda*div(u)div(v) + 2mu*eps(u):eps(v)), [P2]^3 */
+
+typedef struct ffgpu_ctx ffgpu_ctx;
+typedef struct ffgpu_space ffgpu_space;
+typedef struct ffgpu_matrix ffgpu_matrix;
+
+/* varf description.  kappa: P0 coefficient per element (length nt) or NULL (= 1);
+ * the stiffness term is c_stiff*kappa_e, the mass term c_mass (0 = none).
+ * Elasticity uses E and nu (mu = E/(2(1+nu)), lambda = E nu/((1+nu)(1-2nu))).
+ * f: P0 source per element and component (nt*ncomp) or NULL, then f_const[c] applies. */
+typedef struct {
+    int form;
+    const double *kappa;
+    double c_stiff, c_mass;
+    double E, nu;
+    const double *f;
+    double f_const[3];
+} ffgpu_varf;
+
+/* Dirichlet data of `on(labels, u=g)`: onbc[dof] != 0 marks a DOF, g[dof] its value
+ * (NULL = 0).  tgv > 0 follows HashMatrix::SetBC: A_ii := tgv, b_i := tgv*g_i. */
+typedef struct {
+    const uint8_t *onbc;
+    const double *g;
+    double tgv;
+} ffgpu_bc;
+
+/* Krylov parameters, named as in FreeFEM's Data_Sparse_Solver (VirtualSolver.hpp:30-96).
+ * eps > 0 relative, eps < 0 absolute (CG.cpp:226); itmax <= 0 means n (VirtualSolverCG.hpp:135);
+ * dim_krylov is GMRES's restart (NbSpace).  unroll: CG iterations per CUDA-graph body (>=1). */
+typedef struct {
+    double eps;
+    int itmax;
+    int dim_krylov;
+    double tgv;
+    int verb;
+    int unroll;
+} ffgpu_solver_params;
+
+/* Solver report: iterations (FreeFEM's nbitermax / getnbiteration), final C-norm^2 of the
+ * preconditioned residual and its threshold eps2, converged flag. */
+typedef struct {
+    int iterations;
+    int converged;
+    double gcg, eps2;
+    double residual;        /* GMRES: relative residual; IR: final outer ratio */
+    int outer_iterations;   /* IR only */
+    double elapsed_ms;      /* device time of the solve */
+} ffgpu_solver_stats;
+
+/* ------------------------------------------------------------------ context */
+/* One context per GPU and host thread; owns a CUDA stream and reduction scratch. */
+int ffgpu_ctx_create(int device, ffgpu_ctx **out);
+int ffgpu_ctx_destroy(ffgpu_ctx *ctx);
+/* thread-local message of the last failing call */
+const char *ffgpu_last_error(void);
+/* number of kernel executions this library issued on the context since creation; kernels
+ * run inside a CUDA graph count once per execution of their graph node */
+int64_t ffgpu_ctx_kernel_launches(const ffgpu_ctx *ctx);
+/* the cudaStream_t (as void*) every call of this context runs on, for timing with events;
+ * library bookkeeping with no FreeFEM counterpart */
+void *ffgpu_ctx_stream(const ffgpu_ctx *ctx);
+
+/* ------------------------------------------------------------------ mesh + FE space
+ * Replaces reading Mesh/Mesh3 and the FESpace numbering FreeFEM hands to the assembly loop
+ * (src/fflib/problem.cpp:803-1111 / 1117-1411 read Th[k] and Vh(k,i)).
+ * coords: nv*dim doubles; elems: nt*(dim+1) vertex indices (mesh order);
+ * dof: nt*ndofK global DOF numbers, FreeFEM's Vh(k,i) (FESpacen.hpp:651-662), where for
+ * FFGPU_FE_P2VEC3 local DOF c*10+i is component c of scalar node i (dof = 3*node + c).
+ * Builds the node->element incidence on the device. */
+int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, int nt,
+                       const int32_t *elems, int fe, int ndofK, const int32_t *dof, int ndof,
+                       ffgpu_space **out);
+int ffgpu_space_destroy(ffgpu_space *space);
+
+/* ------------------------------------------------------------------ assembly
+ * matrix A = a(Vh,Vh, ...): replaces OpMatrixtoBilinearForm::Op::operator() /
+ * AssembleBilinearForm / HashMatrix::operator+= / AssembleBC+SetBC
+ * (src/fflib/problem.hpp:1611-1660, src/fflib/problem.cpp:803,1117,9881-10034,
+ *  src/femlib/HashMatrix.cpp:1195-1238,1295-1332).
+ * Pattern = every (i,j) two DOFs of one element couple, zeros kept, in FreeFEM's
+ * row-then-column order; values summed in element order.  If rhs != NULL the linear form
+ * of the same varf (a(0,Vh), problem.hpp:1351-1388) is assembled into it in the same pass. */
+int ffgpu_matrix_assemble(ffgpu_space *space, const ffgpu_varf *varf, const ffgpu_bc *bc,
+                          double *rhs, ffgpu_matrix **out);
+/* re-run the numeric phase on an existing pattern (new coefficients, same mesh/space) */
+int ffgpu_matrix_reassemble(ffgpu_matrix *A, const ffgpu_varf *varf, const ffgpu_bc *bc,
+                            double *rhs);
+/* real[int] b = a(0,Vh): replaces OpArraytoLinearForm / AssembleLinearForm / Element_rhs
+ * (src/fflib/problem.hpp:1351-1388, src/fflib/problem.cpp:7839-7911,10555). */
+int ffgpu_rhs_assemble(ffgpu_space *space, const ffgpu_varf *varf, const ffgpu_bc *bc,
+                       double *rhs);
+/* matrix from a sorted CSR (the addsolver path: HashMatrix::CSR, HashMatrix.cpp:859-867) */
+int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *rowptr,
+                          const int32_t *col, const double *val, ffgpu_matrix **out);
+int ffgpu_matrix_destroy(ffgpu_matrix *A);
+int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_size);
+/* [I,J,C] = A in sorted CSR form (HashMatrix::CSR / Sortij, HashMatrix.cpp:671-682,870-876) */
+int ffgpu_matrix_csr(const ffgpu_matrix *A, int32_t *rowptr, int32_t *col, double *val);
+
+/* y = A x (trans = 0) or A' x (trans = 1): HashMatrix::addMatMul (HashMatrix.cpp:1087-1154) */
+int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans);
+
+/* ------------------------------------------------------------------ solvers
+ * u[] = A^-1*b / A'^-1*b with solver=CG: replaces SolverCG::dosolver + HMatVirtPrecon +
+ * ConjugueGradient (src/femlib/VirtualSolverCG.hpp:14-192, src/femlib/CG.cpp:196-265).
+ * x holds the initial guess (RNM.hpp:568-571) and receives the solution; nrhs contiguous
+ * right-hand sides of length n.  Returns FFGPU_ENOCONV if any RHS did not converge. */
+int ffgpu_solve_cg(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                   const ffgpu_solver_params *prm, ffgpu_solver_stats *stats);
+/* solver=GMRES: replaces SolverGMRES::dosolver + fgmres (VirtualSolverCG.hpp:195-257,
+ * CG.cpp:348-517): right Jacobi preconditioning, modified Gram-Schmidt, Givens rotations. */
+int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                      const ffgpu_solver_params *prm, ffgpu_solver_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFGPU_H */

@@ -1,0 +1,362 @@
+"""Generate the golden fixtures of the assemble-and-solve path by running FreeFEM itself.
+
+The fixtures under ``tests/golden/*.npz`` are outputs of the FreeFEM 4.15 interpreter
+(``FreeFem++-nw``, built from the FreeFEM sources) on small seeded inputs.  Each case
+writes an ``.edp`` script, runs it, and parses tagged lines from its stdout:
+
+  V  vertex coordinates (and vertex label)      -> ``coords``, ``vlabel``
+  T  element vertex indices (mesh order)        -> ``elems``
+  B  boundary elements and their labels         -> ``belems``, ``blabel``
+  D  element -> global DOF table  (``Vh(k,i)``)  -> ``dof``
+  A  sorted COO of the matrix (``[I,J,C]=A``)   -> ``I``, ``J``, ``C``
+  b  right-hand side and solution               -> ``b``, ``u``
+  S  scalars (iteration counts, norms)           -> ``scalars`` (name -> value)
+  G  extra per-element / per-DOF vectors          -> by name
+
+The inputs that are random (P0 coefficients, observation noise, mesh jitter) are drawn
+here with numpy ``PCG64`` seeds and written to text files the script reads, so the
+fixture holds the exact inputs too.
+
+Run (in a container where FreeFEM is available)::
+
+    FREEFEM_BIN=/path/to/FreeFem++-nw FF_LOADPATH=/path/to/plugin/seq \
+        python tests/golden/make_golden.py
+
+The test suite only reads the ``.npz`` files; it never runs FreeFEM.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FF_BIN = os.environ.get("FREEFEM_BIN", "/tmp/ffbuild/src/nw/FreeFem++-nw")
+FF_LOADPATH = os.environ.get("FF_LOADPATH", "/tmp/ffbuild/plugin/seq")
+
+# ---------------------------------------------------------------- edp fragments
+DUMP_MESH2 = r"""
+for (int i=0;i<Th.nv;i++) cout << "V " << Th(i).x << " " << Th(i).y << " " << Th(i).label << endl;
+for (int k=0;k<Th.nt;k++) cout << "T " << Th[k][0] << " " << Th[k][1] << " " << Th[k][2] << endl;
+for (int k=0;k<Th.nbe;k++) cout << "B " << Th.be(k)[0] << " " << Th.be(k)[1] << " " << Th.be(k).label << endl;
+"""
+DUMP_MESH3 = r"""
+for (int i=0;i<Th.nv;i++) cout << "V " << Th(i).x << " " << Th(i).y << " " << Th(i).z << " " << Th(i).label << endl;
+for (int k=0;k<Th.nt;k++) cout << "T " << Th[k][0] << " " << Th[k][1] << " " << Th[k][2] << " " << Th[k][3] << endl;
+for (int k=0;k<Th.nbe;k++) cout << "B " << Th.be(k)[0] << " " << Th.be(k)[1] << " " << Th.be(k)[2] << " " << Th.be(k).label << endl;
+"""
+DUMP_DOF = r"""
+for (int k=0;k<Th.nt;k++){ cout << "D"; for(int i=0;i<Vh.ndofK;i++) cout << " " << Vh(k,i); cout << endl;}
+"""
+DUMP_A = r"""
+{ int[int] I(1),J(1); real[int] C(1); [I,J,C]=A;
+  for (int k=0;k<I.n;k++) cout << "A " << I[k] << " " << J[k] << " " << C[k] << endl; }
+"""
+HEAD = "cout.precision(17);\n"
+
+
+def read_vec_edp(name: str, fname: str, n: str) -> str:
+    return (f"real[int] {name}({n}); {{ ifstream ff(\"{fname}\"); "
+            f"for (int k=0;k<{n};k++) ff >> {name}[k]; }}\n")
+
+
+# ---------------------------------------------------------------- cases
+def case_p1_square(n, m=None, qft="qft=qf2pT", solver="CG"):
+    m = n if m is None else m
+    body = HEAD + f"""
+mesh Th=square({n},{m});
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th,{qft})(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th,{qft})(1.*v) + on(1,2,3,4,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver={solver},eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+cout << "S umax " << u[].max << endl;
+cout << "S l2 " << sqrt(u[]'*u[]) << endl;
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
+def case_p1_square_kappa(n, seed, jitter=0.0):
+    """2D P1 diffusion with a P0 lognormal coefficient, default quadrature, optional jitter."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nt = 2 * n * n
+    nv = (n + 1) * (n + 1)
+    kap = np.exp(rng.standard_normal(nt))
+    jit = rng.uniform(-jitter / n, jitter / n, size=(nv, 2))
+    ij = np.array([(i, j) for j in range(n + 1) for i in range(n + 1)])
+    border = (ij[:, 0] == 0) | (ij[:, 0] == n) | (ij[:, 1] == 0) | (ij[:, 1] == n)
+    jit[border] = 0.0
+    files = {"kappa.txt": kap, "jx.txt": jit[:, 0], "jy.txt": jit[:, 1]}
+    body = HEAD + f"""
+mesh Th0=square({n},{n});
+fespace Vh0(Th0,P1);
+""" + read_vec_edp("jxa", "jx.txt", "Th0.nv") + read_vec_edp("jya", "jy.txt", "Th0.nv") + """
+Vh0 jx, jy; jx[]=jxa; jy[]=jya;
+mesh Th=movemesh(Th0,[x+jx,y+jy]);
+fespace Vh(Th,P1); fespace Ph(Th,P0);
+""" + read_vec_edp("kapa", "kappa.txt", "Th.nt") + """
+Ph kappa; kappa[]=kapa;
+Vh u,v;
+varf a(u,v)=int2d(Th)(kappa*(dx(u)*dx(v)+dy(u)*dy(v))) + int2d(Th)(1.*v) + on(1,2,3,4,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+for (int k=0;k<Th.nt;k++) cout << "G p0dof " << Ph(k,0) << endl;
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, files
+
+
+def case_p1_cube_kappa(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nt = 6 * n ** 3
+    kap = np.exp(rng.standard_normal(nt))
+    body = HEAD + f"""
+load "msh3"
+mesh3 Th=cube({n},{n},{n});
+fespace Vh(Th,P1); fespace Ph(Th,P0);
+""" + read_vec_edp("kapa", "kappa.txt", "Th.nt") + """
+Ph kappa; kappa[]=kapa;
+Vh u,v;
+varf a(u,v)=int3d(Th)(kappa*(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v))) + int3d(Th)(1.*v) + on(1,2,3,4,5,6,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+for (int k=0;k<Th.nt;k++) cout << "G p0dof " << Ph(k,0) << endl;
+""" + DUMP_MESH3 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {"kappa.txt": kap}
+
+
+def case_p2_cube_scalar(n):
+    body = HEAD + f"""
+load "msh3"
+mesh3 Th=cube({n},{n},{n});
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)=int3d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v)) + int3d(Th)(1.*v) + on(1,2,3,4,5,6,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + DUMP_MESH3 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
+def case_p2_elasticity(nx, ny, nz):
+    body = HEAD + f"""
+load "msh3"
+mesh3 Th=cube({nx},{ny},{nz});
+fespace Vh(Th,[P2,P2,P2]);
+Vh [u1,u2,u3],[v1,v2,v3];
+real E=1, nu=0.3; real mu=E/(2*(1+nu)); real lambda=E*nu/((1+nu)*(1-2*nu));
+real s2=sqrt(2.);
+macro epsilon(u1,u2,u3) [dx(u1),dy(u2),dz(u3),(dz(u2)+dy(u3))/s2,(dz(u1)+dx(u3))/s2,(dy(u1)+dx(u2))/s2] // EOM
+macro div(u1,u2,u3) (dx(u1)+dy(u2)+dz(u3)) // EOM
+varf a([u1,u2,u3],[v1,v2,v3])=int3d(Th)(lambda*div(u1,u2,u3)*div(v1,v2,v3)+2.*mu*(epsilon(u1,u2,u3)'*epsilon(v1,v2,v3))) + int3d(Th)(-1.*v3) + on(4,u1=0,u2=0,u3=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u1[]=0; u1[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + DUMP_MESH3 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u1[][k] << endl;\n"
+    return body, {}
+
+
+def case_p2_square_scalar(n):
+    """2D P2: FreeFEM renumbers the P2 nodes (Gibbs); the fixture carries its DOF table."""
+    body = HEAD + f"""
+mesh Th=square({n},{n});
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(1.*v) + on(1,2,3,4,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
+def case_adjoint_p1(n, seed):
+    """FP64 adjoint of L = 1/2 (u-uobs)' M (u-uobs) for -div(kappa grad u) = f, written as
+    a FreeFEM script: forward CG solve, transpose solve A'^-1, P0 sensitivities by a varf."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nt = 2 * n * n
+    nv = (n + 1) * (n + 1)
+    kap = np.exp(0.3 * rng.standard_normal(nt))
+    fsrc = 1.0 + 0.5 * rng.standard_normal(nt)
+    uobs = 0.05 * rng.standard_normal(nv)
+    files = {"kappa.txt": kap, "f.txt": fsrc, "uobs.txt": uobs}
+    body = HEAD + f"""
+mesh Th=square({n},{n});
+fespace Vh(Th,P1); fespace Ph(Th,P0);
+""" + read_vec_edp("kapa", "kappa.txt", "Th.nt") + read_vec_edp("fa", "f.txt", "Th.nt") + \
+        read_vec_edp("uoa", "uobs.txt", "Th.nv") + """
+Ph kappa, fs; kappa[]=kapa; fs[]=fa;
+Vh uobs; uobs[]=uoa;
+Vh u,v;
+varf a(u,v)=int2d(Th)(kappa*(dx(u)*dx(v)+dy(u)*dy(v))) + int2d(Th)(fs*v) + on(1,2,3,4,u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-14,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+varf m(u,v)=int2d(Th)(u*v);
+matrix M=m(Vh,Vh);
+real[int] r=u[]; r-=uobs[];
+real[int] Mr=M*r;
+real L=0.5*(r'*Mr);
+cout << "S loss " << L << endl;
+Vh lam; lam[]=0; lam[]=A'^-1*Mr;
+varf gk(unused,w)=int2d(Th)(-(dx(lam)*dx(u)+dy(lam)*dy(u))*w);
+varf gf(unused,w)=int2d(Th)(lam*w);
+Ph gkap, gfs; gkap[]=gk(0,Ph); gfs[]=gf(0,Ph);
+for (int k=0;k<Th.nt;k++) cout << "G gkappa " << gkap[][k] << endl;
+for (int k=0;k<Th.nt;k++) cout << "G gf " << gfs[][k] << endl;
+for (int k=0;k<Th.nv;k++) cout << "G lam " << lam[][k] << endl;
+{ int[int] I(1),J(1); real[int] C(1); [I,J,C]=M;
+  for (int k=0;k<I.n;k++) cout << "G MI " << I[k] << endl;
+  for (int k=0;k<I.n;k++) cout << "G MJ " << J[k] << endl;
+  for (int k=0;k<I.n;k++) cout << "G MC " << C[k] << endl; }
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, files
+
+
+def case_heat_p1(n, nsteps, dt, seed):
+    """Implicit Euler for u_t - div(kappa grad u) = 1, u(0)=0, u=0 on the boundary."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nt = 2 * n * n
+    kap = np.exp(0.3 * rng.standard_normal(nt))
+    body = HEAD + f"""
+mesh Th=square({n},{n});
+fespace Vh(Th,P1); fespace Ph(Th,P0);
+""" + read_vec_edp("kapa", "kappa.txt", "Th.nt") + f"""
+Ph kappa; kappa[]=kapa;
+real dt={dt!r};
+Vh u,v,uold;
+varf a(u,v)=int2d(Th)(u*v/dt + kappa*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,2,3,4,u=0);
+varf m(u,v)=int2d(Th)(u*v/dt);
+varf f(u,v)=int2d(Th)(1.*v) + on(1,2,3,4,u=0);
+matrix A=a(Vh,Vh,solver=CG,eps=1e-14);
+matrix M=m(Vh,Vh);
+real[int] F=f(0,Vh);
+u[]=0;
+for (int s=0;s<{nsteps};s++) {{
+  uold[]=u[];
+  real[int] rhs=M*uold[]; rhs+=F;
+  u[]=A^-1*rhs;
+}}
+for (int k=0;k<Th.nv;k++) cout << "G uT " << u[][k] << endl;
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A
+    return body, {"kappa.txt": kap}
+
+
+CASES = {
+    "p1sq_n2": lambda: case_p1_square(2),
+    "p1sq_n5": lambda: case_p1_square(5),
+    "p1sq_n16": lambda: case_p1_square(16),
+    "p1sq_7x3": lambda: case_p1_square(7, 3),
+    "p1sq_n8_T5": lambda: case_p1_square(8, qft="qft=qf5pT"),
+    "p1sq_n12_gmres": lambda: case_p1_square(12, solver="GMRES"),
+    "p1sqk_n8_jit": lambda: case_p1_square_kappa(8, seed=11, jitter=0.2),
+    "p1sqk_n6": lambda: case_p1_square_kappa(6, seed=12, jitter=0.0),
+    "p1cubek_n2": lambda: case_p1_cube_kappa(2, seed=21),
+    "p1cubek_n4": lambda: case_p1_cube_kappa(4, seed=22),
+    "p2cube_n2": lambda: case_p2_cube_scalar(2),
+    "p2el_n1": lambda: case_p2_elasticity(1, 1, 1),
+    "p2el_n2": lambda: case_p2_elasticity(2, 2, 2),
+    "p2el_3x2x1": lambda: case_p2_elasticity(3, 2, 1),
+    "p2sq_n4": lambda: case_p2_square_scalar(4),
+    "adj_p1_n8": lambda: case_adjoint_p1(8, seed=31),
+    "heat_p1_n6": lambda: case_heat_p1(6, 10, 1e-2, seed=41),
+}
+
+
+def parse(out: str) -> dict:
+    rows: dict[str, list] = {}
+    scal: dict[str, float] = {}
+    extra: dict[str, list] = {}
+    for line in out.splitlines():
+        t = line.split()
+        if not t:
+            continue
+        tag = t[0]
+        if tag == "S":
+            scal[t[1]] = float(t[2])
+        elif tag == "G":
+            extra.setdefault(t[1], []).append(float(t[2]))
+        elif tag in ("V", "T", "B", "D", "A", "b"):
+            rows.setdefault(tag, []).append(t[1:])
+    res = {}
+    if "V" in rows:
+        v = np.array(rows["V"], dtype=np.float64)
+        res["coords"] = v[:, :-1]
+        res["vlabel"] = v[:, -1].astype(np.int64)
+    if "T" in rows:
+        res["elems"] = np.array(rows["T"], dtype=np.int64).astype(np.int32)
+    if "B" in rows:
+        bb = np.array(rows["B"], dtype=np.int64)
+        res["belems"] = bb[:, :-1].astype(np.int32)
+        res["blabel"] = bb[:, -1].astype(np.int32)
+    if "D" in rows:
+        res["dof"] = np.array(rows["D"], dtype=np.int64).astype(np.int32)
+    if "A" in rows:
+        a = rows["A"]
+        res["I"] = np.array([r[0] for r in a], dtype=np.int32)
+        res["J"] = np.array([r[1] for r in a], dtype=np.int32)
+        res["C"] = np.array([r[2] for r in a], dtype=np.float64)
+    if "b" in rows:
+        bu = np.array(rows["b"], dtype=np.float64)
+        res["b"] = bu[:, 0]
+        res["u"] = bu[:, 1]
+    for k, vals in extra.items():
+        res["g_" + k] = np.array(vals, dtype=np.float64)
+    res["scalar_names"] = np.array(sorted(scal), dtype="U32")
+    res["scalar_values"] = np.array([scal[k] for k in sorted(scal)], dtype=np.float64)
+    return res
+
+
+def run_case(name: str) -> None:
+    body, files = CASES[name]()
+    with tempfile.TemporaryDirectory() as td:
+        for fn, arr in files.items():
+            np.savetxt(os.path.join(td, fn), np.asarray(arr), fmt="%.17g")
+        script = os.path.join(td, name + ".edp")
+        with open(script, "w") as f:
+            f.write(body)
+        env = dict(os.environ, FF_LOADPATH=FF_LOADPATH)
+        p = subprocess.run([FF_BIN, "-nw", script, "-v", "0"], cwd=td, env=env,
+                           capture_output=True, text=True, timeout=600)
+        if p.returncode != 0:
+            raise RuntimeError(f"{name}: FreeFEM failed\n{p.stdout[-2000:]}\n{p.stderr[-2000:]}")
+        res = parse(p.stdout)
+        for fn, arr in files.items():
+            res["in_" + fn.split(".")[0]] = np.asarray(arr, dtype=np.float64)
+        res["edp"] = np.array(body)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print(f"{name}: " + ", ".join(f"{k}{tuple(np.shape(v))}" for k, v in res.items()
+                                  if k != "edp"))
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    for nm in names:
+        run_case(nm)

@@ -1,0 +1,220 @@
+"""CUDA path vs the oracle and FreeFEM's golden outputs, through the C ABI.
+
+Bars (the benchmark spec): pattern and DOF numbering bit-exact; matrix values within 1e-12 relative
+per entry (floor 1e-3 x the row's largest non-tgv entry, see golden_cases.value_errors);
+solution within 1e-9 relative in the L2 norm; CG/GMRES iteration counts equal to FreeFEM's
+within 2 (device reductions sum in a different order than the reference's serial loops).
+"""
+import numpy as np
+import pytest
+
+import ffgpu
+import ffo
+from ffgpu import mesh
+from ffgpu.fespace import FESpace
+from golden_cases import MATRIX_CASES, case, load, value_errors
+
+pytestmark = pytest.mark.gpu
+
+VAL_TOL = 1e-12
+SOL_TOL = 1e-9
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_built():
+    from ffgpu.build import build
+    build()
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    ffgpu.context(0)
+    yield
+
+
+def gpu_varf(c):
+    if c["form"] == "elasticity":
+        return ffgpu.varf_elasticity(E=1.0, nu=0.3, f=c["f"], on=c["labels"])
+    return ffgpu.varf_diffusion(kappa=c["kappa"], f=c["f"], on=c["labels"])
+
+
+@pytest.mark.parametrize("name", MATRIX_CASES)
+def test_assembly_and_solve_against_freefem(name):
+    c = case(name)
+    d, sc = c["d"], c["sc"]
+    Vh = FESpace(c["Th"], c["kind"], c.get("dof"))
+    a = gpu_varf(c)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver=c["solver"], eps=c["eps"], rhs_out=b)
+    rp, cl, v = A.csr()
+    I = np.repeat(np.arange(Vh.ndof), np.diff(rp))
+    assert A.nnz == d["J"].size
+    assert np.array_equal(I, d["I"]) and np.array_equal(cl, d["J"]), "pattern differs"
+    assert value_errors(v, d["C"], rp).max() <= VAL_TOL
+    assert np.abs(b - d["b"]).max() <= VAL_TOL * np.abs(d["b"]).max()
+    u = A.solve(b)
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    assert abs(A.stats.iterations - int(sc["nit"])) <= 2
+    # linear form alone (a(0,Vh)) equals the one assembled with the matrix
+    b2 = ffgpu.rhs(a, A.space)
+    assert np.array_equal(b, b2)
+
+
+@pytest.mark.parametrize("name", ["p1sq_n16", "p1cubek_n4", "p2el_n2", "p2cube_n2"])
+def test_transpose_mult_and_solve_against_oracle(name):
+    c = case(name)
+    Th = c["Th"]
+    Vh = FESpace(Th, c["kind"], c.get("dof"))
+    Ao = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"])
+    bo = ffo.rhs(Th, Vh, f=c["f"], quad=c["quad"])
+    ffo.setbc(Ao, bo, Vh.on(c["labels"]))
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(Vh.ndof)
+    for trans in (False, True):
+        y = A.mult(x, trans=trans)
+        yo = Ao.matmul(x, trans=trans)
+        assert np.abs(y - yo).max() <= 1e-12 * np.abs(yo).max()
+    ut = A.solve(bo, trans=True)
+    uo, it, r, _ = ffo.cg(Ao, bo, eps=1e-10, trans=True)
+    assert np.linalg.norm(ut - uo) <= SOL_TOL * np.linalg.norm(uo)
+    assert abs(A.stats.iterations - it) <= 2
+
+
+def test_multiple_rhs():
+    c = case("p1sq_n16")
+    Vh = FESpace(c["Th"], "P1")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10, rhs_out=b)
+    u = A.solve(b)
+    B = np.stack([b, 2 * b, -b]).ravel()
+    U = A.solve(B)
+    U = U.reshape(3, -1)
+    for k, s in enumerate([1, 2, -1]):
+        assert np.linalg.norm(U[k] - s * u) <= 1e-9 * np.linalg.norm(u)
+
+
+def test_addsolver_path_matrix_from_csr():
+    """A FreeFEM-assembled matrix (sorted CSR) solved on the device, as `set(A,solver=GPUCG)`."""
+    c = case("p1sqk_n8_jit")
+    d, sc = c["d"], c["sc"]
+    rp = np.zeros(d["b"].size + 1, np.int32)
+    np.add.at(rp, d["I"] + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    A = ffgpu.matrix_from_csr(rp, d["J"], d["C"], eps=1e-10)
+    u = A.solve(d["b"])
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    assert abs(A.stats.iterations - int(sc["nit"])) <= 2
+    ug = A.solve(d["b"], solver="GMRES")
+    assert np.linalg.norm(ug - d["u"]) <= 1e-8 * np.linalg.norm(d["u"])
+
+
+def test_reassemble_matches_fresh_assembly():
+    c = case("p1cubek_n4")
+    Vh = FESpace(c["Th"], "P1")
+    a1 = gpu_varf(c)
+    A = ffgpu.matrix(a1, Vh)
+    kap2 = np.asarray(c["kappa"]) * 2.5 + 0.1
+    a2 = ffgpu.varf_diffusion(kappa=kap2, f=1.0, on=c["labels"])
+    b = np.empty(Vh.ndof)
+    A.reassemble(a2, rhs_out=b)
+    B = ffgpu.matrix(a2, A.space)
+    assert np.array_equal(A.csr()[2], B.csr()[2])
+    assert np.array_equal(b, ffgpu.rhs(a2, A.space))
+
+
+def test_device_resident_inputs_torch():
+    """Mesh, DOF table and vectors already in HBM (torch CUDA tensors) through the same ABI."""
+    import torch
+    c = case("p2el_n2")
+    d = c["d"]
+    Th = c["Th"]
+    Vh = FESpace(Th, "P2vec")
+    X = torch.from_numpy(Th.coords).cuda()
+    E = torch.from_numpy(Th.elems).cuda()
+    D = torch.from_numpy(Vh.dof).cuda()
+    S = ffgpu.DeviceSpace(Vh, coords=X, elems=E, dof=D)
+    b = torch.empty(Vh.ndof, dtype=torch.float64, device="cuda")
+    A = ffgpu.matrix(gpu_varf(c), S, eps=1e-10, rhs_out=b)
+    u = A.solve(b)
+    torch.cuda.synchronize()
+    uh = u.cpu().numpy()
+    assert np.linalg.norm(uh - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+
+
+def test_full_size_2d_poisson_known_answers():
+    """square(256,256) P1 Poisson, qf2pT (the CPU-runnable headline case): nnz formula
+    7 nv - 8 n - 6 = 460289, FreeFEM's recorded umax 0.0736705 and ||u|| 10.5628 (532 CG
+    iterations), and the oracle's solution at 1e-9."""
+    Th = mesh.square(256)
+    Vh = FESpace(Th, "P1")
+    a = ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, eps=1e-10, rhs_out=b)
+    assert A.nnz == 7 * Th.nv - 8 * 256 - 6 == 460289
+    u = A.solve(b)
+    assert abs(u.max() - 0.0736705) < 5e-7
+    assert abs(np.linalg.norm(u) - 10.5628) < 5e-4
+    assert abs(A.stats.iterations - 532) <= 2
+    Ao = ffo.assemble(Th, Vh, quad="qf2pT")
+    bo = ffo.rhs(Th, Vh, f=1.0, quad="qf2pT")
+    ffo.setbc(Ao, bo, Vh.on((1, 2, 3, 4)))
+    rp, cl, v = A.csr()
+    rpo, clo, vo = Ao.csr()
+    assert np.array_equal(rp, rpo) and np.array_equal(cl, clo)
+    assert value_errors(v, vo, rpo).max() <= VAL_TOL
+    uo, it, r, _ = ffo.cg(Ao, bo, eps=1e-10)
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+
+
+@pytest.mark.parametrize("n", [6, 10])
+def test_elasticity_medium_against_oracle(n):
+    Th = mesh.cube(n)
+    Vh = FESpace(Th, "P2vec")
+    a = ffgpu.varf_elasticity(f=(0, 0, -1.0), on=(4,))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, eps=1e-10, rhs_out=b)
+    Ao = ffo.assemble(Th, Vh, form="elasticity")
+    bo = ffo.rhs(Th, Vh, f=(0, 0, -1.0))
+    ffo.setbc(Ao, bo, Vh.on((4,)))
+    rp, cl, v = A.csr()
+    rpo, clo, vo = Ao.csr()
+    assert np.array_equal(rp, rpo) and np.array_equal(cl, clo)
+    assert value_errors(v, vo, rpo).max() <= VAL_TOL
+    assert np.abs(b - bo).max() <= VAL_TOL * np.abs(bo).max()
+    u = A.solve(b)
+    uo, it, r, _ = ffo.cg(Ao, bo, eps=1e-10)
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    assert abs(A.stats.iterations - it) <= max(2, it // 100)
+
+
+def test_gmres_against_freefem():
+    c = case("p1sq_n12_gmres")
+    d, sc = c["d"], c["sc"]
+    Vh = FESpace(c["Th"], "P1")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, solver="GMRES", eps=1e-10, rhs_out=b)
+    u = A.solve(b)
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    assert abs(A.stats.iterations - int(sc["nit"])) <= 2
+
+
+def test_nonconvergence_is_an_error():
+    """FreeFEM aborts (ffassert) when CG exhausts itmax; the device path returns ENOCONV."""
+    c = case("p1sq_n16")
+    Vh = FESpace(c["Th"], "P1")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10, itmax=3, rhs_out=b)
+    with pytest.raises(ffgpu.FFGPUError) as ei:
+        A.solve(b)
+    assert ei.value.code == -3
+    assert A.stats.iterations == 3
+
+
+def test_bad_inputs_rejected_on_host_or_device():
+    Th = mesh.square(4)
+    Vh = FESpace(Th, "P1")
+    bad = Vh.dof.copy()
+    bad[3, 1] = Vh.ndof + 7          # DOF out of range: found by the device check, no fault
+    with pytest.raises(ffgpu.FFGPUError):
+        ffgpu.DeviceSpace(Vh, dof=bad)
+    with pytest.raises(ffgpu.FFGPUError):
+        ffgpu.matrix(ffgpu.varf_elasticity(on=(1,)), Vh)   # elasticity on a scalar space
