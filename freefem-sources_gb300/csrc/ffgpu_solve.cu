@@ -129,7 +129,11 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_kernel(SpmvArgs A, const
         } else {
             double v[3];
             bsr3_row<T>(A.rp, A.col, A.val, x, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
-            if (a < A.nb && sub < 3) y[3 * (int64_t)a + sub] = sub == 0 ? v[0] : (sub == 1 ? v[1] : v[2]);
+            if (a < A.nb && sub == 0) {
+                y[3 * (int64_t)a] = v[0];
+                y[3 * (int64_t)a + 1] = v[1];
+                y[3 * (int64_t)a + 2] = v[2];
+            }
         }
     }
 }
@@ -154,11 +158,12 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
         } else {
             double v[3];
             bsr3_row<T>(A.rp, A.col, A.val, h, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
-            if (a < A.nb && sub < 3) {
-                int64_t i = 3 * (int64_t)a + sub;
-                double vs = sub == 0 ? v[0] : (sub == 1 ? v[1] : v[2]);
-                q[i] = vs;
-                hq = fma(h[i], vs, hq);
+            if (a < A.nb && sub == 0) {
+                int64_t i = 3 * (int64_t)a;
+                q[i] = v[0]; q[i + 1] = v[1]; q[i + 2] = v[2];
+                hq = fma(h[i], v[0], hq);
+                hq = fma(h[i + 1], v[1], hq);
+                hq = fma(h[i + 2], v[2], hq);
             }
         }
     }
@@ -495,11 +500,16 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
     int n = A->n;
+    // the cached graph only ever touches matrix-owned buffers: the caller's x is staged in
+    // slot 4 of the work vectors and copied back after the solve
     double *g = A->vec, *h = A->vec + n, *q = A->vec + 2 * (int64_t)n;
+    double *xu = x;
+    x = A->vec + 4 * (int64_t)n;
     double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
     int itmax = prm->itmax > 0 ? prm->itmax : n;
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
     FFGPU_TRY(cg_graph(A, trans, unroll, x, g, h, q));
+    FFGPU_CUDA(cudaMemcpyAsync(x, xu, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -512,6 +522,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     cg_init<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, b, h, A->diag_inv, A->ks, prm->eps, itmax, ctx->d_part);
     FFGPU_TRY(launch_check(ctx, "cg_init"));
     FFGPU_CUDA(cudaGraphLaunch(A->cg_exec, s));
+    FFGPU_CUDA(cudaMemcpyAsync(xu, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEventRecord(e1, s);
     KrylovScalars hk;
     FFGPU_CUDA(cudaMemcpyAsync(&hk, A->ks, sizeof(hk), cudaMemcpyDeviceToHost, s));

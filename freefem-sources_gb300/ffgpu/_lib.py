@@ -23,6 +23,7 @@ EXPORTS = [
     "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
+    "ffgpu_matrix_to_f32", "ffgpu_solve_ir",
 ]
 
 
@@ -45,6 +46,11 @@ class SolverStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("gcg", C.c_double),
                 ("eps2", C.c_double), ("residual", C.c_double), ("outer_iterations", C.c_int),
                 ("elapsed_ms", C.c_double)]
+
+
+class IRParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("eps_inner", C.c_double), ("itmax_inner", C.c_int),
+                ("max_outer", C.c_int), ("tgv", C.c_double), ("unroll", C.c_int)]
 
 
 class FFGPUError(RuntimeError):
@@ -83,6 +89,8 @@ def lib():
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),
         "ffgpu_solve_gmres": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),
+        "ffgpu_matrix_to_f32": (i32, [vp]),
+        "ffgpu_solve_ir": (i32, [vp, vp, vp, P(IRParams), P(SolverStats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -234,6 +234,31 @@ class Matrix:
         check(code)
         return out
 
+    def solve_mixed(self, b, x0=None, eps=None, eps_inner=1e-5, itmax_inner=0, max_outer=30,
+                    out=None, unroll=8):
+        """u[] = A^-1*b by FP32 inner PCG + FP64 iterative refinement, same stopping rule
+        as the FP64 CG on the true residual."""
+        dev_in = hasattr(b, "data_ptr")
+        if out is None:
+            if dev_in:
+                import torch
+                out = torch.zeros_like(b) if x0 is None else x0.clone()
+            else:
+                out = np.zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
+        bb = b if dev_in else np.ascontiguousarray(b, np.float64)
+        p = _lib.IRParams()
+        p.eps = self.eps if eps is None else eps
+        p.eps_inner = eps_inner
+        p.itmax_inner = itmax_inner
+        p.max_outer = max_outer
+        p.tgv = self.tgv
+        p.unroll = unroll
+        st = SolverStats()
+        code = lib().ffgpu_solve_ir(self.h, _ptr(bb), _ptr(out), C.byref(p), C.byref(st))
+        self.stats = st
+        check(code)
+        return out
+
     def mult(self, x, trans=False, out=None):
         if out is None:
             out = np.empty(self.n) if not hasattr(x, "data_ptr") else x.new_empty(self.n)

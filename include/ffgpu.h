@@ -147,6 +147,26 @@ int ffgpu_solve_cg(ffgpu_matrix *A, const double *b, double *x, int nrhs, int tr
 int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
                       const ffgpu_solver_params *prm, ffgpu_solver_stats *stats);
 
+/* ------------------------------------------------------------------ mixed precision
+ * FP32 inner Jacobi-PCG (FP32 values, vectors, SpMV and dot products) inside an FP64
+ * iterative-refinement loop (outer residual b - A x in FP64 on the FP64 matrix, FP64 update).
+ * Stops on FreeFEM's CG criterion applied to the true residual, (r, C r) < eps^2 (r0, C r0)
+ * (CG.cpp:226,247), so it answers the same u[] = A^-1*b as ffgpu_solve_cg; no FreeFEM
+ * counterpart of its own (FreeFEM's solvers are FP64). */
+typedef struct {
+    double eps;         /* outer tolerance, as ffgpu_solver_params.eps            */
+    double eps_inner;   /* relative tolerance of each FP32 inner solve (<=0: 1e-5) */
+    int itmax_inner;    /* inner iteration cap (<=0: n)                            */
+    int max_outer;      /* refinement steps cap (<=0: 30)                          */
+    double tgv;
+    int unroll;
+} ffgpu_ir_params;
+
+/* FP32 copy of the values used by the inner solves (built on first use, freed on reassembly) */
+int ffgpu_matrix_to_f32(ffgpu_matrix *A);
+int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_params *prm,
+                   ffgpu_solver_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,20 @@ def test_multiple_rhs():
         assert np.linalg.norm(U[k] - s * u) <= 1e-9 * np.linalg.norm(u)
 
 
+def test_repeated_solves_reuse_graph_safely():
+    """The CUDA graph of the CG loop is cached per matrix; every solve must use its own x/b."""
+    c = case("p1sqk_n8_jit")
+    d = c["d"]
+    Vh = FESpace(c["Th"], "P1")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10, rhs_out=b)
+    ref = A.solve(b)
+    for s in (2.0, -0.5, 3.0):
+        u = A.solve(s * b)
+        assert np.linalg.norm(u - s * ref) <= 1e-9 * np.linalg.norm(s * ref)
+    assert np.linalg.norm(ref - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+
+
 def test_addsolver_path_matrix_from_csr():
     """A FreeFEM-assembled matrix (sorted CSR) solved on the device, as `set(A,solver=GPUCG)`."""
     c = case("p1sqk_n8_jit")
@@ -217,4 +231,4 @@ def test_bad_inputs_rejected_on_host_or_device():
     with pytest.raises(ffgpu.FFGPUError):
         ffgpu.DeviceSpace(Vh, dof=bad)
     with pytest.raises(ffgpu.FFGPUError):
-        ffgpu.matrix(ffgpu.varf_elasticity(on=(1,)), Vh)   # elasticity on a scalar space
+        ffgpu.matrix(ffgpu.varf_elasticity(f=1.0, on=(1,)), Vh)   # elasticity on a scalar space
