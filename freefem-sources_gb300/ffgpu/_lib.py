@@ -23,7 +23,7 @@ EXPORTS = [
     "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
-    "ffgpu_matrix_to_f32", "ffgpu_solve_ir",
+    "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
 ]
 
 
@@ -91,6 +91,7 @@ def lib():
         "ffgpu_solve_gmres": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),
         "ffgpu_matrix_to_f32": (i32, [vp]),
         "ffgpu_solve_ir": (i32, [vp, vp, vp, P(IRParams), P(SolverStats)]),
+        "ffgpu_diffusion_sensitivity": (i32, [vp, vp, vp, dbl, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -1,0 +1,233 @@
+"""Adjoint gradients for -div(kappa grad u) = f (P1, P0 kappa and f) and its implicit-Euler
+heat variant, on the device path.
+
+Loss: L = 1/2 (u - u_obs)' M (u - u_obs), M the P1 mass matrix (varf int(u*v)).
+Adjoint: A' lambda = M (u - u_obs) by the transpose CG (FreeFEM's A'^-1, lgmat.cpp:3219), then
+dL/dkappa_e and dL/df_e from the per-element sensitivity kernel (ffgpu_diffusion_sensitivity).
+
+Heat: (M/dt + K(kappa)) u^n = (M/dt) u^{n-1} + F, u^0 = 0, loss on u^N.  The backward pass
+recomputes the states from checkpoints kept every `checkpoint` steps, so memory holds
+N/checkpoint + checkpoint vectors instead of N.
+
+``DiffusionLoss`` wraps the adjoint in a torch.autograd.Function for gradient checks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import api
+from ._lib import check, lib
+from .fespace import FESpace
+
+
+def _np(a):
+    if hasattr(a, "detach"):
+        return a.detach().cpu().numpy().astype(np.float64)
+    return np.asarray(a, np.float64)
+
+
+def sensitivity(A: api.Matrix, u, lam, c_stiff=1.0):
+    """(dL/dkappa_e, dL/df_e) of every element, given the state u and the adjoint lambda."""
+    nt = A.space.Vh.Th.nt
+    gk = np.empty(nt)
+    gf = np.empty(nt)
+    uu = np.ascontiguousarray(u, np.float64)
+    ll = np.ascontiguousarray(lam, np.float64)
+    check(lib().ffgpu_diffusion_sensitivity(A.h, api._ptr(uu), api._ptr(ll), float(c_stiff),
+                                            api._ptr(gk), api._ptr(gf)))
+    return gk, gf
+
+
+class DiffusionProblem:
+    """P1 diffusion with Dirichlet data on `on` labels; kappa and f are P0 arrays."""
+
+    def __init__(self, Vh: FESpace, on=(1, 2, 3, 4), eps=1e-14, tgv=1e30, device=0):
+        self.Vh = Vh
+        self.on = tuple(on)
+        self.eps = eps
+        self.tgv = tgv
+        self.space = api.DeviceSpace(Vh, device)
+        self.mass = api.matrix(api.varf_diffusion(c_stiff=0.0, c_mass=1.0), self.space)
+        self.A = None
+
+    def assemble(self, kappa, f):
+        a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), on=self.on, tgv=self.tgv)
+        b = np.empty(self.Vh.ndof)
+        if self.A is None:
+            self.A = api.matrix(a, self.space, eps=self.eps, rhs_out=b)
+        else:
+            self.A.reassemble(a, rhs_out=b)
+        return b
+
+    def solve(self, kappa, f):
+        b = self.assemble(kappa, f)
+        return self.A.solve(b)
+
+    def loss(self, u, u_obs):
+        r = u - u_obs
+        return 0.5 * float(r @ self.mass.mult(r))
+
+    def value_and_grad(self, kappa, f, u_obs):
+        u = self.solve(kappa, f)
+        r = u - u_obs
+        Mr = self.mass.mult(r)
+        L = 0.5 * float(r @ Mr)
+        lam = self.A.solve(Mr, trans=True)
+        gk, gf = sensitivity(self.A, u, lam)
+        return L, gk, gf, u, lam
+
+    def element_operator(self, e, u):
+        """(dA/dkappa_e) u restricted to element e: (local DOFs, values), tgv diagonal dropped."""
+        Th = self.Vh.Th
+        v = Th.elems[e].astype(np.int64)
+        X = Th.coords[v]
+        if Th.dim == 2:
+            area = 0.5 * ((X[1, 0] - X[0, 0]) * (X[2, 1] - X[0, 1]) - (X[1, 1] - X[0, 1]) * (X[2, 0] - X[0, 0]))
+            G = np.empty((3, 2))
+            for i in range(3):
+                p1, p2 = X[(i + 1) % 3], X[(i + 2) % 3]
+                G[i] = [-(p2[1] - p1[1]) / (2 * area), (p2[0] - p1[0]) / (2 * area)]
+            meas = area
+        else:
+            V = X[1:] - X[0]
+            meas = np.linalg.det(V) / 6.0
+            Gi = np.linalg.inv(V).T
+            G = np.vstack([-Gi.sum(axis=0), Gi])
+        K = meas * (G @ G.T)
+        on = self.A_wcl() if hasattr(self, "_wcl") else None
+        Ku = K @ u[v]
+        if on is not None:
+            for i in range(len(v)):
+                if on[v[i]]:
+                    Ku[i] -= K[i, i] * u[v[i]]
+        return v, Ku
+
+    def A_wcl(self):
+        return self._wcl
+
+    def fd_gradient(self, kappa, f, u_obs, elements, step=1e-6):
+        """Central finite differences (L(kappa + h e_k) - L(kappa - h e_k)) / 2h, h = step*kappa_k.
+
+        The difference of the two losses is formed without cancellation: with A+- = A(kappa +- h e_k),
+        u- = A-^-1 b and du = u+ - u- solving A+ du = -(A+ - A-) u- = -2h (dA/dkappa_k) u- (exact:
+        A is affine in kappa_k), L+ - L- = du' M r- + 1/2 du' M du with r- = u- - u_obs."""
+        kappa = _np(kappa).copy()
+        self._wcl = self.Vh.on(self.on).astype(bool)
+        out = np.empty(len(elements))
+        for t, e in enumerate(elements):
+            h = step * kappa[e]
+            km = kappa.copy(); km[e] -= h
+            kp = kappa.copy(); kp[e] += h
+            um = self.solve(km, f)
+            rm = um - u_obs
+            v, Ku = self.element_operator(e, um)
+            rhs = np.zeros(self.Vh.ndof)
+            rhs[v] = -2.0 * h * Ku
+            bp = self.assemble(kp, f)
+            del bp
+            du = self.A.solve(rhs)
+            Mdu = self.mass.mult(du)
+            dL = float(du @ self.mass.mult(rm)) + 0.5 * float(du @ Mdu)
+            out[t] = dL / (2.0 * h)
+        return out
+
+
+class HeatProblem:
+    """Implicit Euler for u_t - div(kappa grad u) = f, u(0) = 0, Dirichlet on `on`, loss on u^N."""
+
+    def __init__(self, Vh: FESpace, dt, nsteps, on=(1, 2, 3, 4), checkpoint=20, eps=1e-14,
+                 tgv=1e30, device=0):
+        self.Vh = Vh
+        self.dt = dt
+        self.nsteps = nsteps
+        self.on = tuple(on)
+        self.checkpoint = checkpoint
+        self.eps = eps
+        self.tgv = tgv
+        self.space = api.DeviceSpace(Vh, device)
+        self.mass = api.matrix(api.varf_diffusion(c_stiff=0.0, c_mass=1.0), self.space)
+        self.mdt = api.matrix(api.varf_diffusion(c_stiff=0.0, c_mass=1.0 / dt), self.space)
+        self.A = None
+        self.solves = 0
+
+    def assemble(self, kappa, f):
+        a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), c_mass=1.0 / self.dt, on=self.on, tgv=self.tgv)
+        F = np.empty(self.Vh.ndof)
+        if self.A is None:
+            self.A = api.matrix(a, self.space, eps=self.eps, rhs_out=F)
+        else:
+            self.A.reassemble(a, rhs_out=F)
+        self.F = F
+        return F
+
+    def step(self, u_prev):
+        self.solves += 1
+        return self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev)
+
+    def forward(self, kappa, f, keep_checkpoints=True):
+        self.assemble(kappa, f)
+        u = np.zeros(self.Vh.ndof)
+        ck = {0: u.copy()}
+        for n in range(1, self.nsteps + 1):
+            u = self.step(u)
+            if keep_checkpoints and n % self.checkpoint == 0:
+                ck[n] = u.copy()
+        return u, ck
+
+    def loss(self, uN, u_obs):
+        r = uN - u_obs
+        return 0.5 * float(r @ self.mass.mult(r))
+
+    def value_and_grad(self, kappa, f, u_obs):
+        """Forward with checkpoints, backward with recomputation of each segment."""
+        self.solves = 0
+        uN, ck = self.forward(kappa, f)
+        forward_solves = self.solves
+        r = uN - u_obs
+        L = 0.5 * float(r @ self.mass.mult(r))
+        nt = self.Vh.Th.nt
+        gk = np.zeros(nt)
+        gf = np.zeros(nt)
+        rhs_adj = self.mass.mult(r)          # dL/du^N
+        lam_next = None
+        N, c = self.nsteps, self.checkpoint
+        seg_starts = sorted(k for k in ck if k < N)
+        for s0 in reversed(seg_starts):
+            s1 = min(s0 + c, N)
+            # recompute u^{s0+1..s1} from the checkpoint u^{s0}
+            states = {s0: ck[s0]}
+            u = ck[s0]
+            for n in range(s0 + 1, s1 + 1):
+                u = states[n] = self.step(u) if n not in ck or n == s0 else ck[n]
+            for n in range(s1, s0, -1):
+                rhs = rhs_adj if n == N else self.mdt.mult(lam_next, trans=True)
+                lam = self.A.solve(rhs, trans=True)
+                self.solves += 1
+                g1, g2 = sensitivity(self.A, states[n], lam)
+                gk += g1
+                gf += g2
+                lam_next = lam
+        self.forward_solves = forward_solves
+        return L, gk, gf
+
+
+try:
+    import torch
+
+    class DiffusionLoss(torch.autograd.Function):
+        """L(kappa, f) with the adjoint gradient, for gradient-check harnesses only."""
+
+        @staticmethod
+        def forward(ctx, kappa, f, problem, u_obs):
+            L, gk, gf, u, lam = problem.value_and_grad(kappa, f, _np(u_obs))
+            ctx.save_for_backward(torch.from_numpy(gk), torch.from_numpy(gf))
+            return torch.tensor(L, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, gout):
+            gk, gf = ctx.saved_tensors
+            return gout * gk, gout * gf, None, None
+except ImportError:  # pragma: no cover
+    DiffusionLoss = None

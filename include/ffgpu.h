@@ -167,6 +167,17 @@ int ffgpu_matrix_to_f32(ffgpu_matrix *A);
 int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_params *prm,
                    ffgpu_solver_stats *stats);
 
+/* ------------------------------------------------------------------ adjoint
+ * Per-element sensitivities of A(kappa) u = b(f) for the P1 diffusion varf assembled by
+ * ffgpu_matrix_assemble, given the state u and the adjoint lambda (A' lambda = dL/du, from
+ * ffgpu_solve_cg with trans = 1, FreeFEM's A'^-1 path lgmat.cpp:3219 / HashMatrix.cpp:1094):
+ *   grad_kappa[e] = -c_stiff |K| sum_ij lambda_i (grad phi_i . grad phi_j) u_j  (tgv diagonals excluded)
+ *   grad_f[e]     =  sum_{i not tgv} lambda_i int_K phi_i
+ * FreeFEM has no adjoint of its own; its scripts form the same gradient with a P0 test-function
+ * varf int(-(grad lambda . grad u) w).  Either output may be NULL. */
+int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *lambda, double c_stiff,
+                                double *grad_kappa, double *grad_f);
+
 #ifdef __cplusplus
 }
 #endif
