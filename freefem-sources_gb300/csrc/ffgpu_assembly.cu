@@ -175,41 +175,83 @@ __global__ void geometry_kernel(const double *X, const int32_t *elems, int nt, i
 // so int_K d_alpha(phi_i) d_beta(phi_j) = m (sum_a C_i[a].al C_j[a].be + S_i.al S_j.be),
 // m = |K|/((d+1)(d+2)), S_i = sum_a C_i[a].  This integrates the degree-2 integrand
 // exactly, as FreeFEM's default rules (T_5, Tet_5) do.
-__constant__ int c_tet_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
-__constant__ int c_tri_edge[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+struct V3 {
+    double x, y, z;
+};
+__device__ __forceinline__ V3 v3(const double *p) { return V3{__ldg(p), __ldg(p + 1), __ldg(p + 2)}; }
+__device__ __forceinline__ V3 operator*(double a, V3 v) { return V3{a * v.x, a * v.y, a * v.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ double comp(V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
 
+// local edge e -> vertices (p,q): tets {01,02,03,12,13,23}, triangles edge i opposite vertex i
 template <int DIM>
-struct P2Grad {
-    double C[DIM + 1][3];
-    double S[3];
-    __device__ void make(const double *G /* [4][3] */, int i) {
-        constexpr int nvk = DIM + 1;
-        for (int a = 0; a < nvk; ++a)
-            for (int d = 0; d < 3; ++d) C[a][d] = 0.0;
-        if (i < nvk) {
-            for (int a = 0; a < nvk; ++a)
-                for (int d = 0; d < 3; ++d) C[a][d] = (a == i ? 3.0 : -1.0) * G[3 * i + d];
-        } else {
-            int e = i - nvk;
-            int p = DIM == 3 ? c_tet_edge[e][0] : c_tri_edge[e][0];
-            int q = DIM == 3 ? c_tet_edge[e][1] : c_tri_edge[e][1];
-            for (int d = 0; d < 3; ++d) { C[p][d] = 4.0 * G[3 * q + d]; C[q][d] = 4.0 * G[3 * p + d]; }
-        }
-        for (int d = 0; d < 3; ++d) {
-            double s = 0;
-            for (int a = 0; a < nvk; ++a) s += C[a][d];
-            S[d] = s;
-        }
+__device__ __forceinline__ void edge_vertices(int e, int &p, int &q) {
+    if (DIM == 3) {
+        p = e < 3 ? 0 : (e < 5 ? 1 : 2);
+        q = e < 3 ? e + 1 : (e == 3 ? 2 : 3);
+    } else {
+        p = (e + 1) % 3;
+        q = (e + 2) % 3;
+    }
+}
+
+// One P2 basis function J: C_J[a] is a multiple of one gradient,
+//   vertex j:   C_J[a] = (a == j ? 3 : -1) g_j,        S_J = (3 - d) g_j
+//   edge (r,s): C_J[r] = 4 g_s, C_J[s] = 4 g_r, else 0, S_J = 4 (g_r + g_s)
+template <int DIM>
+struct P2Basis {
+    int J, r, s;
+    __device__ __forceinline__ explicit P2Basis(int JJ) : J(JJ), r(0), s(0) {
+        if (J > DIM) edge_vertices<DIM>(J - DIM - 1, r, s);
+    }
+    __device__ __forceinline__ V3 C(const double *G, int a) const {
+        if (J <= DIM) return (a == J ? 3.0 : -1.0) * v3(G + 3 * J);
+        if (a == r) return 4.0 * v3(G + 3 * s);
+        if (a == s) return 4.0 * v3(G + 3 * r);
+        return V3{0.0, 0.0, 0.0};
+    }
+    __device__ __forceinline__ V3 S(const double *G) const {
+        if (J <= DIM) return (3.0 - DIM) * v3(G + 3 * J);
+        return 4.0 * (v3(G + 3 * r) + v3(G + 3 * s));
     }
 };
 
+// The 3x3 matrix (1/m) int_K d_a(phi_I) d_b(phi_J) = sum_c C_I[c]_a C_J[c]_b + S_I,a S_J,b as a sum
+// of at most three outer products u_k (x) w_k:
+//   I vertex i:  u = g_i, w = 4 C_J[i] - (d-2) S_J                              (rank 1)
+//   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J             (rank 3)
 template <int DIM>
-__device__ __forceinline__ double p2_gab(const P2Grad<DIM> &I, const P2Grad<DIM> &J, int al, int be) {
-    double s = I.S[al] * J.S[be];
-#pragma unroll
-    for (int a = 0; a < DIM + 1; ++a) s += I.C[a][al] * J.C[a][be];
-    return s;
-}
+struct P2Pair {
+    V3 u0, w0, u1, w1, u2, w2;
+    bool vertex;
+    __device__ __forceinline__ P2Pair(const double *G, int I, int Jidx) {
+        P2Basis<DIM> J(Jidx);
+        vertex = I <= DIM;
+        if (vertex) {
+            u0 = v3(G + 3 * I);
+            w0 = 4.0 * J.C(G, I) - (double)(DIM - 2) * J.S(G);
+            u1 = w1 = u2 = w2 = V3{0.0, 0.0, 0.0};
+        } else {
+            int p, q;
+            edge_vertices<DIM>(I - DIM - 1, p, q);
+            V3 gp = v3(G + 3 * p), gq = v3(G + 3 * q);
+            u0 = 4.0 * gq; w0 = J.C(G, p);
+            u1 = 4.0 * gp; w1 = J.C(G, q);
+            u2 = 4.0 * (gp + gq); w2 = J.S(G);
+        }
+    }
+    __device__ __forceinline__ double g(int a, int b) const {
+        double t = comp(u0, a) * comp(w0, b);
+        if (!vertex) t += comp(u1, a) * comp(w1, b) + comp(u2, a) * comp(w2, b);
+        return t;
+    }
+    __device__ __forceinline__ double trace() const {
+        double t = u0.x * w0.x + u0.y * w0.y + u0.z * w0.z;
+        if (!vertex) t += u1.x * w1.x + u1.y * w1.y + u1.z * w1.z + u2.x * w2.x + u2.y * w2.y + u2.z * w2.z;
+        return t;
+    }
+};
 
 // int_K phi_i for the linear form with a constant source on the element
 template <int DIM, int ORDER>
@@ -275,6 +317,7 @@ struct FillArgs {
     const double *geo;
     const int32_t *browptr;
     int32_t *bcol;            // NULL: numeric only (pattern already built)
+    int32_t *diagpos;         // block index of the diagonal block, written with the pattern
     double *val;              // NULL: no matrix (linear form only)
     double *rhs;              // NULL: no linear form
     const double *fP0;        // nt*bs or NULL
@@ -295,8 +338,8 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
     constexpr int NN = FE == 1 ? nvk : (DIM == 3 ? 10 : 6);
     constexpr int BS = FE == 3 ? 3 : 1;
     constexpr int BS2 = BS * BS;
-    // lanes: FE 1/2 -> slot*NN + lb (several elements per step); FE 3 -> lb*3 + c
-    constexpr int SLOTS = FE == 3 ? 1 : 32 / NN;
+    // lanes = slot * NN + lb: SLOTS incident elements per step, each lane one block (la, lb)
+    constexpr int SLOTS = 32 / NN;
     extern __shared__ __align__(16) unsigned char sh_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
@@ -317,66 +360,55 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
         const int ib = A.inc_ptr[a], ie = A.inc_ptr[a + 1];
         for (int t0 = ib; t0 < ie; t0 += SLOTS) {
             // ---- element contributions of this step
-            int slot = FE == 3 ? 0 : lane / NN;
-            int lb = FE == 3 ? lane / 3 : lane - slot * NN;
-            int t = t0 + slot;
-            bool act = (FE == 3 ? lane < 30 : slot < SLOTS) && t < ie;
+            const int slot = lane / NN;
+            const int lb = lane - slot * NN;
+            const int t = t0 + slot;
+            const bool act = slot < SLOTS && t < ie;
             int rank = -1;
-            double v[BS];
+            double v[BS2];
 #pragma unroll
-            for (int c = 0; c < BS; ++c) v[c] = 0.0;
-            int e = 0, la = 0;
+            for (int q = 0; q < BS2; ++q) v[q] = 0.0;
             if (act) {
-                e = A.inc_elem[t];
-                la = A.inc_loc[t];
+                const int e = A.inc_elem[t];
+                const int la = A.inc_loc[t];
                 const double *ge = A.geo + (int64_t)e * kGeoStride;
-                const double meas = ge[0], kap = ge[1];
+                const double meas = __ldg(ge), kap = __ldg(ge + 1);
                 const double *G = ge + 4;
-                int nb = A.nodes[(int64_t)e * NN + lb];
+                const int nb = A.nodes[(int64_t)e * NN + lb];
                 rank = find_sorted(cols, deg, nb);
                 if (FE == 1) {
                     double s = 0;
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) s += G[3 * la + d] * G[3 * lb + d];
+                    for (int d = 0; d < DIM; ++d) s += __ldg(G + 3 * la + d) * __ldg(G + 3 * lb + d);
                     double val = kap * meas * s;
                     if (A.c_mass != 0.0) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
                     v[0] = val;
                 } else {
-                    P2Grad<DIM> I, J;
-                    I.make(G, la);
-                    J.make(G, lb);
-                    double m = meas * mfac;
+                    const P2Pair<DIM> P(G, la, lb);
+                    const double m = meas * mfac;
                     if (FE == 2) {
-                        double s = 0;
-#pragma unroll
-                        for (int d = 0; d < DIM; ++d) s += p2_gab<DIM>(I, J, d, d);
-                        v[0] = kap * m * s;
+                        v[0] = kap * m * P.trace();
                     } else {
-                        int c = lane - 3 * lb;
-                        double tr = p2_gab<DIM>(I, J, 0, 0) + p2_gab<DIM>(I, J, 1, 1) + p2_gab<DIM>(I, J, 2, 2);
+                        const double tr = P.trace();
 #pragma unroll
-                        for (int cp = 0; cp < 3; ++cp) {
-                            double x = A.lam * p2_gab<DIM>(I, J, c, cp) + A.mu * p2_gab<DIM>(I, J, cp, c);
-                            if (cp == c) x += A.mu * tr;
-                            v[cp] = m * x;
-                        }
+                        for (int c = 0; c < 3; ++c)
+#pragma unroll
+                            for (int cp = 0; cp < 3; ++cp) {
+                                double x = A.lam * P.g(c, cp) + A.mu * P.g(cp, c);
+                                if (cp == c) x += A.mu * tr;
+                                v[3 * c + cp] = m * x;
+                            }
                     }
                 }
                 if (rank < 0) dev_fail(A.status, kDevNotFound);
             }
-            // ---- accumulate in element order
-            if (FE == 3) {
-                if (act && rank >= 0) {
-                    int c = lane - 3 * lb;
+            // ---- accumulate slot by slot: element order, no two lanes on one entry at once
+            for (int sl = 0; sl < SLOTS; ++sl) {
+                if (act && slot == sl && rank >= 0) {
 #pragma unroll
-                    for (int cp = 0; cp < 3; ++cp) acc[rank * 9 + 3 * c + cp] += v[cp];
+                    for (int q = 0; q < BS2; ++q) acc[rank * BS2 + q] += v[q];
                 }
                 __syncwarp();
-            } else {
-                for (int sl = 0; sl < SLOTS; ++sl) {
-                    if (act && slot == sl && rank >= 0) acc[rank] += v[0];
-                    __syncwarp();
-                }
             }
             // ---- linear form: lanes < BS accumulate component `lane`, element order
             if (A.rhs) {
@@ -396,6 +428,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
         // ---- Dirichlet rows (tgv > 0): diagonal := tgv, rhs := tgv * g
         int self = find_sorted(cols, deg, a);
         if (self < 0) { if (lane == 0) dev_fail(A.status, kDevNotFound); continue; }
+        if (A.bcol && lane == 0) A.diagpos[a] = (int32_t)(rb + self);
         if (lane < BS) {
             int64_t dof = (int64_t)a * BS + lane;
             bool on = A.onbc && A.onbc[dof];
@@ -449,6 +482,20 @@ __global__ void export_csr_kernel(int nb, int bs, const int32_t *browptr, const 
             }
     }
     if (a == nb - 1) rowptr[(int64_t)nb * bs] = (int32_t)((int64_t)browptr[nb] * bs * bs);
+}
+
+// diagonal block of each row of a sorted CSR (-1 if absent)
+__global__ void diagpos_kernel(int n, const int32_t *rp, const int32_t *col, int32_t *pos) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    int lo = rp[a], hi = rp[a + 1] - 1, p = -1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        int c = col[mid];
+        if (c == a) { p = mid; break; }
+        if (c < a) lo = mid + 1; else hi = mid - 1;
+    }
+    pos[a] = p;
 }
 
 static int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
@@ -517,6 +564,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     fa.inc_ptr = S->inc_ptr; fa.inc_elem = S->inc_elem; fa.inc_loc = S->inc_loc;
     fa.nodes = S->nodes; fa.geo = M->geo; fa.browptr = M->browptr;
     fa.bcol = build_cols ? M->bcol : nullptr;
+    fa.diagpos = M->diagpos;
     fa.val = M->val; fa.rhs = rh.d; fa.fP0 = fP0.d;
     fa.f0 = v->f_const[0]; fa.f1 = v->f_const[1]; fa.f2 = v->f_const[2];
     fa.c_mass = v->form == FFGPU_FORM_DIFFUSION ? v->c_mass : 0.0;
@@ -663,6 +711,7 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     cudaFreeAsync(deg, s);
     deg = nullptr;
     if (cudaMalloc((void **)&M->bcol, sizeof(int32_t) * M->nnzb) ||
+        cudaMalloc((void **)&M->diagpos, sizeof(int32_t) * M->nb) ||
         cudaMalloc((void **)&M->val, sizeof(double) * M->nnz)) {
         set_error("ffgpu_matrix_assemble: allocation of %lld values failed", (long long)M->nnz);
         rc = FFGPU_ENOMEM; goto fail;
@@ -729,6 +778,7 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
     M->ctx = ctx; M->bs = 1; M->nb = n; M->n = n; M->nnzb = nnz; M->nnz = nnz; M->ntgv = -1;
     if (cudaMalloc((void **)&M->browptr, sizeof(int32_t) * (n + 1)) ||
         cudaMalloc((void **)&M->bcol, sizeof(int32_t) * nnz) ||
+        cudaMalloc((void **)&M->diagpos, sizeof(int32_t) * n) ||
         cudaMalloc((void **)&M->val, sizeof(double) * nnz)) {
         set_error("ffgpu_matrix_from_csr: device allocation failed");
         ffgpu_matrix_destroy(M);
@@ -750,6 +800,8 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
         cudaFreeAsync(deg, s);
         FFGPU_CHECK(hp[n] == nnz && hp[0] == 0, FFGPU_EINVAL, "rowptr inconsistent with nnz");
     }
+    diagpos_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, M->bcol, M->diagpos);
+    FFGPU_TRY(launch_check(ctx, "diagpos"));
     FFGPU_CUDA(cudaStreamSynchronize(s));
     *out = M;
     return FFGPU_OK;
@@ -759,7 +811,7 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     if (!M) return FFGPU_OK;
     cudaStreamSynchronize(M->ctx->stream);
     if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
-    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->val); cudaFree(M->geo);
+    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->diagpos); cudaFree(M->val); cudaFree(M->geo);
     cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
     cudaFree(M->val32); cudaFree(M->ks);
     delete M;

@@ -94,6 +94,7 @@ struct ffgpu_matrix {
     int max_deg;
     int32_t *browptr;     // nb+1
     int32_t *bcol;        // nnzb
+    int32_t *diagpos;     // nb: index of the diagonal block of each block row
     double *val;          // nnzb*bs*bs, each block row-major
     double *geo;          // per-element geometry cache (16 doubles per element)
     // solver state (lazily allocated)

@@ -283,26 +283,47 @@ __global__ void __launch_bounds__(kVecThreads) cg_init(int n, double *__restrict
 }
 
 // ------------------------------------------------------------------ Jacobi + gettgv
-__global__ void diag_kernel(int nb, int bs, const int32_t *brp, const int32_t *bcol, const double *val,
-                            double *diag, unsigned long long *maxbits) {
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// diagonal entries through the recorded diagonal block positions; max diagonal for gettgv
+__global__ void diag_kernel(int64_t n, int bs, const int32_t *diagpos, const double *val, double *diag,
+                            unsigned long long *maxbits) {
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)nb * bs) return;
-    int a = (int)(t / bs), c = (int)(t % bs);
-    double d = 0;
-    bool found = false;
-    for (int k = brp[a]; k < brp[a + 1]; ++k)
-        if (bcol[k] == a) { d = val[(int64_t)k * bs * bs + c * bs + c]; found = true; break; }
-    diag[t] = d;
-    if (found && d > 0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(d));
+    unsigned long long m = 0;
+    if (t < n) {
+        int a = (int)(t / bs), c = (int)(t % bs);
+        int p = diagpos[a];
+        double d = p >= 0 ? val[(int64_t)p * bs * bs + c * bs + c] : 0.0;
+        diag[t] = d;
+        if (p >= 0 && d > 0) m = (unsigned long long)__double_as_longlong(d);
+    }
+    m = warp_max_u64(m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(maxbits, m);
 }
 
 __global__ void diag_second_kernel(int64_t n, const double *diag, double top, unsigned long long *max1bits,
                                    int *count) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double d = diag[i];
-    if (d == top) atomicAdd(count, 1);
-    else if (d > 0 && d < top) atomicMax(max1bits, (unsigned long long)__double_as_longlong(d));
+    unsigned long long m = 0;
+    int c = 0;
+    if (i < n) {
+        double d = diag[i];
+        if (d == top) c = 1;
+        else if (d > 0 && d < top) m = (unsigned long long)__double_as_longlong(d);
+    }
+    m = warp_max_u64(m);
+    unsigned bal = __ballot_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0) {
+        if (m) atomicMax(max1bits, m);
+        if (bal) atomicAdd(count, __popc(bal));
+    }
 }
 
 __global__ void jacobi_kernel(int64_t n, double *diag, uint8_t *wcl, double tgve, int ntgv) {
@@ -415,7 +436,7 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
     unsigned long long *bits = (unsigned long long *)ctx->d_iscratch;   // [0] max, [1] max1
     int *cnt = ctx->d_iscratch + 4;
     FFGPU_CUDA(cudaMemsetAsync(ctx->d_iscratch, 0, sizeof(int) * 8, s));
-    diag_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(A->nb, A->bs, A->browptr, A->bcol, A->val, A->diag_inv, bits);
+    diag_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(n, A->bs, A->diagpos, A->val, A->diag_inv, bits);
     FFGPU_TRY(launch_check(ctx, "diag"));
     unsigned long long hb[2] = {0, 0};
     FFGPU_CUDA(cudaMemcpyAsync(hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, s));
