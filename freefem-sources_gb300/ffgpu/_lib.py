@@ -24,6 +24,7 @@ EXPORTS = [
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
+    "ffgpu_solve_cg_csr_noalloc",
 ]
 
 
@@ -92,6 +93,8 @@ def lib():
         "ffgpu_matrix_to_f32": (i32, [vp]),
         "ffgpu_solve_ir": (i32, [vp, vp, vp, P(IRParams), P(SolverStats)]),
         "ffgpu_diffusion_sensitivity": (i32, [vp, vp, vp, dbl, vp, vp]),
+        "ffgpu_solve_cg_csr_noalloc": (i32, [i32, i64, vp, vp, vp, vp, vp, dbl, i32, dbl, vp,
+                                              P(i32), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

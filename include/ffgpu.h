@@ -178,6 +178,22 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
 int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *lambda, double c_stiff,
                                 double *grad_kappa, double *grad_f);
 
+/* ------------------------------------------------------------------ allocation-free CG
+ * Jacobi-PCG on a caller's CSR matrix that allocates no memory: for callers that cannot
+ * allocate device memory while they run (an application that hands the GPU's memory to its
+ * own pool at start-up and calls the solver from its time loop).  No counterpart in FreeFEM;
+ * the algorithm is ffgpu_solve_cg's.  Every array (rowptr, col, val, b, x) must be in device
+ * memory; x holds the initial guess and receives the solution.  n <= 524288: the work vectors
+ * live in a fixed ~17 MB device array that every GPU loading the library keeps until exit.
+ * The first call on a device (made with that device current) looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race, so serialise them.  stream: cudaStream_t as void* (NULL =
+ * default stream).  iterations and gcg_out[2] = {final gCg, eps2} may be NULL.
+ * Returns FFGPU_EINVAL for n above the limit or non-device arrays, FFGPU_ENOCONV at itmax. */
+int ffgpu_solve_cg_csr_noalloc(int n, int64_t nnz, const int32_t *rowptr, const int32_t *col,
+                               const double *val, const double *b, double *x, double eps, int itmax,
+                               double tgv, void *stream, int *iterations, double *gcg_out);
+
 #ifdef __cplusplus
 }
 #endif
