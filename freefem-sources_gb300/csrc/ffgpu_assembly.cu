@@ -484,6 +484,11 @@ __global__ void export_csr_kernel(int nb, int bs, const int32_t *browptr, const 
     if (a == nb - 1) rowptr[(int64_t)nb * bs] = (int32_t)((int64_t)browptr[nb] * bs * bs);
 }
 
+__global__ void row_degree_kernel(int n, const int32_t *rp, int32_t *deg) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < n) deg[a] = rp[a + 1] - rp[a];
+}
+
 // diagonal block of each row of a sorted CSR (-1 if absent)
 __global__ void diagpos_kernel(int n, const int32_t *rp, const int32_t *col, int32_t *pos) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -701,6 +706,12 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     if ((rc = check_device_status(ctx, "pattern"))) goto fail;
     if ((rc = device_max_i32(ctx, deg, M->nb, &M->max_deg))) goto fail;
     if ((rc = device_scan_i32(ctx, deg, M->browptr, M->nb))) goto fail;
+    // SpMV row order: block rows grouped by degree so that the lanes of a warp share trip counts
+    if (cudaMalloc((void **)&M->rowperm, sizeof(int32_t) * M->nb)) {
+        set_error("ffgpu_matrix_assemble: device allocation failed");
+        rc = FFGPU_ENOMEM; goto fail;
+    }
+    if ((rc = device_order_by_key_desc(ctx, deg, M->nb, M->max_deg, M->rowperm))) goto fail;
     {
         int32_t nnzb = 0;
         cudaMemcpyAsync(&nnzb, M->browptr + M->nb, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
@@ -788,17 +799,24 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
     cudaMemcpyAsync(M->bcol, col, sizeof(int32_t) * nnz, cudaMemcpyDefault, s);
     cudaMemcpyAsync(M->val, val, sizeof(double) * nnz, cudaMemcpyDefault, s);
     {
+        int32_t first = -1, last = -1;
+        cudaMemcpyAsync(&first, M->browptr, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&last, M->browptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        FFGPU_CUDA(cudaStreamSynchronize(s));
+        if (first != 0 || last != nnz) {
+            set_error("rowptr inconsistent with nnz");
+            ffgpu_matrix_destroy(M);
+            return FFGPU_EINVAL;
+        }
         int32_t *deg = nullptr;
-        cudaMallocAsync((void **)&deg, sizeof(int32_t) * n, s);
-        // row degrees from the row pointer, for the max-degree bookkeeping
-        std::vector<int32_t> hp(n + 1);
-        cudaMemcpyAsync(hp.data(), M->browptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        int md = 0;
-        for (int i = 0; i < n; ++i) md = max(md, hp[i + 1] - hp[i]);
-        M->max_deg = md;
+        FFGPU_CUDA(cudaMallocAsync((void **)&deg, sizeof(int32_t) * n, s));
+        row_degree_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, deg);
+        int rc = launch_check(ctx, "row_degree");
+        if (!rc) rc = device_max_i32(ctx, deg, n, &M->max_deg);
+        if (!rc && cudaMalloc((void **)&M->rowperm, sizeof(int32_t) * n)) { set_error("allocation failed"); rc = FFGPU_ENOMEM; }
+        if (!rc) rc = device_order_by_key_desc(ctx, deg, n, M->max_deg, M->rowperm);
         cudaFreeAsync(deg, s);
-        FFGPU_CHECK(hp[n] == nnz && hp[0] == 0, FFGPU_EINVAL, "rowptr inconsistent with nnz");
+        if (rc) { ffgpu_matrix_destroy(M); return rc; }
     }
     diagpos_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, M->bcol, M->diagpos);
     FFGPU_TRY(launch_check(ctx, "diagpos"));
@@ -811,7 +829,8 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     if (!M) return FFGPU_OK;
     cudaStreamSynchronize(M->ctx->stream);
     if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
-    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->diagpos); cudaFree(M->val); cudaFree(M->geo);
+    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->diagpos); cudaFree(M->rowperm); cudaFree(M->val);
+    cudaFree(M->geo);
     cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
     cudaFree(M->val32); cudaFree(M->ks);
     delete M;

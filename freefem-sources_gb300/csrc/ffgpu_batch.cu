@@ -1,0 +1,442 @@
+// ffgpu_batch.cu -- many independent small problems solved in one persistent launch.
+//
+// A batch is the disjoint union of nprob meshes: one FE space and one assembly pass give a
+// block-diagonal matrix whose blocks are each problem's own FreeFEM matrix (problem p's DOFs
+// are offset by voff[p]; its pattern and values are those of a lone assembly).  The solve is
+// one persistent kernel: every CTA takes problems from a queue (largest first) and runs the
+// whole mixed-precision solve of a problem -- FP64 outer refinement r = b - A x, FP32 inner
+// Jacobi-PCG on A d = r -- with CTA barriers only (no grid-wide waits).  The launch sequence
+// (FP32 values, Jacobi, queue reset, persistent solve) is captured in a CUDA graph.  The CTA
+// size and lanes per SpMV row are picked by timing the candidates on the batch (autotune).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "ffgpu_internal.cuh"
+
+extern "C" int ffgpu_matrix_to_f32(ffgpu_matrix *A);
+
+namespace ffgpu {
+
+struct BatchArgs {
+    int nprob;
+    const int32_t *order;      // problems sorted by decreasing size
+    const int32_t *voff;       // nprob+1 DOF offsets
+    const int32_t *rp, *col;   // CSR of the union (global column numbers)
+    const double *val;
+    const float *val32;
+    const double *dinv;
+    const float *dinv32;
+    const uint8_t *wcl;
+    const double *b;
+    double *x;
+    float *g, *h, *q, *d;      // FP32 work vectors (union length)
+    double *r;                 // FP64 residual
+    int *queue;
+    int *iters, *outers, *conv;
+    double *resid;
+    double eps, tgv;
+    float eps_in;
+    int itmax_in, max_outer;
+};
+
+template <int NT>
+__device__ __forceinline__ double cta_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (w == 0) {
+        t = lane < NT / 32 ? sh[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+template <int NT>
+__device__ __forceinline__ float cta_sum_f(float v, float *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    float t = 0;
+    if (w == 0) {
+        t = lane < NT / 32 ? sh[lane] : 0.0f;
+        t = warp_sum(t);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+// rows [r0, r1) with T lanes per row: y = A x in FP64
+template <int NT, int T>
+__device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, const double *x, double *y) {
+    const int sub = threadIdx.x % T;
+    for (int base = r0; base < r1; base += NT / T) {
+        int i = base + threadIdx.x / T;
+        int ii = i < r1 ? i : r0;
+        int kb = B.rp[ii], ke = B.rp[ii + 1];
+        double s = 0;
+        for (int k = kb + sub; k < ke; k += T) s = fma(B.val[k], x[B.col[k]], s);
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (i < r1 && sub == 0) y[i] = s;
+    }
+}
+
+template <int NT, int T>
+__device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *x, float *y) {
+    const int sub = threadIdx.x % T;
+    float dot = 0;
+    for (int base = r0; base < r1; base += NT / T) {
+        int i = base + threadIdx.x / T;
+        int ii = i < r1 ? i : r0;
+        int kb = B.rp[ii], ke = B.rp[ii + 1];
+        float s = 0;
+        for (int k = kb + sub; k < ke; k += T) s = fmaf(B.val32[k], x[B.col[k]], s);
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (i < r1 && sub == 0) { y[i] = s; dot = fmaf(x[i], s, dot); }
+    }
+    return dot;
+}
+
+template <int NT, int T>
+__global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
+    __shared__ double sh[33];
+    __shared__ float shf[33];
+    __shared__ int s_p;
+    for (;;) {
+        if (threadIdx.x == 0) s_p = atomicAdd(B.queue, 1);
+        __syncthreads();
+        const int slot = s_p;
+        __syncthreads();
+        if (slot >= B.nprob) return;
+        const int p = B.order[slot];
+        const int r0 = B.voff[p], r1 = B.voff[p + 1];
+        // x0 = b / tgv on tgv rows (SolverCG::dosolver), x = 0 elsewhere
+        for (int i = r0 + threadIdx.x; i < r1; i += NT) B.x[i] = B.wcl[i] ? B.b[i] / B.tgv : 0.0;
+        __syncthreads();
+        double eps2 = 0, gcg = 0, gcg0 = 0;
+        int outer = 0, inner = 0, conv = 0;
+        for (outer = 0; outer <= B.max_outer; ++outer) {
+            cta_spmv64<NT, T>(B, r0, r1, B.x, B.r);
+            __syncthreads();
+            double s64 = 0;
+            float sa = 0, sb = 0;
+            for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+                double ri = B.b[i] - B.r[i];
+                s64 = fma(ri, B.dinv[i] * ri, s64);
+                float gi = -(float)ri, zi = B.dinv32[i] * gi;
+                B.g[i] = gi; B.h[i] = -zi; B.d[i] = 0.0f;
+                sa = fmaf(gi, zi, sa);
+                sb = fmaf(gi, -zi, sb);
+            }
+            gcg = cta_sum<NT>(s64, sh);
+            if (outer == 0) {
+                gcg0 = gcg;
+                eps2 = B.eps > 0 ? B.eps * B.eps * gcg : B.eps * B.eps;
+                if (gcg < 1e-30) { conv = 1; break; }
+            }
+            if (gcg < eps2) { conv = 1; break; }
+            if (outer == B.max_outer) break;
+            float ig = cta_sum_f<NT>(sa, shf);
+            float s_gh = cta_sum_f<NT>(sb, shf);
+            const float ieps2 = B.eps_in * B.eps_in * ig;
+            for (int it = 0; it < B.itmax_in && ig >= 1e-30f && ig >= ieps2; ++it) {
+                float hq = cta_spmv32_dot<NT, T>(B, r0, r1, B.h, B.q);
+                hq = cta_sum_f<NT>(hq, shf);
+                const float rho = -s_gh / hq;
+                float sg = 0;
+                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+                    B.d[i] = fmaf(rho, B.h[i], B.d[i]);
+                    float gi = fmaf(rho, B.q[i], B.g[i]);
+                    B.g[i] = gi;
+                    sg = fmaf(gi, B.dinv32[i] * gi, sg);
+                }
+                float ign = cta_sum_f<NT>(sg, shf);
+                const float gamma = ign / ig;
+                ig = ign;
+                float sgh = 0;
+                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+                    float gi = B.g[i];
+                    float hi = gamma * B.h[i] - B.dinv32[i] * gi;
+                    B.h[i] = hi;
+                    sgh = fmaf(gi, hi, sgh);
+                }
+                s_gh = cta_sum_f<NT>(sgh, shf);
+                ++inner;
+                if (!(ig == ig)) break;
+            }
+            for (int i = r0 + threadIdx.x; i < r1; i += NT) B.x[i] += (double)B.d[i];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            B.iters[p] = inner;
+            B.outers[p] = outer;
+            B.conv[p] = conv;
+            B.resid[p] = gcg0 > 0 ? sqrt(gcg / gcg0) : 0.0;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void f32_copy_kernel(int64_t n, const double *a, float *b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+__global__ void reset_queue_kernel(int *q) { *q = 0; }
+
+typedef void (*BatchKernel)(BatchArgs);
+
+struct Candidate {
+    BatchKernel k;
+    int nt, lanes, per_sm;
+};
+
+}  // namespace ffgpu
+
+using namespace ffgpu;
+
+struct ffgpu_batch {
+    ffgpu_ctx *ctx;
+    int nprob;
+    std::vector<int32_t> voff_h;
+    ffgpu_space *space;
+    ffgpu_matrix *A;
+    double *b;
+    int32_t *voff, *order;
+    float *work32;
+    double *r;
+    float *dinv32;
+    int *queue, *iters, *outers, *conv;
+    double *resid;
+    int tuned;          // index of the chosen candidate, -1 before tuning
+    cudaGraphExec_t exec;
+    BatchArgs args;
+    float tuned_ms;
+};
+
+static Candidate g_cands[] = {
+    {batch_ir_kernel<256, 2>, 256, 2, 4}, {batch_ir_kernel<256, 4>, 256, 4, 4},
+    {batch_ir_kernel<512, 2>, 512, 2, 2}, {batch_ir_kernel<512, 4>, 512, 4, 2},
+    {batch_ir_kernel<1024, 2>, 1024, 2, 1}, {batch_ir_kernel<1024, 4>, 1024, 4, 1},
+    {batch_ir_kernel<128, 2>, 128, 2, 8},
+};
+static const int g_ncands = sizeof(g_cands) / sizeof(g_cands[0]);
+
+static int batch_graph(ffgpu_batch *B, int cand) {
+    ffgpu_ctx *ctx = B->ctx;
+    cudaStream_t s = ctx->stream;
+    if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+    const Candidate &c = g_cands[cand];
+    int grid = kNumSM * c.per_sm;
+    cudaGraph_t g;
+    FFGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    reset_queue_kernel<<<1, 1, 0, s>>>(B->queue);
+    void *args[] = {&B->args};
+    cudaLaunchKernel((void *)c.k, grid, c.nt, args, 0, s);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B->exec, g, 0);
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        set_error("batch graph: %s", cudaGetErrorString(e));
+        B->exec = nullptr;
+        return FFGPU_ECUDA;
+    }
+    return FFGPU_OK;
+}
+
+extern "C" {
+
+int ffgpu_batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int32_t *nt, const double *coords,
+                       const int32_t *elems, ffgpu_batch **out) {
+    FFGPU_CHECK(ctx && out && nv && nt && coords && elems && nprob > 0, FFGPU_EINVAL,
+                "ffgpu_batch_create: bad argument");
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    // union mesh: offset vertex numbers on the host (these are small int arrays)
+    std::vector<int32_t> voff(nprob + 1, 0), toff(nprob + 1, 0);
+    for (int p = 0; p < nprob; ++p) {
+        FFGPU_CHECK(nv[p] > 0 && nt[p] > 0, FFGPU_EINVAL, "problem %d is empty", p);
+        voff[p + 1] = voff[p] + nv[p];
+        toff[p + 1] = toff[p] + nt[p];
+    }
+    const int NV = voff[nprob], NT = toff[nprob];
+    std::vector<int32_t> el(elems, elems + (size_t)3 * NT);
+    for (int p = 0; p < nprob; ++p)
+        for (int64_t k = (int64_t)3 * toff[p]; k < (int64_t)3 * toff[p + 1]; ++k) {
+            FFGPU_CHECK(el[k] >= 0 && el[k] < nv[p], FFGPU_EINVAL, "problem %d: vertex index out of range", p);
+            el[k] += voff[p];
+        }
+    ffgpu_batch *B = new ffgpu_batch();
+    B->ctx = ctx; B->nprob = nprob; B->voff_h = voff; B->space = nullptr; B->A = nullptr; B->tuned = -1;
+    B->exec = nullptr; B->b = nullptr; B->work32 = nullptr; B->r = nullptr; B->dinv32 = nullptr;
+    int rc = ffgpu_space_create(ctx, 2, NV, coords, NT, el.data(), FFGPU_FE_P1, 3, el.data(), NV, &B->space);
+    if (rc) { delete B; return rc; }
+    std::vector<int32_t> order(nprob);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nv[a] > nv[b]; });
+    if (cudaMalloc((void **)&B->voff, sizeof(int32_t) * (nprob + 1)) ||
+        cudaMalloc((void **)&B->order, sizeof(int32_t) * nprob) ||
+        cudaMalloc((void **)&B->queue, sizeof(int) * 4) ||
+        cudaMalloc((void **)&B->iters, sizeof(int) * nprob) || cudaMalloc((void **)&B->outers, sizeof(int) * nprob) ||
+        cudaMalloc((void **)&B->conv, sizeof(int) * nprob) || cudaMalloc((void **)&B->resid, sizeof(double) * nprob) ||
+        cudaMalloc((void **)&B->b, sizeof(double) * NV) || cudaMalloc((void **)&B->r, sizeof(double) * NV) ||
+        cudaMalloc((void **)&B->work32, sizeof(float) * (size_t)NV * 5)) {
+        set_error("ffgpu_batch_create: device allocation failed");
+        ffgpu_space_destroy(B->space);
+        delete B;
+        return FFGPU_ENOMEM;
+    }
+    B->dinv32 = B->work32 + (size_t)4 * NV;
+    cudaMemcpy(B->voff, voff.data(), sizeof(int32_t) * (nprob + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(B->order, order.data(), sizeof(int32_t) * nprob, cudaMemcpyHostToDevice);
+    *out = B;
+    return FFGPU_OK;
+}
+
+int ffgpu_batch_assemble(ffgpu_batch *B, const double *kappa, double f, const uint8_t *onbc, double tgv) {
+    FFGPU_CHECK(B, FFGPU_EINVAL, "ffgpu_batch_assemble: NULL batch");
+    ffgpu_varf v;
+    memset(&v, 0, sizeof(v));
+    v.form = FFGPU_FORM_DIFFUSION;
+    v.kappa = kappa;
+    v.c_stiff = 1.0;
+    v.f_const[0] = f;
+    ffgpu_bc bc = {onbc, nullptr, tgv};
+    if (!B->A) {
+        FFGPU_TRY(ffgpu_matrix_assemble(B->space, &v, &bc, B->b, &B->A));
+    } else {
+        FFGPU_TRY(ffgpu_matrix_reassemble(B->A, &v, &bc, B->b));
+    }
+    ffgpu_matrix *A = B->A;
+    FFGPU_TRY(matrix_prepare_solver(A));
+    FFGPU_TRY(ffgpu_matrix_to_f32(A));
+    cudaStream_t s = B->ctx->stream;
+    f32_copy_kernel<<<4 * kNumSM, 256, 0, s>>>(A->n, A->diag_inv, B->dinv32);
+    FFGPU_TRY(launch_check(B->ctx, "f32_copy"));
+    float *w = B->work32;
+    size_t NV = A->n;
+    B->args = BatchArgs{B->nprob, B->order, B->voff, A->browptr, A->bcol, A->val, A->val32, A->diag_inv,
+                        B->dinv32, A->wcl, B->b, nullptr, w, w + NV, w + 2 * NV, w + 3 * NV, B->r, B->queue,
+                        B->iters, B->outers, B->conv, B->resid, 1e-8, tgv > 0 ? tgv : 1e30, 1e-4f, 0, 30};
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    return FFGPU_OK;
+}
+
+int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int32_t *iterations,
+                      ffgpu_solver_stats *stats) {
+    FFGPU_CHECK(B && B->A && x && prm, FFGPU_EINVAL, "ffgpu_batch_solve: assemble the batch first");
+    ffgpu_ctx *ctx = B->ctx;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int NV = B->A->n;
+    DevOut<double> xd(x, NV, s, false);
+    FFGPU_TRY(xd.err);
+    BatchArgs &a = B->args;
+    bool changed = a.x != xd.d || a.eps != prm->eps ||
+                   a.eps_in != (float)(prm->eps_inner > 0 ? prm->eps_inner : 1e-4) ||
+                   a.itmax_in != (prm->itmax_inner > 0 ? prm->itmax_inner : 100000) ||
+                   a.max_outer != (prm->max_outer > 0 ? prm->max_outer : 30);
+    a.x = xd.d;
+    a.eps = prm->eps;
+    a.eps_in = (float)(prm->eps_inner > 0 ? prm->eps_inner : 1e-4);
+    a.itmax_in = prm->itmax_inner > 0 ? prm->itmax_inner : 100000;
+    a.max_outer = prm->max_outer > 0 ? prm->max_outer : 30;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    if (B->tuned < 0) {
+        // autotune: time every candidate (CTA size x lanes per row) on this batch
+        float best = 1e30f;
+        int bi = 0;
+        for (int c = 0; c < g_ncands; ++c) {
+            FFGPU_TRY(batch_graph(B, c));
+            cudaGraphLaunch(B->exec, s);   // warm
+            cudaEventRecord(e0, s);
+            cudaGraphLaunch(B->exec, s);
+            cudaEventRecord(e1, s);
+            FFGPU_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ctx->launches += 4;
+            if (ms < best) { best = ms; bi = c; }
+        }
+        B->tuned = bi;
+        B->tuned_ms = best;
+        changed = true;
+    }
+    if (changed || !B->exec) FFGPU_TRY(batch_graph(B, B->tuned));
+    cudaEventRecord(e0, s);
+    FFGPU_CUDA(cudaGraphLaunch(B->exec, s));
+    cudaEventRecord(e1, s);
+    ctx->launches += 2;
+    FFGPU_TRY(xd.finish(s));
+    FFGPU_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::vector<int> it(B->nprob), ou(B->nprob), cv(B->nprob);
+    cudaMemcpy(it.data(), B->iters, sizeof(int) * B->nprob, cudaMemcpyDeviceToHost);
+    cudaMemcpy(ou.data(), B->outers, sizeof(int) * B->nprob, cudaMemcpyDeviceToHost);
+    cudaMemcpy(cv.data(), B->conv, sizeof(int) * B->nprob, cudaMemcpyDeviceToHost);
+    if (iterations) memcpy(iterations, it.data(), sizeof(int) * B->nprob);
+    int nconv = 0;
+    long long tot = 0;
+    int maxo = 0;
+    for (int p = 0; p < B->nprob; ++p) { nconv += cv[p]; tot += it[p]; maxo = max(maxo, ou[p]); }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations = (int)tot;
+        stats->outer_iterations = maxo;
+        stats->converged = nconv == B->nprob;
+        stats->elapsed_ms = ms;
+    }
+    if (nconv != B->nprob) {
+        set_error("batch: %d of %d problems did not converge", B->nprob - nconv, B->nprob);
+        return FFGPU_ENOCONV;
+    }
+    return FFGPU_OK;
+}
+
+int ffgpu_batch_rhs(const ffgpu_batch *B, double *b) {
+    FFGPU_CHECK(B && B->A && b, FFGPU_EINVAL, "ffgpu_batch_rhs: assemble first");
+    FFGPU_CUDA(cudaMemcpy(b, B->b, sizeof(double) * B->A->n, cudaMemcpyDefault));
+    return FFGPU_OK;
+}
+
+ffgpu_matrix *ffgpu_batch_matrix(const ffgpu_batch *B) { return B ? B->A : nullptr; }
+
+int ffgpu_batch_info(const ffgpu_batch *B, int *cta_threads, int *lanes_per_row, float *tuned_ms) {
+    FFGPU_CHECK(B, FFGPU_EINVAL, "ffgpu_batch_info: NULL batch");
+    int c = B->tuned;
+    if (cta_threads) *cta_threads = c >= 0 ? g_cands[c].nt : 0;
+    if (lanes_per_row) *lanes_per_row = c >= 0 ? g_cands[c].lanes : 0;
+    if (tuned_ms) *tuned_ms = c >= 0 ? B->tuned_ms : 0.0f;
+    return FFGPU_OK;
+}
+
+int ffgpu_batch_destroy(ffgpu_batch *B) {
+    if (!B) return FFGPU_OK;
+    cudaStreamSynchronize(B->ctx->stream);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    ffgpu_matrix_destroy(B->A);
+    ffgpu_space_destroy(B->space);
+    cudaFree(B->voff); cudaFree(B->order); cudaFree(B->queue); cudaFree(B->iters); cudaFree(B->outers);
+    cudaFree(B->conv); cudaFree(B->resid); cudaFree(B->b); cudaFree(B->r); cudaFree(B->work32);
+    delete B;
+    return FFGPU_OK;
+}
+
+}  // extern "C"

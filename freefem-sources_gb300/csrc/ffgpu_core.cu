@@ -173,6 +173,65 @@ int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max) {
     return FFGPU_OK;
 }
 
+// ------------------------------------------------------------------ stable order by key
+// Counting sort by decreasing key, stable in the index: per-tile histograms laid out
+// (key-major, tile-minor), one exclusive scan, then each tile places its rows in index order
+// (32 at a time, ranks among equal keys from __match_any_sync).  Deterministic.
+constexpr int kOrdTile = 1024;
+
+__global__ void order_hist_kernel(const int32_t *key, int n, int maxkey, int ntiles, int32_t *hist) {
+    extern __shared__ int sh_hist[];
+    const int K = maxkey + 1;
+    for (int d = threadIdx.x; d < K; d += blockDim.x) sh_hist[d] = 0;
+    __syncthreads();
+    int64_t i = (int64_t)blockIdx.x * kOrdTile + threadIdx.x;
+    for (int k = 0; k < kOrdTile / 1024; ++k, i += 1024)
+        if (i < n) atomicAdd(&sh_hist[maxkey - key[i]], 1);
+    __syncthreads();
+    for (int d = threadIdx.x; d < K; d += blockDim.x) hist[(int64_t)d * ntiles + blockIdx.x] = sh_hist[d];
+}
+
+__global__ void order_place_kernel(const int32_t *key, int n, int maxkey, int ntiles, const int32_t *off,
+                                   int32_t *order) {
+    extern __shared__ int sh_run[];
+    const int K = maxkey + 1, lane = threadIdx.x;
+    for (int d = lane; d < K; d += 32) sh_run[d] = off[(int64_t)d * ntiles + blockIdx.x];
+    __syncwarp();
+    for (int c = 0; c < kOrdTile; c += 32) {
+        int64_t i = (int64_t)blockIdx.x * kOrdTile + c + lane;
+        bool ok = i < n;
+        int d = ok ? maxkey - key[i] : -1;
+        unsigned same = __match_any_sync(0xffffffffu, d);
+        int rank = __popc(same & ((1u << lane) - 1u));
+        int pos = ok ? sh_run[d] + rank : 0;
+        __syncwarp();
+        if (ok) order[pos] = (int32_t)i;
+        if (ok && rank == __popc(same) - 1) sh_run[d] += __popc(same);
+        __syncwarp();
+    }
+}
+
+int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order) {
+    if (n <= 0) return FFGPU_OK;
+    const int ntiles = (n + kOrdTile - 1) / kOrdTile;
+    const int K = maxkey + 1;
+    int64_t m = (int64_t)K * ntiles;
+    FFGPU_CHECK(m < (int64_t)1 << 30, FFGPU_EINVAL, "row ordering: %d keys x %d tiles too large", K, ntiles);
+    int32_t *hist = nullptr;
+    FFGPU_CUDA(cudaMallocAsync((void **)&hist, sizeof(int32_t) * (2 * m + 1), ctx->stream));
+    int32_t *off = hist + m;
+    size_t smem = sizeof(int) * K;
+    order_hist_kernel<<<ntiles, 1024, smem, ctx->stream>>>(key, n, maxkey, ntiles, hist);
+    int r = launch_check(ctx, "order_hist");
+    if (!r) r = device_scan_i32(ctx, hist, off, (int)m);
+    if (!r) {
+        order_place_kernel<<<ntiles, 32, smem, ctx->stream>>>(key, n, maxkey, ntiles, off, order);
+        r = launch_check(ctx, "order_place");
+    }
+    cudaFreeAsync(hist, ctx->stream);
+    return r;
+}
+
 }  // namespace ffgpu
 
 using namespace ffgpu;

@@ -72,6 +72,9 @@ struct ffgpu_ctx {
     int *d_status;              // DevStatus word
     unsigned int *d_ticket;     // last-block counters
     int *d_iscratch;            // small integer scratch (max reductions)
+    // SpMV lanes-per-row chosen by timing, per matrix shape (nb, nnzb, bs)
+    struct Tuned { int64_t nb, nnzb; int bs, lanes; } tuned[32];
+    int ntuned;
 };
 
 struct ffgpu_space {
@@ -95,6 +98,7 @@ struct ffgpu_matrix {
     int32_t *browptr;     // nb+1
     int32_t *bcol;        // nnzb
     int32_t *diagpos;     // nb: index of the diagonal block of each block row
+    int32_t *rowperm;     // nb: block rows by decreasing degree (stable), the SpMV's row order
     double *val;          // nnzb*bs*bs, each block row-major
     double *geo;          // per-element geometry cache (16 doubles per element)
     // solver state (lazily allocated)
@@ -178,6 +182,8 @@ int check_device_status(ffgpu_ctx *ctx, const char *where);
 int launch_check(ffgpu_ctx *ctx, const char *what);
 int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n);  // exclusive, out[n]=total
 int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
+// order[0..n): indices sorted by decreasing key (0 <= key <= maxkey), ties by increasing index
+int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order);
 
 // matrix-level operations shared by the solvers
 int matrix_prepare_solver(ffgpu_matrix *A);

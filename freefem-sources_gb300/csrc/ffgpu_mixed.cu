@@ -100,6 +100,7 @@ struct Spmv32 {
     int nb, bs;
     const int32_t *rp, *col;
     const float *val;
+    const int32_t *perm;
 };
 
 // inner K_a: q = A h (FP32) and (h,q) -> rho
@@ -114,14 +115,15 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(Spmv32 A, const float *__
     int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
     float hq = 0;
     for (int base = 0; base < A.nb; base += gridDim.x * groups) {
-        int a = base + g;
-        bool ok = a < A.nb;
+        const int slot = base + g;
+        const bool ok = slot < A.nb;
+        const int a = ok ? __ldg(A.perm + slot) : 0;
         if (BS == 1) {
-            float s = csr_row_f<T>(A.rp, A.col, A.val, h, ok ? a : 0, ok ? sub : T);
+            float s = csr_row_f<T>(A.rp, A.col, A.val, h, a, ok ? sub : T);
             if (ok && sub == 0) { q[a] = s; hq = fmaf(h[a], s, hq); }
         } else {
             float y0, y1, y2;
-            bsr3_row_f<T>(A.rp, A.col, A.val, h, ok ? a : 0, ok ? sub : T, y0, y1, y2);
+            bsr3_row_f<T>(A.rp, A.col, A.val, h, a, ok ? sub : T, y0, y1, y2);
             if (ok && sub == 0) {
                 int64_t i = 3 * (int64_t)a;
                 q[i] = y0; q[i + 1] = y1; q[i + 2] = y2;
@@ -319,7 +321,7 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int T = ir_lanes(A);
-    Spmv32 sa{A->nb, A->bs, A->browptr, A->bcol, A->val32};
+    Spmv32 sa{A->nb, A->bs, A->browptr, A->bcol, A->val32, A->rowperm};
     void *ka = A->bs == 3 ? ir_ka_fn<3>(T) : ir_ka_fn<1>(T);
     float *part = (float *)ctx->d_part;
     int n = A->n;

@@ -109,6 +109,7 @@ struct SpmvArgs {
     int nb, bs;
     const int32_t *rp, *col;
     const double *val;
+    const int32_t *perm;   // row order (rows of equal degree share a warp)
 };
 
 // y = A x, optionally with the partial of (w, y) (w may alias x); persistent grid.
@@ -120,16 +121,16 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_kernel(SpmvArgs A, const
     const int groups = (blockDim.x / 32) * (32 / T);
     int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
     for (int base = 0; base < A.nb; base += gridDim.x * groups) {
-        int a = base + g;
+        const int slot = base + g;
+        const bool ok = slot < A.nb;
+        const int a = ok ? __ldg(A.perm + slot) : 0;
         if (BS == 1) {
-            double s = 0;
-            if (a < A.nb) s = csr_row<T>(A.rp, A.col, A.val, x, a, sub);
-            else s = csr_row<T>(A.rp, A.col, A.val, x, 0, T);   // keep the warp converged
-            if (a < A.nb && sub == 0) y[a] = s;
+            double s = csr_row<T>(A.rp, A.col, A.val, x, a, ok ? sub : T);
+            if (ok && sub == 0) y[a] = s;
         } else {
             double v[3];
-            bsr3_row<T>(A.rp, A.col, A.val, x, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
-            if (a < A.nb && sub == 0) {
+            bsr3_row<T>(A.rp, A.col, A.val, x, a, ok ? sub : T, v);
+            if (ok && sub == 0) {
                 y[3 * (int64_t)a] = v[0];
                 y[3 * (int64_t)a + 1] = v[1];
                 y[3 * (int64_t)a + 2] = v[2];
@@ -151,14 +152,16 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
     int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
     double hq = 0;
     for (int base = 0; base < A.nb; base += gridDim.x * groups) {
-        int a = base + g;
+        const int slot = base + g;
+        const bool ok = slot < A.nb;
+        const int a = ok ? __ldg(A.perm + slot) : 0;
         if (BS == 1) {
-            double s = csr_row<T>(A.rp, A.col, A.val, h, a < A.nb ? a : 0, a < A.nb ? sub : T);
-            if (a < A.nb && sub == 0) { q[a] = s; hq = fma(h[a], s, hq); }
+            double s = csr_row<T>(A.rp, A.col, A.val, h, a, ok ? sub : T);
+            if (ok && sub == 0) { q[a] = s; hq = fma(h[a], s, hq); }
         } else {
             double v[3];
-            bsr3_row<T>(A.rp, A.col, A.val, h, a < A.nb ? a : 0, a < A.nb ? sub : T, v);
-            if (a < A.nb && sub == 0) {
+            bsr3_row<T>(A.rp, A.col, A.val, h, a, ok ? sub : T, v);
+            if (ok && sub == 0) {
                 int64_t i = 3 * (int64_t)a;
                 q[i] = v[0]; q[i + 1] = v[1]; q[i + 2] = v[2];
                 hq = fma(h[i], v[0], hq);
@@ -398,7 +401,49 @@ static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
     SpmvArgs s;
     s.nb = A->nb; s.bs = A->bs; s.rp = A->browptr; s.col = A->bcol;
     s.val = trans ? A->val_t : A->val;
+    s.perm = A->rowperm;
     return s;
+}
+
+// Times the SpMV with each candidate lanes-per-row on this matrix (once per shape and context).
+static int tune_lanes(ffgpu_matrix *A) {
+    if (A->csr_lanes > 0) return FFGPU_OK;
+    ffgpu_ctx *ctx = A->ctx;
+    for (int i = 0; i < ctx->ntuned; ++i)
+        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs) {
+            A->csr_lanes = ctx->tuned[i].lanes;
+            return FFGPU_OK;
+        }
+    if (!A->vec) { A->csr_lanes = pick_lanes(A); return FFGPU_OK; }
+    const int cands[] = {2, 4, 8, 16};
+    double *x = A->vec + 5 * (int64_t)A->n, *y = A->vec + 6 * (int64_t)A->n;
+    cudaStream_t s = ctx->stream;
+    FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bestT = pick_lanes(A);
+    SpmvArgs sa = spmv_args(A, 0);
+    for (int T : cands) {
+        if (A->bs == 3 && T > 8) continue;
+        void *fn = A->bs == 3 ? spmv_fn<3>(T) : spmv_fn<1>(T);
+        void *args[] = {&sa, &x, &y};
+        cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);   // warm
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < 3; ++r) cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);
+        cudaEventRecord(e1, s);
+        FFGPU_CUDA(cudaEventSynchronize(e1));
+        ctx->launches += 4;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; bestT = T; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    A->csr_lanes = bestT;
+    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT};
+    return FFGPU_OK;
 }
 
 int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st) {
@@ -432,6 +477,7 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
         FFGPU_CUDA(cudaMalloc((void **)&A->ks, sizeof(KrylovScalars)));
         FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
     }
+    FFGPU_TRY(tune_lanes(A));
     if (A->ntgv >= 0) return FFGPU_OK;
     unsigned long long *bits = (unsigned long long *)ctx->d_iscratch;   // [0] max, [1] max1
     int *cnt = ctx->d_iscratch + 4;

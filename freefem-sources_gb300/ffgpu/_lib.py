@@ -25,6 +25,8 @@ EXPORTS = [
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
+    "ffgpu_batch_create", "ffgpu_batch_assemble", "ffgpu_batch_solve", "ffgpu_batch_rhs",
+    "ffgpu_batch_matrix", "ffgpu_batch_info", "ffgpu_batch_destroy",
 ]
 
 
@@ -95,6 +97,13 @@ def lib():
         "ffgpu_diffusion_sensitivity": (i32, [vp, vp, vp, dbl, vp, vp]),
         "ffgpu_solve_cg_csr_noalloc": (i32, [i32, i64, vp, vp, vp, vp, vp, dbl, i32, dbl, vp,
                                               P(i32), vp]),
+        "ffgpu_batch_create": (i32, [vp, i32, vp, vp, vp, vp, P(vp)]),
+        "ffgpu_batch_assemble": (i32, [vp, vp, dbl, vp, dbl]),
+        "ffgpu_batch_solve": (i32, [vp, vp, P(IRParams), vp, P(SolverStats)]),
+        "ffgpu_batch_rhs": (i32, [vp, vp]),
+        "ffgpu_batch_matrix": (vp, [vp]),
+        "ffgpu_batch_info": (i32, [vp, P(i32), P(i32), P(C.c_float)]),
+        "ffgpu_batch_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

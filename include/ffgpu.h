@@ -178,6 +178,33 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
 int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *lambda, double c_stiff,
                                 double *grad_kappa, double *grad_f);
 
+/* ------------------------------------------------------------------ batched problems
+ * Many independent 2D P1 diffusion problems (int(kappa grad u.grad v) + int(f v) + on(...,u=0))
+ * assembled in one pass and solved in one persistent, graph-captured launch with FP32 inner
+ * Jacobi-PCG and FP64 refinement.  Each problem is what FreeFEM would assemble and solve alone
+ * (pattern, values, stopping rule of SolverCG applied to the true residual); FreeFEM has no
+ * batched path, it runs one script per problem.
+ * create: nprob meshes, nv[p] vertices and nt[p] triangles each; coords (sum nv) x 2, elems
+ *         (sum nt) x 3 with per-problem vertex numbers.
+ * assemble: kappa (sum nt) P0 values, constant source f, onbc (sum nv) Dirichlet mask, tgv.
+ * solve: x (sum nv) receives all solutions; iterations[p] (may be NULL) the inner iterations.
+ *        prm->eps is each problem's outer tolerance.  The first solve autotunes the CTA size
+ *        and lanes per SpMV row by timing the candidates on the batch. */
+typedef struct ffgpu_batch ffgpu_batch;
+int ffgpu_batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int32_t *nt,
+                       const double *coords, const int32_t *elems, ffgpu_batch **out);
+int ffgpu_batch_assemble(ffgpu_batch *B, const double *kappa, double f, const uint8_t *onbc,
+                         double tgv);
+int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int32_t *iterations,
+                      ffgpu_solver_stats *stats);
+/* right-hand sides of all problems (sum nv) as assembled */
+int ffgpu_batch_rhs(const ffgpu_batch *B, double *b);
+/* the block-diagonal matrix of the batch (owned by the batch) */
+ffgpu_matrix *ffgpu_batch_matrix(const ffgpu_batch *B);
+/* the autotuned launch shape: threads per CTA, lanes per SpMV row, its batch time */
+int ffgpu_batch_info(const ffgpu_batch *B, int *cta_threads, int *lanes_per_row, float *tuned_ms);
+int ffgpu_batch_destroy(ffgpu_batch *B);
+
 /* ------------------------------------------------------------------ allocation-free CG
  * Jacobi-PCG on a caller's CSR matrix that allocates no memory: for callers that cannot
  * allocate device memory while they run (an application that hands the GPU's memory to its
