@@ -33,13 +33,18 @@ UNIT = "DOFs/s"
 ITMAX = 20000   # iteration cap of the timed solves (CG needs a few thousand here)
 
 CONFIGS = {
-    # name: (builder, kind, varf kwargs)
     "elasticity_p2_cube64": dict(mesh=("cube", 64), kind="P2vec", form="elasticity", on=(4,),
                                  eps=1e-10),
     "poisson_p1_square256": dict(mesh=("square", 256), kind="P1", form="diffusion",
                                  on=(1, 2, 3, 4), eps=1e-10),
+    # 3D scalar diffusion, kappa P0 with ln kappa ~ N(0,1) i.i.d. per tet (seed 3)
+    "diffusion_p1_cube160": dict(mesh=("cube", 160), kind="P1", form="diffusion",
+                                 on=(1, 2, 3, 4, 5, 6), eps=1e-10, kappa_seed=3),
+    # 1024 independent jittered squares, N ~ U{16..128}, FP32 inner / FP64 refinement to 1e-8
+    "batched_p1_1024": dict(batch=True, nprob=1024, nmin=16, nmax=128, eps=1e-8, seed=0),
 }
-SAMPLE = {"elasticity_p2_cube64": ("cube", 12), "poisson_p1_square256": ("square", 256)}
+SAMPLE = {"elasticity_p2_cube64": ("cube", 12), "poisson_p1_square256": ("square", 256),
+          "diffusion_p1_cube160": ("cube", 40), "batched_p1_1024": ("square", 64)}
 
 
 def build_problem(cfg, size=None):
@@ -52,7 +57,10 @@ def build_problem(cfg, size=None):
     if cfg["form"] == "elasticity":
         a = ffgpu.varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=cfg["on"])
     else:
-        a = ffgpu.varf_diffusion(f=1.0, on=cfg["on"])
+        kappa = None
+        if "kappa_seed" in cfg:
+            kappa = np.exp(np.random.Generator(np.random.PCG64(cfg["kappa_seed"])).standard_normal(Th.nt))
+        a = ffgpu.varf_diffusion(kappa=kappa, f=1.0, on=cfg["on"])
     return Th, Vh, a, np
 
 
@@ -65,7 +73,7 @@ def _oracle_run(args):
     Th, Vh, a, np = build_problem(cfg, size)
     t0 = time.perf_counter()
     quad = None if cfg["kind"] != "P1" or Th.dim == 3 else "qf2pT"
-    A = ffo.assemble(Th, Vh, form=cfg["form"], quad=quad)
+    A = ffo.assemble(Th, Vh, form=cfg["form"], quad=quad, kappa=a.kappa)
     b = ffo.rhs(Th, Vh, f=(0.0, 0.0, -1.0) if cfg["form"] == "elasticity" else 1.0, quad=quad)
     ffo.setbc(A, b, Vh.on(cfg["on"]))
     u, it, r, _ = ffo.cg(A, b, eps=cfg["eps"])
@@ -160,14 +168,26 @@ def run_gpu(args, rank, world):
     X = torch.from_numpy(Th.coords).cuda(dev)
     E = torch.from_numpy(np.ascontiguousarray(Th.elems)).cuda(dev)
     D = torch.from_numpy(np.ascontiguousarray(Vh.dof)).cuda(dev)
+    BE = torch.from_numpy(np.ascontiguousarray(Th.belems)).cuda(dev)
+    BL = torch.from_numpy(np.ascontiguousarray(Th.blabel)).cuda(dev)
     onbc = Vh.on(cfg["on"])
     a.on = cfg["on"]
     b = torch.empty(Vh.ndof, dtype=torch.float64, device=dev)
+    phase = {"space": [], "assemble": [], "solve": []}
 
     def step_device():
-        S = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D)
+        t = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        t[0].record(stream)
+        S = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+        t[1].record(stream)
         A = ffgpu.matrix(a, S, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
+        t[2].record(stream)
         u = A.solve(b)
+        t[3].record(stream)
+        t[3].synchronize()
+        phase["space"].append(t[0].elapsed_time(t[1]))
+        phase["assemble"].append(t[1].elapsed_time(t[2]))
+        phase["solve"].append(t[2].elapsed_time(t[3]))
         return S, A, u
 
     def barrier():
@@ -197,7 +217,6 @@ def run_gpu(args, rank, world):
         evs[k + 1].synchronize()
         times.append(evs[k].elapsed_time(evs[k + 1]))
         iters.append(A.stats.iterations)
-        asm_ms.append(times[-1] - A.stats.elapsed_ms)
         keep = (S, A, u)
     ev1.record(stream)
     barrier()
@@ -243,6 +262,44 @@ def run_gpu(args, rank, world):
         traffic = tr.get(cfgname, {}).get("spmv_bytes_per_launch")
     except Exception:
         pass
+    # variants on the same workload: the double-float SpMV CG and the mixed-precision IR,
+    # each with its error against this run's FP64 solution
+    u_ref = u.clone()
+    variants = {}
+
+    def timed_variant(fn, reps):
+        out, ms = None, []
+        for r in range(reps + 1):
+            e0v = torch.cuda.Event(enable_timing=True)
+            e1v = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            e0v.record(stream)
+            out = fn()
+            e1v.record(stream)
+            e1v.synchronize()
+            if r > 0:
+                ms.append(e0v.elapsed_time(e1v))
+        return out, statistics.median(ms)
+
+    if not args.no_variants:
+        def run_df():
+            S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+            A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
+            return A2.solve(b, spmv_mode=1), A2.stats.iterations
+        (udf, itdf), msdf = timed_variant(run_df, 2)
+        variants["fp64_values_doublefloat_spmv"] = {
+            "value": Vh.ndof / (msdf * 1e-3), "ms_per_step": msdf, "cg_iterations": itdf,
+            "rel_err_vs_fp64": float(torch.linalg.norm(udf - u_ref) / torch.linalg.norm(u_ref))}
+
+        def run_ir():
+            S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+            A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
+            return A2.solve_mixed(b, eps=cfg["eps"]), A2.stats.iterations, A2.stats.outer_iterations
+        (uir, itir, outir), msir = timed_variant(run_ir, 1)
+        variants["mixed_fp32_inner_fp64_refinement"] = {
+            "value": Vh.ndof / (msir * 1e-3), "ms_per_step": msir, "inner_iterations": itir,
+            "outer_iterations": outir,
+            "rel_err_vs_fp64": float(torch.linalg.norm(uir - u_ref) / torch.linalg.norm(u_ref))}
     # e2e: public API from host arrays (H2D of mesh/DOF table/BC mask, D2H of b and u)
     e2e_times = []
     bh = np.empty(Vh.ndof)
@@ -255,7 +312,7 @@ def run_gpu(args, rank, world):
         if s >= max(1, args.warmup // 3):
             e2e_times.append((t1 - t0) * 1e3)
         del Ah
-    h2d = Th.coords.nbytes + Th.elems.nbytes + Vh.dof.nbytes + onbc.nbytes + bh.nbytes
+    h2d = Th.coords.nbytes + Th.elems.nbytes + Vh.dof.nbytes + Th.belems.nbytes + Th.blabel.nbytes + bh.nbytes
     d2h = bh.nbytes + uh.nbytes
     # max over ranks
     t_step = total_ms / args.steps
@@ -275,7 +332,11 @@ def run_gpu(args, rank, world):
                    "solver": "Jacobi-PCG", "eps": cfg["eps"], "cg_iterations": iters[-1],
                    "l2": "inputs larger than L2 (matrix %.1f GB)" % (nnz * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "assembly_ms": statistics.median(asm_ms), "rel_residual": rel_res},
+                   "space_ms": statistics.median(phase["space"][-args.steps:]),
+                   "assemble_ms": statistics.median(phase["assemble"][-args.steps:]),
+                   "solve_ms": statistics.median(phase["solve"][-args.steps:]),
+                   "ms_per_cg_iteration": statistics.median(phase["solve"][-args.steps:]) / max(1, iters[-1]),
+                   "rel_residual": rel_res},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e},
         "gpu_launches": int(launches),
@@ -284,8 +345,140 @@ def run_gpu(args, rank, world):
                      "kernel": "spmv BSR3 FP64 (cg_ka body)", "bytes_per_launch": spmv_bytes,
                      "ms_per_launch": spmv_avg, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "clocks": clk,
+        "variants": variants,
     }
     return out
+
+
+def profile_case(kind, n, iters, spmv_mode):
+    """Small case for ncu: space + assembly + a fixed number of CG iterations, twice."""
+    import numpy as np
+    import torch
+    import ffgpu
+    from ffgpu.build import build
+    from ffgpu.fespace import FESpace
+    build()
+    if kind == "elasticity":
+        Th = ffgpu.cube(n); Vh = FESpace(Th, "P2vec"); a = ffgpu.varf_elasticity(f=(0, 0, -1.0), on=(4,))
+    elif kind == "diffusion3d":
+        Th = ffgpu.cube(n); Vh = FESpace(Th, "P1")
+        kap = np.exp(np.random.Generator(np.random.PCG64(1)).standard_normal(Th.nt))
+        a = ffgpu.varf_diffusion(kappa=kap, f=1.0, on=(1, 2, 3, 4, 5, 6))
+    else:
+        Th = ffgpu.square(n); Vh = FESpace(Th, "P1"); a = ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4))
+    dev = torch.device("cuda", 0)
+    X = torch.from_numpy(Th.coords).to(dev); E = torch.from_numpy(np.ascontiguousarray(Th.elems)).to(dev)
+    D = torch.from_numpy(Vh.dof).to(dev)
+    BE = torch.from_numpy(np.ascontiguousarray(Th.belems)).to(dev)
+    BL = torch.from_numpy(np.ascontiguousarray(Th.blabel)).to(dev)
+    b = torch.empty(Vh.ndof, dtype=torch.float64, device=dev)
+    for rep in range(2):
+        S = ffgpu.DeviceSpace(Vh, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+        A = ffgpu.matrix(a, S, eps=1e-10, itmax=iters, rhs_out=b)
+        try:
+            A.solve(b, spmv_mode=spmv_mode)
+        except ffgpu.FFGPUError as e:
+            if e.code != -3:
+                raise
+        torch.cuda.synchronize()
+        print(f"profile case {kind}({n}): ndof {Vh.ndof} nnz {A.nnz} iterations {A.stats.iterations} "
+              f"device {A.stats.elapsed_ms:.2f} ms")
+        del A, S
+
+
+def run_batch(args):
+    """Batched independent problems: one assembly pass and one persistent solve per step."""
+    import numpy as np
+    import torch
+    import ffgpu
+    from ffgpu import batch
+    from ffgpu.build import build
+    build()
+    cfg = CONFIGS[args.config]
+    meshes, kappas, Ns = batch.c5_meshes(cfg["nprob"], cfg["nmin"], cfg["nmax"], seed=cfg["seed"])
+    ndof = int(sum(m.nv for m in meshes))
+    ffgpu.context(0)
+    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(0), device=0)
+    B = batch.Batch(meshes)
+    kap = torch.from_numpy(np.concatenate(kappas)).cuda()
+    x = torch.zeros(ndof, dtype=torch.float64, device="cuda")
+
+    def step():
+        B.assemble(kap, f=1.0)
+        return B.solve(eps=cfg["eps"], out=x)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = ffgpu.kernel_launches()
+    clocks = ClockSampler()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    launches = ffgpu.kernel_launches() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    solve_ms = B.stats.elapsed_ms
+    nt_, lanes, tms = B.tuned()
+    # accuracy against the FP64 oracle on a sample of problems
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ffo
+    from ffgpu.fespace import FESpace
+    xs = B.split(x.cpu().numpy())
+    errs = []
+    rng = np.random.Generator(np.random.PCG64(1))
+    for p in rng.choice(len(meshes), size=8, replace=False):
+        Th = meshes[p]
+        Vh = FESpace(Th, "P1")
+        A = ffo.assemble(Th, Vh, kappa=kappas[p])
+        bo = ffo.rhs(Th, Vh, f=1.0)
+        ffo.setbc(A, bo, Vh.on((1, 2, 3, 4)))
+        uo, it, r, _ = ffo.cg(A, bo, eps=1e-10)
+        errs.append(float(np.linalg.norm(xs[p] - uo) / np.linalg.norm(uo)))
+    # e2e from host arrays
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        B2 = batch.Batch(meshes)
+        B2.assemble(kappas, f=1.0)
+        xh = B2.solve(eps=cfg["eps"])
+        B2.close()
+    t_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+    h2d = sum(m.coords.nbytes + m.elems.nbytes for m in meshes) + sum(k.nbytes for k in kappas) + ndof
+    # CPU: the oracle (single core) on 16 sampled problems, FP64 CG to the same eps
+    t0 = time.perf_counter()
+    nd = 0
+    for p in rng.choice(len(meshes), size=16, replace=False):
+        Th = meshes[p]
+        Vh = FESpace(Th, "P1")
+        A = ffo.assemble(Th, Vh, kappa=kappas[p])
+        bo = ffo.rhs(Th, Vh, f=1.0)
+        ffo.setbc(A, bo, Vh.on((1, 2, 3, 4)))
+        ffo.cg(A, bo, eps=cfg["eps"])
+        nd += Vh.ndof
+    cpu_v = nd / (time.perf_counter() - t0)
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
+    out = {"metric": METRIC, "value": ndof / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+           "config": {"workload": args.config, "nprob": len(meshes), "ndof": ndof,
+                      "N_range": [int(Ns.min()), int(Ns.max())], "eps": cfg["eps"],
+                      "solve_ms": solve_ms, "inner_iterations_total": int(B.stats.iterations),
+                      "max_outer": int(B.stats.outer_iterations), "tuned_cta_threads": nt_,
+                      "tuned_lanes_per_row": lanes, "rel_err_vs_fp64_oracle_max": max(errs),
+                      "l2": "working set %.0f MB" % ((ndof * 7 * 12) / 1e6)},
+           "e2e": {"value": ndof / (t_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(ndof * 8), "ms_per_step": t_e2e},
+           "gpu_launches": int(launches), "clocks": clk,
+           "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": "16 of the batch's problems, oracle FP64 CG, single core"},
+           "roofline": None, "peak_hbm_gbs": peaks.get("hbm_gbs")}
+    print(json.dumps(out))
 
 
 def main():
@@ -296,9 +489,22 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="elasticity_p2_cube64", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--profile-case", choices=["elasticity", "diffusion3d", "poisson2d"], default=None,
+                    help="run a small case for ncu instead of the benchmark")
+    ap.add_argument("--n", type=int, default=32)
+    ap.add_argument("--iters", type=int, default=40)
+    ap.add_argument("--spmv-mode", type=int, default=0)
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case, args.n, args.iters, args.spmv_mode)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if CONFIGS[args.config].get("batch") and args.impl != "reference":
+        if rank == 0:
+            run_batch(args)
+        return
     if args.impl == "reference":
         if rank != 0:
             return

@@ -196,49 +196,57 @@ __device__ __forceinline__ void edge_vertices(int e, int &p, int &q) {
     }
 }
 
-// One P2 basis function J: C_J[a] is a multiple of one gradient,
-//   vertex j:   C_J[a] = (a == j ? 3 : -1) g_j,        S_J = (3 - d) g_j
-//   edge (r,s): C_J[r] = 4 g_s, C_J[s] = 4 g_r, else 0, S_J = 4 (g_r + g_s)
+// One P2 basis function J in the two-gradient form used below, with no divergent branches:
+//   C_J[a] = c1(a) g_p1 + c2(a) g_p2,   S_J = sum_a C_J[a] = d1 g_p1 + d2 g_p2
+//   vertex j:   p1 = p2 = j, c1(a) = (a == j ? 3 : -1), c2 = 0,  d1 = 3 - dim, d2 = 0
+//   edge (r,s): p1 = s, p2 = r, c1(a) = 4 [a == r], c2(a) = 4 [a == s], d1 = d2 = 4
+// (grad(phi_j) = (4 lambda_j - 1) g_j and grad(4 lambda_r lambda_s) = 4 (lambda_r g_s + lambda_s g_r)).
 template <int DIM>
 struct P2Basis {
-    int J, r, s;
-    __device__ __forceinline__ explicit P2Basis(int JJ) : J(JJ), r(0), s(0) {
-        if (J > DIM) edge_vertices<DIM>(J - DIM - 1, r, s);
+    int p1, p2;
+    bool vtx;
+    __device__ __forceinline__ explicit P2Basis(int J) {
+        vtx = J <= DIM;
+        int r = 0, s = 0;
+        edge_vertices<DIM>(vtx ? 0 : J - DIM - 1, r, s);
+        p1 = vtx ? J : s;
+        p2 = vtx ? J : r;
     }
-    __device__ __forceinline__ V3 C(const double *G, int a) const {
-        if (J <= DIM) return (a == J ? 3.0 : -1.0) * v3(G + 3 * J);
-        if (a == r) return 4.0 * v3(G + 3 * s);
-        if (a == s) return 4.0 * v3(G + 3 * r);
-        return V3{0.0, 0.0, 0.0};
+    __device__ __forceinline__ double c1(int a) const {
+        return vtx ? (a == p1 ? 3.0 : -1.0) : (a == p2 ? 4.0 : 0.0);
     }
-    __device__ __forceinline__ V3 S(const double *G) const {
-        if (J <= DIM) return (3.0 - DIM) * v3(G + 3 * J);
-        return 4.0 * (v3(G + 3 * r) + v3(G + 3 * s));
-    }
+    __device__ __forceinline__ double c2(int a) const { return vtx ? 0.0 : (a == p1 ? 4.0 : 0.0); }
+    __device__ __forceinline__ double d1() const { return vtx ? 3.0 - DIM : 4.0; }
+    __device__ __forceinline__ double d2() const { return vtx ? 0.0 : 4.0; }
 };
 
 // The 3x3 matrix (1/m) int_K d_a(phi_I) d_b(phi_J) = sum_c C_I[c]_a C_J[c]_b + S_I,a S_J,b as a sum
 // of at most three outer products u_k (x) w_k:
-//   I vertex i:  u = g_i, w = 4 C_J[i] - (d-2) S_J                              (rank 1)
-//   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J             (rank 3)
+//   I vertex i:   u = g_i,  w = 4 C_J[i] - (d-2) S_J                    (rank 1)
+//   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J    (rank 3)
+// The I type is the same on every lane of a warp (a row's node is either a vertex or an edge
+// of all its elements); the J side is evaluated without branches.
 template <int DIM>
 struct P2Pair {
     V3 u0, w0, u1, w1, u2, w2;
     bool vertex;
     __device__ __forceinline__ P2Pair(const double *G, int I, int Jidx) {
-        P2Basis<DIM> J(Jidx);
+        const P2Basis<DIM> J(Jidx);
+        const V3 g1 = v3(G + 3 * J.p1), g2 = v3(G + 3 * J.p2);
         vertex = I <= DIM;
         if (vertex) {
             u0 = v3(G + 3 * I);
-            w0 = 4.0 * J.C(G, I) - (double)(DIM - 2) * J.S(G);
+            // 4 C_J[i] - (d-2) S_J, with the coefficients selected, not branched on
+            const double a1 = 4.0 * J.c1(I) - (DIM - 2) * J.d1(), a2 = 4.0 * J.c2(I) - (DIM - 2) * J.d2();
+            w0 = a1 * g1 + a2 * g2;
             u1 = w1 = u2 = w2 = V3{0.0, 0.0, 0.0};
         } else {
             int p, q;
             edge_vertices<DIM>(I - DIM - 1, p, q);
-            V3 gp = v3(G + 3 * p), gq = v3(G + 3 * q);
-            u0 = 4.0 * gq; w0 = J.C(G, p);
-            u1 = 4.0 * gp; w1 = J.C(G, q);
-            u2 = 4.0 * (gp + gq); w2 = J.S(G);
+            const V3 gp = v3(G + 3 * p), gq = v3(G + 3 * q);
+            u0 = 4.0 * gq; w0 = J.c1(p) * g1 + J.c2(p) * g2;
+            u1 = 4.0 * gp; w1 = J.c1(q) * g1 + J.c2(q) * g2;
+            u2 = 4.0 * (gp + gq); w2 = J.d1() * g1 + J.d2() * g2;
         }
     }
     __device__ __forceinline__ double g(int a, int b) const {
@@ -435,10 +443,31 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
             if (on && A.tgv > 0) {
                 if (A.val) acc[self * BS2 + lane * BS + lane] = A.tgv;
                 racc = A.tgv * (A.g ? A.g[dof] : 0.0);
+            } else if (on) {
+                racc = A.g ? A.g[dof] : 0.0;   // tgv < 0: b_i = g_i (tgv1 = 1, problem.cpp:9937)
             }
             if (A.rhs) A.rhs[dof] = racc;
         }
         __syncwarp();
+        // tgv < 0 (HashMatrix::SetBC, HashMatrix.cpp:1195-1238): Dirichlet rows get a unit
+        // diagonal (0 when tgv <= -10) and, except for -3/-30, zero off-diagonals; for
+        // -2/-20/-3/-30 the Dirichlet columns are zeroed too (the diagonal also for -20/-30).
+        if (A.val && A.onbc && A.tgv < 0) {
+            const double tgv = A.tgv;
+            const bool keep_row = fabs(tgv + 3.0) < 1e-10 || fabs(tgv + 30.0) < 1e-10;
+            const bool zero_col = fabs(tgv + 2.0) < 1e-10 || fabs(tgv + 20.0) < 1e-10 || fabs(tgv + 3.0) < 1e-10 ||
+                                  fabs(tgv + 30.0) < 1e-10;
+            for (int q = lane; q < deg * BS2; q += 32) {
+                const int k = q / BS2, r = (q % BS2) / BS, cp = q % BS;
+                const int col = cols[k];
+                const bool diag = col == a && r == cp;
+                double v = acc[q];
+                if (A.onbc[(int64_t)a * BS + r]) v = diag ? (tgv < -9.0 ? 0.0 : 1.0) : (keep_row ? v : 0.0);
+                if (zero_col && A.onbc[(int64_t)col * BS + cp] && (!diag || tgv < -19.0)) v = 0.0;
+                acc[q] = v;
+            }
+            __syncwarp();
+        }
         if (A.val)
             for (int q = lane; q < deg * BS2; q += 32) A.val[rb * BS2 + q] = acc[q];
         __syncwarp();
@@ -462,7 +491,7 @@ __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *in
         double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
         s += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
     }
-    if (onbc && onbc[t] && tgv > 0) s = tgv * (g ? g[t] : 0.0);
+    if (onbc && onbc[t]) s = (tgv > 0 ? tgv : 1.0) * (g ? g[t] : 0.0);
     rhs[t] = s;
 }
 
@@ -482,6 +511,70 @@ __global__ void export_csr_kernel(int nb, int bs, const int32_t *browptr, const 
             }
     }
     if (a == nb - 1) rowptr[(int64_t)nb * bs] = (int32_t)((int64_t)browptr[nb] * bs * bs);
+}
+
+// ------------------------------------------------------------------ on(labels): DOF marking
+// AssembleBC (problem.cpp:9881-10034) marks the DOFs of the boundary elements carrying one of
+// the labels.  On the device: (1) vertices of the selected boundary elements, (2) vertex nodes
+// of those vertices, (3) edge nodes whose two endpoints lie on one common selected boundary
+// element (scanning the vertex -> boundary-element incidence of one endpoint).
+__device__ __forceinline__ bool label_selected(int lab, int nlabels, const int32_t *labels) {
+    for (int k = 0; k < nlabels; ++k)
+        if (labels[k] == lab) return true;
+    return false;
+}
+
+__global__ void bmark_vertices_kernel(int nbe, int bdim, const int32_t *belems, const int32_t *blabel,
+                                      int nlabels, const int32_t *labels, uint8_t *vmark) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbe || !label_selected(blabel[b], nlabels, labels)) return;
+    for (int k = 0; k < bdim; ++k) vmark[belems[(int64_t)b * bdim + k]] = 1;
+}
+
+__device__ __forceinline__ void mark_node(uint8_t *onbc, int node, int bs, int comp_mask) {
+    for (int c = 0; c < bs; ++c)
+        if (comp_mask == 0 || (comp_mask >> c) & 1) onbc[(int64_t)node * bs + c] = 1;
+}
+
+template <int DIM>
+__global__ void bmark_nodes_kernel(int nt, int nn, const int32_t *elems, const int32_t *nodes, const uint8_t *vmark,
+                                   const int32_t *bv_ptr, const int32_t *bv_elem, const int32_t *belems,
+                                   const int32_t *blabel, int nlabels, const int32_t *labels, int bs,
+                                   int comp_mask, uint8_t *onbc) {
+    constexpr int NV = DIM + 1;
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nt * nn) return;
+    int e = (int)(t / nn), i = (int)(t % nn);
+    const int32_t *v = elems + (int64_t)e * NV;
+    if (i < NV) {
+        if (vmark[v[i]]) mark_node(onbc, nodes[t], bs, comp_mask);
+        return;
+    }
+    int p, q;
+    edge_vertices<DIM>(i - NV, p, q);
+    int a = v[p], b = v[q];
+    if (!vmark[a] || !vmark[b]) return;
+    for (int k = bv_ptr[a]; k < bv_ptr[a + 1]; ++k) {
+        int f = bv_elem[k];
+        if (!label_selected(blabel[f], nlabels, labels)) continue;
+        const int32_t *fv = belems + (int64_t)f * DIM;
+        bool has_b = false;
+        for (int j = 0; j < DIM; ++j) has_b |= fv[j] == b;
+        if (has_b) { mark_node(onbc, nodes[t], bs, comp_mask); return; }
+    }
+}
+
+__global__ void bcount_kernel(int nbe, int bdim, const int32_t *belems, int32_t *cnt) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < (int64_t)nbe * bdim) atomicAdd(&cnt[belems[t]], 1);
+}
+
+__global__ void bfill_kernel(int nbe, int bdim, const int32_t *belems, const int32_t *ptr, int32_t *cursor,
+                             int32_t *out) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nbe * bdim) return;
+    int v = belems[t];
+    out[ptr[v] + atomicAdd(&cursor[v], 1)] = (int32_t)(t / bdim);
 }
 
 __global__ void row_degree_kernel(int n, const int32_t *rp, int32_t *deg) {
@@ -504,6 +597,30 @@ __global__ void diagpos_kernel(int n, const int32_t *rp, const int32_t *col, int
 }
 
 static int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc) {
+    FFGPU_CHECK(S->belems, FFGPU_EINVAL, "on(labels): the space has no boundary elements (ffgpu_space_set_boundary)");
+    FFGPU_CHECK(nlabels > 0 && nlabels <= 64 && labels, FFGPU_EINVAL, "on(labels): 1..64 labels expected");
+    ffgpu_ctx *ctx = S->ctx;
+    cudaStream_t s = ctx->stream;
+    DevIn<int32_t> lab(labels, nlabels, s);
+    FFGPU_TRY(lab.err);
+    FFGPU_CUDA(cudaMemsetAsync(S->vmark, 0, S->nv, s));
+    FFGPU_CUDA(cudaMemsetAsync(onbc, 0, S->ndof, s));
+    bmark_vertices_kernel<<<grid_for(S->nbe, 256), 256, 0, s>>>(S->nbe, S->dim, S->belems, S->blabel, nlabels,
+                                                                 lab.d, S->vmark);
+    FFGPU_TRY(launch_check(ctx, "bmark_vertices"));
+    int64_t m = (int64_t)S->nt * S->nn;
+    if (S->dim == 2)
+        bmark_nodes_kernel<2><<<grid_for(m, 256), 256, 0, s>>>(S->nt, S->nn, S->elems, S->nodes, S->vmark, S->bv_ptr,
+                                                               S->bv_elem, S->belems, S->blabel, nlabels, lab.d,
+                                                               S->bs, comp_mask, onbc);
+    else
+        bmark_nodes_kernel<3><<<grid_for(m, 256), 256, 0, s>>>(S->nt, S->nn, S->elems, S->nodes, S->vmark, S->bv_ptr,
+                                                               S->bv_elem, S->belems, S->blabel, nlabels, lab.d,
+                                                               S->bs, comp_mask, onbc);
+    return launch_check(ctx, "bmark_nodes");
+}
 
 }  // namespace ffgpu
 
@@ -563,6 +680,12 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, ctx->stream);
     DevOut<double> rh(rhs, rhs ? S->ndof : 0, ctx->stream, false);
     FFGPU_TRY(fP0.err); FFGPU_TRY(onbc.err); FFGPU_TRY(gv.err); FFGPU_TRY(rh.err);
+    const uint8_t *mask = onbc.d;
+    if (bc && !bc->onbc && bc->nlabels > 0) {
+        if (!M->bcmask) FFGPU_CUDA(cudaMalloc((void **)&M->bcmask, S->ndof));
+        FFGPU_TRY(space_bc_mask_device(S, bc->nlabels, bc->labels, bc->comp_mask, M->bcmask));
+        mask = M->bcmask;
+    }
     FillArgs fa;
     memset(&fa, 0, sizeof(fa));
     fa.nnodes = S->nnodes; fa.nt = S->nt;
@@ -577,7 +700,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
         fa.mu = v->E / (2 * (1 + v->nu));
         fa.lam = v->E * v->nu / ((1 + v->nu) * (1 - 2 * v->nu));
     }
-    fa.onbc = onbc.d; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
+    fa.onbc = mask; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
     FFGPU_TRY(fill_launch(S, fa));
     FFGPU_TRY(check_device_status(ctx, "assembly"));
@@ -586,6 +709,8 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     M->ntgv = -1;
     if (M->val_t) { cudaFree(M->val_t); M->val_t = nullptr; }
     if (M->val32) { cudaFree(M->val32); M->val32 = nullptr; }
+    if (M->valx) { cudaFree(M->valx); M->valx = nullptr; }
+    if (M->valx_t) { cudaFree(M->valx_t); M->valx_t = nullptr; }
     return FFGPU_OK;
 }
 
@@ -676,7 +801,64 @@ int ffgpu_space_destroy(ffgpu_space *S) {
     cudaStreamSynchronize(S->ctx->stream);
     cudaFree(S->coords); cudaFree(S->elems); cudaFree(S->nodes);
     cudaFree(S->inc_ptr); cudaFree(S->inc_elem); cudaFree(S->inc_loc);
+    cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
     delete S;
+    return FFGPU_OK;
+}
+
+int ffgpu_space_set_boundary(ffgpu_space *S, int nbe, const int32_t *belems, const int32_t *blabel) {
+    FFGPU_CHECK(S && nbe > 0 && belems && blabel, FFGPU_EINVAL, "ffgpu_space_set_boundary: bad argument");
+    ffgpu_ctx *ctx = S->ctx;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int bdim = S->dim;   // vertices per boundary element
+    cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
+    S->belems = S->blabel = S->bv_ptr = S->bv_elem = nullptr;
+    S->vmark = nullptr;
+    S->nbe = nbe;
+    int32_t *cnt = nullptr;
+    if (cudaMalloc((void **)&S->belems, sizeof(int32_t) * nbe * bdim) ||
+        cudaMalloc((void **)&S->blabel, sizeof(int32_t) * nbe) ||
+        cudaMalloc((void **)&S->bv_ptr, sizeof(int32_t) * (S->nv + 1)) ||
+        cudaMalloc((void **)&S->bv_elem, sizeof(int32_t) * nbe * bdim) ||
+        cudaMalloc((void **)&S->vmark, S->nv) ||
+        cudaMalloc((void **)&cnt, sizeof(int32_t) * (S->nv + 1))) {
+        set_error("ffgpu_space_set_boundary: device allocation failed");
+        cudaFree(cnt);
+        return FFGPU_ENOMEM;
+    }
+    FFGPU_CUDA(cudaMemcpyAsync(S->belems, belems, sizeof(int32_t) * nbe * bdim, cudaMemcpyDefault, s));
+    FFGPU_CUDA(cudaMemcpyAsync(S->blabel, blabel, sizeof(int32_t) * nbe, cudaMemcpyDefault, s));
+    check_elems_kernel<<<grid_for((int64_t)nbe * bdim, 256), 256, 0, s>>>(S->belems, (int64_t)nbe * bdim, S->nv,
+                                                                           ctx->d_status);
+    FFGPU_TRY(launch_check(ctx, "check_belems"));
+    int rc = check_device_status(ctx, "ffgpu_space_set_boundary");
+    if (!rc) {
+        cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (S->nv + 1), s);
+        bcount_kernel<<<grid_for((int64_t)nbe * bdim, 256), 256, 0, s>>>(nbe, bdim, S->belems, cnt);
+        rc = launch_check(ctx, "bcount");
+    }
+    if (!rc) rc = device_scan_i32(ctx, cnt, S->bv_ptr, S->nv);
+    if (!rc) {
+        cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (S->nv + 1), s);
+        bfill_kernel<<<grid_for((int64_t)nbe * bdim, 256), 256, 0, s>>>(nbe, bdim, S->belems, S->bv_ptr, cnt,
+                                                                         S->bv_elem);
+        rc = launch_check(ctx, "bfill");
+    }
+    cudaFreeAsync(cnt, s);
+    if (!rc && cudaStreamSynchronize(s) != cudaSuccess) { set_error("ffgpu_space_set_boundary failed"); rc = FFGPU_ECUDA; }
+    return rc;
+}
+
+int ffgpu_space_bc_mask(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc) {
+    FFGPU_CHECK(S && onbc, FFGPU_EINVAL, "ffgpu_space_bc_mask: NULL argument");
+    cudaStream_t s = S->ctx->stream;
+    FFGPU_CUDA(cudaSetDevice(S->ctx->device));
+    DevOut<uint8_t> m(onbc, S->ndof, s, false);
+    FFGPU_TRY(m.err);
+    FFGPU_TRY(space_bc_mask_device(S, nlabels, labels, comp_mask, m.d));
+    FFGPU_TRY(m.finish(s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }
 
@@ -757,6 +939,13 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
         DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, s);
         DevOut<double> rh(rhs, S->ndof, s, false);
         if (!rc) rc = fP0.err ? fP0.err : (onbc.err ? onbc.err : (gv.err ? gv.err : rh.err));
+        uint8_t *lmask = nullptr;
+        const uint8_t *mask = onbc.d;
+        if (!rc && bc && !bc->onbc && bc->nlabels > 0) {
+            if (cudaMallocAsync((void **)&lmask, S->ndof, s) != cudaSuccess) rc = FFGPU_ENOMEM;
+            if (!rc) rc = space_bc_mask_device(S, bc->nlabels, bc->labels, bc->comp_mask, lmask);
+            mask = lmask;
+        }
         if (!rc) {
             void (*k)(int, const int32_t *, const int32_t *, const uint8_t *, const double *,
                       const double *, double, double, double, const uint8_t *, const double *,
@@ -768,10 +957,11 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
             if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) k = rhs_kernel<3, 3>;
             k<<<grid_for((int64_t)S->ndof, 256), 256, 0, s>>>(
                 S->nnodes, S->inc_ptr, S->inc_elem, S->inc_loc, geo, fP0.d, v->f_const[0],
-                v->f_const[1], v->f_const[2], onbc.d, gv.d, bc ? bc->tgv : 0.0, rh.d);
+                v->f_const[1], v->f_const[2], mask, gv.d, bc ? bc->tgv : 0.0, rh.d);
             rc = launch_check(ctx, "rhs_kernel");
         }
         if (!rc) rc = rh.finish(s);
+        if (lmask) cudaFreeAsync(lmask, s);
     }
     cudaFreeAsync(geo, s);
     cudaStreamSynchronize(s);
@@ -830,9 +1020,9 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     cudaStreamSynchronize(M->ctx->stream);
     if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
     cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->diagpos); cudaFree(M->rowperm); cudaFree(M->val);
-    cudaFree(M->geo);
+    cudaFree(M->geo); cudaFree(M->bcmask);
     cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
-    cudaFree(M->val32); cudaFree(M->ks);
+    cudaFree(M->val32); cudaFree(M->valx); cudaFree(M->valx_t); cudaFree(M->hx); cudaFree(M->ks);
     delete M;
     return FFGPU_OK;
 }

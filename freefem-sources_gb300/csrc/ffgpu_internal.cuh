@@ -73,7 +73,7 @@ struct ffgpu_ctx {
     unsigned int *d_ticket;     // last-block counters
     int *d_iscratch;            // small integer scratch (max reductions)
     // SpMV lanes-per-row chosen by timing, per matrix shape (nb, nnzb, bs)
-    struct Tuned { int64_t nb, nnzb; int bs, lanes; } tuned[32];
+    struct Tuned { int64_t nb, nnzb; int bs, lanes, mode; } tuned[32];
     int ntuned;
 };
 
@@ -87,6 +87,10 @@ struct ffgpu_space {
     int32_t *inc_elem;   // node -> incident elements, ascending
     uint8_t *inc_loc;    // local index of the node in that element
     int max_inc;
+    // boundary elements (for on(labels)): nbe x dim vertices, labels, vertex -> element CSR
+    int nbe;
+    int32_t *belems, *blabel, *bv_ptr, *bv_elem;
+    uint8_t *vmark;       // scratch: vertex on a selected boundary element (nv)
 };
 
 struct ffgpu_matrix {
@@ -101,6 +105,7 @@ struct ffgpu_matrix {
     int32_t *rowperm;     // nb: block rows by decreasing degree (stable), the SpMV's row order
     double *val;          // nnzb*bs*bs, each block row-major
     double *geo;          // per-element geometry cache (16 doubles per element)
+    uint8_t *bcmask;      // on(labels) DOF mask computed on the device (ndof)
     // solver state (lazily allocated)
     double *diag_inv;     // Jacobi 1/A_ii (1 if tiny)
     uint8_t *wcl;         // tgv rows found by gettgv
@@ -109,13 +114,16 @@ struct ffgpu_matrix {
     double *vec;          // work vectors (8*n)
     double *val_t;        // transpose values (same pattern), built on demand
     float *val32;         // FP32 copy for the mixed-precision inner solve
+    float2 *valx, *valx_t;  // exact hi/lo FP32 splits of val (and of val_t) for the double-float SpMV
+    float2 *hx;           // split copy of the CG search vector
     ffgpu::KrylovScalars *ks;
     // cached CG graph
     cudaGraphExec_t cg_exec;
-    int cg_unroll, cg_trans;
+    int cg_unroll, cg_trans, cg_mode;
     int cg_kernels_init, cg_kernels_body;
     // tuning
-    int csr_lanes;        // lanes per row of the bs=1 SpMV
+    int csr_lanes;        // lanes per block row of the FP64 SpMV (tuned)
+    int csr_lanes_x;      // lanes per block row of the double-float SpMV (tuned)
 };
 
 namespace ffgpu {
@@ -184,10 +192,13 @@ int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n);  //
 int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
 // order[0..n): indices sorted by decreasing key (0 <= key <= maxkey), ties by increasing index
 int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order);
+// on(labels) DOF mask on the device (onbc: ndof bytes, device)
+int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 
 // matrix-level operations shared by the solvers
 int matrix_prepare_solver(ffgpu_matrix *A);
 int matrix_prepare_transpose(ffgpu_matrix *A);
+int matrix_prepare_split(ffgpu_matrix *A, int trans);
 int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t s);
 
 // -------------------------------------------------------------------- device helpers

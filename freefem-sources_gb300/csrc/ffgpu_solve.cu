@@ -13,6 +13,7 @@
 // a CUDA graph `while` node whose condition K_b clears on convergence or at itmax, so a
 // whole solve is one graph launch with no host round trip.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -182,10 +183,10 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
 __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
                                                      const double *__restrict__ h, const double *__restrict__ q,
                                                      const double *__restrict__ dinv, KrylovScalars *ks,
-                                                     double *part, cudaGraphConditionalHandle cond) {
+                                                     double *part, cudaGraphConditionalHandle cond, int in_graph) {
     __shared__ double sh[32];
     if (ks->done) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0);
+        if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0);
         return;
     }
     const double rho = ks->rho;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         ks->iter += 1;
         if (tot < ks->eps2) { ks->converged = 1; ks->done = 1; }
         else if (ks->iter >= ks->itmax) ks->done = 1;
-        if (ks->done) cudaGraphSetConditional(cond, 0);
+        if (ks->done && in_graph) cudaGraphSetConditional(cond, 0);
     }
 }
 
@@ -227,6 +228,157 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc(int n, const double *__rest
     double tot;
     double p = block_sum(s, sh);
     if (last_block_total(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
+}
+
+// ------------------------------------------------------------------ double-float SpMV
+// FP64 values and vectors, products formed on the FP32 pipe with error-free transformations:
+// a = a_hi + a_lo and x = x_hi + x_lo are exact FP32 splits (to 48 of the 53 bits), a_hi x_hi
+// is formed exactly as p + e with e = fma(a_hi, x_hi, -p), the cross terms a_hi x_lo + a_lo x_hi
+// are added in FP32, and the sums are kept as an unevaluated pair (S, C) with TwoSum.  The row
+// result is (double)S + (double)C, about 2^-44 relative; GB300 issues 64 FP32 FMAs per FP64
+// FMA, so this moves the SpMV from the FP64 pipe bound to the HBM bound.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void df_fma(float2 a, float2 x, float &S, float &C) {
+    float p = __fmul_rn(a.x, x.x);
+    float pe = __fmaf_rn(a.x, x.x, -p);
+    float t = __fmaf_rn(a.x, x.y, __fmaf_rn(a.y, x.x, pe));
+    float s2, e;
+    two_sum(S, p, s2, e);
+    S = s2;
+    C = __fadd_rn(C, __fadd_rn(e, t));
+}
+
+__device__ __forceinline__ void df_add_shfl(float &S, float &C, int o) {
+    float S2 = __shfl_xor_sync(0xffffffffu, S, o), C2 = __shfl_xor_sync(0xffffffffu, C, o);
+    float s2, e;
+    two_sum(S, S2, s2, e);
+    S = s2;
+    C = __fadd_rn(__fadd_rn(C, C2), e);
+}
+
+__device__ __forceinline__ float2 split_f64(double v) {
+    float hi = __double2float_rn(v);
+    float lo = __double2float_rn(v - (double)hi);
+    return make_float2(hi, lo);
+}
+
+__global__ void split_kernel(int64_t n, const double *__restrict__ v, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = split_f64(v[i]);
+}
+
+struct SpmvArgsX {
+    int nb, bs;
+    const int32_t *rp, *col;
+    const float2 *val;
+    const int32_t *perm;
+};
+
+template <int T>
+__device__ __forceinline__ double csr_row_x(const SpmvArgsX &A, const float2 *__restrict__ x, int r, int sub) {
+    int b = __ldg(A.rp + r), e = __ldg(A.rp + r + 1);
+    float S = 0.f, C = 0.f;
+    for (int k = b + sub; k < e; k += T) {
+        float2 a = A.val[k];
+        float2 xv = x[__ldg(A.col + k)];
+        df_fma(a, xv, S, C);
+    }
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) df_add_shfl(S, C, o);
+    return (double)S + (double)C;
+}
+
+template <int T>
+__device__ __forceinline__ void bsr3_row_x(const SpmvArgsX &A, const float2 *__restrict__ x, int a, int sub,
+                                           double y[3]) {
+    int b = __ldg(A.rp + a), e = __ldg(A.rp + a + 1);
+    float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
+    for (int k = b + sub; k < e; k += T) {
+        int c = __ldg(A.col + k);
+        const float2 *v = A.val + (int64_t)k * 9;
+        float2 x0 = x[3 * (int64_t)c], x1 = x[3 * (int64_t)c + 1], x2 = x[3 * (int64_t)c + 2];
+        df_fma(v[0], x0, S0, C0); df_fma(v[1], x1, S0, C0); df_fma(v[2], x2, S0, C0);
+        df_fma(v[3], x0, S1, C1); df_fma(v[4], x1, S1, C1); df_fma(v[5], x2, S1, C1);
+        df_fma(v[6], x0, S2, C2); df_fma(v[7], x1, S2, C2); df_fma(v[8], x2, S2, C2);
+    }
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) {
+        df_add_shfl(S0, C0, o);
+        df_add_shfl(S1, C1, o);
+        df_add_shfl(S2, C2, o);
+    }
+    y[0] = (double)S0 + (double)C0;
+    y[1] = (double)S1 + (double)C1;
+    y[2] = (double)S2 + (double)C2;
+}
+
+// K_a with the double-float SpMV: AH = A H from the split H, (H, AH) in FP64
+template <int BS, int T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const float2 *__restrict__ hx,
+                                                           const double *__restrict__ h, double *__restrict__ q,
+                                                           KrylovScalars *ks, double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const int lane = threadIdx.x & 31;
+    const int gsub = lane / T, sub = lane % T;
+    const int groups = (blockDim.x / 32) * (32 / T);
+    int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
+    double hq = 0;
+    for (int base = 0; base < A.nb; base += gridDim.x * groups) {
+        const int slot = base + g;
+        const bool ok = slot < A.nb;
+        const int a = ok ? __ldg(A.perm + slot) : 0;
+        if (BS == 1) {
+            double s = csr_row_x<T>(A, hx, a, ok ? sub : T);
+            if (ok && sub == 0) { q[a] = s; hq = fma(h[a], s, hq); }
+        } else {
+            double v[3];
+            bsr3_row_x<T>(A, hx, a, ok ? sub : T, v);
+            if (ok && sub == 0) {
+                int64_t i = 3 * (int64_t)a;
+                q[i] = v[0]; q[i + 1] = v[1]; q[i + 2] = v[2];
+                hq = fma(h[i], v[0], hq);
+                hq = fma(h[i + 1], v[1], hq);
+                hq = fma(h[i + 2], v[2], hq);
+            }
+        }
+    }
+    double tot;
+    double p = block_sum(hq, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
+        ks->s_hq = tot;
+        ks->rho = -ks->s_gh / tot;
+    }
+}
+
+// K_c that also refreshes the split copy of H for the next double-float SpMV
+__global__ void __launch_bounds__(kVecThreads) cg_kc_x(int n, const double *__restrict__ g, double *__restrict__ h,
+                                                       float2 *__restrict__ hx, const double *__restrict__ dinv,
+                                                       KrylovScalars *ks, double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const double gamma = ks->gamma;
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double gi = g[i];
+        double hi = gamma * h[i] - dinv[i] * gi;
+        h[i] = hi;
+        hx[i] = split_f64(hi);
+        s = fma(gi, hi, s);
+    }
+    double tot;
+    double p = block_sum(s, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
+}
+
+__global__ void split_vec_kernel(int n, const double *__restrict__ h, float2 *__restrict__ hx) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        hx[i] = split_f64(h[i]);
 }
 
 // init: x_i = b_i/tgv on tgv rows (done before the SpMV), then with G = A x:
@@ -391,6 +543,18 @@ static void *ka_fn(int T) {
     }
 }
 
+template <int BS>
+static void *kax_fn(int T) {
+    switch (T) {
+        case 1: return (void *)cg_ka_x<BS, 1>;
+        case 2: return (void *)cg_ka_x<BS, 2>;
+        case 4: return (void *)cg_ka_x<BS, 4>;
+        case 8: return (void *)cg_ka_x<BS, 8>;
+        case 16: return (void *)cg_ka_x<BS, 16>;
+        default: return (void *)cg_ka_x<BS, 32>;
+    }
+}
+
 static int spmv_grid(const ffgpu_matrix *A, int T) {
     int groups = kSpmvWarps * (32 / T);
     int need = (A->nb + groups - 1) / groups;
@@ -405,30 +569,47 @@ static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
     return s;
 }
 
-// Times the SpMV with each candidate lanes-per-row on this matrix (once per shape and context).
-static int tune_lanes(ffgpu_matrix *A) {
-    if (A->csr_lanes > 0) return FFGPU_OK;
+// Times the SpMV kernel of one mode (0: FP64, 1: double-float) with each candidate
+// lanes-per-row on this matrix; the choice is cached per matrix shape in the context.
+static int tune_lanes(ffgpu_matrix *A, int mode) {
+    int *slot = mode == 1 ? &A->csr_lanes_x : &A->csr_lanes;
+    if (*slot > 0) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
     for (int i = 0; i < ctx->ntuned; ++i)
-        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs) {
-            A->csr_lanes = ctx->tuned[i].lanes;
+        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs &&
+            ctx->tuned[i].mode == mode) {
+            *slot = ctx->tuned[i].lanes;
             return FFGPU_OK;
         }
-    if (!A->vec) { A->csr_lanes = pick_lanes(A); return FFGPU_OK; }
-    const int cands[] = {2, 4, 8, 16};
-    double *x = A->vec + 5 * (int64_t)A->n, *y = A->vec + 6 * (int64_t)A->n;
+    if (!A->vec || (mode == 1 && !A->valx)) { *slot = pick_lanes(A); return FFGPU_OK; }
+    // FP64: reductions across lanes cost FP64 adds, so few lanes per row; double-float:
+    // reductions are FP32, so wide lane groups with coalesced block runs
+    const int cands64[] = {1, 2, 4, 8};
+    const int candsx[] = {4, 8, 16, 32};
+    const int *cands = mode == 1 ? candsx : cands64;
+    double *y = A->vec + 6 * (int64_t)A->n, *x = A->vec + 5 * (int64_t)A->n;
     cudaStream_t s = ctx->stream;
     FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
+    if (mode == 1) FFGPU_CUDA(cudaMemsetAsync(A->hx, 0, sizeof(float2) * A->n, s));
+    KrylovScalars *ks = A->ks;
+    FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+    double *part = ctx->d_part;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
     int bestT = pick_lanes(A);
     SpmvArgs sa = spmv_args(A, 0);
-    for (int T : cands) {
-        if (A->bs == 3 && T > 8) continue;
-        void *fn = A->bs == 3 ? spmv_fn<3>(T) : spmv_fn<1>(T);
-        void *args[] = {&sa, &x, &y};
+    SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, A->valx, A->rowperm};
+    float2 *hx = A->hx;
+    for (int c = 0; c < 4; ++c) {
+        int T = cands[c];
+        void *fn;
+        void *args64[] = {&sa, &x, &y};
+        void *argsx[] = {&sx, &hx, &x, &y, &ks, &part};
+        void **args = mode == 1 ? argsx : args64;
+        if (mode == 1) fn = A->bs == 3 ? kax_fn<3>(T) : kax_fn<1>(T);
+        else fn = A->bs == 3 ? spmv_fn<3>(T) : spmv_fn<1>(T);
         cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);   // warm
         cudaEventRecord(e0, s);
         for (int r = 0; r < 3; ++r) cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);
@@ -441,8 +622,9 @@ static int tune_lanes(ffgpu_matrix *A) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    A->csr_lanes = bestT;
-    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT};
+    FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+    *slot = bestT;
+    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT, mode};
     return FFGPU_OK;
 }
 
@@ -454,6 +636,17 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
     void *args[] = {&s, &x, &y};
     FFGPU_CUDA(cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, st));
     return launch_check(A->ctx, "spmv");
+}
+
+int matrix_prepare_split(ffgpu_matrix *A, int trans) {
+    ffgpu_ctx *ctx = A->ctx;
+    if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * A->n));
+    float2 **dst = trans ? &A->valx_t : &A->valx;
+    if (*dst) return FFGPU_OK;
+    if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
+    FFGPU_CUDA(cudaMalloc((void **)dst, sizeof(float2) * A->nnz));
+    split_kernel<<<8 * kNumSM, 256, 0, ctx->stream>>>(A->nnz, trans ? A->val_t : A->val, *dst);
+    return launch_check(ctx, "split");
 }
 
 int matrix_prepare_transpose(ffgpu_matrix *A) {
@@ -477,7 +670,7 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
         FFGPU_CUDA(cudaMalloc((void **)&A->ks, sizeof(KrylovScalars)));
         FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
     }
-    FFGPU_TRY(tune_lanes(A));
+    FFGPU_TRY(tune_lanes(A, 0));
     if (A->ntgv >= 0) return FFGPU_OK;
     unsigned long long *bits = (unsigned long long *)ctx->d_iscratch;   // [0] max, [1] max1
     int *cnt = ctx->d_iscratch + 4;
@@ -508,8 +701,8 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
 }
 
 // Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }].
-static int cg_graph(ffgpu_matrix *A, int trans, int unroll, double *x, double *g, double *h, double *q) {
-    if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans) return FFGPU_OK;
+static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x, double *g, double *h, double *q) {
+    if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans && A->cg_mode == mode) return FFGPU_OK;
     if (A->cg_exec) { cudaGraphExecDestroy(A->cg_exec); A->cg_exec = nullptr; }
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
@@ -530,17 +723,29 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, double *x, double *g
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int T = pick_lanes(A);
+    const int TX = A->csr_lanes_x > 0 ? A->csr_lanes_x : T;
     SpmvArgs sa = spmv_args(A, trans);
     void *ka = A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T);
     int n = A->n;
     KrylovScalars *ks = A->ks;
     double *part = ctx->d_part;
     const double *dinv = A->diag_inv;
+    SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, trans ? A->valx_t : A->valx, A->rowperm};
+    void *kax = A->bs == 3 ? kax_fn<3>(TX) : kax_fn<1>(TX);
+    float2 *hx = A->hx;
     for (int u = 0; u < unroll; ++u) {
-        void *aa[] = {&sa, &h, &q, &ks, &part};
-        cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
-        cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond);
-        cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, dinv, ks, part);
+        if (mode == 1) {
+            void *aa[] = {&sx, &hx, &h, &q, &ks, &part};
+            cudaLaunchKernel(kax, spmv_grid(A, TX), kSpmvWarps * 32, aa, 0, s);
+        } else {
+            void *aa[] = {&sa, &h, &q, &ks, &part};
+            cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
+        }
+        cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, 1);
+        if (mode == 1)
+            cg_kc_x<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
+        else
+            cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, dinv, ks, part);
     }
     cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e != cudaSuccess) {
@@ -557,6 +762,7 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, double *x, double *g
     }
     A->cg_unroll = unroll;
     A->cg_trans = trans;
+    A->cg_mode = mode;
     A->cg_kernels_body = 3 * unroll;
     return FFGPU_OK;
 }
@@ -575,7 +781,12 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
     int itmax = prm->itmax > 0 ? prm->itmax : n;
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
-    FFGPU_TRY(cg_graph(A, trans, unroll, x, g, h, q));
+    const int mode = prm->spmv_mode == 1 ? 1 : 0;
+    if (mode == 1) {
+        FFGPU_TRY(matrix_prepare_split(A, trans));
+        FFGPU_TRY(tune_lanes(A, 1));
+    }
+    FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
     FFGPU_CUDA(cudaMemcpyAsync(x, xu, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -588,7 +799,47 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     FFGPU_TRY(spmv(A, x, g, trans, s));
     cg_init<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, b, h, A->diag_inv, A->ks, prm->eps, itmax, ctx->d_part);
     FFGPU_TRY(launch_check(ctx, "cg_init"));
-    FFGPU_CUDA(cudaGraphLaunch(A->cg_exec, s));
+    if (mode == 1) {
+        split_vec_kernel<<<kVecBlocks, kVecThreads, 0, s>>>(n, h, A->hx);
+        FFGPU_TRY(launch_check(ctx, "split_vec"));
+    }
+    const char *ge = getenv("FFGPU_CG_GRAPH");
+    int bodies_host = -1;
+    if (ge && ge[0] == '0') {
+        // Same kernels launched from the host (for profilers that do not trace conditional
+        // graph nodes): poll the done flag after every `unroll` iterations.
+        int T = mode == 1 ? (A->csr_lanes_x > 0 ? A->csr_lanes_x : pick_lanes(A)) : pick_lanes(A);
+        SpmvArgs sa = spmv_args(A, trans);
+        SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, trans ? A->valx_t : A->valx, A->rowperm};
+        void *ka = mode == 1 ? (A->bs == 3 ? kax_fn<3>(T) : kax_fn<1>(T)) : (A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T));
+        KrylovScalars *ks = A->ks;
+        double *part = ctx->d_part;
+        float2 *hx = A->hx;
+        bodies_host = 0;
+        for (int it = 0; it <= itmax; it += unroll) {
+            for (int u = 0; u < unroll; ++u) {
+                if (mode == 1) {
+                    void *aa[] = {&sx, &hx, &h, &q, &ks, &part};
+                    cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
+                } else {
+                    void *aa[] = {&sa, &h, &q, &ks, &part};
+                    cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
+                }
+                cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, A->diag_inv, ks, part, 0, 0);
+                if (mode == 1)
+                    cg_kc_x<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, hx, A->diag_inv, ks, part);
+                else
+                    cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, A->diag_inv, ks, part);
+            }
+            ++bodies_host;
+            int done = 0;
+            FFGPU_CUDA(cudaMemcpyAsync(&done, &ks->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FFGPU_CUDA(cudaStreamSynchronize(s));
+            if (done) break;
+        }
+    } else {
+        FFGPU_CUDA(cudaGraphLaunch(A->cg_exec, s));
+    }
     FFGPU_CUDA(cudaMemcpyAsync(xu, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEventRecord(e1, s);
     KrylovScalars hk;
@@ -598,7 +849,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int bodies = hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll;
+    int bodies = bodies_host >= 0 ? bodies_host : (hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll);
     ctx->launches += (int64_t)bodies * A->cg_kernels_body;
     if (st) {
         st->iterations = hk.iter;

@@ -20,7 +20,7 @@ FORM_DIFFUSION, FORM_ELASTICITY = 0, 1
 EXPORTS = [
     "ffgpu_ctx_create", "ffgpu_ctx_destroy", "ffgpu_last_error", "ffgpu_ctx_kernel_launches",
     "ffgpu_ctx_stream",
-    "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
+    "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_space_set_boundary", "ffgpu_space_bc_mask", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
@@ -37,12 +37,13 @@ class Varf(C.Structure):
 
 
 class BC(C.Structure):
-    _fields_ = [("onbc", C.c_void_p), ("g", C.c_void_p), ("tgv", C.c_double)]
+    _fields_ = [("onbc", C.c_void_p), ("g", C.c_void_p), ("tgv", C.c_double), ("nlabels", C.c_int),
+                ("labels", C.c_void_p), ("comp_mask", C.c_int)]
 
 
 class SolverParams(C.Structure):
     _fields_ = [("eps", C.c_double), ("itmax", C.c_int), ("dim_krylov", C.c_int),
-                ("tgv", C.c_double), ("verb", C.c_int), ("unroll", C.c_int)]
+                ("tgv", C.c_double), ("verb", C.c_int), ("unroll", C.c_int), ("spmv_mode", C.c_int)]
 
 
 class SolverStats(C.Structure):
@@ -82,6 +83,8 @@ def lib():
         "ffgpu_ctx_stream": (vp, [vp]),
         "ffgpu_space_create": (i32, [vp, i32, i32, vp, i32, vp, i32, i32, vp, i32, P(vp)]),
         "ffgpu_space_destroy": (i32, [vp]),
+        "ffgpu_space_set_boundary": (i32, [vp, i32, vp, vp]),
+        "ffgpu_space_bc_mask": (i32, [vp, i32, vp, i32, vp]),
         "ffgpu_matrix_assemble": (i32, [vp, P(Varf), P(BC), vp, P(vp)]),
         "ffgpu_matrix_reassemble": (i32, [vp, P(Varf), P(BC), vp]),
         "ffgpu_rhs_assemble": (i32, [vp, P(Varf), P(BC), vp]),

@@ -68,7 +68,8 @@ def fespace(Th: Mesh, kind: str, dof=None) -> FESpace:
 class DeviceSpace:
     """Mesh + FE space resident on the GPU (ffgpu_space_create)."""
 
-    def __init__(self, Vh: FESpace, device: int = 0, coords=None, elems=None, dof=None):
+    def __init__(self, Vh: FESpace, device: int = 0, coords=None, elems=None, dof=None, boundary=True,
+                 belems=None, blabel=None):
         self.Vh = Vh
         Th = Vh.Th
         self.device = device
@@ -81,6 +82,21 @@ class DeviceSpace:
         check(lib().ffgpu_space_create(context(device), Th.dim, Th.nv, _ptr(X), Th.nt, _ptr(E),
                                        Vh.fe, Vh.ndofK, _ptr(D), Vh.ndof, C.byref(h)))
         self.h = h
+        self.has_boundary = False
+        if boundary and Th.nbe > 0:
+            be = belems if belems is not None else np.ascontiguousarray(Th.belems, np.int32)
+            bl = blabel if blabel is not None else np.ascontiguousarray(Th.blabel, np.int32)
+            self._keep += [be, bl]
+            check(lib().ffgpu_space_set_boundary(h, Th.nbe, _ptr(be), _ptr(bl)))
+            self.has_boundary = True
+
+    def bc_mask(self, labels, components=None):
+        """The on(labels) DOF mask as the device assembly computes it (host uint8 array)."""
+        lab = np.ascontiguousarray(np.atleast_1d(labels), np.int32)
+        cm = 0 if components is None else sum(1 << c for c in components)
+        out = np.empty(self.Vh.ndof, np.uint8)
+        check(lib().ffgpu_space_bc_mask(self.h, lab.size, _ptr(lab), cm, _ptr(out)))
+        return out
 
     def close(self):
         if getattr(self, "h", None):
@@ -141,12 +157,27 @@ class VarForm:
                 v.f = _ptr(fa).value
         return v
 
-    def c_bc(self, Vh: FESpace) -> BC:
+    def c_bc(self, Vh: FESpace, device_marking: bool = False) -> BC:
+        """on(labels): with device_marking the assembly marks the DOFs on the device from the
+        space's boundary elements; otherwise the host mask FESpace.on is passed."""
         bc = BC()
         bc.tgv = self.tgv
         bc.onbc = None
         bc.g = None
-        if self.on:
+        bc.nlabels = 0
+        bc.labels = None
+        bc.comp_mask = 0
+        if self.on and device_marking:
+            lab = np.ascontiguousarray(self.on, np.int32)
+            self._keep.append(lab)
+            bc.nlabels = lab.size
+            bc.labels = _ptr(lab).value
+            bc.comp_mask = 0 if self.components is None else sum(1 << c for c in self.components)
+            if self.g is not None:
+                g = np.ascontiguousarray(self.g, np.float64)
+                self._keep.append(g)
+                bc.g = _ptr(g).value
+        elif self.on:
             m = Vh.on(self.on, self.components)
             self._keep.append(m)
             bc.onbc = _ptr(m).value
@@ -200,8 +231,9 @@ class Matrix:
         except Exception:
             pass
 
-    def params(self, eps=None, itmax=None, unroll=8) -> SolverParams:
+    def params(self, eps=None, itmax=None, unroll=8, spmv_mode=0) -> SolverParams:
         p = SolverParams()
+        p.spmv_mode = spmv_mode
         p.eps = self.eps if eps is None else eps
         p.itmax = self.itmax if itmax is None else itmax
         p.dim_krylov = self.dim_krylov
@@ -210,7 +242,8 @@ class Matrix:
         p.unroll = unroll
         return p
 
-    def solve(self, b, x0=None, trans=False, solver=None, eps=None, itmax=None, out=None, unroll=8):
+    def solve(self, b, x0=None, trans=False, solver=None, eps=None, itmax=None, out=None, unroll=8,
+              spmv_mode=0):
         """u[] = A^-1*b (A'^-1*b when trans).  x0 is the initial guess (FreeFEM: u[] before)."""
         solver = (solver or self.solver).upper()
         dev_in = hasattr(b, "data_ptr")
@@ -225,7 +258,7 @@ class Matrix:
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
         nrhs = int(np.prod(np.shape(b))) // self.n
         st = SolverStats()
-        p = self.params(eps, itmax, unroll)
+        p = self.params(eps, itmax, unroll, spmv_mode)
         fn = lib().ffgpu_solve_cg if solver == "CG" else lib().ffgpu_solve_gmres
         if solver not in ("CG", "GMRES"):
             raise ValueError(f"solver {solver!r}: the device path provides CG and GMRES")
@@ -282,7 +315,7 @@ class Matrix:
     def reassemble(self, varf: VarForm, rhs_out=None):
         Vh = self.space.Vh
         v = varf.c_varf(Vh)
-        bc = varf.c_bc(Vh)
+        bc = varf.c_bc(Vh, device_marking=self.space.has_boundary)
         check(lib().ffgpu_matrix_reassemble(self.h, C.byref(v), C.byref(bc), _ptr(rhs_out)))
         return rhs_out
 
@@ -294,7 +327,7 @@ def matrix(varf: VarForm, Vh, solver="CG", eps=1e-6, itmax=0, dim_krylov=50, rhs
     space = Vh if isinstance(Vh, DeviceSpace) else DeviceSpace(Vh, device)
     V = space.Vh
     v = varf.c_varf(V)
-    bc = varf.c_bc(V)
+    bc = varf.c_bc(V, device_marking=space.has_boundary)
     h = C.c_void_p()
     check(lib().ffgpu_matrix_assemble(space.h, C.byref(v), C.byref(bc), _ptr(rhs_out), C.byref(h)))
     return Matrix(h, space, solver=solver, eps=eps, itmax=itmax, dim_krylov=dim_krylov,
@@ -308,7 +341,7 @@ def rhs(varf: VarForm, Vh, out=None, device=0):
     if out is None:
         out = np.empty(V.ndof)
     v = varf.c_varf(V)
-    bc = varf.c_bc(V)
+    bc = varf.c_bc(V, device_marking=space.has_boundary)
     check(lib().ffgpu_rhs_assemble(space.h, C.byref(v), C.byref(bc), _ptr(out)))
     return out
 

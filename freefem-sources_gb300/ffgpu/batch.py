@@ -54,8 +54,11 @@ class Batch:
 
     def assemble(self, kappa, f=1.0, tgv=1e30):
         """kappa: list of P0 arrays (one per problem) or one concatenated array."""
-        k = np.ascontiguousarray(np.concatenate(kappa) if isinstance(kappa, (list, tuple)) else kappa,
-                                 np.float64)
+        if hasattr(kappa, "data_ptr"):
+            k = kappa
+        else:
+            k = np.ascontiguousarray(np.concatenate(kappa) if isinstance(kappa, (list, tuple)) else kappa,
+                                     np.float64)
         self._kappa = k
         check(lib().ffgpu_batch_assemble(self.h, api._ptr(k), float(f), api._ptr(self.onbc), float(tgv)))
 

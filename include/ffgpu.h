@@ -51,17 +51,27 @@ typedef struct {
     double f_const[3];
 } ffgpu_varf;
 
-/* Dirichlet data of `on(labels, u=g)`: onbc[dof] != 0 marks a DOF, g[dof] its value
- * (NULL = 0).  tgv > 0 follows HashMatrix::SetBC: A_ii := tgv, b_i := tgv*g_i. */
+/* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or
+ * (onbc == NULL) the device marks them from the space's boundary elements
+ * (ffgpu_space_set_boundary) whose label is one of labels[0..nlabels), for the components in
+ * comp_mask (bit c = component c; 0 = all), as AssembleBC does (problem.cpp:9881-10034).
+ * g[dof] is the value (NULL = 0).  tgv > 0 follows HashMatrix::SetBC: A_ii := tgv,
+ * b_i := tgv*g_i. */
 typedef struct {
     const uint8_t *onbc;
     const double *g;
     double tgv;
+    int nlabels;
+    const int32_t *labels;
+    int comp_mask;
 } ffgpu_bc;
 
 /* Krylov parameters, named as in FreeFEM's Data_Sparse_Solver (VirtualSolver.hpp:30-96).
  * eps > 0 relative, eps < 0 absolute (CG.cpp:226); itmax <= 0 means n (VirtualSolverCG.hpp:135);
- * dim_krylov is GMRES's restart (NbSpace).  unroll: CG iterations per CUDA-graph body (>=1). */
+ * dim_krylov is GMRES's restart (NbSpace).  unroll: CG iterations per CUDA-graph body (>=1).
+ * spmv_mode (CG): 0 = SpMV in FP64 arithmetic; 1 = FP64 values and vectors with the products
+ * formed exactly on the FP32 pipe and summed as double-float (about 2^-44 relative), every
+ * other CG operation in FP64. */
 typedef struct {
     double eps;
     int itmax;
@@ -69,6 +79,7 @@ typedef struct {
     double tgv;
     int verb;
     int unroll;
+    int spmv_mode;
 } ffgpu_solver_params;
 
 /* Solver report: iterations (FreeFEM's nbitermax / getnbiteration), final C-norm^2 of the
@@ -106,6 +117,12 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
                        const int32_t *elems, int fe, int ndofK, const int32_t *dof, int ndof,
                        ffgpu_space **out);
 int ffgpu_space_destroy(ffgpu_space *space);
+/* Boundary elements of the mesh (Th.be(k): nbe x dim vertex indices and labels), kept on the
+ * device for `on(...)` marking; builds the vertex -> boundary-element incidence once. */
+int ffgpu_space_set_boundary(ffgpu_space *space, int nbe, const int32_t *belems, const int32_t *blabel);
+/* The DOF mask of on(labels) (ndof bytes, host or device), as the assembly computes it. */
+int ffgpu_space_bc_mask(ffgpu_space *space, int nlabels, const int32_t *labels, int comp_mask,
+                        uint8_t *onbc);
 
 /* ------------------------------------------------------------------ assembly
  * matrix A = a(Vh,Vh, ...): replaces OpMatrixtoBilinearForm::Op::operator() /

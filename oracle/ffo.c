@@ -371,13 +371,33 @@ int ffo_rhs(double *b, int dim, int nt, const double *X, const int *elems, int n
     return 0;
 }
 
-/* SetBC, tgv > 0: diagonal := tgv on marked rows; rhs b_i = tgv * g_i */
+/* SetBC (HashMatrix.cpp:1195-1238) with the rhs of AssembleBC (problem.cpp:9937,10020):
+ *   tgv > 0: diagonal := tgv on marked rows, b_i = tgv g_i;
+ *   tgv < 0: b_i = g_i; marked rows get diagonal 1 (0 if tgv <= -10) and zero off-diagonals
+ *            (rows kept for -3/-30); for -2/-20/-3/-30 the marked columns are zeroed too,
+ *            the diagonal included for -20/-30. */
 void ffo_setbc(void *hm, double *b, const char *onbc, const double *g, double tgv) {
     ffo_hm *A = (ffo_hm *)hm;
     for (int i = 0; i < A->n; ++i)
         if (onbc[i]) {
-            *hm_npij(A, i, i) = tgv;
-            if (b) b[i] = tgv * (g ? g[i] : 0.0);
+            if (tgv > 0) *hm_npij(A, i, i) = tgv;
+            else hm_npij(A, i, i);
+            if (b) b[i] = (tgv > 0 ? tgv : 1.0) * (g ? g[i] : 0.0);
+        }
+    if (tgv >= 0) return;
+    int keep_row = fabs(tgv + 3.0) < 1e-10 || fabs(tgv + 30.0) < 1e-10;
+    int zero_col = fabs(tgv + 2.0) < 1e-10 || fabs(tgv + 20.0) < 1e-10 || keep_row;
+    for (int64_t k = 0; k < A->nnz; ++k) {
+        int ii = A->i[k], jj = A->j[k];
+        if (onbc[ii]) {
+            if (jj == ii) A->a[k] = tgv < -9.0 ? 0.0 : 1.0;
+            else if (!keep_row) A->a[k] = 0.0;
+        }
+    }
+    if (zero_col)
+        for (int64_t k = 0; k < A->nnz; ++k) {
+            int ii = A->i[k], jj = A->j[k];
+            if (onbc[jj] && (ii != jj || tgv < -19.0)) A->a[k] = 0.0;
         }
 }
 

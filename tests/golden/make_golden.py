@@ -83,6 +83,24 @@ cout << "S l2 " << sqrt(u[]'*u[]) << endl;
     return body, {}
 
 
+def case_p1_square_tgv(n, tgv, solver):
+    """P1 Poisson with non-zero Dirichlet data u = x on all sides, for the tgv < 0 variants of
+    HashMatrix::SetBC (-1: unit diagonal, row zeroed; -2: also the column; -3: column only)."""
+    body = HEAD + f"""
+mesh Th=square({n},{n});
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th,qft=qf2pT)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th,qft=qf2pT)(1.*v) + on(1,2,3,4,u=x);
+int nit=0;
+matrix A=a(Vh,Vh,solver={solver},eps=1e-12,tgv={tgv},getnbiteration=nit);
+real[int] b=a(0,Vh,tgv={tgv});
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + DUMP_MESH2 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
 def case_p1_square_kappa(n, seed, jitter=0.0):
     """2D P1 diffusion with a P0 lognormal coefficient, default quadrature, optional jitter."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -285,6 +303,10 @@ CASES = {
     "p2el_n2": lambda: case_p2_elasticity(2, 2, 2),
     "p2el_3x2x1": lambda: case_p2_elasticity(3, 2, 1),
     "p2sq_n4": lambda: case_p2_square_scalar(4),
+    "p1sq_n6_tgvm1": lambda: case_p1_square_tgv(6, -1, "GMRES"),
+    "p1sq_n6_tgvm2": lambda: case_p1_square_tgv(6, -2, "CG"),
+    "p1sq_n6_tgvm3": lambda: case_p1_square_tgv(6, -3, "GMRES"),
+    "p1sq_n6_tgvp": lambda: case_p1_square_tgv(6, 1e30, "CG"),
     "adj_p1_n8": lambda: case_adjoint_p1(8, seed=31),
     "heat_p1_n6": lambda: case_heat_p1(6, 10, 1e-2, seed=41),
 }

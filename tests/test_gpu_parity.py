@@ -79,6 +79,57 @@ def test_transpose_mult_and_solve_against_oracle(name):
     assert abs(A.stats.iterations - it) <= 2
 
 
+@pytest.mark.parametrize("name", [n for n in MATRIX_CASES if "gmres" not in n])
+def test_double_float_spmv_mode(name):
+    """spmv_mode=1 (products formed exactly on the FP32 pipe, double-float sums): same bars as
+    the FP64 path -- solution 1e-9 relative to FreeFEM's, iterations within 2 (or 1%)."""
+    c = case(name)
+    d, sc = c["d"], c["sc"]
+    Vh = FESpace(c["Th"], c["kind"], c.get("dof"))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=c["eps"], rhs_out=b)
+    u = A.solve(b, spmv_mode=1)
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    it = int(sc["nit"])
+    assert abs(A.stats.iterations - it) <= max(2, it // 100)
+    ut = A.solve(b, trans=True, spmv_mode=1)
+    assert np.linalg.norm(ut - d["u"]) <= 1e-8 * np.linalg.norm(d["u"])
+
+
+def test_double_float_spmv_mode_medium_elasticity():
+    Th = mesh.cube(10)
+    Vh = FESpace(Th, "P2vec")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(ffgpu.varf_elasticity(f=(0, 0, -1.0), on=(4,)), Vh, eps=1e-10, rhs_out=b)
+    u0 = A.solve(b)
+    it0 = A.stats.iterations
+    u1 = A.solve(b, spmv_mode=1)
+    assert np.linalg.norm(u1 - u0) <= SOL_TOL * np.linalg.norm(u0)
+    assert abs(A.stats.iterations - it0) <= max(2, it0 // 100)
+
+
+@pytest.mark.parametrize("tag,tgv,solver", [("m1", -1.0, "GMRES"), ("m2", -2.0, "CG"), ("m3", -3.0, "GMRES"),
+                                            ("p", 1e30, "CG")])
+def test_tgv_variants_against_freefem(tag, tgv, solver):
+    """FreeFEM's on(..., u=x) with tgv = -1 (unit diagonal, row zeroed), -2 (row and column),
+    -3 (column only) and 1e30, non-zero Dirichlet data, on the device path."""
+    d, sc = load("p1sq_n6_tgv" + tag)
+    Th = mesh.square(6)
+    Vh = FESpace(Th, "P1")
+    g = np.ascontiguousarray(Th.coords[:, 0])
+    a = ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4), g=g, tgv=tgv)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver=solver, eps=1e-12, rhs_out=b)
+    rp, cl, v = A.csr()
+    assert np.array_equal(np.repeat(np.arange(Vh.ndof), np.diff(rp)), d["I"]) and np.array_equal(cl, d["J"])
+    assert value_errors(v, d["C"], rp).max() <= VAL_TOL
+    assert np.abs(b - d["b"]).max() <= VAL_TOL * np.abs(d["b"]).max()
+    assert np.array_equal(ffgpu.rhs(a, A.space), b)
+    u = A.solve(b)
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    assert abs(A.stats.iterations - int(sc["nit"])) <= 2
+
+
 def test_multiple_rhs():
     c = case("p1sq_n16")
     Vh = FESpace(c["Th"], "P1")
@@ -221,6 +272,20 @@ def test_nonconvergence_is_an_error():
         A.solve(b)
     assert ei.value.code == -3
     assert A.stats.iterations == 3
+
+
+@pytest.mark.parametrize("name", MATRIX_CASES)
+def test_bc_mask_device_equals_host(name):
+    """on(labels) marked on the device from the boundary elements = the host FESpace.on mask
+    (which the FreeFEM fixtures pin through the assembled tgv rows)."""
+    c = case(name)
+    Vh = FESpace(c["Th"], c["kind"], c.get("dof"))
+    S = ffgpu.DeviceSpace(Vh)
+    assert np.array_equal(S.bc_mask(c["labels"]), Vh.on(c["labels"]))
+    if c["kind"] == "P2vec":
+        assert np.array_equal(S.bc_mask(c["labels"], components=(0, 2)), Vh.on(c["labels"], (0, 2)))
+    for labels in [(1,), (2, 3)]:
+        assert np.array_equal(S.bc_mask(labels), Vh.on(labels))
 
 
 def test_bad_inputs_rejected_on_host_or_device():

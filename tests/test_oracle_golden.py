@@ -143,3 +143,26 @@ def test_adjoint_fixture_consistency():
     assert abs(L - sc["loss"]) <= 1e-10 * abs(sc["loss"])
     lam, it, r, _ = ffo.cg(A, Mr, eps=1e-14, trans=True)
     assert np.linalg.norm(lam - d["g_lam"]) <= 1e-8 * np.linalg.norm(d["g_lam"])
+
+
+@pytest.mark.parametrize("tag,tgv,solver", [("m1", -1.0, "GMRES"), ("m2", -2.0, "CG"), ("m3", -3.0, "GMRES"),
+                                            ("p", 1e30, "CG")])
+def test_oracle_tgv_variants(tag, tgv, solver):
+    """on(1,2,3,4, u=x) with tgv = -1, -2, -3 and 1e30 against FreeFEM."""
+    d, sc = load("p1sq_n6_tgv" + tag)
+    Th = mesh.square(6)
+    Vh = FESpace(Th, "P1")
+    A = ffo.assemble(Th, Vh, quad="qf2pT")
+    b = ffo.rhs(Th, Vh, f=1.0, quad="qf2pT")
+    on = Vh.on((1, 2, 3, 4))
+    ffo.setbc(A, b, on, g=Th.coords[:, 0].copy(), tgv=tgv)
+    rp, cl, v = A.csr()
+    assert np.array_equal(np.repeat(np.arange(Vh.ndof), np.diff(rp)), d["I"]) and np.array_equal(cl, d["J"])
+    assert value_errors(v, d["C"], rp).max() <= 1e-12
+    assert np.abs(b - d["b"]).max() <= 1e-12 * np.abs(d["b"]).max()
+    if solver == "CG":
+        x, it, r, _ = ffo.cg(A, b, eps=1e-12, tgv=tgv)
+    else:
+        x, it, r, _ = ffo.fgmres(A, b, eps=1e-12, tgv=tgv)
+    assert np.linalg.norm(x - d["u"]) <= 1e-9 * np.linalg.norm(d["u"])
+    assert it == int(sc["nit"])
