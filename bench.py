@@ -42,9 +42,32 @@ CONFIGS = {
                                  on=(1, 2, 3, 4, 5, 6), eps=1e-10, kappa_seed=3),
     # 1024 independent jittered squares, N ~ U{16..128}, FP32 inner / FP64 refinement to 1e-8
     "batched_p1_1024": dict(batch=True, nprob=1024, nmin=16, nmax=128, eps=1e-8, seed=0),
+    # 2D inverse diffusion on square(512): dL/dkappa by the adjoint at kappa = 1, with
+    # ln kappa_true a Gaussian field (squared-exponential, length 0.1, sigma 1), 1% noise;
+    # heat variant: 200 implicit-Euler steps, dt 1e-3, checkpoints every 20 steps
+    "inverse_diffusion_p1_square512": dict(adjoint=True, mesh=("square", 512), kind="P1",
+                                           form="diffusion", on=(1, 2, 3, 4), eps=1e-12, seed=4,
+                                           ell=0.1, sigma=1.0, noise=0.01, nfd=64,
+                                           heat_steps=200, heat_dt=1e-3, heat_checkpoint=20),
 }
 SAMPLE = {"elasticity_p2_cube64": ("cube", 12), "poisson_p1_square256": ("square", 256),
-          "diffusion_p1_cube160": ("cube", 40), "batched_p1_1024": ("square", 64)}
+          "diffusion_p1_cube160": ("cube", 40), "batched_p1_1024": ("square", 64),
+          "inverse_diffusion_p1_square512": ("square", 256)}
+
+
+def gaussian_field(n, ell, sigma, seed):
+    """A stationary Gaussian field on the n x n cell centres of the unit square, covariance
+    sigma^2 exp(-r^2 / (2 ell^2)), sampled by circulant embedding (Dietrich & Newsam 1997) on
+    the 2n x 2n periodic grid of spacing 1/n.  Returns field[i + j*n] for cell (i, j)."""
+    import numpy as np
+    m = 2 * n
+    d = np.minimum(np.arange(m), m - np.arange(m)) / n
+    cov = sigma ** 2 * np.exp(-(d[:, None] ** 2 + d[None, :] ** 2) / (2 * ell ** 2))
+    lam = np.maximum(np.fft.fft2(cov).real, 0.0)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xi = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+    z = np.fft.fft2(np.sqrt(lam / (m * m)) * xi).real[:n, :n]   # z[j, i]: row j = y index
+    return np.ascontiguousarray(z).ravel()
 
 
 def build_problem(cfg, size=None):
@@ -65,11 +88,49 @@ def build_problem(cfg, size=None):
 
 
 # ------------------------------------------------------------------ CPU: the oracle port
+def _oracle_adjoint_run(cfg, size):
+    """CPU gradient of the inverse problem: forward CG, transpose CG, P0 sensitivities."""
+    import numpy as np
+    import ffgpu
+    import ffo
+    from ffgpu.fespace import FESpace
+    Th = ffgpu.square(size[1])
+    Vh = FESpace(Th, "P1")
+    u_obs = np.zeros(Vh.ndof)
+    M = ffo.assemble(Th, Vh, mass=1.0, c_stiff=0.0)     # the loss's mass matrix, set up once
+    t0 = time.perf_counter()
+    A = ffo.assemble(Th, Vh, kappa=np.ones(Th.nt))
+    b = ffo.rhs(Th, Vh, f=1.0)
+    on = Vh.on(cfg["on"])
+    ffo.setbc(A, b, on)
+    u, it, _, _ = ffo.cg(A, b, eps=cfg["eps"])
+    r = u - u_obs
+    Mr = M.matmul(r)
+    lam, it2, _, _ = ffo.cg(A, Mr, eps=cfg["eps"], trans=True)
+    # dL/dkappa_e = -lam_e' K_e u_e (K_e = |K| G G'), the varf FreeFEM scripts use for it
+    X = Th.coords[Th.elems]
+    e1, e2 = X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]
+    area = 0.5 * (e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0])
+    gu = np.zeros((Th.nt, 2))
+    gl = np.zeros((Th.nt, 2))
+    for i in range(3):
+        p1, p2 = X[:, (i + 1) % 3], X[:, (i + 2) % 3]
+        G = np.stack([-(p2[:, 1] - p1[:, 1]), p2[:, 0] - p1[:, 0]], axis=1) / (2 * area[:, None])
+        gu += G * u[Th.elems[:, i], None]
+        gl += G * lam[Th.elems[:, i], None]
+    gk = -area * (gu * gl).sum(axis=1)
+    dt = time.perf_counter() - t0
+    del gk
+    return Vh.ndof, dt, it + it2
+
+
 def _oracle_run(args):
     cfgname, size = args
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import ffo
     cfg = CONFIGS[cfgname]
+    if cfg.get("adjoint"):
+        return _oracle_adjoint_run(cfg, size)
     Th, Vh, a, np = build_problem(cfg, size)
     t0 = time.perf_counter()
     quad = None if cfg["kind"] != "P1" or Th.dim == 3 else "qf2pT"
@@ -98,8 +159,10 @@ def cpu_baseline(cfgname, procs=1, reps=1):
     ndof = res[0][0]
     per = statistics.median(r[1] for r in res)
     value = ndof * len(res) / wall if procs > 1 else ndof / per
+    what = ("forward CG + transpose CG + P0 sensitivities" if CONFIGS[cfgname].get("adjoint")
+            else "full assemble+rhs+CG")
     return dict(value=value, unit=UNIT, cores=procs, kind="port",
-                sample=f"{size[0]}({size[1]}) same varf, full assemble+rhs+CG(eps={CONFIGS[cfgname]['eps']}), "
+                sample=f"{size[0]}({size[1]}) same varf, {what} (eps={CONFIGS[cfgname]['eps']}), "
                        f"{len(res)} run(s), {res[0][2]} CG iterations, single-threaded oracle "
                        f"(oracle/ffo.c) per core"), wall
 
@@ -248,7 +311,15 @@ def run_gpu(args, rank, world):
     n, nnz, bs = A.n, A.nnz, A.block_size
     nnzb = nnz // (bs * bs)
     nb = n // bs
-    spmv_bytes = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
+    layout = A.spmv_layout(0)
+    # algorithmic bytes of one SpMV (CSR with FP64 values and int32 columns, x read once, y
+    # written): 12 nnz + 4 (n+1) + 8 n + 8 n; the bytes the chosen layout actually streams
+    # (block/sliced storage shares one column index per 3x3 block) are reported beside it
+    spmv_bytes = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    if bs == 3:
+        stored = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
+    else:
+        stored = 8 * nnz + (2 if layout == "sell32" else 4) * nnz + 4 * (nb + 1) + 8 * n + 8 * n
     achieved = spmv_bytes / (spmv_avg * 1e-3) / 1e9
     peaks = {}
     try:
@@ -285,10 +356,11 @@ def run_gpu(args, rank, world):
         def run_df():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
             A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
-            return A2.solve(b, spmv_mode=1), A2.stats.iterations
-        (udf, itdf), msdf = timed_variant(run_df, 2)
+            return A2.solve(b, spmv_mode=1), A2.stats.iterations, A2.spmv_layout(1)
+        (udf, itdf, lay), msdf = timed_variant(run_df, 2)
         variants["fp64_values_doublefloat_spmv"] = {
             "value": Vh.ndof / (msdf * 1e-3), "ms_per_step": msdf, "cg_iterations": itdf,
+            "spmv_layout": lay,
             "rel_err_vs_fp64": float(torch.linalg.norm(udf - u_ref) / torch.linalg.norm(u_ref))}
 
         def run_ir():
@@ -336,14 +408,18 @@ def run_gpu(args, rank, world):
                    "assemble_ms": statistics.median(phase["assemble"][-args.steps:]),
                    "solve_ms": statistics.median(phase["solve"][-args.steps:]),
                    "ms_per_cg_iteration": statistics.median(phase["solve"][-args.steps:]) / max(1, iters[-1]),
+                   "spmv_layout": layout,
                    "rel_residual": rel_res},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "spmv BSR3 FP64 (cg_ka body)", "bytes_per_launch": spmv_bytes,
-                     "ms_per_launch": spmv_avg, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+                     "kernel": f"FP64 SpMV of the CG (K_a), layout {layout}, block size {bs}",
+                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_avg,
+                     "stored_bytes_per_launch": stored,
+                     "frac_of_stored_bytes": stored / (spmv_avg * 1e-3) / 1e9 / peak,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": clk,
         "variants": variants,
     }
@@ -376,7 +452,10 @@ def profile_case(kind, n, iters, spmv_mode):
         S = ffgpu.DeviceSpace(Vh, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
         A = ffgpu.matrix(a, S, eps=1e-10, itmax=iters, rhs_out=b)
         try:
-            A.solve(b, spmv_mode=spmv_mode)
+            if spmv_mode == 2:      # mixed precision: one refinement step of `iters` FP32 iterations
+                A.solve_mixed(b, eps=1e-10, eps_inner=1e-30, itmax_inner=iters, max_outer=1)
+            else:
+                A.solve(b, spmv_mode=spmv_mode)
         except ffgpu.FFGPUError as e:
             if e.code != -3:
                 raise
@@ -384,6 +463,120 @@ def profile_case(kind, n, iters, spmv_mode):
         print(f"profile case {kind}({n}): ndof {Vh.ndof} nnz {A.nnz} iterations {A.stats.iterations} "
               f"device {A.stats.elapsed_ms:.2f} ms")
         del A, S
+
+
+def run_adjoint(args):
+    """dL/dkappa by the adjoint (forward CG, transpose CG, sensitivity kernel) on the device;
+    the heat variant with checkpoint-and-recompute; FD check on seeded elements."""
+    import numpy as np
+    import torch
+    import ffgpu
+    from ffgpu import adjoint
+    from ffgpu.build import build
+    from ffgpu.fespace import FESpace
+    build()
+    cfg = CONFIGS[args.config]
+    n = cfg["mesh"][1]
+    Th = ffgpu.square(n)
+    Vh = FESpace(Th, "P1")
+    dev = torch.device("cuda", 0)
+    ffgpu.context(0)
+    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(0), device=0)
+    cells = gaussian_field(n, cfg["ell"], cfg["sigma"], cfg["seed"])
+    k_true = torch.from_numpy(np.exp(np.repeat(cells, 2))).to(dev)      # both triangles of a cell
+    ones = torch.ones(Th.nt, dtype=torch.float64, device=dev)
+    P = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"])
+    u_true = P.solve(k_true, 1.0)
+    rng = np.random.Generator(np.random.PCG64(cfg["seed"] + 1))
+    rms = float(torch.sqrt(torch.mean(u_true * u_true)))
+    u_obs = u_true + cfg["noise"] * rms * torch.from_numpy(rng.standard_normal(Vh.ndof)).to(dev)
+    kappa = ones
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    fwd_ms, grad_ms = [], []
+    clocks = ClockSampler()
+    for k in range(args.warmup + args.steps):
+        if k == args.warmup:
+            l0 = ffgpu.kernel_launches()
+            clocks.start()
+        e0, e1, e2 = ev(), ev(), ev()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        u = P.solve(kappa, 1.0)
+        e1.record(stream)
+        it_fwd = P.A.stats.iterations
+        L, gk, gf, u2, lam = P.value_and_grad(kappa, 1.0, u_obs)
+        e2.record(stream)
+        e2.synchronize()
+        if k >= args.warmup:
+            fwd_ms.append(e0.elapsed_time(e1))
+            grad_ms.append(e1.elapsed_time(e2))
+    clk = clocks.stop()
+    launches = (ffgpu.kernel_launches() - l0) // args.steps
+    it_adj = P.A.stats.iterations
+    t_fwd = statistics.median(fwd_ms)
+    t_grad = statistics.median(grad_ms)
+    # central FD on seeded elements (host path of the same library), outside the timed region
+    ek = rng.choice(Th.nt, size=cfg["nfd"], replace=False)
+    gk_h = gk.cpu().numpy()
+    fd = P.fd_gradient(np.ones(Th.nt), np.ones(Th.nt), u_obs.cpu().numpy(), ek, step=1e-6)
+    floor = 1e-3 * np.abs(gk_h).max()
+    fd_err = float((np.abs(fd - gk_h[ek]) / np.maximum(np.abs(gk_h[ek]), floor)).max())
+    # heat variant: forward alone, then forward + checkpointed backward
+    H = adjoint.HeatProblem(Vh, dt=cfg["heat_dt"], nsteps=cfg["heat_steps"], on=cfg["on"],
+                            checkpoint=cfg["heat_checkpoint"], eps=cfg["eps"])
+    uN, _ = H.forward(k_true, 1.0, keep_checkpoints=False)
+    h_obs = uN + cfg["noise"] * float(torch.sqrt(torch.mean(uN * uN))) * torch.from_numpy(
+        rng.standard_normal(Vh.ndof)).to(dev)
+    hf, hg = [], []
+    for k in range(1 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H.forward(kappa, 1.0, keep_checkpoints=False)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        H.value_and_grad(kappa, 1.0, h_obs)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if k >= 1:
+            hf.append((t1 - t0) * 1e3)
+            hg.append((t2 - t1) * 1e3)
+    # e2e: the same gradient from host arrays through the public API
+    P2 = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"])
+    uo_h = u_obs.cpu().numpy()
+    e2e = []
+    for k in range(1 + args.steps):
+        t0 = time.perf_counter()
+        P2.value_and_grad(np.ones(Th.nt), np.ones(Th.nt), uo_h)
+        if k >= 1:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    t_e2e = statistics.median(e2e)
+    value = Vh.ndof / (t_grad * 1e-3)
+    cb, _ = (None, None) if args.no_cpu_baseline else cpu_baseline(args.config, procs=1)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_grad, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.config, "mesh": f"square({n})", "fe": "P1", "ndof": Vh.ndof,
+                      "params": Th.nt, "eps": cfg["eps"], "step": "L and dL/dkappa, dL/df at kappa=1",
+                      "forward_ms": t_fwd, "gradient_ms": t_grad,
+                      "gradient_over_forward": t_grad / t_fwd, "cg_iterations_forward": it_fwd,
+                      "cg_iterations_adjoint": it_adj, "fd_elements": int(cfg["nfd"]),
+                      "fd_max_rel_err": fd_err,
+                      "heat": {"steps": cfg["heat_steps"], "dt": cfg["heat_dt"],
+                               "checkpoint": cfg["heat_checkpoint"], "forward_ms": statistics.median(hf),
+                               "gradient_ms": statistics.median(hg),
+                               "gradient_over_forward": statistics.median(hg) / statistics.median(hf),
+                               "solves_gradient": H.solves},
+                      "l2": "working set below L2 (square(512)); timing is of repeated gradients"},
+           "e2e": {"value": Vh.ndof / (t_e2e * 1e-3), "unit": UNIT,
+                   "h2d_bytes_per_step": int(2 * Th.nt * 8 + Vh.ndof * 8),
+                   "d2h_bytes_per_step": int(2 * Th.nt * 8 + 2 * Vh.ndof * 8), "ms_per_step": t_e2e},
+           "gpu_launches": int(launches) * args.steps, "clocks": clk, "roofline": None}
+    if cb:
+        out["cpu_baseline"] = cb
+    print(json.dumps(out))
 
 
 def run_batch(args):
@@ -494,7 +687,8 @@ def main():
                     help="run a small case for ncu instead of the benchmark")
     ap.add_argument("--n", type=int, default=32)
     ap.add_argument("--iters", type=int, default=40)
-    ap.add_argument("--spmv-mode", type=int, default=0)
+    ap.add_argument("--spmv-mode", type=int, default=0,
+                    help="profile case: 0 FP64 CG, 1 double-float SpMV CG, 2 FP32-inner refinement")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args.profile_case, args.n, args.iters, args.spmv_mode)
@@ -504,6 +698,10 @@ def main():
     if CONFIGS[args.config].get("batch") and args.impl != "reference":
         if rank == 0:
             run_batch(args)
+        return
+    if CONFIGS[args.config].get("adjoint") and args.impl != "reference":
+        if rank == 0:
+            run_adjoint(args)
         return
     if args.impl == "reference":
         if rank != 0:

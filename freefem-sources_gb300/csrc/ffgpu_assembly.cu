@@ -705,12 +705,15 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     FFGPU_TRY(fill_launch(S, fa));
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish(ctx->stream));
-    // the solver data of a previous numeric state are stale
+    // the solver data of a previous numeric state are stale; so is a cached CG graph, which
+    // holds the addresses of the derived value arrays
     M->ntgv = -1;
     if (M->val_t) { cudaFree(M->val_t); M->val_t = nullptr; }
     if (M->val32) { cudaFree(M->val32); M->val32 = nullptr; }
     if (M->valx) { cudaFree(M->valx); M->valx = nullptr; }
     if (M->valx_t) { cudaFree(M->valx_t); M->valx_t = nullptr; }
+    sell_release_values(M);
+    if (M->cg_exec) { cudaGraphExecDestroy(M->cg_exec); M->cg_exec = nullptr; }
     return FFGPU_OK;
 }
 
@@ -1023,6 +1026,8 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     cudaFree(M->geo); cudaFree(M->bcmask);
     cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
     cudaFree(M->val32); cudaFree(M->valx); cudaFree(M->valx_t); cudaFree(M->hx); cudaFree(M->ks);
+    sell_release_values(M);
+    cudaFree(M->sperm); cudaFree(M->slen); cudaFree(M->soff); cudaFree(M->scol); cudaFree(M->scol16);
     delete M;
     return FFGPU_OK;
 }

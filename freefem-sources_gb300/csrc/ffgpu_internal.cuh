@@ -124,6 +124,19 @@ struct ffgpu_matrix {
     // tuning
     int csr_lanes;        // lanes per block row of the FP64 SpMV (tuned)
     int csr_lanes_x;      // lanes per block row of the double-float SpMV (tuned)
+    // SELL-32 copy for the Krylov SpMVs: block rows sliced into chunks of 32 (one row per
+    // lane), rows sorted by decreasing degree inside windows of 1024 rows, each chunk padded
+    // to its longest row and stored slot-major so that a warp reads 32 consecutive entries.
+    int nchunk;           // ceil(nb/32)
+    int64_t nslot;        // slot rows (sum of the chunk lengths)
+    int32_t *sperm;       // nchunk*32: block row of each lane (-1: padding lane)
+    int32_t *slen;        // nchunk: slots of each chunk
+    int32_t *soff;        // nchunk+1: first slot row of each chunk
+    int32_t *scol;        // nslot*32 block columns (NULL when scol16 is used)
+    int16_t *scol16;      // nslot*32 column - row, when bs == 1 and every |column - row| < 2^15
+    double *sval, *sval_t;      // FP64 values of A and A^T, (slot row, entry, lane) order
+    float2 *svalx, *svalx_t;    // double-float splits of the same
+    float *sval32;              // FP32 values for the mixed-precision inner solve
 };
 
 namespace ffgpu {
@@ -194,6 +207,25 @@ int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
 int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
+
+// Work-vector slot stride: slots start on 512-byte boundaries (16-byte vector accesses).
+inline int64_t vstride(int64_t n) { return (n + 63) & ~(int64_t)63; }
+
+// SELL-32 layout of a matrix (see ffgpu_matrix): kinds of value arrays
+enum SellKind { kSell64 = 0, kSell64T = 1, kSellX = 2, kSellXT = 3, kSell32 = 4 };
+struct SellArgs {
+    int nchunk;
+    const int32_t *perm, *len, *off, *col;
+    const int16_t *col16;
+};
+int sell_prepare(ffgpu_matrix *A);               // structure (once per pattern)
+int sell_values(ffgpu_matrix *A, int kind);      // value array of one kind (once per numeric state)
+void sell_release_values(ffgpu_matrix *A);       // drop the value arrays (new numeric state)
+inline SellArgs sell_args(const ffgpu_matrix *A) {
+    return SellArgs{A->nchunk, A->sperm, A->slen, A->soff, A->scol, A->scol16};
+}
+// Persistent grid of a kernel: resident blocks per SM (occupancy calculator) x SMs
+int resident_grid(const void *kernel, int threads, size_t smem = 0);
 
 // matrix-level operations shared by the solvers
 int matrix_prepare_solver(ffgpu_matrix *A);

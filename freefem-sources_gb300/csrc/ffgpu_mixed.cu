@@ -1,6 +1,12 @@
 // ffgpu_mixed.cu -- mixed precision: FP32 inner Jacobi-PCG inside an FP64 iterative
 // refinement loop.
 //
+// Two refinement schemes: (default) residual replacement that keeps the inner search
+// direction -- after each inner segment the FP32 iterated residual is replaced by the FP64
+// true residual and the conjugate-gradient recurrence continues (the reliable updates of
+// Sleijpen & van der Vorst, 1996), so the FP32 iterations add up to about the FP64 CG's count;
+// or (restart_inner = 1) classical iterative refinement, a fresh inner PCG per step.
+//
 // FP64 stays where accuracy is decided: the element geometry and assembled values, the
 // outer residual r = b - A x (FP64 SpMV on the FP64 matrix) and the update x += d.
 // The inner solve of A d = r runs on an FP32 copy of the values with FP32 vectors, SpMV,
@@ -14,6 +20,7 @@
 #include <string.h>
 
 #include "ffgpu_internal.cuh"
+#include "ffgpu_sell.cuh"
 
 namespace ffgpu {
 
@@ -29,142 +36,82 @@ struct InnerScalars {
     int pad1;
 };
 
-__device__ __forceinline__ float block_sum_f(float v, float *sh) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    float t = 0;
-    if (w == 0) {
-        t = lane < nw ? sh[lane] : 0.0f;
-        t = warp_sum(t);
-    }
-    __syncthreads();
-    return t;
-}
+__device__ __noinline__ void ir_graph_stop(cudaGraphConditionalHandle cond) { cudaGraphSetConditional(cond, 0); }
 
-__device__ __forceinline__ bool last_block_f(float partial, float *part, unsigned *ticket, float *tot, float *sh) {
-    __shared__ bool s_last;
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = partial;
-        __threadfence();
-        unsigned t = atomicAdd(ticket, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    float s = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(part + i);
-    s = block_sum_f(s, sh);
-    if (threadIdx.x == 0) { *tot = s; *ticket = 0u; return true; }
-    return false;
-}
-
-template <int T>
-__device__ __forceinline__ float csr_row_f(const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
-                                           const float *__restrict__ val, const float *__restrict__ x, int r,
-                                           int sub) {
-    int b = __ldg(rp + r), e = __ldg(rp + r + 1);
-    float s = 0;
-    for (int k = b + sub; k < e; k += T) s = fmaf(__ldg(val + k), __ldg(x + __ldg(col + k)), s);
-#pragma unroll
-    for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    return s;
-}
-
-template <int T>
-__device__ __forceinline__ void bsr3_row_f(const int32_t *__restrict__ brp, const int32_t *__restrict__ bcol,
-                                           const float *__restrict__ val, const float *__restrict__ x, int a,
-                                           int sub, float &y0, float &y1, float &y2) {
-    int b = __ldg(brp + a), e = __ldg(brp + a + 1);
-    float s0 = 0, s1 = 0, s2 = 0;
-    for (int k = b + sub; k < e; k += T) {
-        int c = __ldg(bcol + k);
-        const float *v = val + (int64_t)k * 9;
-        float x0 = __ldg(x + 3 * (int64_t)c), x1 = __ldg(x + 3 * (int64_t)c + 1), x2 = __ldg(x + 3 * (int64_t)c + 2);
-        s0 = fmaf(__ldg(v + 0), x0, s0); s0 = fmaf(__ldg(v + 1), x1, s0); s0 = fmaf(__ldg(v + 2), x2, s0);
-        s1 = fmaf(__ldg(v + 3), x0, s1); s1 = fmaf(__ldg(v + 4), x1, s1); s1 = fmaf(__ldg(v + 5), x2, s1);
-        s2 = fmaf(__ldg(v + 6), x0, s2); s2 = fmaf(__ldg(v + 7), x1, s2); s2 = fmaf(__ldg(v + 8), x2, s2);
-    }
-#pragma unroll
-    for (int o = T / 2; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    y0 = s0; y1 = s1; y2 = s2;
-}
-
-struct Spmv32 {
-    int nb, bs;
-    const int32_t *rp, *col;
-    const float *val;
-    const int32_t *perm;
-};
-
-// inner K_a: q = A h (FP32) and (h,q) -> rho
-template <int BS, int T>
-__global__ void __launch_bounds__(kMxWarps * 32) ir_ka(Spmv32 A, const float *__restrict__ h, float *__restrict__ q,
+// inner K_a on the SELL-32 FP32 copy: q = A h and (h, q) -> rho
+template <int BS, bool C16>
+__global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *__restrict__ val,
+                                                       const float *__restrict__ h, float *__restrict__ q,
                                                        InnerScalars *ks, float *part) {
     __shared__ float sh[32];
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
-    const int gsub = lane / T, sub = lane % T;
-    const int groups = (blockDim.x / 32) * (32 / T);
-    int g = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     float hq = 0;
-    for (int base = 0; base < A.nb; base += gridDim.x * groups) {
-        const int slot = base + g;
-        const bool ok = slot < A.nb;
-        const int a = ok ? __ldg(A.perm + slot) : 0;
-        if (BS == 1) {
-            float s = csr_row_f<T>(A.rp, A.col, A.val, h, a, ok ? sub : T);
-            if (ok && sub == 0) { q[a] = s; hq = fmaf(h[a], s, hq); }
-        } else {
-            float y0, y1, y2;
-            bsr3_row_f<T>(A.rp, A.col, A.val, h, a, ok ? sub : T, y0, y1, y2);
-            if (ok && sub == 0) {
-                int64_t i = 3 * (int64_t)a;
-                q[i] = y0; q[i + 1] = y1; q[i + 2] = y2;
-                hq = fmaf(h[i], y0, hq);
-                hq = fmaf(h[i + 1], y1, hq);
-                hq = fmaf(h[i + 2], y2, hq);
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+        float y[BS];
+        sell_row32<BS, C16>(S, val, h, c, lane, a, y);
+        if (a >= 0) {
+#pragma unroll
+            for (int m = 0; m < BS; ++m) {
+                const int64_t i = (int64_t)BS * a + m;
+                q[i] = y[m];
+                hq = fmaf(h[i], y[m], hq);
             }
         }
     }
     float tot;
-    float p = block_sum_f(hq, sh);
-    if (last_block_f(p, part, &ks->ticket, &tot, sh)) { ks->s_hq = tot; ks->rho = -ks->s_gh / tot; }
+    float p = block_sum_t(hq, sh);
+    if (last_block_sum(p, part, &ks->ticket, &tot, sh)) { ks->s_hq = tot; ks->rho = -ks->s_gh / tot; }
 }
 
+// inner K_b / K_c, four elements per access (16-byte aligned vectors); the last n % 4
+// elements are done by the first threads of block 0
 __global__ void __launch_bounds__(kMxThreads) ir_kb(int n, float *__restrict__ x, float *__restrict__ g,
                                                     const float *__restrict__ h, const float *__restrict__ q,
                                                     const float *__restrict__ dinv, InnerScalars *ks, float *part,
                                                     cudaGraphConditionalHandle cond) {
     __shared__ float sh[32];
     if (ks->done) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0);
+        if (blockIdx.x == 0 && threadIdx.x == 0) ir_graph_stop(cond);
         return;
     }
     const float rho = ks->rho;
     float s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int n4 = n >> 2;
+    float4 *x4 = reinterpret_cast<float4 *>(x), *g4 = reinterpret_cast<float4 *>(g);
+    const float4 *h4 = reinterpret_cast<const float4 *>(h), *q4 = reinterpret_cast<const float4 *>(q),
+                 *d4 = reinterpret_cast<const float4 *>(dinv);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const float4 hv = h4[i], qv = q4[i], dv = d4[i];
+        float4 xv = x4[i], gv = g4[i];
+        xv.x = fmaf(rho, hv.x, xv.x); xv.y = fmaf(rho, hv.y, xv.y);
+        xv.z = fmaf(rho, hv.z, xv.z); xv.w = fmaf(rho, hv.w, xv.w);
+        gv.x = fmaf(rho, qv.x, gv.x); gv.y = fmaf(rho, qv.y, gv.y);
+        gv.z = fmaf(rho, qv.z, gv.z); gv.w = fmaf(rho, qv.w, gv.w);
+        x4[i] = xv;
+        g4[i] = gv;
+        s = fmaf(gv.x, dv.x * gv.x, s); s = fmaf(gv.y, dv.y * gv.y, s);
+        s = fmaf(gv.z, dv.z * gv.z, s); s = fmaf(gv.w, dv.w * gv.w, s);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+        const int i = 4 * n4 + threadIdx.x;
         x[i] = fmaf(rho, h[i], x[i]);
-        float gi = fmaf(rho, q[i], g[i]);
+        const float gi = fmaf(rho, q[i], g[i]);
         g[i] = gi;
         s = fmaf(gi, dinv[i] * gi, s);
     }
     float tot;
-    float p = block_sum_f(s, sh);
-    if (last_block_f(p, part, &ks->ticket, &tot, sh)) {
+    float p = block_sum_t(s, sh);
+    if (last_block_sum(p, part, &ks->ticket, &tot, sh)) {
         ks->gcgp = ks->gcg;
         ks->gcg = tot;
         ks->gamma = tot / ks->gcgp;
         ks->iter += 1;
         if (tot < ks->eps2) { ks->converged = 1; ks->done = 1; }
         else if (ks->iter >= ks->itmax || !(tot == tot)) ks->done = 1;
-        if (ks->done) cudaGraphSetConditional(cond, 0);
+        if (ks->done) ir_graph_stop(cond);
     }
 }
 
@@ -174,15 +121,28 @@ __global__ void __launch_bounds__(kMxThreads) ir_kc(int n, const float *__restri
     if (ks->done) return;
     const float gamma = ks->gamma;
     float s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float gi = g[i];
-        float hi = gamma * h[i] - dinv[i] * gi;
+    const int n4 = n >> 2;
+    float4 *h4 = reinterpret_cast<float4 *>(h);
+    const float4 *g4 = reinterpret_cast<const float4 *>(g), *d4 = reinterpret_cast<const float4 *>(dinv);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const float4 gv = g4[i], dv = d4[i];
+        float4 hv = h4[i];
+        hv.x = gamma * hv.x - dv.x * gv.x; hv.y = gamma * hv.y - dv.y * gv.y;
+        hv.z = gamma * hv.z - dv.z * gv.z; hv.w = gamma * hv.w - dv.w * gv.w;
+        h4[i] = hv;
+        s = fmaf(gv.x, hv.x, s); s = fmaf(gv.y, hv.y, s);
+        s = fmaf(gv.z, hv.z, s); s = fmaf(gv.w, hv.w, s);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+        const int i = 4 * n4 + threadIdx.x;
+        const float gi = g[i];
+        const float hi = gamma * h[i] - dinv[i] * gi;
         h[i] = hi;
         s = fmaf(gi, hi, s);
     }
     float tot;
-    float p = block_sum_f(s, sh);
-    if (last_block_f(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
+    float p = block_sum_t(s, sh);
+    if (last_block_sum(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
 }
 
 // Outer step (FP64): r = b - A x from y = A x; (r, C r); inner RHS in FP32; d = 0;
@@ -193,7 +153,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_outer_kernel(int n, const doubl
                                                               const float *__restrict__ dinv32,
                                                               float *__restrict__ g, float *__restrict__ h,
                                                               float *__restrict__ d, double *part64,
-                                                              unsigned *ticket, double *out3) {
+                                                              unsigned *ticket, double *out3, int restart) {
     __shared__ double sh[32];
     __shared__ bool s_last;
     double s64 = 0, s32a = 0, s32b = 0;
@@ -203,7 +163,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_outer_kernel(int n, const doubl
         float gi = -(float)r;
         float zi = dinv32[i] * gi;
         g[i] = gi;
-        h[i] = -zi;
+        if (restart) h[i] = -zi;
         d[i] = 0.0f;
         s32a += (double)(gi * zi);
         s32b += (double)(gi * -zi);
@@ -245,6 +205,18 @@ __global__ void __launch_bounds__(kMxThreads) ir_outer_kernel(int n, const doubl
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// Residual replacement that keeps the search direction (reliable update): the iterated
+// gradient of the finished inner segment is replaced by the true one, G = -(b - A x), and the
+// recurrence continues with gamma = (G, C G) / gCg_k, H = gamma H - C G (ir_kc).
+__global__ void ir_inner_keep(InnerScalars *ks, const double *out3, float eps_in, int itmax) {
+    float gcg = (float)out3[1];
+    ks->gamma = gcg / ks->gcgp;
+    ks->gcg = gcg; ks->gcgp = gcg;
+    ks->eps2 = eps_in * eps_in * gcg;
+    ks->iter = 0; ks->itmax = itmax; ks->converged = 0; ks->done = gcg < 1e-30f ? 1 : 0;
+    ks->ticket = 0u;
+}
+
 __global__ void ir_inner_init(InnerScalars *ks, const double *out3, float eps_in, int itmax) {
     float gcg = (float)out3[1];
     ks->gcg = gcg; ks->gcgp = gcg; ks->s_gh = (float)out3[2];
@@ -268,18 +240,6 @@ __global__ void x0_tgv_kernel(int n, double *x, const double *b, const uint8_t *
     if (i < n && wcl[i]) x[i] = b[i] / tgv;
 }
 
-template <int BS>
-static void *ir_ka_fn(int T) {
-    switch (T) {
-        case 1: return (void *)ir_ka<BS, 1>;
-        case 2: return (void *)ir_ka<BS, 2>;
-        case 4: return (void *)ir_ka<BS, 4>;
-        case 8: return (void *)ir_ka<BS, 8>;
-        case 16: return (void *)ir_ka<BS, 16>;
-        default: return (void *)ir_ka<BS, 32>;
-    }
-}
-
 struct IRState {
     cudaGraphExec_t exec = nullptr;
     int unroll = 0;
@@ -287,20 +247,6 @@ struct IRState {
     InnerScalars *ks = nullptr;
     double *y = nullptr, *out3 = nullptr;
 };
-
-static int ir_lanes(const ffgpu_matrix *A) {
-    if (A->csr_lanes > 0) return A->csr_lanes;
-    double avg = (double)A->nnzb / (double)max(1, A->nb);
-    if (A->bs == 3) return avg >= 24 ? 4 : 2;
-    if (avg >= 24) return 8;
-    if (avg >= 10) return 4;
-    return 2;
-}
-
-static int ir_grid(const ffgpu_matrix *A, int T) {
-    int groups = kMxWarps * (32 / T);
-    return max(1, min(kMxSpmvBlocks, (A->nb + groups - 1) / groups));
-}
 
 static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     ffgpu_ctx *ctx = A->ctx;
@@ -320,16 +266,19 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int T = ir_lanes(A);
-    Spmv32 sa{A->nb, A->bs, A->browptr, A->bcol, A->val32, A->rowperm};
-    void *ka = A->bs == 3 ? ir_ka_fn<3>(T) : ir_ka_fn<1>(T);
+    SellArgs sa = sell_args(A);
+    const float *sv = A->sval32;
+    void *ka = A->bs == 3 ? (void *)ir_ka<3, false> : (A->scol16 ? (void *)ir_ka<1, true> : (void *)ir_ka<1, false>);
+    const int gka = resident_grid(ka, kMxWarps * 32);
+    const int gkb = min(4096, resident_grid((const void *)ir_kb, kMxThreads));
+    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
     float *part = (float *)ctx->d_part;
     int n = A->n;
     for (int u = 0; u < unroll; ++u) {
-        void *aa[] = {&sa, &S.h, &S.q, &S.ks, &part};
-        cudaLaunchKernel(ka, ir_grid(A, T), kMxWarps * 32, aa, 0, s);
-        ir_kb<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, S.d, S.g, S.h, S.q, S.dinv, S.ks, part, cond);
-        ir_kc<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, part);
+        void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
+        cudaLaunchKernel(ka, gka, kMxWarps * 32, aa, 0, s);
+        ir_kb<<<gkb, kMxThreads, 0, s>>>(n, S.d, S.g, S.h, S.q, S.dinv, S.ks, part, cond);
+        ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, part);
     }
     cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&S.exec, graph, 0);
@@ -374,20 +323,21 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     cudaStream_t s = ctx->stream;
     const int n = A->n;
     FFGPU_TRY(matrix_prepare_solver(A));
-    FFGPU_TRY(ffgpu_matrix_to_f32(A));
+    FFGPU_TRY(sell_values(A, kSell32));
     DevIn<double> bd(b, n, s);
     DevOut<double> xd(x, n, s, true);
     FFGPU_TRY(bd.err);
     FFGPU_TRY(xd.err);
     IRState S;
-    if (cudaMallocAsync((void **)&S.g, sizeof(float) * (size_t)n * 5, s) != cudaSuccess ||
+    const int64_t vs = vstride(n);
+    if (cudaMallocAsync((void **)&S.g, sizeof(float) * (size_t)vs * 5, s) != cudaSuccess ||
         cudaMallocAsync((void **)&S.ks, sizeof(InnerScalars), s) != cudaSuccess ||
         cudaMallocAsync((void **)&S.y, sizeof(double) * ((size_t)n + 8), s) != cudaSuccess) {
         set_error("ffgpu_solve_ir: device allocation failed");
         ir_free(S, s);
         return FFGPU_ENOMEM;
     }
-    S.h = S.g + n; S.q = S.g + 2 * (size_t)n; S.d = S.g + 3 * (size_t)n; S.dinv = S.g + 4 * (size_t)n;
+    S.h = S.g + vs; S.q = S.g + 2 * vs; S.d = S.g + 3 * vs; S.dinv = S.g + 4 * vs;
     S.out3 = S.y + n;
     to_f32_kernel<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, A->diag_inv, S.dinv);
     ctx->launches++;
@@ -398,7 +348,15 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     const int itmax_in = prm->itmax_inner > 0 ? prm->itmax_inner : n;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 30;
     const double eps = prm->eps;
-    const float eps_in = (float)(prm->eps_inner > 0 ? prm->eps_inner : 1e-5);
+    // Inner tolerance: per restarted solve, or the residual drop between two replacements.
+    // Segments that keep the search direction are capped at twice the iterations the first
+    // (fresh) segment needed for the same drop; one that misses its drop within the cap means
+    // FP32 round-off has broken the recurrence (very ill-conditioned systems), and the solve
+    // continues with restarted inner solves.
+    bool keep = prm->restart_inner == 0;
+    float eps_in = (float)(prm->eps_inner > 0 ? prm->eps_inner : (keep ? 1e-2 : 1e-5));
+    int first_its = -1;
+    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -412,8 +370,9 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     double *part64 = ctx->d_part;
     for (outer = 0; outer <= max_outer; ++outer) {
         if ((rc = spmv(A, xd.d, S.y, 0, s))) break;
+        const int fresh = !keep || outer == 0;
         ir_outer_kernel<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, bd.d, S.y, A->diag_inv, S.dinv, S.g, S.h, S.d,
-                                                            part64, ctx->d_ticket, S.out3);
+                                                            part64, ctx->d_ticket, S.out3, fresh);
         ctx->launches++;
         double o3[3];
         cudaMemcpyAsync(o3, S.out3, sizeof(o3), cudaMemcpyDeviceToHost, s);
@@ -430,13 +389,25 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
         }
         if (gcg < eps2) { converged = 1; break; }
         if (outer == max_outer) break;
-        ir_inner_init<<<1, 1, 0, s>>>(S.ks, S.out3, eps_in, itmax_in);
-        ctx->launches++;
+        if (fresh) {
+            ir_inner_init<<<1, 1, 0, s>>>(S.ks, S.out3, eps_in, itmax_in);
+            ctx->launches++;
+        } else {
+            const int cap = first_its > 0 ? min(itmax_in, max(64, 2 * first_its)) : itmax_in;
+            ir_inner_keep<<<1, 1, 0, s>>>(S.ks, S.out3, eps_in, cap);
+            ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, (float *)ctx->d_part);
+            ctx->launches += 2;
+        }
         if (cudaGraphLaunch(S.exec, s) != cudaSuccess) { set_error("ffgpu_solve_ir: graph launch failed"); rc = FFGPU_ECUDA; break; }
         InnerScalars hk;
         cudaMemcpyAsync(&hk, S.ks, sizeof(hk), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
         inner_total += hk.iter;
+        if (fresh && first_its < 0) first_its = hk.iter;
+        if (!fresh && !hk.converged) {
+            keep = false;
+            if (prm->eps_inner <= 0) eps_in = 1e-5f;
+        }
         int bodies = hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll;
         ctx->launches += (int64_t)bodies * 3 * unroll;
         ir_update_kernel<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, xd.d, S.d);

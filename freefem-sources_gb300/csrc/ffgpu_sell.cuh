@@ -1,0 +1,171 @@
+// ffgpu_sell.cuh -- device row kernels of the SELL-32 SpMV (layout in ffgpu_sell.cu) and the
+// block reductions shared by the fused Krylov kernels.
+#pragma once
+#include "ffgpu_internal.cuh"
+
+namespace ffgpu {
+
+// ------------------------------------------------------------------ block reductions
+// Block sum; the block total is returned in every thread of warp 0 (thread 0 uses it).
+template <typename T>
+__device__ __forceinline__ T block_sum_t(T v, T *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    T t = 0;
+    if (w == 0) {
+        t = lane < nw ? sh[lane] : T(0);
+        t = warp_sum(t);
+    }
+    __syncthreads();
+    return t;
+}
+
+// Stores this block's partial; returns true in exactly one thread of the last block to finish,
+// whose `tot` receives the sum of all partials in block order (deterministic).
+template <typename T>
+__device__ __forceinline__ bool last_block_sum(T partial, T *part, unsigned *ticket, T *tot, T *sh) {
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = partial;
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    T s = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(part + i);
+    s = block_sum_t(s, sh);
+    if (threadIdx.x == 0) {
+        *tot = s;
+        *ticket = 0u;
+        return true;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ double-float arithmetic
+// FP64 values and vectors split exactly into FP32 pairs v = hi + lo (48 of the 53 bits); a
+// product hi*hi is formed exactly as p + e (e = fma(a, x, -p)), the cross terms are added in
+// FP32, and sums are kept as an unevaluated pair (S, C) with Knuth's TwoSum.  The row result
+// (double)S + (double)C is accurate to about 2^-44 relative.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void df_fma(float2 a, float2 x, float &S, float &C) {
+    float p = __fmul_rn(a.x, x.x);
+    float pe = __fmaf_rn(a.x, x.x, -p);
+    float t = __fmaf_rn(a.x, x.y, __fmaf_rn(a.y, x.x, pe));
+    float s2, e;
+    two_sum(S, p, s2, e);
+    S = s2;
+    C = __fadd_rn(C, __fadd_rn(e, t));
+}
+
+__device__ __forceinline__ float2 split_f64(double v) {
+    float hi = __double2float_rn(v);
+    float lo = __double2float_rn(v - (double)hi);
+    return make_float2(hi, lo);
+}
+
+// ------------------------------------------------------------------ SELL-32 rows
+// One block row per lane: lane `lane` of chunk c holds row a (a < 0: padding lane, its
+// entries are zero blocks on column 0).  Entries are read in column order; matrix streams use
+// evict-first loads so that the gathered vector stays in L2.
+template <bool C16>
+__device__ __forceinline__ int sell_col(const SellArgs &S, int64_t e, int ar) {
+    if (C16) return ar + (int)__ldcs(S.col16 + e);
+    return __ldcs(S.col + e);
+}
+
+template <int BS, bool C16>
+__device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__restrict__ val,
+                                           const double *__restrict__ x, int c, int lane, int a, double *y) {
+    const int L = __ldg(S.len + c);
+    const int64_t sr = __ldg(S.off + c);
+    const int ar = a < 0 ? 0 : a;
+    const int64_t ce = sr * 32 + lane;
+    const double *v = val + sr * (BS * BS * 32) + lane;
+    double s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll 2
+    for (int j = 0; j < L; ++j) {
+        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
+        if (BS == 1) {
+            s0 = fma(__ldcs(v + (int64_t)j * 32), __ldg(x + col), s0);
+        } else {
+            const double x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
+                         x2 = __ldg(x + 3 * (int64_t)col + 2);
+            const double *w = v + (int64_t)j * 288;
+            s0 = fma(__ldcs(w), x0, s0); s0 = fma(__ldcs(w + 32), x1, s0); s0 = fma(__ldcs(w + 64), x2, s0);
+            s1 = fma(__ldcs(w + 96), x0, s1); s1 = fma(__ldcs(w + 128), x1, s1); s1 = fma(__ldcs(w + 160), x2, s1);
+            s2 = fma(__ldcs(w + 192), x0, s2); s2 = fma(__ldcs(w + 224), x1, s2); s2 = fma(__ldcs(w + 256), x2, s2);
+        }
+    }
+    y[0] = s0;
+    if (BS == 3) { y[1] = s1; y[2] = s2; }
+}
+
+template <int BS, bool C16>
+__device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__restrict__ val,
+                                          const float2 *__restrict__ x, int c, int lane, int a, double *y) {
+    const int L = __ldg(S.len + c);
+    const int64_t sr = __ldg(S.off + c);
+    const int ar = a < 0 ? 0 : a;
+    const int64_t ce = sr * 32 + lane;
+    const float2 *v = val + sr * (BS * BS * 32) + lane;
+    float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
+#pragma unroll 2
+    for (int j = 0; j < L; ++j) {
+        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
+        if (BS == 1) {
+            df_fma(__ldcs(v + (int64_t)j * 32), __ldg(x + col), S0, C0);
+        } else {
+            const float2 x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
+                         x2 = __ldg(x + 3 * (int64_t)col + 2);
+            const float2 *w = v + (int64_t)j * 288;
+            df_fma(__ldcs(w), x0, S0, C0); df_fma(__ldcs(w + 32), x1, S0, C0); df_fma(__ldcs(w + 64), x2, S0, C0);
+            df_fma(__ldcs(w + 96), x0, S1, C1); df_fma(__ldcs(w + 128), x1, S1, C1); df_fma(__ldcs(w + 160), x2, S1, C1);
+            df_fma(__ldcs(w + 192), x0, S2, C2); df_fma(__ldcs(w + 224), x1, S2, C2); df_fma(__ldcs(w + 256), x2, S2, C2);
+        }
+    }
+    y[0] = (double)S0 + (double)C0;
+    if (BS == 3) {
+        y[1] = (double)S1 + (double)C1;
+        y[2] = (double)S2 + (double)C2;
+    }
+}
+
+template <int BS, bool C16>
+__device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__restrict__ val,
+                                           const float *__restrict__ x, int c, int lane, int a, float *y) {
+    const int L = __ldg(S.len + c);
+    const int64_t sr = __ldg(S.off + c);
+    const int ar = a < 0 ? 0 : a;
+    const int64_t ce = sr * 32 + lane;
+    const float *v = val + sr * (BS * BS * 32) + lane;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < L; ++j) {
+        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
+        if (BS == 1) {
+            s0 = fmaf(__ldcs(v + (int64_t)j * 32), __ldg(x + col), s0);
+        } else {
+            const float x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
+                        x2 = __ldg(x + 3 * (int64_t)col + 2);
+            const float *w = v + (int64_t)j * 288;
+            s0 = fmaf(__ldcs(w), x0, s0); s0 = fmaf(__ldcs(w + 32), x1, s0); s0 = fmaf(__ldcs(w + 64), x2, s0);
+            s1 = fmaf(__ldcs(w + 96), x0, s1); s1 = fmaf(__ldcs(w + 128), x1, s1); s1 = fmaf(__ldcs(w + 160), x2, s1);
+            s2 = fmaf(__ldcs(w + 192), x0, s2); s2 = fmaf(__ldcs(w + 224), x1, s2); s2 = fmaf(__ldcs(w + 256), x2, s2);
+        }
+    }
+    y[0] = s0;
+    if (BS == 3) { y[1] = s1; y[2] = s2; }
+}
+
+}  // namespace ffgpu

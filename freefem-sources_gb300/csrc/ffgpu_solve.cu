@@ -13,12 +13,14 @@
 // a CUDA graph `while` node whose condition K_b clears on convergence or at itmax, so a
 // whole solve is one graph launch with no host round trip.
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <vector>
 
 #include "ffgpu_internal.cuh"
+#include "ffgpu_sell.cuh"
 
 namespace ffgpu {
 
@@ -28,45 +30,15 @@ constexpr int kVecBlocks = 4 * kNumSM;        // grid of the fused vector kernel
 constexpr int kVecThreads = 256;
 
 // ------------------------------------------------------------------ reductions
-// Block sum of one double; returns the block total in thread 0.
-__device__ __forceinline__ double block_sum(double v, double *sh) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_sum(v);
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double t = 0;
-    if (w == 0) {
-        t = lane < nw ? sh[lane] : 0.0;
-        t = warp_sum(t);
-    }
-    __syncthreads();
-    return t;
-}
-
-// Stores this block's partial, returns true in exactly one thread of the last block to
-// finish; that thread's `tot` receives the deterministic sum of all partials (fixed order).
+__device__ __forceinline__ double block_sum(double v, double *sh) { return block_sum_t(v, sh); }
 __device__ __forceinline__ bool last_block_total(double partial, double *part, unsigned *ticket,
                                                   double *tot, double *sh) {
-    __shared__ bool s_last;
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = partial;
-        __threadfence();
-        unsigned t = atomicAdd(ticket, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double s = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(part + i);
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) {
-        *tot = s;
-        *ticket = 0u;
-        return true;
-    }
-    return false;
+    return last_block_sum(partial, part, ticket, tot, sh);
 }
+
+// cudaGraphSetConditional out of line: inlined, its call sequence raises the register count
+// of the whole kernel
+__device__ __noinline__ void graph_stop(cudaGraphConditionalHandle cond) { cudaGraphSetConditional(cond, 0); }
 
 // ------------------------------------------------------------------ SpMV rows
 // CSR (block size 1): T lanes per row, lanes stride the row.
@@ -179,6 +151,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
     }
 }
 
+// The vector kernels run on a resident grid and read/write two elements per access (all
+// work vectors are 16-byte aligned); an odd last element is done by thread 0 of block 0.
 // K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence
 __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
                                                      const double *__restrict__ h, const double *__restrict__ q,
@@ -186,15 +160,29 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
                                                      double *part, cudaGraphConditionalHandle cond, int in_graph) {
     __shared__ double sh[32];
     if (ks->done) {
-        if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0);
+        if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) graph_stop(cond);
         return;
     }
     const double rho = ks->rho;
     double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double hi = h[i];
-        x[i] = fma(rho, hi, x[i]);
-        double gi = fma(rho, q[i], g[i]);
+    const int n2 = n >> 1;
+    double2 *x2 = reinterpret_cast<double2 *>(x), *g2 = reinterpret_cast<double2 *>(g);
+    const double2 *h2 = reinterpret_cast<const double2 *>(h), *q2 = reinterpret_cast<const double2 *>(q),
+                  *d2 = reinterpret_cast<const double2 *>(dinv);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        const double2 hv = h2[i], qv = q2[i], dv = d2[i];
+        double2 xv = x2[i], gv = g2[i];
+        xv.x = fma(rho, hv.x, xv.x); xv.y = fma(rho, hv.y, xv.y);
+        gv.x = fma(rho, qv.x, gv.x); gv.y = fma(rho, qv.y, gv.y);
+        x2[i] = xv;
+        g2[i] = gv;
+        s = fma(gv.x, dv.x * gv.x, s);
+        s = fma(gv.y, dv.y * gv.y, s);
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int i = n - 1;
+        x[i] = fma(rho, h[i], x[i]);
+        const double gi = fma(rho, q[i], g[i]);
         g[i] = gi;
         s = fma(gi, dinv[i] * gi, s);
     }
@@ -207,22 +195,43 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         ks->iter += 1;
         if (tot < ks->eps2) { ks->converged = 1; ks->done = 1; }
         else if (ks->iter >= ks->itmax) ks->done = 1;
-        if (ks->done && in_graph) cudaGraphSetConditional(cond, 0);
+        if (ks->done && in_graph) graph_stop(cond);
     }
 }
 
-// K_c: H = gamma H - C G and (G, H)
-__global__ void __launch_bounds__(kVecThreads) cg_kc(int n, const double *__restrict__ g, double *__restrict__ h,
-                                                     const double *__restrict__ dinv, KrylovScalars *ks,
-                                                     double *part) {
+// K_c: H = gamma H - C G and (G, H); with hx != NULL also the split copy of H for the next
+// double-float SpMV
+template <bool SPLIT>
+__global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__restrict__ g, double *__restrict__ h,
+                                                       float2 *__restrict__ hx, const double *__restrict__ dinv,
+                                                       KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
     if (ks->done) return;
     const double gamma = ks->gamma;
     double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double gi = g[i];
-        double hi = gamma * h[i] - dinv[i] * gi;
+    const int n2 = n >> 1;
+    double2 *h2 = reinterpret_cast<double2 *>(h);
+    const double2 *g2 = reinterpret_cast<const double2 *>(g), *d2 = reinterpret_cast<const double2 *>(dinv);
+    float4 *hx2 = reinterpret_cast<float4 *>(hx);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
+        const double2 gv = g2[i], dv = d2[i];
+        double2 hv = h2[i];
+        hv.x = gamma * hv.x - dv.x * gv.x;
+        hv.y = gamma * hv.y - dv.y * gv.y;
+        h2[i] = hv;
+        if (SPLIT) {
+            const float2 a = split_f64(hv.x), b = split_f64(hv.y);
+            hx2[i] = make_float4(a.x, a.y, b.x, b.y);
+        }
+        s = fma(gv.x, hv.x, s);
+        s = fma(gv.y, hv.y, s);
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int i = n - 1;
+        const double gi = g[i];
+        const double hi = gamma * h[i] - dinv[i] * gi;
         h[i] = hi;
+        if (SPLIT) hx[i] = split_f64(hi);
         s = fma(gi, hi, s);
     }
     double tot;
@@ -231,40 +240,14 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc(int n, const double *__rest
 }
 
 // ------------------------------------------------------------------ double-float SpMV
-// FP64 values and vectors, products formed on the FP32 pipe with error-free transformations:
-// a = a_hi + a_lo and x = x_hi + x_lo are exact FP32 splits (to 48 of the 53 bits), a_hi x_hi
-// is formed exactly as p + e with e = fma(a_hi, x_hi, -p), the cross terms a_hi x_lo + a_lo x_hi
-// are added in FP32, and the sums are kept as an unevaluated pair (S, C) with TwoSum.  The row
-// result is (double)S + (double)C, about 2^-44 relative; GB300 issues 64 FP32 FMAs per FP64
-// FMA, so this moves the SpMV from the FP64 pipe bound to the HBM bound.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-__device__ __forceinline__ void df_fma(float2 a, float2 x, float &S, float &C) {
-    float p = __fmul_rn(a.x, x.x);
-    float pe = __fmaf_rn(a.x, x.x, -p);
-    float t = __fmaf_rn(a.x, x.y, __fmaf_rn(a.y, x.x, pe));
-    float s2, e;
-    two_sum(S, p, s2, e);
-    S = s2;
-    C = __fadd_rn(C, __fadd_rn(e, t));
-}
-
+// FP64 values and vectors with the products formed on the FP32 pipe (df_fma): GB300 issues 64
+// FP32 FMAs per FP64 FMA, so this moves the SpMV from the FP64-pipe bound to the HBM bound.
 __device__ __forceinline__ void df_add_shfl(float &S, float &C, int o) {
     float S2 = __shfl_xor_sync(0xffffffffu, S, o), C2 = __shfl_xor_sync(0xffffffffu, C, o);
     float s2, e;
     two_sum(S, S2, s2, e);
     S = s2;
     C = __fadd_rn(__fadd_rn(C, C2), e);
-}
-
-__device__ __forceinline__ float2 split_f64(double v) {
-    float hi = __double2float_rn(v);
-    float lo = __double2float_rn(v - (double)hi);
-    return make_float2(hi, lo);
 }
 
 __global__ void split_kernel(int64_t n, const double *__restrict__ v, float2 *__restrict__ out) {
@@ -312,9 +295,15 @@ __device__ __forceinline__ void bsr3_row_x(const SpmvArgsX &A, const float2 *__r
         df_add_shfl(S1, C1, o);
         df_add_shfl(S2, C2, o);
     }
-    y[0] = (double)S0 + (double)C0;
-    y[1] = (double)S1 + (double)C1;
-    y[2] = (double)S2 + (double)C2;
+    if (T >= 4) {
+        // conversions to FP64 issue on the FP64 pipe: lane `sub` < 3 forms output `sub` only
+        const float S = sub == 0 ? S0 : (sub == 1 ? S1 : S2), C = sub == 0 ? C0 : (sub == 1 ? C1 : C2);
+        y[0] = (double)S + (double)C;
+    } else {
+        y[0] = (double)S0 + (double)C0;
+        y[1] = (double)S1 + (double)C1;
+        y[2] = (double)S2 + (double)C2;
+    }
 }
 
 // K_a with the double-float SpMV: AH = A H from the split H, (H, AH) in FP64
@@ -339,7 +328,13 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
         } else {
             double v[3];
             bsr3_row_x<T>(A, hx, a, ok ? sub : T, v);
-            if (ok && sub == 0) {
+            if (T >= 4) {
+                if (ok && sub < 3) {
+                    int64_t i = 3 * (int64_t)a + sub;
+                    q[i] = v[0];
+                    hq = fma(h[i], v[0], hq);
+                }
+            } else if (ok && sub == 0) {
                 int64_t i = 3 * (int64_t)a;
                 q[i] = v[0]; q[i + 1] = v[1]; q[i + 2] = v[2];
                 hq = fma(h[i], v[0], hq);
@@ -356,24 +351,86 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
     }
 }
 
-// K_c that also refreshes the split copy of H for the next double-float SpMV
-__global__ void __launch_bounds__(kVecThreads) cg_kc_x(int n, const double *__restrict__ g, double *__restrict__ h,
-                                                       float2 *__restrict__ hx, const double *__restrict__ dinv,
-                                                       KrylovScalars *ks, double *part) {
+// ------------------------------------------------------------------ SELL-32 K_a
+// One block row per lane, one chunk of 32 rows per warp (resident grid, chunks strided over
+// warps).  FP64: AH = A H and (H, AH) -> rho; padding lanes (a < 0) write nothing.
+template <int BS, bool C16>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const double *__restrict__ val,
+                                                              const double *__restrict__ h, double *__restrict__ q,
+                                                              KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
     if (ks->done) return;
-    const double gamma = ks->gamma;
-    double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double gi = g[i];
-        double hi = gamma * h[i] - dinv[i] * gi;
-        h[i] = hi;
-        hx[i] = split_f64(hi);
-        s = fma(gi, hi, s);
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double hq = 0;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+        double y[BS];
+        sell_row64<BS, C16>(S, val, h, c, lane, a, y);
+        if (a >= 0) {
+#pragma unroll
+            for (int m = 0; m < BS; ++m) {
+                const int64_t i = (int64_t)BS * a + m;
+                q[i] = y[m];
+                hq = fma(h[i], y[m], hq);
+            }
+        }
     }
     double tot;
-    double p = block_sum(s, sh);
-    if (last_block_total(p, part, &ks->ticket, &tot, sh)) ks->s_gh = tot;
+    double p = block_sum(hq, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
+        ks->s_hq = tot;
+        ks->rho = -ks->s_gh / tot;
+    }
+}
+
+// double-float: AH = A H from the split H, (H, AH) in FP64
+template <int BS, bool C16>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const float2 *__restrict__ val,
+                                                               const float2 *__restrict__ hx,
+                                                               const double *__restrict__ h, double *__restrict__ q,
+                                                               KrylovScalars *ks, double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double hq = 0;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+        double y[BS];
+        sell_rowx<BS, C16>(S, val, hx, c, lane, a, y);
+        if (a >= 0) {
+#pragma unroll
+            for (int m = 0; m < BS; ++m) {
+                const int64_t i = (int64_t)BS * a + m;
+                q[i] = y[m];
+                hq = fma(h[i], y[m], hq);
+            }
+        }
+    }
+    double tot;
+    double p = block_sum(hq, sh);
+    if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
+        ks->s_hq = tot;
+        ks->rho = -ks->s_gh / tot;
+    }
+}
+
+// y = A x (FP64)
+template <int BS, bool C16>
+__global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const double *__restrict__ val,
+                                                             const double *__restrict__ x, double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+        double r[BS];
+        sell_row64<BS, C16>(S, val, x, c, lane, a, r);
+        if (a >= 0) {
+#pragma unroll
+            for (int m = 0; m < BS; ++m) y[(int64_t)BS * a + m] = r[m];
+        }
+    }
 }
 
 __global__ void split_vec_kernel(int n, const double *__restrict__ h, float2 *__restrict__ hx) {
@@ -511,8 +568,11 @@ __global__ void transpose_kernel(int nb, int bs, const int32_t *brp, const int32
 }
 
 // ------------------------------------------------------------------ host side
+constexpr int kSellLanes = 64;   // tuner's code for the SELL-32 kernels (one row per lane)
+
+// lanes per block row of the block-CSR kernels
 static int pick_lanes(const ffgpu_matrix *A) {
-    if (A->csr_lanes > 0) return A->csr_lanes;
+    if (A->csr_lanes > 0 && A->csr_lanes != kSellLanes) return A->csr_lanes;
     double avg = (double)A->nnzb / (double)max(1, A->nb);
     if (A->bs == 3) return avg >= 24 ? 4 : 2;
     if (avg >= 24) return 8;
@@ -569,8 +629,68 @@ static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
     return s;
 }
 
-// Times the SpMV kernel of one mode (0: FP64, 1: double-float) with each candidate
-// lanes-per-row on this matrix; the choice is cached per matrix shape in the context.
+// One K_a launch of the CG loop, with its argument storage.
+struct KaCall {
+    void *fn = nullptr;
+    int grid = 0;
+    SpmvArgs sa;
+    SpmvArgsX sx;
+    SellArgs sl;
+    const double *v64 = nullptr;
+    const float2 *vx = nullptr;
+    const float2 *hx = nullptr;
+    const double *h = nullptr;
+    double *q = nullptr;
+    KrylovScalars *ks = nullptr;
+    double *part = nullptr;
+    void *args[7];
+    cudaError_t launch(cudaStream_t s) { return cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, s); }
+};
+
+// K_a for mode (0 FP64, 1 double-float) and lanes choice T (kSellLanes: SELL-32)
+static int ka_setup(ffgpu_matrix *A, int mode, int trans, int T, const double *h, double *q, KaCall &k) {
+    k.h = h; k.q = q; k.ks = A->ks; k.part = A->ctx->d_part; k.hx = A->hx;
+    if (T == kSellLanes) {
+        FFGPU_TRY(sell_values(A, mode == 1 ? (trans ? kSellXT : kSellX) : (trans ? kSell64T : kSell64)));
+        // the column format is known only once the layout exists
+        const bool c16 = A->scol16 != nullptr;
+        k.sl = sell_args(A);
+        if (mode == 1) {
+            k.vx = trans ? A->svalx_t : A->svalx;
+            k.fn = A->bs == 3 ? (void *)cg_kax_sell<3, false>
+                              : (c16 ? (void *)cg_kax_sell<1, true> : (void *)cg_kax_sell<1, false>);
+            k.args[0] = &k.sl; k.args[1] = &k.vx; k.args[2] = &k.hx; k.args[3] = &k.h; k.args[4] = &k.q;
+            k.args[5] = &k.ks; k.args[6] = &k.part;
+        } else {
+            k.v64 = trans ? A->sval_t : A->sval;
+            k.fn = A->bs == 3 ? (void *)cg_ka_sell<3, false>
+                              : (c16 ? (void *)cg_ka_sell<1, true> : (void *)cg_ka_sell<1, false>);
+            k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.h; k.args[3] = &k.q; k.args[4] = &k.ks;
+            k.args[5] = &k.part;
+        }
+        k.grid = resident_grid(k.fn, kSpmvWarps * 32);
+        return FFGPU_OK;
+    }
+    if (mode == 1) {
+        FFGPU_TRY(matrix_prepare_split(A, trans));
+        k.sx = SpmvArgsX{A->nb, A->bs, A->browptr, A->bcol, trans ? A->valx_t : A->valx, A->rowperm};
+        k.fn = A->bs == 3 ? kax_fn<3>(T) : kax_fn<1>(T);
+        k.args[0] = &k.sx; k.args[1] = &k.hx; k.args[2] = &k.h; k.args[3] = &k.q; k.args[4] = &k.ks;
+        k.args[5] = &k.part;
+    } else {
+        if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
+        k.sa = spmv_args(A, trans);
+        k.fn = A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T);
+        k.args[0] = &k.sa; k.args[1] = &k.h; k.args[2] = &k.q; k.args[3] = &k.ks; k.args[4] = &k.part;
+    }
+    k.grid = spmv_grid(A, T);
+    return FFGPU_OK;
+}
+
+// Times the K_a kernel of one mode (0: FP64, 1: double-float) for the SELL-32 layout and for
+// block CSR with each candidate lanes-per-row on this matrix, and keeps the fastest; the
+// choice is cached per matrix shape in the context.  Value arrays of the losing layout are
+// released.
 static int tune_lanes(ffgpu_matrix *A, int mode) {
     int *slot = mode == 1 ? &A->csr_lanes_x : &A->csr_lanes;
     if (*slot > 0) return FFGPU_OK;
@@ -581,54 +701,70 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
             *slot = ctx->tuned[i].lanes;
             return FFGPU_OK;
         }
-    if (!A->vec || (mode == 1 && !A->valx)) { *slot = pick_lanes(A); return FFGPU_OK; }
-    // FP64: reductions across lanes cost FP64 adds, so few lanes per row; double-float:
-    // reductions are FP32, so wide lane groups with coalesced block runs
-    const int cands64[] = {1, 2, 4, 8};
-    const int candsx[] = {4, 8, 16, 32};
+    if (!A->vec) { *slot = kSellLanes; return FFGPU_OK; }
+    // FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row;
+    // double-float: reductions are FP32, so wider lane groups
+    const int cands64[] = {kSellLanes, 1, 2, 4, 8};
+    const int candsx[] = {kSellLanes, 4, 8, 16, 32};
     const int *cands = mode == 1 ? candsx : cands64;
-    double *y = A->vec + 6 * (int64_t)A->n, *x = A->vec + 5 * (int64_t)A->n;
+    const int64_t vs = vstride(A->n);
+    double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
     cudaStream_t s = ctx->stream;
+    if (mode == 1 && !A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vs));
     FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
     if (mode == 1) FFGPU_CUDA(cudaMemsetAsync(A->hx, 0, sizeof(float2) * A->n, s));
     KrylovScalars *ks = A->ks;
     FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
-    double *part = ctx->d_part;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int bestT = pick_lanes(A);
-    SpmvArgs sa = spmv_args(A, 0);
-    SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, A->valx, A->rowperm};
-    float2 *hx = A->hx;
-    for (int c = 0; c < 4; ++c) {
-        int T = cands[c];
-        void *fn;
-        void *args64[] = {&sa, &x, &y};
-        void *argsx[] = {&sx, &hx, &x, &y, &ks, &part};
-        void **args = mode == 1 ? argsx : args64;
-        if (mode == 1) fn = A->bs == 3 ? kax_fn<3>(T) : kax_fn<1>(T);
-        else fn = A->bs == 3 ? spmv_fn<3>(T) : spmv_fn<1>(T);
-        cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);   // warm
+    int bestT = kSellLanes;
+    for (int c = 0; c < 5; ++c) {
+        const int T = cands[c];
+        KaCall k;
+        FFGPU_TRY(ka_setup(A, mode, 0, T, x, y, k));
+        k.launch(s);   // warm
         cudaEventRecord(e0, s);
-        for (int r = 0; r < 3; ++r) cudaLaunchKernel(fn, spmv_grid(A, T), kSpmvWarps * 32, args, 0, s);
+        for (int r = 0; r < 3; ++r) k.launch(s);
         cudaEventRecord(e1, s);
         FFGPU_CUDA(cudaEventSynchronize(e1));
+        FFGPU_CUDA(cudaGetLastError());
         ctx->launches += 4;
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        if (getenv("FFGPU_VERBOSE"))
+            fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s%d %.4f ms\n", mode,
+                    A->nb, (long long)A->nnzb, T == kSellLanes ? "sell32 " : "bsr lanes ",
+                    T == kSellLanes ? 32 : T, ms / 3);
         if (ms < best) { best = ms; bestT = T; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    if (bestT == kSellLanes) {
+        if (mode == 1) { cudaFree(A->valx); A->valx = nullptr; }
+    } else if (mode == 1) {
+        cudaFree(A->svalx); A->svalx = nullptr;
+    } else {
+        cudaFree(A->sval); A->sval = nullptr;
+    }
     *slot = bestT;
     if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT, mode};
     return FFGPU_OK;
 }
 
 int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st) {
+    const double *sv = trans ? A->sval_t : A->sval;
+    if (sv) {
+        SellArgs sl = sell_args(A);
+        void *fn = A->bs == 3 ? (void *)spmv_sell<3, false>
+                              : (A->scol16 ? (void *)spmv_sell<1, true> : (void *)spmv_sell<1, false>);
+        void *args[] = {&sl, &sv, &x, &y};
+        FFGPU_CUDA(cudaLaunchKernel(fn, resident_grid(fn, kSpmvWarps * 32), kSpmvWarps * 32, args, 0, st));
+        return launch_check(A->ctx, "spmv");
+    }
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
     int T = pick_lanes(A);
     SpmvArgs s = spmv_args(A, trans);
@@ -640,7 +776,7 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
 
 int matrix_prepare_split(ffgpu_matrix *A, int trans) {
     ffgpu_ctx *ctx = A->ctx;
-    if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * A->n));
+    if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vstride(A->n)));
     float2 **dst = trans ? &A->valx_t : &A->valx;
     if (*dst) return FFGPU_OK;
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
@@ -664,8 +800,8 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
     cudaStream_t s = ctx->stream;
     int64_t n = A->n;
     if (!A->vec) {
-        FFGPU_CUDA(cudaMalloc((void **)&A->vec, sizeof(double) * n * 8));
-        FFGPU_CUDA(cudaMalloc((void **)&A->diag_inv, sizeof(double) * n));
+        FFGPU_CUDA(cudaMalloc((void **)&A->vec, sizeof(double) * vstride(n) * 8));
+        FFGPU_CUDA(cudaMalloc((void **)&A->diag_inv, sizeof(double) * vstride(n)));
         FFGPU_CUDA(cudaMalloc((void **)&A->wcl, n));
         FFGPU_CUDA(cudaMalloc((void **)&A->ks, sizeof(KrylovScalars)));
         FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
@@ -700,12 +836,40 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
     return launch_check(ctx, "jacobi");
 }
 
+static int vec_grid_kb() {
+    static int g = 0;
+    if (!g) g = min(4096, resident_grid((const void *)cg_kb, kVecThreads));
+    return g;
+}
+static int vec_grid_kc() {
+    static int g = 0;
+    if (!g) g = min(4096, max(resident_grid((const void *)cg_kc_t<false>, kVecThreads),
+                              resident_grid((const void *)cg_kc_t<true>, kVecThreads)));
+    return g;
+}
+
+// One CG iteration (K_a K_b K_c) on stream s.
+static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h, double *q, const double *dinv,
+                    float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
+                    cudaStream_t s) {
+    ka.launch(s);
+    cg_kb<<<vec_grid_kb(), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, in_graph);
+    if (mode == 1)
+        cg_kc_t<true><<<vec_grid_kc(), kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
+    else
+        cg_kc_t<false><<<vec_grid_kc(), kVecThreads, 0, s>>>(n, g, h, nullptr, dinv, ks, part);
+}
+
 // Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }].
 static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x, double *g, double *h, double *q) {
     if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans && A->cg_mode == mode) return FFGPU_OK;
     if (A->cg_exec) { cudaGraphExecDestroy(A->cg_exec); A->cg_exec = nullptr; }
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
+    KaCall ka;
+    FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
+    vec_grid_kb();
+    vec_grid_kc();
     cudaGraph_t graph, body;
     FFGPU_CUDA(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle cond;
@@ -722,31 +886,8 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int T = pick_lanes(A);
-    const int TX = A->csr_lanes_x > 0 ? A->csr_lanes_x : T;
-    SpmvArgs sa = spmv_args(A, trans);
-    void *ka = A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T);
-    int n = A->n;
-    KrylovScalars *ks = A->ks;
-    double *part = ctx->d_part;
-    const double *dinv = A->diag_inv;
-    SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, trans ? A->valx_t : A->valx, A->rowperm};
-    void *kax = A->bs == 3 ? kax_fn<3>(TX) : kax_fn<1>(TX);
-    float2 *hx = A->hx;
-    for (int u = 0; u < unroll; ++u) {
-        if (mode == 1) {
-            void *aa[] = {&sx, &hx, &h, &q, &ks, &part};
-            cudaLaunchKernel(kax, spmv_grid(A, TX), kSpmvWarps * 32, aa, 0, s);
-        } else {
-            void *aa[] = {&sa, &h, &q, &ks, &part};
-            cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
-        }
-        cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, 1);
-        if (mode == 1)
-            cg_kc_x<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
-        else
-            cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, dinv, ks, part);
-    }
+    for (int u = 0; u < unroll; ++u)
+        cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s);
     cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e != cudaSuccess) {
         set_error("CG graph capture failed: %s", cudaGetErrorString(e));
@@ -773,17 +914,18 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
     int n = A->n;
+    const int64_t vs = vstride(n);
     // the cached graph only ever touches matrix-owned buffers: the caller's x is staged in
     // slot 4 of the work vectors and copied back after the solve
-    double *g = A->vec, *h = A->vec + n, *q = A->vec + 2 * (int64_t)n;
+    double *g = A->vec, *h = A->vec + vs, *q = A->vec + 2 * vs;
     double *xu = x;
-    x = A->vec + 4 * (int64_t)n;
+    x = A->vec + 4 * vs;
     double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
     int itmax = prm->itmax > 0 ? prm->itmax : n;
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
     const int mode = prm->spmv_mode == 1 ? 1 : 0;
     if (mode == 1) {
-        FFGPU_TRY(matrix_prepare_split(A, trans));
+        if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vs));
         FFGPU_TRY(tune_lanes(A, 1));
     }
     FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
@@ -808,32 +950,15 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     if (ge && ge[0] == '0') {
         // Same kernels launched from the host (for profilers that do not trace conditional
         // graph nodes): poll the done flag after every `unroll` iterations.
-        int T = mode == 1 ? (A->csr_lanes_x > 0 ? A->csr_lanes_x : pick_lanes(A)) : pick_lanes(A);
-        SpmvArgs sa = spmv_args(A, trans);
-        SpmvArgsX sx{A->nb, A->bs, A->browptr, A->bcol, trans ? A->valx_t : A->valx, A->rowperm};
-        void *ka = mode == 1 ? (A->bs == 3 ? kax_fn<3>(T) : kax_fn<1>(T)) : (A->bs == 3 ? ka_fn<3>(T) : ka_fn<1>(T));
-        KrylovScalars *ks = A->ks;
-        double *part = ctx->d_part;
-        float2 *hx = A->hx;
+        KaCall ka;
+        FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
         bodies_host = 0;
         for (int it = 0; it <= itmax; it += unroll) {
-            for (int u = 0; u < unroll; ++u) {
-                if (mode == 1) {
-                    void *aa[] = {&sx, &hx, &h, &q, &ks, &part};
-                    cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
-                } else {
-                    void *aa[] = {&sa, &h, &q, &ks, &part};
-                    cudaLaunchKernel(ka, spmv_grid(A, T), kSpmvWarps * 32, aa, 0, s);
-                }
-                cg_kb<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, g, h, q, A->diag_inv, ks, part, 0, 0);
-                if (mode == 1)
-                    cg_kc_x<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, hx, A->diag_inv, ks, part);
-                else
-                    cg_kc<<<kVecBlocks, kVecThreads, 0, s>>>(n, g, h, A->diag_inv, ks, part);
-            }
+            for (int u = 0; u < unroll; ++u)
+                cg_body(ka, mode, n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, 0, 0, s);
             ++bodies_host;
             int done = 0;
-            FFGPU_CUDA(cudaMemcpyAsync(&done, &ks->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+            FFGPU_CUDA(cudaMemcpyAsync(&done, &A->ks->done, sizeof(int), cudaMemcpyDeviceToHost, s));
             FFGPU_CUDA(cudaStreamSynchronize(s));
             if (done) break;
         }
@@ -960,7 +1085,7 @@ static int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, con
     FFGPU_CUDA(cudaMemsetAsync(dev, 0, sizeof(double) * nsc, s));
     double *Hn = dev, *rot0 = Hn + (size_t)(m + 2) * ld, *rot1 = rot0 + (m + 2), *gv = rot1 + (m + 2);
     double *y = gv + (m + 2), *dotv = y + (m + 2), *relres_d = dotv + 2;
-    double *wi = A->vec, *ri = A->vec + 2 * (int64_t)n, *x0 = A->vec + 3 * (int64_t)n;
+    double *wi = A->vec, *ri = A->vec + 2 * vstride(n), *x0 = A->vec + 3 * vstride(n);
     unsigned *tk = ctx->d_ticket;
     double *part = ctx->d_part;
     int rc = FFGPU_OK;
@@ -1097,6 +1222,11 @@ int ffgpu_solve_cg(ffgpu_matrix *A, const double *b, double *x, int nrhs, int tr
 int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
                       const ffgpu_solver_params *prm, ffgpu_solver_stats *stats) {
     return solve_many(A, b, x, nrhs, trans, prm, stats, gmres_one);
+}
+
+int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode) {
+    if (!A) return 0;
+    return mode == 1 ? A->csr_lanes_x : A->csr_lanes;
 }
 
 int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans) {

@@ -22,6 +22,7 @@ EXPORTS = [
     "ffgpu_ctx_stream",
     "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_space_set_boundary", "ffgpu_space_bc_mask", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
+    "ffgpu_matrix_spmv_layout",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
@@ -54,7 +55,8 @@ class SolverStats(C.Structure):
 
 class IRParams(C.Structure):
     _fields_ = [("eps", C.c_double), ("eps_inner", C.c_double), ("itmax_inner", C.c_int),
-                ("max_outer", C.c_int), ("tgv", C.c_double), ("unroll", C.c_int)]
+                ("max_outer", C.c_int), ("tgv", C.c_double), ("unroll", C.c_int),
+                ("restart_inner", C.c_int)]
 
 
 class FFGPUError(RuntimeError):
@@ -91,6 +93,7 @@ def lib():
         "ffgpu_matrix_from_csr": (i32, [vp, i32, i64, vp, vp, vp, P(vp)]),
         "ffgpu_matrix_destroy": (i32, [vp]),
         "ffgpu_matrix_info": (i32, [vp, P(i32), P(i64), P(i32)]),
+        "ffgpu_matrix_spmv_layout": (i32, [vp, i32]),
         "ffgpu_matrix_csr": (i32, [vp, vp, vp, vp]),
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),

@@ -28,9 +28,33 @@ def _np(a):
     return np.asarray(a, np.float64)
 
 
+def _on_device(a):
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _zeros(n, like):
+    """Zero vector of length n on the side (host numpy / CUDA torch) of `like`."""
+    if _on_device(like):
+        import torch
+        return torch.zeros(n, dtype=torch.float64, device=like.device)
+    return np.zeros(n)
+
+
+def _copy(a):
+    return a.clone() if _on_device(a) else np.array(a, copy=True)
+
+
 def sensitivity(A: api.Matrix, u, lam, c_stiff=1.0):
-    """(dL/dkappa_e, dL/df_e) of every element, given the state u and the adjoint lambda."""
+    """(dL/dkappa_e, dL/df_e) of every element, given the state u and the adjoint lambda.
+    Host arrays give numpy results; CUDA tensors give CUDA tensors (no host copy)."""
     nt = A.space.Vh.Th.nt
+    if _on_device(u):
+        import torch
+        gk = torch.empty(nt, dtype=torch.float64, device=u.device)
+        gf = torch.empty(nt, dtype=torch.float64, device=u.device)
+        check(lib().ffgpu_diffusion_sensitivity(A.h, api._ptr(u.contiguous()), api._ptr(lam.contiguous()),
+                                                float(c_stiff), api._ptr(gk), api._ptr(gf)))
+        return gk, gf
     gk = np.empty(nt)
     gf = np.empty(nt)
     uu = np.ascontiguousarray(u, np.float64)
@@ -53,8 +77,14 @@ class DiffusionProblem:
         self.A = None
 
     def assemble(self, kappa, f):
-        a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), on=self.on, tgv=self.tgv)
-        b = np.empty(self.Vh.ndof)
+        """A(kappa) and b(f) on the device; CUDA tensors for kappa (and f) keep b on the device."""
+        if _on_device(kappa):
+            a = api.varf_diffusion(kappa=kappa.contiguous(), f=f if np.isscalar(f) else f.contiguous(),
+                                   on=self.on, tgv=self.tgv)
+            b = _zeros(self.Vh.ndof, kappa)
+        else:
+            a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), on=self.on, tgv=self.tgv)
+            b = np.empty(self.Vh.ndof)
         if self.A is None:
             self.A = api.matrix(a, self.space, eps=self.eps, rhs_out=b)
         else:
@@ -70,6 +100,8 @@ class DiffusionProblem:
         return 0.5 * float(r @ self.mass.mult(r))
 
     def value_and_grad(self, kappa, f, u_obs):
+        """L, dL/dkappa, dL/df, u, lambda: one forward solve, one transpose solve, one
+        sensitivity pass (all on the device when kappa and u_obs are CUDA tensors)."""
         u = self.solve(kappa, f)
         r = u - u_obs
         Mr = self.mass.mult(r)
@@ -153,8 +185,13 @@ class HeatProblem:
         self.solves = 0
 
     def assemble(self, kappa, f):
-        a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), c_mass=1.0 / self.dt, on=self.on, tgv=self.tgv)
-        F = np.empty(self.Vh.ndof)
+        if _on_device(kappa):
+            a = api.varf_diffusion(kappa=kappa.contiguous(), f=f if np.isscalar(f) else f.contiguous(),
+                                   c_mass=1.0 / self.dt, on=self.on, tgv=self.tgv)
+            F = _zeros(self.Vh.ndof, kappa)
+        else:
+            a = api.varf_diffusion(kappa=_np(kappa), f=_np(f), c_mass=1.0 / self.dt, on=self.on, tgv=self.tgv)
+            F = np.empty(self.Vh.ndof)
         if self.A is None:
             self.A = api.matrix(a, self.space, eps=self.eps, rhs_out=F)
         else:
@@ -167,13 +204,17 @@ class HeatProblem:
         return self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev)
 
     def forward(self, kappa, f, keep_checkpoints=True):
-        self.assemble(kappa, f)
-        u = np.zeros(self.Vh.ndof)
-        ck = {0: u.copy()}
-        for n in range(1, self.nsteps + 1):
+        """u^N and the checkpoints: every `checkpoint`-th state, plus the states of the last
+        segment, which the backward pass needs first and would otherwise recompute."""
+        F = self.assemble(kappa, f)
+        u = _zeros(self.Vh.ndof, F)
+        ck = {0: _copy(u)}
+        N, c = self.nsteps, self.checkpoint
+        last0 = ((N - 1) // c) * c
+        for n in range(1, N + 1):
             u = self.step(u)
-            if keep_checkpoints and n % self.checkpoint == 0:
-                ck[n] = u.copy()
+            if keep_checkpoints and (n % c == 0 or n > last0):
+                ck[n] = _copy(u)
         return u, ck
 
     def loss(self, uN, u_obs):
@@ -188,12 +229,12 @@ class HeatProblem:
         r = uN - u_obs
         L = 0.5 * float(r @ self.mass.mult(r))
         nt = self.Vh.Th.nt
-        gk = np.zeros(nt)
-        gf = np.zeros(nt)
+        gk = _zeros(nt, uN)
+        gf = _zeros(nt, uN)
         rhs_adj = self.mass.mult(r)          # dL/du^N
         lam_next = None
         N, c = self.nsteps, self.checkpoint
-        seg_starts = sorted(k for k in ck if k < N)
+        seg_starts = sorted(k for k in ck if k < N and k % c == 0)
         for s0 in reversed(seg_starts):
             s1 = min(s0 + c, N)
             # recompute u^{s0+1..s1} from the checkpoint u^{s0}
@@ -203,7 +244,7 @@ class HeatProblem:
                 u = states[n] = self.step(u) if n not in ck or n == s0 else ck[n]
             for n in range(s1, s0, -1):
                 rhs = rhs_adj if n == N else self.mdt.mult(lam_next, trans=True)
-                lam = self.A.solve(rhs, trans=True)
+                lam = self.A.solve(rhs, trans=True, x0=lam_next)
                 self.solves += 1
                 g1, g2 = sensitivity(self.A, states[n], lam)
                 gk += g1

@@ -267,10 +267,12 @@ class Matrix:
         check(code)
         return out
 
-    def solve_mixed(self, b, x0=None, eps=None, eps_inner=1e-5, itmax_inner=0, max_outer=30,
-                    out=None, unroll=8):
+    def solve_mixed(self, b, x0=None, eps=None, eps_inner=0.0, itmax_inner=0, max_outer=30,
+                    out=None, unroll=8, restart_inner=False):
         """u[] = A^-1*b by FP32 inner PCG + FP64 iterative refinement, same stopping rule
-        as the FP64 CG on the true residual."""
+        as the FP64 CG on the true residual.  Default: residual replacement keeping the search
+        direction, eps_inner the residual drop between replacements (0: 1e-2); with
+        restart_inner a fresh inner PCG per refinement step (0: 1e-5)."""
         dev_in = hasattr(b, "data_ptr")
         if out is None:
             if dev_in:
@@ -286,11 +288,17 @@ class Matrix:
         p.max_outer = max_outer
         p.tgv = self.tgv
         p.unroll = unroll
+        p.restart_inner = int(bool(restart_inner))
         st = SolverStats()
         code = lib().ffgpu_solve_ir(self.h, _ptr(bb), _ptr(out), C.byref(p), C.byref(st))
         self.stats = st
         check(code)
         return out
+
+    def spmv_layout(self, mode=0):
+        """The SpMV layout the tuner chose: 'sell32', 'bsr/T' (T lanes per row) or None."""
+        v = int(lib().ffgpu_matrix_spmv_layout(self.h, int(mode)))
+        return None if v <= 0 else ("sell32" if v == 64 else f"bsr/{v}")
 
     def mult(self, x, trans=False, out=None):
         if out is None:

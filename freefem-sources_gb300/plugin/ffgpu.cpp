@@ -82,7 +82,7 @@ class SolverGpu : public VirtualSolver<int, double> {
         ffgpu_solver_stats st;
         int r;
         if (KIND == kMixed) {
-            ffgpu_ir_params p = {eps, 1e-5, 0, 30, tgv, 8};
+            ffgpu_ir_params p = {eps, 0.0, 0, 30, tgv, 8, 0};
             r = FFGPU_OK;
             for (int k = 0; k < N && r == FFGPU_OK; ++k)
                 r = ffgpu_solve_ir(M, b + (size_t)k * A.n, x + (size_t)k * A.n, &p, &st);

@@ -146,6 +146,10 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
                           const int32_t *col, const double *val, ffgpu_matrix **out);
 int ffgpu_matrix_destroy(ffgpu_matrix *A);
 int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_size);
+/* SpMV layout the solver's tuner chose for this matrix: mode 0 (FP64) or 1 (double-float).
+ * Returns 64 for the SELL-32 copy (one row per lane), T in {1,..,32} for block CSR with T
+ * lanes per block row, 0 before the first solve.  No FreeFEM counterpart (diagnostics). */
+int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
 /* [I,J,C] = A in sorted CSR form (HashMatrix::CSR / Sortij, HashMatrix.cpp:671-682,870-876) */
 int ffgpu_matrix_csr(const ffgpu_matrix *A, int32_t *rowptr, int32_t *col, double *val);
 
@@ -167,16 +171,22 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
 /* ------------------------------------------------------------------ mixed precision
  * FP32 inner Jacobi-PCG (FP32 values, vectors, SpMV and dot products) inside an FP64
  * iterative-refinement loop (outer residual b - A x in FP64 on the FP64 matrix, FP64 update).
+ * By default each refinement step replaces the inner iterated residual by the true one and
+ * continues the conjugate-gradient recurrence (reliable updates); restart_inner = 1 starts a
+ * fresh inner PCG instead.
  * Stops on FreeFEM's CG criterion applied to the true residual, (r, C r) < eps^2 (r0, C r0)
  * (CG.cpp:226,247), so it answers the same u[] = A^-1*b as ffgpu_solve_cg; no FreeFEM
  * counterpart of its own (FreeFEM's solvers are FP64). */
 typedef struct {
-    double eps;         /* outer tolerance, as ffgpu_solver_params.eps            */
-    double eps_inner;   /* relative tolerance of each FP32 inner solve (<=0: 1e-5) */
-    int itmax_inner;    /* inner iteration cap (<=0: n)                            */
-    int max_outer;      /* refinement steps cap (<=0: 30)                          */
+    double eps;         /* outer tolerance, as ffgpu_solver_params.eps                       */
+    double eps_inner;   /* residual drop of each FP32 inner segment (<=0: 1e-2; 1e-5 when
+                           restart_inner)                                                     */
+    int itmax_inner;    /* inner iteration cap per segment (<=0: n)                           */
+    int max_outer;      /* refinement steps cap (<=0: 30)                                     */
     double tgv;
     int unroll;
+    int restart_inner;  /* 0: replace the residual and keep the search direction (reliable
+                           updates); 1: restart the inner PCG at every refinement step        */
 } ffgpu_ir_params;
 
 /* FP32 copy of the values used by the inner solves (built on first use, freed on reassembly) */

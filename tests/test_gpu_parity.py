@@ -186,6 +186,51 @@ def test_reassemble_matches_fresh_assembly():
     assert np.array_equal(b, ffgpu.rhs(a2, A.space))
 
 
+def test_reassemble_then_solve_uses_new_values():
+    """A solve caches the solver layout and graph; a reassembly must invalidate both."""
+    c = case("p1cubek_n4")
+    Vh = FESpace(c["Th"], "P1")
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-12, rhs_out=b)
+    A.solve(b)
+    A.solve(b, trans=True)
+    kap2 = np.asarray(c["kappa"]) * 2.5 + 0.1
+    a2 = ffgpu.varf_diffusion(kappa=kap2, f=1.0, on=c["labels"])
+    A.reassemble(a2, rhs_out=b)
+    B = ffgpu.matrix(a2, A.space, eps=1e-12)
+    for trans in (False, True):
+        ua = A.solve(b, trans=trans)
+        ub = B.solve(b, trans=trans)
+        assert np.array_equal(ua, ub)
+
+
+def test_wide_band_matrix_against_oracle():
+    """Rows and columns randomly permuted (bandwidth above 2^15, so the SpMV keeps 32-bit
+    column indices): same solution as the oracle's on the unpermuted matrix."""
+    Th = mesh.square(200)
+    Vh = FESpace(Th, "P1")
+    Ao = ffo.assemble(Th, Vh)
+    bo = ffo.rhs(Th, Vh, f=1.0)
+    ffo.setbc(Ao, bo, Vh.on((1, 2, 3, 4)))
+    uo, it, _, _ = ffo.cg(Ao, bo, eps=1e-10)
+    rp, cl, v = Ao.csr()
+    n = Vh.ndof
+    p = np.random.Generator(np.random.PCG64(5)).permutation(n)      # new row k = old row p[k]
+    inv = np.empty(n, np.int64); inv[p] = np.arange(n)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    ni, nj = inv[rows], inv[cl]
+    order = np.lexsort((nj, ni))
+    ni, nj, nv = ni[order], nj[order], v[order]
+    assert np.abs(ni - nj).max() >= 1 << 15
+    prp = np.zeros(n + 1, np.int64)
+    np.add.at(prp, ni + 1, 1)
+    A = ffgpu.matrix_from_csr(np.cumsum(prp).astype(np.int32), nj.astype(np.int32), nv, eps=1e-10)
+    up = A.solve(bo[p])
+    u = up[inv]
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    assert abs(A.stats.iterations - it) <= 2
+
+
 def test_device_resident_inputs_torch():
     """Mesh, DOF table and vectors already in HBM (torch CUDA tensors) through the same ABI."""
     import torch
