@@ -366,11 +366,18 @@ def run_gpu(args, rank, world):
         def run_ir():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
             A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
-            return A2.solve_mixed(b, eps=cfg["eps"]), A2.stats.iterations, A2.stats.outer_iterations
-        (uir, itir, outir), msir = timed_variant(run_ir, 1)
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            ur = A2.solve_mixed(b, eps=cfg["eps"])
+            t1.record(stream)
+            t1.synchronize()
+            return ur, A2.stats.iterations, A2.stats.outer_iterations, A2.spmv_layout(2), t0.elapsed_time(t1)
+        (uir, itir, outir, lay32, solve_ir_ms), msir = timed_variant(run_ir, 1)
         variants["mixed_fp32_inner_fp64_refinement"] = {
             "value": Vh.ndof / (msir * 1e-3), "ms_per_step": msir, "inner_iterations": itir,
-            "outer_iterations": outir,
+            "outer_iterations": outir, "spmv_layout": lay32, "solve_ms": solve_ir_ms,
+            "solve_speedup_vs_fp64": statistics.median(phase["solve"][-args.steps:]) / solve_ir_ms,
             "rel_err_vs_fp64": float(torch.linalg.norm(uir - u_ref) / torch.linalg.norm(u_ref))}
     # e2e: public API from host arrays (H2D of mesh/DOF table/BC mask, D2H of b and u)
     e2e_times = []

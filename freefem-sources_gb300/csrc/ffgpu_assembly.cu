@@ -270,6 +270,47 @@ __device__ __forceinline__ double basis_integral(double meas, int i) {
 }
 
 // ------------------------------------------------------------------ row gather (both passes)
+// Register path for rows with at most 32 distinct neighbours: the candidates are read 32 at
+// a time, duplicates inside a batch are merged with __match_any_sync, the new ones are
+// appended to a list held one entry per lane, and the list is sorted by a 32-lane bitonic
+// network on shuffles.  Returns the degree, or -1 when the row has more than 32 neighbours.
+__device__ int gather_row_small(int b, int m, const int32_t *inc_elem, const int32_t *nodes, int nn, int *s) {
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    int u = 0, mine = 0x7fffffff;
+    for (int p0 = 0; p0 < m; p0 += 32) {
+        const int p = p0 + lane;
+        int v = 0x7fffffff;
+        if (p < m) {
+            const int t = p / nn, i = p - t * nn;
+            v = nodes[(int64_t)inc_elem[b + t] * nn + i];
+        }
+        const unsigned grp = __match_any_sync(full, v);
+        bool fresh = v != 0x7fffffff && lane == __ffs(grp) - 1;
+        for (int L = 0; L < u; ++L) fresh &= __shfl_sync(full, mine, L) != v;
+        const unsigned bal = __ballot_sync(full, fresh);
+        const int cnt = __popc(bal);
+        if (u + cnt > 32) return -1;
+        if (fresh) s[u + __popc(bal & ((1u << lane) - 1u))] = v;
+        __syncwarp();
+        if (lane >= u && lane < u + cnt) mine = s[lane];
+        __syncwarp();
+        u += cnt;
+    }
+    // ascending bitonic sort of one value per lane (unused lanes hold INT_MAX)
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int o = __shfl_xor_sync(full, mine, j);
+            const bool lower = (lane & j) == 0, up = (lane & k) == 0;
+            mine = (lower == up) ? min(mine, o) : max(mine, o);
+        }
+    if (lane < u) s[lane] = mine;
+    __syncwarp();
+    return u;
+}
+
 // Gathers the candidate neighbour nodes of node a into s, sorts and compacts them in
 // place; returns the row degree (or -1 on overflow).
 __device__ int gather_row(int a, const int32_t *inc_ptr, const int32_t *inc_elem,
@@ -278,6 +319,10 @@ __device__ int gather_row(int a, const int32_t *inc_ptr, const int32_t *inc_elem
     int b = inc_ptr[a], e = inc_ptr[a + 1];
     int m = (e - b) * nn;
     if (m > kCandMax) { if (lane == 0) dev_fail(status, kDevCandOverflow); return -1; }
+    if (nn <= 4) {
+        const int u = gather_row_small(b, m, inc_elem, nodes, nn, s);
+        if (u >= 0) return u;
+    }
     int P = pow2_ceil(max(m, 32));
     for (int p = lane; p < P; p += 32) {
         int v = 0x7fffffff;
@@ -346,14 +391,19 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
     constexpr int NN = FE == 1 ? nvk : (DIM == 3 ? 10 : 6);
     constexpr int BS = FE == 3 ? 3 : 1;
     constexpr int BS2 = BS * BS;
-    // lanes = slot * NN + lb: SLOTS incident elements per step, each lane one block (la, lb)
+    // lanes = slot * NN + lb: SLOTS incident elements per step, each lane one block (la, lb).
+    // Every slot accumulates into its own copy of the row (acc[slot][k][q]) so that one step
+    // is one full-warp FP64 add; the copies are summed in slot order at the end.  Entries are
+    // therefore formed as sum_s (sum of the slot's elements in element order): deterministic,
+    // and the same association rhs_kernel uses for the linear form.
     constexpr int SLOTS = 32 / NN;
     extern __shared__ __align__(16) unsigned char sh_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
     int *cols = (int *)sh_raw + w * kCandMax;
-    double *acc = (double *)((int *)sh_raw + warps * kCandMax) + (int64_t)w * A.max_deg * BS2;
+    double *acc = (double *)((int *)sh_raw + warps * kCandMax) + (int64_t)w * SLOTS * A.max_deg * BS2;
     const double mfac = DIM == 3 ? 1.0 / 20.0 : 1.0 / 12.0;
+    const bool has_mass = A.c_mass != 0.0;
 
     for (int a = blockIdx.x * warps + w; a < A.nnodes; a += gridDim.x * warps) {
         int deg = gather_row(a, A.inc_ptr, A.inc_elem, A.nodes, NN, cols, A.status);
@@ -362,8 +412,9 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
         const int64_t rb = A.browptr[a];
         if (A.bcol)
             for (int r = lane; r < deg; r += 32) A.bcol[rb + r] = cols[r];
-        for (int q = lane; q < deg * BS2; q += 32) acc[q] = 0.0;
-        double racc = 0.0;   // rhs of component `lane` (lanes < BS)
+        const int span = deg * BS2;   // one slot copy
+        for (int q = lane; q < SLOTS * span; q += 32) acc[q] = 0.0;
+        double racc = 0.0;   // rhs partial of slot `lane / NN`, component `lane % NN` (< BS)
         __syncwarp();
         const int ib = A.inc_ptr[a], ie = A.inc_ptr[a + 1];
         for (int t0 = ib; t0 < ie; t0 += SLOTS) {
@@ -389,7 +440,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
 #pragma unroll
                     for (int d = 0; d < DIM; ++d) s += __ldg(G + 3 * la + d) * __ldg(G + 3 * lb + d);
                     double val = kap * meas * s;
-                    if (A.c_mass != 0.0) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
+                    if (has_mass) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
                     v[0] = val;
                 } else {
                     const P2Pair<DIM> P(G, la, lb);
@@ -410,27 +461,33 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                 }
                 if (rank < 0) dev_fail(A.status, kDevNotFound);
             }
-            // ---- accumulate slot by slot: element order, no two lanes on one entry at once
-            for (int sl = 0; sl < SLOTS; ++sl) {
-                if (act && slot == sl && rank >= 0) {
+            // ---- accumulate: each slot into its own copy, no two lanes on one entry
+            if (act && rank >= 0) {
 #pragma unroll
-                    for (int q = 0; q < BS2; ++q) acc[rank * BS2 + q] += v[q];
-                }
-                __syncwarp();
+                for (int q = 0; q < BS2; ++q) acc[slot * span + rank * BS2 + q] += v[q];
             }
-            // ---- linear form: lanes < BS accumulate component `lane`, element order
-            if (A.rhs) {
-                for (int sl = 0; sl < SLOTS; ++sl) {
-                    int tt = t0 + sl;
-                    if (tt < ie && lane < BS) {
-                        int ee = A.inc_elem[tt], ll = A.inc_loc[tt];
-                        double meas = A.geo[(int64_t)ee * kGeoStride];
-                        double f = A.fP0 ? A.fP0[(int64_t)ee * BS + lane]
-                                         : (lane == 0 ? A.f0 : (lane == 1 ? A.f1 : A.f2));
-                        racc += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
-                    }
-                }
+            // ---- linear form: lane (slot, c < BS) adds its element's share to component c
+            if (A.rhs && act && lb < BS) {
+                const int ee = A.inc_elem[t], ll = A.inc_loc[t];
+                const double meas = A.geo[(int64_t)ee * kGeoStride];
+                const double f = A.fP0 ? A.fP0[(int64_t)ee * BS + lb] : (lb == 0 ? A.f0 : (lb == 1 ? A.f1 : A.f2));
+                racc += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
             }
+            __syncwarp();
+        }
+        // ---- sum the slot copies (slot order)
+        for (int q = lane; q < span; q += 32) {
+            double t = acc[q];
+            for (int sl = 1; sl < SLOTS; ++sl) t += acc[sl * span + q];
+            acc[q] = t;
+        }
+        {
+            double r = 0.0;
+            for (int sl = 0; sl < SLOTS; ++sl) {
+                const double p = __shfl_sync(0xffffffffu, racc, sl * NN + (lane < BS ? lane : 0));
+                r = sl == 0 ? p : r + p;
+            }
+            racc = r;   // lanes < BS: component `lane`
         }
         __syncwarp();
         // ---- Dirichlet rows (tgv > 0): diagonal := tgv, rhs := tgv * g
@@ -481,16 +538,32 @@ __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *in
                            double f0, double f1, double f2, const uint8_t *onbc, const double *g,
                            double tgv, double *rhs) {
     constexpr int BS = FE == 3 ? 3 : 1;
+    // same association as the fill kernel's fused linear form: element p of the node goes to
+    // partial p % SLOTS, partials summed in order
+    constexpr int NN = FE == 1 ? DIM + 1 : (DIM == 3 ? 10 : 6);
+    constexpr int SLOTS = 32 / NN;
     int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= (int64_t)nnodes * BS) return;
     int a = (int)(t / BS), c = (int)(t % BS);
-    double s = 0;
-    for (int p = inc_ptr[a]; p < inc_ptr[a + 1]; ++p) {
-        int e = inc_elem[p], l = inc_loc[p];
-        double meas = geo[(int64_t)e * kGeoStride];
-        double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
-        s += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
+    double part[SLOTS];
+#pragma unroll
+    for (int sl = 0; sl < SLOTS; ++sl) part[sl] = 0.0;
+    const int ib = inc_ptr[a], ie = inc_ptr[a + 1];
+    for (int p0 = ib; p0 < ie; p0 += SLOTS) {
+#pragma unroll
+        for (int sl = 0; sl < SLOTS; ++sl) {
+            const int p = p0 + sl;
+            if (p < ie) {
+                int e = inc_elem[p], l = inc_loc[p];
+                double meas = geo[(int64_t)e * kGeoStride];
+                double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
+                part[sl] += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
+            }
+        }
     }
+    double s = part[0];
+#pragma unroll
+    for (int sl = 1; sl < SLOTS; ++sl) s += part[sl];
     if (onbc && onbc[t]) s = (tgv > 0 ? tgv : 1.0) * (g ? g[t] : 0.0);
     rhs[t] = s;
 }
@@ -631,7 +704,8 @@ static int fill_launch(ffgpu_space *S, FillArgs &fa) {
     ffgpu_ctx *ctx = S->ctx;
     const int warps = 4;
     int bs2 = S->bs * S->bs;
-    size_t smem = (size_t)warps * kCandMax * sizeof(int) + (size_t)warps * fa.max_deg * bs2 * sizeof(double);
+    const int nn = S->nn, slots = 32 / nn;
+    size_t smem = (size_t)warps * kCandMax * sizeof(int) + (size_t)warps * slots * fa.max_deg * bs2 * sizeof(double);
     int grid = min(kNumSM * 16, max(1, (S->nnodes + warps - 1) / warps));
     void (*kern)(FillArgs) = nullptr;
     if (S->dim == 2 && S->fe == FFGPU_FE_P1) kern = row_fill_kernel<2, 1>;
@@ -1026,8 +1100,7 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     cudaFree(M->geo); cudaFree(M->bcmask);
     cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
     cudaFree(M->val32); cudaFree(M->valx); cudaFree(M->valx_t); cudaFree(M->hx); cudaFree(M->ks);
-    sell_release_values(M);
-    cudaFree(M->sperm); cudaFree(M->slen); cudaFree(M->soff); cudaFree(M->scol); cudaFree(M->scol16);
+    sell_release(M);
     delete M;
     return FFGPU_OK;
 }

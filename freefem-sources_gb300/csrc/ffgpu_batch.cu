@@ -356,8 +356,13 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    if (B->tuned < 0)
+        for (int i = 0; i < ctx->nbtuned; ++i)
+            if (ctx->btuned[i].nprob == B->nprob && ctx->btuned[i].n == NV && ctx->btuned[i].nnz == B->A->nnz)
+                B->tuned = ctx->btuned[i].cand;
     if (B->tuned < 0) {
-        // autotune: time every candidate (CTA size x lanes per row) on this batch
+        // autotune: time every candidate (CTA size x lanes per row) on this batch; the choice is
+        // kept in the context for later batches of the same shape
         float best = 1e30f;
         int bi = 0;
         for (int c = 0; c < g_ncands; ++c) {
@@ -375,6 +380,7 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
         B->tuned = bi;
         B->tuned_ms = best;
         changed = true;
+        ctx->btuned[ctx->nbtuned < 8 ? ctx->nbtuned++ : 7] = ffgpu_ctx::BatchTuned{B->nprob, NV, B->A->nnz, bi};
     }
     if (changed || !B->exec) FFGPU_TRY(batch_graph(B, B->tuned));
     cudaEventRecord(e0, s);

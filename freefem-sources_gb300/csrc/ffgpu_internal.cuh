@@ -75,6 +75,9 @@ struct ffgpu_ctx {
     // SpMV lanes-per-row chosen by timing, per matrix shape (nb, nnzb, bs)
     struct Tuned { int64_t nb, nnzb; int bs, lanes, mode; } tuned[32];
     int ntuned;
+    // batched solver launch shape chosen by timing, per batch shape (problems, DOFs, nnz)
+    struct BatchTuned { int64_t nprob, n, nnz; int cand; } btuned[8];
+    int nbtuned;
 };
 
 struct ffgpu_space {
@@ -137,6 +140,10 @@ struct ffgpu_matrix {
     double *sval, *sval_t;      // FP64 values of A and A^T, (slot row, entry, lane) order
     float2 *svalx, *svalx_t;    // double-float splits of the same
     float *sval32;              // FP32 values for the mixed-precision inner solve
+    // per-grid partitions of the chunks over warps, balanced by slot count (nw+1 starts)
+    int spart_nw[4];
+    int32_t *spart[4];
+    int sell32_kind;      // chunk assignment of the FP32 SELL SpMV (tuned): 64 ranges, 65 rotated
 };
 
 namespace ffgpu {
@@ -217,12 +224,16 @@ struct SellArgs {
     int nchunk;
     const int32_t *perm, *len, *off, *col;
     const int16_t *col16;
+    const int32_t *part;   // chunks [part[w], part[w+1]) belong to warp w of the launch
 };
 int sell_prepare(ffgpu_matrix *A);               // structure (once per pattern)
+// chunk ranges of the nw warps of a launch, equal slot counts (built once per nw)
+int sell_partition(ffgpu_matrix *A, int nw, const int32_t **part);
 int sell_values(ffgpu_matrix *A, int kind);      // value array of one kind (once per numeric state)
 void sell_release_values(ffgpu_matrix *A);       // drop the value arrays (new numeric state)
+void sell_release(ffgpu_matrix *A);              // drop everything (matrix destruction)
 inline SellArgs sell_args(const ffgpu_matrix *A) {
-    return SellArgs{A->nchunk, A->sperm, A->slen, A->soff, A->scol, A->scol16};
+    return SellArgs{A->nchunk, A->sperm, A->slen, A->soff, A->scol, A->scol16, nullptr};
 }
 // Persistent grid of a kernel: resident blocks per SM (occupancy calculator) x SMs
 int resident_grid(const void *kernel, int threads, size_t smem = 0);

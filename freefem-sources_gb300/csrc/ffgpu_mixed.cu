@@ -17,6 +17,8 @@
 // tgv rows (A_ii = 1e30) stay in the FP32 system: 1e30 and 1/tgv are normal FP32 numbers,
 // and the corrections on those rows are of order r_i/tgv, also representable.
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "ffgpu_internal.cuh"
@@ -25,7 +27,6 @@
 namespace ffgpu {
 
 constexpr int kMxWarps = 8;
-constexpr int kMxSpmvBlocks = 16 * kNumSM;
 constexpr int kMxVecBlocks = 4 * kNumSM;
 constexpr int kMxThreads = 256;
 
@@ -39,16 +40,15 @@ struct InnerScalars {
 __device__ __noinline__ void ir_graph_stop(cudaGraphConditionalHandle cond) { cudaGraphSetConditional(cond, 0); }
 
 // inner K_a on the SELL-32 FP32 copy: q = A h and (h, q) -> rho
-template <int BS, bool C16>
+template <int BS, bool C16, int ASSIGN>
 __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *__restrict__ val,
                                                        const float *__restrict__ h, float *__restrict__ q,
                                                        InnerScalars *ks, float *part) {
     __shared__ float sh[32];
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     float hq = 0;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+    sell_for_chunks<ASSIGN>(S, [&](int c) {
         const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
         float y[BS];
         sell_row32<BS, C16>(S, val, h, c, lane, a, y);
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *
                 hq = fmaf(h[i], y[m], hq);
             }
         }
-    }
+    });
     float tot;
     float p = block_sum_t(hq, sh);
     if (last_block_sum(p, part, &ks->ticket, &tot, sh)) { ks->s_hq = tot; ks->rho = -ks->s_gh / tot; }
@@ -71,10 +71,10 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *
 __global__ void __launch_bounds__(kMxThreads) ir_kb(int n, float *__restrict__ x, float *__restrict__ g,
                                                     const float *__restrict__ h, const float *__restrict__ q,
                                                     const float *__restrict__ dinv, InnerScalars *ks, float *part,
-                                                    cudaGraphConditionalHandle cond) {
+                                                    cudaGraphConditionalHandle cond, int in_graph) {
     __shared__ float sh[32];
     if (ks->done) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) ir_graph_stop(cond);
+        if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) ir_graph_stop(cond);
         return;
     }
     const float rho = ks->rho;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_kb(int n, float *__restrict__ x
         ks->iter += 1;
         if (tot < ks->eps2) { ks->converged = 1; ks->done = 1; }
         else if (ks->iter >= ks->itmax || !(tot == tot)) ks->done = 1;
-        if (ks->done) ir_graph_stop(cond);
+        if (ks->done && in_graph) ir_graph_stop(cond);
     }
 }
 
@@ -248,9 +248,95 @@ struct IRState {
     double *y = nullptr, *out3 = nullptr;
 };
 
+constexpr int kSellCode = 64;   // layout codes shared with the FP64 tuner: 64 + chunk assignment
+
+static void *ir_ka_fn(const ffgpu_matrix *A, int kind) {
+    const int assign = kind >= kSellCode ? kind - kSellCode : kSellRanges;
+    void *t[3][3] = {{(void *)ir_ka<1, false, 0>, (void *)ir_ka<1, false, 1>, (void *)ir_ka<1, false, 2>},
+                     {(void *)ir_ka<1, true, 0>, (void *)ir_ka<1, true, 1>, (void *)ir_ka<1, true, 2>},
+                     {(void *)ir_ka<3, false, 0>, (void *)ir_ka<3, false, 1>, (void *)ir_ka<3, false, 2>}};
+    return t[A->bs == 3 ? 2 : (A->scol16 ? 1 : 0)][assign];
+}
+static bool ir_ranges(const ffgpu_matrix *A) { return A->sell32_kind - kSellCode == kSellRanges || !A->sell32_kind; }
+
+// `unroll` inner iterations (K_a K_b K_c) on stream s
+static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditionalHandle cond, int in_graph,
+                   cudaStream_t s) {
+    SellArgs sa = sell_args(A);
+    const float *sv = A->sval32;
+    void *ka = ir_ka_fn(A, A->sell32_kind);
+    const int gka = resident_grid(ka, kMxWarps * 32);
+    if (ir_ranges(A)) FFGPU_TRY(sell_partition(A, gka * kMxWarps, &sa.part));
+    const int gkb = min(4096, resident_grid((const void *)ir_kb, kMxThreads));
+    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
+    float *part = (float *)A->ctx->d_part;
+    int n = A->n;
+    for (int u = 0; u < unroll; ++u) {
+        void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
+        cudaLaunchKernel(ka, gka, kMxWarps * 32, aa, 0, s);
+        ir_kb<<<gkb, kMxThreads, 0, s>>>(n, S.d, S.g, S.h, S.q, S.dinv, S.ks, part, cond, in_graph);
+        ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, part);
+    }
+    return FFGPU_OK;
+}
+
+// Times the FP32 K_a with both chunk assignments on this matrix (cached per shape).
+static int ir_tune(ffgpu_matrix *A, IRState &S) {
+    if (A->sell32_kind) return FFGPU_OK;
+    ffgpu_ctx *ctx = A->ctx;
+    for (int i = 0; i < ctx->ntuned; ++i)
+        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs &&
+            ctx->tuned[i].mode == 2) {
+            A->sell32_kind = ctx->tuned[i].lanes;
+            return FFGPU_OK;
+        }
+    cudaStream_t s = ctx->stream;
+    FFGPU_CUDA(cudaMemsetAsync(S.h, 0, sizeof(float) * A->n, s));
+    FFGPU_CUDA(cudaMemsetAsync(S.ks, 0, sizeof(InnerScalars), s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bestk = kSellCode + kSellRanges;
+    const int kinds[3] = {kSellCode + kSellRanges, kSellCode + kSellRotated, kSellCode + kSellStride};
+    const char *names[3] = {"ranges", "rotated", "stride"};
+    for (int kk = 0; kk < 3; ++kk) {
+        SellArgs sa = sell_args(A);
+        const float *sv = A->sval32;
+        void *ka = ir_ka_fn(A, kinds[kk]);
+        const int g = resident_grid(ka, kMxWarps * 32);
+        if (kk == 0) FFGPU_TRY(sell_partition(A, g * kMxWarps, &sa.part));
+        float *part = (float *)ctx->d_part;
+        void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
+        cudaLaunchKernel(ka, g, kMxWarps * 32, aa, 0, s);
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < 3; ++r) cudaLaunchKernel(ka, g, kMxWarps * 32, aa, 0, s);
+        cudaEventRecord(e1, s);
+        FFGPU_CUDA(cudaEventSynchronize(e1));
+        FFGPU_CUDA(cudaGetLastError());
+        ctx->launches += 4;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (getenv("FFGPU_VERBOSE"))
+            fprintf(stderr, "ffgpu: FP32 SpMV tuner (%d block rows): sell32 %s %.4f ms\n", A->nb, names[kk],
+                    ms / 3);
+        if (ms < best) { best = ms; bestk = kinds[kk]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    A->sell32_kind = bestk;
+    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestk, 2};
+    return FFGPU_OK;
+}
+
 static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
+    // the warp partition is built before the capture starts (no allocation inside a capture)
+    if (ir_ranges(A)) {
+        const int32_t *part = nullptr;
+        FFGPU_TRY(sell_partition(A, resident_grid(ir_ka_fn(A, A->sell32_kind), kMxWarps * 32) * kMxWarps, &part));
+    }
     cudaGraph_t graph, body;
     FFGPU_CUDA(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle cond;
@@ -266,20 +352,7 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    SellArgs sa = sell_args(A);
-    const float *sv = A->sval32;
-    void *ka = A->bs == 3 ? (void *)ir_ka<3, false> : (A->scol16 ? (void *)ir_ka<1, true> : (void *)ir_ka<1, false>);
-    const int gka = resident_grid(ka, kMxWarps * 32);
-    const int gkb = min(4096, resident_grid((const void *)ir_kb, kMxThreads));
-    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
-    float *part = (float *)ctx->d_part;
-    int n = A->n;
-    for (int u = 0; u < unroll; ++u) {
-        void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
-        cudaLaunchKernel(ka, gka, kMxWarps * 32, aa, 0, s);
-        ir_kb<<<gkb, kMxThreads, 0, s>>>(n, S.d, S.g, S.h, S.q, S.dinv, S.ks, part, cond);
-        ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, part);
-    }
+    ir_body(A, S, unroll, cond, 1, s);
     cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&S.exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -342,7 +415,10 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     to_f32_kernel<<<kMxVecBlocks, kMxThreads, 0, s>>>(n, A->diag_inv, S.dinv);
     ctx->launches++;
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
-    int rc = ir_build_graph(A, S, unroll);
+    const char *ge = getenv("FFGPU_CG_GRAPH");
+    const bool host_loop = ge && ge[0] == '0';
+    int rc = ir_tune(A, S);
+    if (!rc && !host_loop) rc = ir_build_graph(A, S, unroll);
     if (rc) { ir_free(S, s); return rc; }
     const double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
     const int itmax_in = prm->itmax_inner > 0 ? prm->itmax_inner : n;
@@ -398,7 +474,19 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
             ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, (float *)ctx->d_part);
             ctx->launches += 2;
         }
-        if (cudaGraphLaunch(S.exec, s) != cudaSuccess) { set_error("ffgpu_solve_ir: graph launch failed"); rc = FFGPU_ECUDA; break; }
+        if (host_loop) {
+            // the same kernels launched from the host (profilers that do not trace conditional
+            // graph nodes); the done flag is polled after every `unroll` iterations
+            for (int it = 0; it <= itmax_in; it += unroll) {
+                if ((rc = ir_body(A, S, unroll, 0, 0, s))) break;
+                int done = 0;
+                cudaMemcpyAsync(&done, &S.ks->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+                if (cudaStreamSynchronize(s) != cudaSuccess || done) break;
+            }
+            if (rc) break;
+        } else if (cudaGraphLaunch(S.exec, s) != cudaSuccess) {
+            set_error("ffgpu_solve_ir: graph launch failed"); rc = FFGPU_ECUDA; break;
+        }
         InnerScalars hk;
         cudaMemcpyAsync(&hk, S.ks, sizeof(hk), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);

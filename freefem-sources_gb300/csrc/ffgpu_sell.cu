@@ -9,8 +9,11 @@
 //   * entry j of lane r of chunk c is stored at slot row soff[c] + j, lane r: a warp reads
 //     32 consecutive column indices and, for each of the bs*bs values, 32 consecutive values.
 // Every lane of a warp runs the same trip count, every load is a full 128/256-byte line, and
-// no lane-group reductions are needed.  Within a row the entries keep their column order, so
-// the row sums are formed in the same order as the block-CSR kernels form them.
+// no lane-group reductions are needed.  Each warp of a launch owns a contiguous range of
+// chunks holding an equal share of the slots (sell_partition): windows start with their
+// longest rows, so a fixed stride over chunks would give some warps only long chunks.
+// Within a row the entries keep their column order, so the row sums are formed in the same
+// order as the block-CSR kernels form them.
 // For bs == 1 the column is stored as the 16-bit difference column - row whenever the
 // matrix bandwidth allows (2 instead of 4 bytes per entry).
 #include <string.h>
@@ -120,6 +123,34 @@ __global__ void sell_val_kernel(int nchunk, const int32_t *__restrict__ perm, co
     }
 }
 
+// start chunk of warp w: the first chunk whose first slot row is at or past w * nslot / nw
+__global__ void sell_part_kernel(int nchunk, const int32_t *__restrict__ off, int nw, int32_t *__restrict__ part) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w > nw) return;
+    const int64_t target = (int64_t)off[nchunk] * w / nw;
+    int lo = 0, hi = nchunk;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] < target) lo = mid + 1;
+        else hi = mid;
+    }
+    part[w] = w == nw ? nchunk : lo;
+}
+
+int sell_partition(ffgpu_matrix *A, int nw, const int32_t **part) {
+    for (int i = 0; i < 4; ++i)
+        if (A->spart[i] && A->spart_nw[i] == nw) { *part = A->spart[i]; return FFGPU_OK; }
+    int slot = 0;
+    while (slot < 4 && A->spart[slot]) ++slot;
+    if (slot == 4) { cudaFree(A->spart[3]); A->spart[3] = nullptr; slot = 3; }
+    FFGPU_CUDA(cudaMalloc((void **)&A->spart[slot], sizeof(int32_t) * ((size_t)nw + 1)));
+    A->spart_nw[slot] = nw;
+    sell_part_kernel<<<(nw + 256) / 256, 256, 0, A->ctx->stream>>>(A->nchunk, A->soff, nw, A->spart[slot]);
+    FFGPU_TRY(launch_check(A->ctx, "sell_partition"));
+    *part = A->spart[slot];
+    return FFGPU_OK;
+}
+
 int resident_grid(const void *kernel, int threads, size_t smem) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
@@ -203,6 +234,12 @@ int sell_values(ffgpu_matrix *A, int kind) {
         case kSellXT: return sell_fill<float2, ToDF>(A, A->val_t, &A->svalx_t);
         default: return sell_fill<float, ToF32>(A, A->val, &A->sval32);
     }
+}
+
+void sell_release(ffgpu_matrix *A) {
+    sell_release_values(A);
+    cudaFree(A->sperm); cudaFree(A->slen); cudaFree(A->soff); cudaFree(A->scol); cudaFree(A->scol16);
+    for (int i = 0; i < 4; ++i) cudaFree(A->spart[i]);
 }
 
 void sell_release_values(ffgpu_matrix *A) {

@@ -74,6 +74,30 @@ __device__ __forceinline__ float2 split_f64(double v) {
     return make_float2(hi, lo);
 }
 
+// ------------------------------------------------------------------ SELL-32 chunk assignment
+// kSellRanges: warp w takes the contiguous chunks [part[w], part[w+1]) (equal slot shares).
+// kSellRotated: pass k of warp w takes chunk k*nw + (w + 5k) mod nw -- the chunks in flight at
+//   a time stay one contiguous band of the matrix, and the rotation by an odd step walks every
+//   warp through all 32 positions of the degree-sorted windows.
+// kSellStride: pass k of warp w takes chunk k*nw + w (a band too; a warp always meets the same
+//   window position, which only costs where degrees vary inside windows).
+// The tuners time all three on the matrix.
+enum SellAssign { kSellRanges = 0, kSellRotated = 1, kSellStride = 2 };
+
+template <int ASSIGN, typename F>
+__device__ __forceinline__ void sell_for_chunks(const SellArgs &S, F &&body) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if constexpr (ASSIGN == kSellRanges) {
+        for (int c = __ldg(S.part + w), ce = __ldg(S.part + w + 1); c < ce; ++c) body(c);
+    } else {
+        const int nw = (gridDim.x * blockDim.x) >> 5;
+        for (int k = 0; (int64_t)k * nw < S.nchunk; ++k) {
+            const int c = k * nw + (ASSIGN == kSellRotated ? (w + 5 * k) % nw : w);
+            if (c < S.nchunk) body(c);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ SELL-32 rows
 // One block row per lane: lane `lane` of chunk c holds row a (a < 0: padding lane, its
 // entries are zero blocks on column 0).  Entries are read in column order; matrix streams use
@@ -93,7 +117,9 @@ __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__re
     const int64_t ce = sr * 32 + lane;
     const double *v = val + sr * (BS * BS * 32) + lane;
     double s0 = 0, s1 = 0, s2 = 0;
-#pragma unroll 2
+    // scalar rows: 8 slots in flight hide the column -> gather dependency; 3x3 blocks: 2
+    constexpr int UNR = BS == 1 ? 8 : 2;
+#pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
         if (BS == 1) {
@@ -120,7 +146,8 @@ __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__res
     const int64_t ce = sr * 32 + lane;
     const float2 *v = val + sr * (BS * BS * 32) + lane;
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
-#pragma unroll 2
+    constexpr int UNR = BS == 1 ? 8 : 2;
+#pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
         if (BS == 1) {
@@ -150,7 +177,8 @@ __device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__res
     const int64_t ce = sr * 32 + lane;
     const float *v = val + sr * (BS * BS * 32) + lane;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-#pragma unroll 4
+    constexpr int UNR = BS == 1 ? 8 : 4;
+#pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
         if (BS == 1) {

@@ -354,16 +354,15 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
 // ------------------------------------------------------------------ SELL-32 K_a
 // One block row per lane, one chunk of 32 rows per warp (resident grid, chunks strided over
 // warps).  FP64: AH = A H and (H, AH) -> rho; padding lanes (a < 0) write nothing.
-template <int BS, bool C16>
+template <int BS, bool C16, int ASSIGN>
 __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const double *__restrict__ val,
                                                               const double *__restrict__ h, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     double hq = 0;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+    sell_for_chunks<ASSIGN>(S, [&](int c) {
         const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
         double y[BS];
         sell_row64<BS, C16>(S, val, h, c, lane, a, y);
@@ -375,7 +374,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
                 hq = fma(h[i], y[m], hq);
             }
         }
-    }
+    });
     double tot;
     double p = block_sum(hq, sh);
     if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
@@ -385,7 +384,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
 }
 
 // double-float: AH = A H from the split H, (H, AH) in FP64
-template <int BS, bool C16>
+template <int BS, bool C16, int ASSIGN>
 __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const float2 *__restrict__ val,
                                                                const float2 *__restrict__ hx,
                                                                const double *__restrict__ h, double *__restrict__ q,
@@ -393,9 +392,8 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
     __shared__ double sh[32];
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
     double hq = 0;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+    sell_for_chunks<ASSIGN>(S, [&](int c) {
         const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
         double y[BS];
         sell_rowx<BS, C16>(S, val, hx, c, lane, a, y);
@@ -407,7 +405,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
                 hq = fma(h[i], y[m], hq);
             }
         }
-    }
+    });
     double tot;
     double p = block_sum(hq, sh);
     if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
@@ -417,12 +415,11 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
 }
 
 // y = A x (FP64)
-template <int BS, bool C16>
+template <int BS, bool C16, int ASSIGN>
 __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const double *__restrict__ val,
                                                              const double *__restrict__ x, double *__restrict__ y) {
     const int lane = threadIdx.x & 31;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < S.nchunk; c += nw) {
+    sell_for_chunks<ASSIGN>(S, [&](int c) {
         const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
         double r[BS];
         sell_row64<BS, C16>(S, val, x, c, lane, a, r);
@@ -430,7 +427,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const d
 #pragma unroll
             for (int m = 0; m < BS; ++m) y[(int64_t)BS * a + m] = r[m];
         }
-    }
+    });
 }
 
 __global__ void split_vec_kernel(int n, const double *__restrict__ h, float2 *__restrict__ hx) {
@@ -568,11 +565,26 @@ __global__ void transpose_kernel(int nb, int bs, const int32_t *brp, const int32
 }
 
 // ------------------------------------------------------------------ host side
-constexpr int kSellLanes = 64;   // tuner's code for the SELL-32 kernels (one row per lane)
+// tuner codes of the SELL-32 kernels (one row per lane), 64 + the chunk assignment
+// (sell_for_chunks); block CSR is coded by its lanes per row
+constexpr int kSellCode = 64;
+static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 3; }
+
+#define FFGPU_SELL_FN(K)                                                                           \
+    static void *K##_fn(int bs, bool c16, int assign) {                                           \
+        void *t[3][3] = {{(void *)K<1, false, 0>, (void *)K<1, false, 1>, (void *)K<1, false, 2>}, \
+                         {(void *)K<1, true, 0>, (void *)K<1, true, 1>, (void *)K<1, true, 2>},    \
+                         {(void *)K<3, false, 0>, (void *)K<3, false, 1>, (void *)K<3, false, 2>}}; \
+        return t[bs == 3 ? 2 : (c16 ? 1 : 0)][assign];                                             \
+    }
+FFGPU_SELL_FN(cg_ka_sell)
+FFGPU_SELL_FN(cg_kax_sell)
+FFGPU_SELL_FN(spmv_sell)
+#undef FFGPU_SELL_FN
 
 // lanes per block row of the block-CSR kernels
 static int pick_lanes(const ffgpu_matrix *A) {
-    if (A->csr_lanes > 0 && A->csr_lanes != kSellLanes) return A->csr_lanes;
+    if (A->csr_lanes > 0 && !is_sell(A->csr_lanes)) return A->csr_lanes;
     double avg = (double)A->nnzb / (double)max(1, A->nb);
     if (A->bs == 3) return avg >= 24 ? 4 : 2;
     if (avg >= 24) return 8;
@@ -647,28 +659,29 @@ struct KaCall {
     cudaError_t launch(cudaStream_t s) { return cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, s); }
 };
 
-// K_a for mode (0 FP64, 1 double-float) and lanes choice T (kSellLanes: SELL-32)
+// K_a for mode (0 FP64, 1 double-float) and layout choice T (SELL-32 codes or BSR lanes)
 static int ka_setup(ffgpu_matrix *A, int mode, int trans, int T, const double *h, double *q, KaCall &k) {
     k.h = h; k.q = q; k.ks = A->ks; k.part = A->ctx->d_part; k.hx = A->hx;
-    if (T == kSellLanes) {
+    if (is_sell(T)) {
         FFGPU_TRY(sell_values(A, mode == 1 ? (trans ? kSellXT : kSellX) : (trans ? kSell64T : kSell64)));
         // the column format is known only once the layout exists
         const bool c16 = A->scol16 != nullptr;
+        const int assign = T - kSellCode;
+        const bool range = assign == kSellRanges;
         k.sl = sell_args(A);
         if (mode == 1) {
             k.vx = trans ? A->svalx_t : A->svalx;
-            k.fn = A->bs == 3 ? (void *)cg_kax_sell<3, false>
-                              : (c16 ? (void *)cg_kax_sell<1, true> : (void *)cg_kax_sell<1, false>);
+            k.fn = cg_kax_sell_fn(A->bs, c16, assign);
             k.args[0] = &k.sl; k.args[1] = &k.vx; k.args[2] = &k.hx; k.args[3] = &k.h; k.args[4] = &k.q;
             k.args[5] = &k.ks; k.args[6] = &k.part;
         } else {
             k.v64 = trans ? A->sval_t : A->sval;
-            k.fn = A->bs == 3 ? (void *)cg_ka_sell<3, false>
-                              : (c16 ? (void *)cg_ka_sell<1, true> : (void *)cg_ka_sell<1, false>);
+            k.fn = cg_ka_sell_fn(A->bs, c16, assign);
             k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.h; k.args[3] = &k.q; k.args[4] = &k.ks;
             k.args[5] = &k.part;
         }
         k.grid = resident_grid(k.fn, kSpmvWarps * 32);
+        if (range) FFGPU_TRY(sell_partition(A, k.grid * kSpmvWarps, &k.sl.part));
         return FFGPU_OK;
     }
     if (mode == 1) {
@@ -701,11 +714,12 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
             *slot = ctx->tuned[i].lanes;
             return FFGPU_OK;
         }
-    if (!A->vec) { *slot = kSellLanes; return FFGPU_OK; }
+    if (!A->vec) { *slot = kSellCode; return FFGPU_OK; }
     // FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row;
     // double-float: reductions are FP32, so wider lane groups
-    const int cands64[] = {kSellLanes, 1, 2, 4, 8};
-    const int candsx[] = {kSellLanes, 4, 8, 16, 32};
+    const int S0 = kSellCode;
+    const int cands64[] = {S0 + kSellRanges, S0 + kSellRotated, S0 + kSellStride, 1, 2, 4, 8};
+    const int candsx[] = {S0 + kSellRanges, S0 + kSellRotated, S0 + kSellStride, 4, 8, 16, 32};
     const int *cands = mode == 1 ? candsx : cands64;
     const int64_t vs = vstride(A->n);
     double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
@@ -719,8 +733,8 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int bestT = kSellLanes;
-    for (int c = 0; c < 5; ++c) {
+    int bestT = kSellCode;
+    for (int c = 0; c < 7; ++c) {
         const int T = cands[c];
         KaCall k;
         FFGPU_TRY(ka_setup(A, mode, 0, T, x, y, k));
@@ -734,16 +748,19 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         if (getenv("FFGPU_VERBOSE"))
-            fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s%d %.4f ms\n", mode,
-                    A->nb, (long long)A->nnzb, T == kSellLanes ? "sell32 " : "bsr lanes ",
-                    T == kSellLanes ? 32 : T, ms / 3);
+            fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s %.4f ms\n", mode,
+                    A->nb, (long long)A->nnzb,
+                    T == S0 + kSellRanges ? "sell32 ranges"
+                                          : (T == S0 + kSellRotated ? "sell32 rotated"
+                                                                    : (T == S0 + kSellStride ? "sell32 stride" : "bsr lanes")),
+                    ms / 3);
         if (ms < best) { best = ms; bestT = T; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
     FFGPU_CUDA(cudaStreamSynchronize(s));
-    if (bestT == kSellLanes) {
+    if (is_sell(bestT)) {
         if (mode == 1) { cudaFree(A->valx); A->valx = nullptr; }
     } else if (mode == 1) {
         cudaFree(A->svalx); A->svalx = nullptr;
@@ -759,10 +776,13 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
     const double *sv = trans ? A->sval_t : A->sval;
     if (sv) {
         SellArgs sl = sell_args(A);
-        void *fn = A->bs == 3 ? (void *)spmv_sell<3, false>
-                              : (A->scol16 ? (void *)spmv_sell<1, true> : (void *)spmv_sell<1, false>);
+        const int assign = is_sell(A->csr_lanes) ? A->csr_lanes - kSellCode : kSellRanges;
+        const bool range = assign == kSellRanges;
+        void *fn = spmv_sell_fn(A->bs, A->scol16 != nullptr, assign);
+        const int grid = resident_grid(fn, kSpmvWarps * 32);
+        if (range) FFGPU_TRY(sell_partition(A, grid * kSpmvWarps, &sl.part));
         void *args[] = {&sl, &sv, &x, &y};
-        FFGPU_CUDA(cudaLaunchKernel(fn, resident_grid(fn, kSpmvWarps * 32), kSpmvWarps * 32, args, 0, st));
+        FFGPU_CUDA(cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, st));
         return launch_check(A->ctx, "spmv");
     }
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
@@ -1226,7 +1246,7 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
 
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode) {
     if (!A) return 0;
-    return mode == 1 ? A->csr_lanes_x : A->csr_lanes;
+    return mode == 2 ? A->sell32_kind : (mode == 1 ? A->csr_lanes_x : A->csr_lanes);
 }
 
 int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans) {

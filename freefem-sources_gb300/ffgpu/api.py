@@ -296,9 +296,11 @@ class Matrix:
         return out
 
     def spmv_layout(self, mode=0):
-        """The SpMV layout the tuner chose: 'sell32', 'bsr/T' (T lanes per row) or None."""
+        """The SpMV layout the tuner chose for mode 0 (FP64 CG), 1 (double-float CG) or 2 (FP32
+        inner solve): 'sell32' (chunk ranges), 'sell32-rot', 'sell32-stride', 'bsr/T' (T lanes per
+        block row) or None."""
         v = int(lib().ffgpu_matrix_spmv_layout(self.h, int(mode)))
-        return None if v <= 0 else ("sell32" if v == 64 else f"bsr/{v}")
+        return None if v <= 0 else {64: "sell32", 65: "sell32-rot", 66: "sell32-stride"}.get(v, f"bsr/{v}")
 
     def mult(self, x, trans=False, out=None):
         if out is None:
