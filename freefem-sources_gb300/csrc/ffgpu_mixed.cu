@@ -48,10 +48,9 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     float hq = 0;
-    sell_for_chunks<ASSIGN>(S, [&](int c) {
-        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+    sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         float y[BS];
-        sell_row32<BS, C16>(S, val, h, c, lane, a, y);
+        sell_row32<BS, C16>(S, val, h, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {

@@ -84,17 +84,57 @@ __device__ __forceinline__ float2 split_f64(double v) {
 // The tuners time all three on the matrix.
 enum SellAssign { kSellRanges = 0, kSellRotated = 1, kSellStride = 2 };
 
+template <int ASSIGN>
+struct ChunkWalk {
+    int c, ce, k, w, nw;
+    __device__ __forceinline__ ChunkWalk(const SellArgs &S) {
+        w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        nw = (gridDim.x * blockDim.x) >> 5;
+        k = 0;
+        if constexpr (ASSIGN == kSellRanges) {
+            c = __ldg(S.part + w);
+            ce = __ldg(S.part + w + 1);
+        } else {
+            ce = S.nchunk;
+            c = at(0);
+        }
+    }
+    __device__ __forceinline__ int at(int kk) const {
+        return kk * nw + (ASSIGN == kSellRotated ? (w + 5 * kk) % nw : w);
+    }
+    // next chunk of this warp (>= ce when done)
+    __device__ __forceinline__ int next() {
+        if constexpr (ASSIGN == kSellRanges) return c + 1;
+        return (int64_t)(k + 1) * nw < ce ? at(k + 1) : ce;
+    }
+    __device__ __forceinline__ void advance(int cn) { c = cn; ++k; }
+};
+
+// Calls body(c, a, L, sr) for every chunk of this warp (a: the lane's row, L: slots, sr: first
+// slot row), loading the next chunk's row, length and offset while the current one runs.
 template <int ASSIGN, typename F>
 __device__ __forceinline__ void sell_for_chunks(const SellArgs &S, F &&body) {
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if constexpr (ASSIGN == kSellRanges) {
-        for (int c = __ldg(S.part + w), ce = __ldg(S.part + w + 1); c < ce; ++c) body(c);
-    } else {
-        const int nw = (gridDim.x * blockDim.x) >> 5;
-        for (int k = 0; (int64_t)k * nw < S.nchunk; ++k) {
-            const int c = k * nw + (ASSIGN == kSellRotated ? (w + 5 * k) % nw : w);
-            if (c < S.nchunk) body(c);
+    const int lane = threadIdx.x & 31;
+    ChunkWalk<ASSIGN> it(S);
+    // the rotated and plain strides can land past the last chunk on a warp's final pass
+    while (it.c < it.ce && it.c >= S.nchunk) it.advance(it.next());
+    if (it.c >= it.ce) return;
+    int a = __ldg(S.perm + (int64_t)it.c * 32 + lane), L = __ldg(S.len + it.c);
+    int64_t sr = __ldg(S.off + it.c);
+    for (;;) {
+        int cn = it.next();
+        while (cn < it.ce && cn >= S.nchunk) { it.advance(cn); cn = it.next(); }
+        int an = 0, Ln = 0;
+        int64_t srn = 0;
+        if (cn < it.ce) {
+            an = __ldg(S.perm + (int64_t)cn * 32 + lane);
+            Ln = __ldg(S.len + cn);
+            srn = __ldg(S.off + cn);
         }
+        body(it.c, a, L, sr);
+        if (cn >= it.ce) break;
+        it.advance(cn);
+        a = an; L = Ln; sr = srn;
     }
 }
 
@@ -110,15 +150,14 @@ __device__ __forceinline__ int sell_col(const SellArgs &S, int64_t e, int ar) {
 
 template <int BS, bool C16>
 __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__restrict__ val,
-                                           const double *__restrict__ x, int c, int lane, int a, double *y) {
-    const int L = __ldg(S.len + c);
-    const int64_t sr = __ldg(S.off + c);
+                                           const double *__restrict__ x, int L, int64_t sr, int lane, int a,
+                                           double *y) {
     const int ar = a < 0 ? 0 : a;
     const int64_t ce = sr * 32 + lane;
     const double *v = val + sr * (BS * BS * 32) + lane;
     double s0 = 0, s1 = 0, s2 = 0;
-    // scalar rows: 8 slots in flight hide the column -> gather dependency; 3x3 blocks: 2
-    constexpr int UNR = BS == 1 ? 8 : 2;
+    // scalar rows: 16 slots in flight hide the column -> gather dependency; 3x3 blocks: 2
+    constexpr int UNR = BS == 1 ? 16 : 2;
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
@@ -139,14 +178,13 @@ __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__re
 
 template <int BS, bool C16>
 __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__restrict__ val,
-                                          const float2 *__restrict__ x, int c, int lane, int a, double *y) {
-    const int L = __ldg(S.len + c);
-    const int64_t sr = __ldg(S.off + c);
+                                          const float2 *__restrict__ x, int L, int64_t sr, int lane, int a,
+                                          double *y) {
     const int ar = a < 0 ? 0 : a;
     const int64_t ce = sr * 32 + lane;
     const float2 *v = val + sr * (BS * BS * 32) + lane;
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
-    constexpr int UNR = BS == 1 ? 8 : 2;
+    constexpr int UNR = BS == 1 ? 16 : 2;
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
@@ -170,14 +208,13 @@ __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__res
 
 template <int BS, bool C16>
 __device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__restrict__ val,
-                                           const float *__restrict__ x, int c, int lane, int a, float *y) {
-    const int L = __ldg(S.len + c);
-    const int64_t sr = __ldg(S.off + c);
+                                           const float *__restrict__ x, int L, int64_t sr, int lane, int a,
+                                           float *y) {
     const int ar = a < 0 ? 0 : a;
     const int64_t ce = sr * 32 + lane;
     const float *v = val + sr * (BS * BS * 32) + lane;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    constexpr int UNR = BS == 1 ? 8 : 4;
+    constexpr int UNR = BS == 1 ? 16 : 4;
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);

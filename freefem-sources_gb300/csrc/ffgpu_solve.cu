@@ -362,10 +362,9 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     double hq = 0;
-    sell_for_chunks<ASSIGN>(S, [&](int c) {
-        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+    sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double y[BS];
-        sell_row64<BS, C16>(S, val, h, c, lane, a, y);
+        sell_row64<BS, C16>(S, val, h, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -393,10 +392,9 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     double hq = 0;
-    sell_for_chunks<ASSIGN>(S, [&](int c) {
-        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+    sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double y[BS];
-        sell_rowx<BS, C16>(S, val, hx, c, lane, a, y);
+        sell_rowx<BS, C16>(S, val, hx, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -419,10 +417,9 @@ template <int BS, bool C16, int ASSIGN>
 __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const double *__restrict__ val,
                                                              const double *__restrict__ x, double *__restrict__ y) {
     const int lane = threadIdx.x & 31;
-    sell_for_chunks<ASSIGN>(S, [&](int c) {
-        const int a = __ldg(S.perm + (int64_t)c * 32 + lane);
+    sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double r[BS];
-        sell_row64<BS, C16>(S, val, x, c, lane, a, r);
+        sell_row64<BS, C16>(S, val, x, L, sr, lane, a, r);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) y[(int64_t)BS * a + m] = r[m];

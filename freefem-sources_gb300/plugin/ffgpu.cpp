@@ -17,10 +17,22 @@
 // which the matrix owns (VirtualMatrix.hpp:71-94).  Errors become ExecError / ffassert as in
 // FreeFEM's own solvers; there is no CPU fallback.
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <iomanip>
 #include <iostream>
+#include <set>
+#include <string>
+#include <vector>
 
 #include "ff++.hpp"
 #include "ffgpu.h"
+
+// label set of an on(...) condition (defined in FreeFEM, lgfem.cpp:7792)
+namespace Fem2D {
+void Expandsetoflab(Stack stack, const BC_set &bc, set<long> &setoflab);
+}
 
 namespace {
 
@@ -106,6 +118,358 @@ template <> const int SolverGpu<kCG>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 template <> const int SolverGpu<kGMRES>::orTypeSol = 1 | 2 | 4 | 8 | 16 | 32;
 template <> const int SolverGpu<kMixed>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 
+// ------------------------------------------------------------------ device assembly
+// `matrix A = a(Vh, Vh, ...)` is routed here (an OpMatrixtoBilinearForm with a higher
+// overload preference, problem.hpp:1611, AFunction2.cpp:87-100).  A form the device assembles
+// is recognised from its terms; anything else -- other elements, coefficients that are not
+// piecewise constant, quadratures that are not exact for the form, symmetric storage, other
+// terms -- is assembled by FreeFEM's own operator, unchanged.
+//   scalar P1 / P2 (2D, 3D):  int(Th)(k*(grad u . grad v) [+ m*u*v]) + on(labels, u = ...)
+//     with k piecewise constant (a P0 function, a constant, any expression constant per
+//     element) and m constant;
+//   3D [P2,P2,P2]:            int3d(Th)(lambda*div(u)*div(v) + 2*mu*(eps(u):eps(v)))
+//     + on(labels, ...) with constant lambda, mu (any way of writing it whose terms add up
+//     to the isotropic tensor).
+// The device matrix is built by ffgpu_matrix_assemble (pattern, values and tgv rows) and
+// handed to FreeFEM as its HashMatrix (sorted CSR, HashMatrix::set).
+
+template <class MMesh> struct Dim;
+template <> struct Dim<Mesh> { static const int d = 2; typedef R2 Rd; };
+template <> struct Dim<Mesh3> { static const int d = 3; typedef R3 Rd; };
+
+struct Recognised {
+    int fe = 0, form = FFGPU_FORM_DIFFUSION;
+    std::vector<double> kappa;
+    double c_mass = 0, lam = 0, mu = 0, tgv = 1e30;
+    int comp_mask = -1;   // components constrained by on(...) (-1: no on)
+    std::vector<int32_t> labels;
+    std::string why;
+};
+
+// element type of a space: FFGPU_FE_* or 0
+static int fe_kind(const FESpace &Uh) {
+    if (Uh.N != 1) return 0;
+    if (Uh.TFE[0] == &P1Lagrange) return FFGPU_FE_P1;
+    if (Uh.TFE[0] == &P2Lagrange) return FFGPU_FE_P2;
+    return 0;
+}
+static int fe_kind(const FESpace3 &Uh) {
+    if (Uh.TFE[0] == &DataFE<Mesh3>::P1) return FFGPU_FE_P1;
+    if (Uh.TFE[0] == &DataFE<Mesh3>::P2) return FFGPU_FE_P2;
+    const GTypeOfFESum<Mesh3> *s = dynamic_cast<const GTypeOfFESum<Mesh3> *>(Uh.TFE[0]);
+    if (s && s->k == 3 && s->teb[0] == &DataFE<Mesh3>::P2 && s->teb[1] == &DataFE<Mesh3>::P2 &&
+        s->teb[2] == &DataFE<Mesh3>::P2)
+        return FFGPU_FE_P2VEC3;
+    return 0;
+}
+
+// position of a FreeFEM operator code among (id, dx, dy[, dz]), -1 for anything else
+static int op_index(int op, int d) {
+    op %= last_operatortype;
+    if (op == op_id) return 0;
+    if (op == op_dx) return 1;
+    if (op == op_dy) return 2;
+    if (op == op_dz && d == 3) return 3;
+    return -1;
+}
+
+// two interior reference points of a simplex (barycentre and an off-centre point)
+static void ref_points(R2 &a, R2 &b) { a = R2(1. / 3., 1. / 3.); b = R2(0.2, 0.3); }
+static void ref_points(R3 &a, R3 &b) { a = R3(0.25, 0.25, 0.25); b = R3(0.1, 0.2, 0.3); }
+
+// quadrature exactness of a domain of integration
+static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).exact; }
+static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).exact; }
+
+// Reads the form's terms.  Returns true when the device can assemble it; r.why otherwise.
+template <class MMesh, class FES>
+static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, const FES &Uh, Recognised &r) {
+    typedef typename Dim<MMesh>::Rd Rd;
+    const int d = Dim<MMesh>::d;
+    r.fe = fe_kind(Uh);
+    if (!r.fe) { r.why = "element type"; return false; }
+    const int nc = r.fe == FFGPU_FE_P2VEC3 ? 3 : 1;
+    r.form = nc == 3 ? FFGPU_FORM_ELASTICITY : FFGPU_FORM_DIFFUSION;
+    const int nt = Th.nt;
+    // coefficient of (u_j, op_p) (v_i, op_q), ops 0 id, 1..d derivatives: per element (scalar)
+    // or constant (vector space), accumulated over all terms
+    const int NO = 1 + d, NT = nc * NO;
+    std::vector<double> tab((size_t)NT * NT, 0.0);
+    std::vector<double> kx(r.fe == FFGPU_FE_P2VEC3 ? 0 : (size_t)nt * (d + 1), 0.0);   // k_dd per element, mass
+    std::set<long> on;
+    FreeFempp::TypeVarForm<double> *tvf = FreeFempp::TypeVarForm<double>::Global;
+    MeshPoint mp = *MeshPointStack(stack);
+    Rd pa, pb;
+    ref_points(pa, pb);
+    bool ok = true;
+    for (list<C_F0>::const_iterator ii = largs.begin(); ok && ii != largs.end(); ++ii) {
+        aType t = ii->left();
+        Expression e = ii->LeftValue();
+        if (t == tvf->tBC) {
+            const BC_set *bc = dynamic_cast<const BC_set *>(e);
+            if (!bc) { r.why = "boundary condition"; ok = false; break; }
+            // constrained components: one set for all on(...) of the form
+            int mask = 0;
+            for (size_t i = 0; i < bc->bc.size(); ++i) mask |= 1 << bc->bc[i].first;
+            if (r.comp_mask >= 0 && r.comp_mask != mask) { r.why = "on() with different components"; ok = false; break; }
+            r.comp_mask = mask;
+            Fem2D::Expandsetoflab(stack, *bc, on);
+            continue;
+        }
+        if (t == tvf->tFL) continue;   // linear terms: not part of the matrix
+        if (t != tvf->tFB) { r.why = "term kind"; ok = false; break; }
+        const FormBilinear *bf = dynamic_cast<const FormBilinear *>(e);
+        const CDomainOfIntegration &di = *bf->di;
+        if (di.d != d || di.dHat != d || !di.what.empty() || di.islevelset() || di.withmap()) {
+            r.why = "domain of integration"; ok = false; break;
+        }
+        if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { r.why = "integration mesh"; ok = false; break; }
+        const int ex = exactness(stack, di, &Th);
+        const BilinearOperator &op = *bf->b;
+        for (BilinearOperator::const_iterator l = op.v.begin(); ok && l != op.v.end(); ++l) {
+            const int ju = l->first.first.first, jv = l->first.second.first;
+            const int pu = op_index(l->first.first.second, d), pv = op_index(l->first.second.second, d);
+            if (ju >= nc || jv >= nc || pu < 0 || pv < 0) { r.why = "operator"; ok = false; break; }
+            // degree of the integrand for these two operators (coefficient constant on elements)
+            const int order = r.fe == FFGPU_FE_P1 ? 1 : 2;
+            const int deg = (pu ? order - 1 : order) + (pv ? order - 1 : order);
+            if (ex < deg) { r.why = "quadrature not exact for the form"; ok = false; break; }
+            const bool constant = l->second.LeftValue()->MeshIndependent();
+            if (nc == 3) {
+                // elasticity: coefficients independent of the mesh point
+                if (!constant) { r.why = "coefficient not constant"; ok = false; break; }
+                typename FES::FElement FK = Uh[0];
+                MeshPointStack(stack)->set(Th[0](pa), pa, FK);
+                tab[(size_t)(ju * NO + pu) * NT + (jv * NO + pv)] += GetAny<double>(l->second.eval(stack));
+                continue;
+            }
+            if (constant) {
+                typename FES::FElement FK = Uh[0];
+                MeshPointStack(stack)->set(Th[0](pa), pa, FK);
+                const double c = GetAny<double>(l->second.eval(stack));
+                if (pu == pv && pu > 0) for (int k = 0; k < nt; ++k) kx[(size_t)k * (d + 1) + pu - 1] += c;
+                else if (pu == 0 && pv == 0) for (int k = 0; k < nt; ++k) kx[(size_t)k * (d + 1) + d] += c;
+                else if (c != 0.0) { r.why = "mixed derivative term"; ok = false; }
+                continue;
+            }
+            // coefficient depending on the point: it must be constant on every element (P0)
+            for (int k = 0; k < nt; ++k) {
+                typename FES::FElement FK = Uh[k];
+                MeshPointStack(stack)->set(Th[k](pa), pa, FK);
+                const double ca = GetAny<double>(l->second.eval(stack));
+                MeshPointStack(stack)->set(Th[k](pb), pb, FK);
+                const double cb = GetAny<double>(l->second.eval(stack));
+                if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
+                    r.why = "coefficient not constant on elements"; ok = false; break;
+                }
+                if (pu == pv && pu > 0) kx[(size_t)k * (d + 1) + pu - 1] += ca;
+                else if (pu == 0 && pv == 0) kx[(size_t)k * (d + 1) + d] += ca;
+                else if (ca != 0.0) { r.why = "mixed derivative term"; ok = false; break; }
+            }
+        }
+    }
+    *MeshPointStack(stack) = mp;
+    if (!ok) return false;
+    r.labels.assign(on.begin(), on.end());
+    if (nc == 1) {
+        r.kappa.resize(nt);
+        const double m0 = kx[d];
+        for (int k = 0; k < nt; ++k) {
+            const double *c = &kx[(size_t)k * (d + 1)];
+            for (int a = 1; a < d; ++a)
+                if (c[a] != c[0]) { r.why = "anisotropic diffusion"; return false; }
+            if (c[d] != m0) { r.why = "mass coefficient not constant"; return false; }
+            r.kappa[k] = c[0];
+        }
+        r.c_mass = m0;
+        return true;
+    }
+    // isotropic elasticity: T[(j,p),(i,q)] = lambda d_jp d_iq + mu (d_ij d_pq + d_jq d_ip)
+    const double lam = tab[(size_t)(0 * NO + 1) * NT + (1 * NO + 2)];
+    const double mu = tab[(size_t)(0 * NO + 2) * NT + (0 * NO + 2)];
+    for (int j = 0; j < 3; ++j)
+        for (int p = 0; p <= 3; ++p)
+            for (int i = 0; i < 3; ++i)
+                for (int q = 0; q <= 3; ++q) {
+                    double want = 0;
+                    if (p > 0 && q > 0) {
+                        const int pp = p - 1, qq = q - 1;
+                        want = lam * (j == pp) * (i == qq) + mu * ((i == j) * (pp == qq) + (j == qq) * (i == pp));
+                    }
+                    const double got = tab[(size_t)(j * NO + p) * NT + (i * NO + q)];
+                    if (std::fabs(got - want) > 1e-13 * (std::fabs(lam) + std::fabs(mu)))
+                        { r.why = "not isotropic elasticity"; return false; }
+                }
+    r.lam = lam;
+    r.mu = mu;
+    return true;
+}
+
+// mesh arrays in the C ABI's layout
+static void mesh_arrays(const Mesh &Th, std::vector<double> &X, std::vector<int32_t> &E, std::vector<int32_t> &BE,
+                        std::vector<int32_t> &BL) {
+    X.resize(2 * (size_t)Th.nv);
+    for (int i = 0; i < Th.nv; ++i) { X[2 * i] = Th(i).x; X[2 * i + 1] = Th(i).y; }
+    E.resize(3 * (size_t)Th.nt);
+    for (int k = 0; k < Th.nt; ++k)
+        for (int j = 0; j < 3; ++j) E[3 * (size_t)k + j] = Th(Th[k][j]);
+    BE.resize(2 * (size_t)Th.neb);
+    BL.resize(Th.neb);
+    for (int i = 0; i < Th.neb; ++i) {
+        for (int j = 0; j < 2; ++j) BE[2 * (size_t)i + j] = Th(Th.bedges[i][j]);
+        BL[i] = Th.bedges[i].lab;
+    }
+}
+static void mesh_arrays(const Mesh3 &Th, std::vector<double> &X, std::vector<int32_t> &E, std::vector<int32_t> &BE,
+                        std::vector<int32_t> &BL) {
+    X.resize(3 * (size_t)Th.nv);
+    for (int i = 0; i < Th.nv; ++i) { X[3 * i] = Th(i).x; X[3 * i + 1] = Th(i).y; X[3 * i + 2] = Th(i).z; }
+    E.resize(4 * (size_t)Th.nt);
+    for (int k = 0; k < Th.nt; ++k)
+        for (int j = 0; j < 4; ++j) E[4 * (size_t)k + j] = Th(Th[k][j]);
+    BE.resize(3 * (size_t)Th.nbe);
+    BL.resize(Th.nbe);
+    for (int i = 0; i < Th.nbe; ++i) {
+        for (int j = 0; j < 3; ++j) BE[3 * (size_t)i + j] = Th(Th.be(i)[j]);
+        BL[i] = Th.be(i).lab;
+    }
+}
+
+static void dump(const std::string &path, const void *p, size_t n) {
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) ExecError(("ffgpu: cannot write " + path).c_str());
+    if (n) fwrite(p, 1, n, f);
+    fclose(f);
+}
+
+static const char *fe_name(int fe) { return fe == FFGPU_FE_P1 ? "P1" : (fe == FFGPU_FE_P2 ? "P2" : "[P2,P2,P2]"); }
+
+// The device assembly of a recognised form into FreeFEM's matrix object; false: not ours.
+template <class MMesh, class FES>
+static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, const Data_Sparse_Solver &ds,
+                          Matrice_Creuse<double> &A) {
+    const MMesh &Th = Uh.Th;
+    const int d = Dim<MMesh>::d;
+    Recognised r;
+    if (ds.sym) r.why = "symmetric storage requested";
+    else if (!recognise(stack, largs, Th, Uh, r)) {}
+    if (!r.why.empty()) {
+        if (verbosity > 1) std::cout << "  ffgpu: form assembled by FreeFEM (" << r.why << ")" << std::endl;
+        return false;
+    }
+    double ksum = 0;
+    for (size_t k = 0; k < r.kappa.size(); ++k) ksum += r.kappa[k] * (double)(k % 7 + 1);
+    if (verbosity > 1) {
+        std::cout << "  ffgpu: device assembly " << fe_name(r.fe) << " dim " << d << " nt " << Th.nt
+                  << " ndof " << Uh.NbOfDF;
+        if (r.form == FFGPU_FORM_ELASTICITY) std::cout << " lambda " << r.lam << " mu " << r.mu;
+        else std::cout << " kappa-check " << std::setprecision(17) << ksum << " mass " << r.c_mass;
+        std::cout << " tgv " << ds.tgv << " components " << r.comp_mask << " labels";
+        for (size_t i = 0; i < r.labels.size(); ++i) std::cout << " " << r.labels[i];
+        std::cout << std::setprecision(6) << std::endl;
+    }
+    std::vector<double> X;
+    std::vector<int32_t> E, BE, BL;
+    mesh_arrays(Th, X, E, BE, BL);
+    const int ndofK = Uh[0].NbDoF();
+    std::vector<int32_t> dof((size_t)Th.nt * ndofK);
+    for (int k = 0; k < Th.nt; ++k) {
+        typename FES::FElement K = Uh[k];
+        if (K.NbDoF() != ndofK) ExecError("ffgpu: elements with different numbers of DOFs");
+        for (int i = 0; i < ndofK; ++i) dof[(size_t)k * ndofK + i] = K(i);
+    }
+    if (const char *dir = getenv("FFGPU_PLUGIN_DUMP")) {
+        // the arrays handed to the C ABI, for checking the extraction against other builders
+        const std::string p(dir);
+        dump(p + "/coords.bin", X.data(), X.size() * sizeof(double));
+        dump(p + "/elems.bin", E.data(), E.size() * sizeof(int32_t));
+        dump(p + "/dof.bin", dof.data(), dof.size() * sizeof(int32_t));
+        dump(p + "/belems.bin", BE.data(), BE.size() * sizeof(int32_t));
+        dump(p + "/blabel.bin", BL.data(), BL.size() * sizeof(int32_t));
+        dump(p + "/kappa.bin", r.kappa.data(), r.kappa.size() * sizeof(double));
+    }
+    ffgpu_ctx *ctx = context();
+    ffgpu_space *S = nullptr;
+    ffgpu_matrix *M = nullptr;
+    int rc = ffgpu_space_create(ctx, d, Th.nv, X.data(), Th.nt, E.data(), r.fe, ndofK, dof.data(), Uh.NbOfDF, &S);
+    if (!rc && !BL.empty()) rc = ffgpu_space_set_boundary(S, (int)BL.size(), BE.data(), BL.data());
+    if (!rc) {
+        ffgpu_varf v;
+        memset(&v, 0, sizeof(v));
+        v.form = r.form;
+        v.c_stiff = 1.0;
+        if (r.form == FFGPU_FORM_ELASTICITY) {
+            v.E = r.mu * (3 * r.lam + 2 * r.mu) / (r.lam + r.mu);
+            v.nu = r.lam / (2 * (r.lam + r.mu));
+        } else {
+            v.kappa = r.kappa.data();
+            v.c_mass = r.c_mass;
+        }
+        ffgpu_bc bc;
+        memset(&bc, 0, sizeof(bc));
+        bc.tgv = ds.tgv;
+        bc.nlabels = (int)r.labels.size();
+        bc.labels = r.labels.data();
+        bc.comp_mask = r.fe == FFGPU_FE_P2VEC3 && r.comp_mask != 7 ? r.comp_mask : 0;
+        rc = ffgpu_matrix_assemble(S, &v, r.labels.empty() ? nullptr : &bc, nullptr, &M);
+    }
+    int n = 0, bs = 0;
+    int64_t nnz = 0;
+    std::vector<int32_t> rp, col;
+    std::vector<double> val;
+    if (!rc) rc = ffgpu_matrix_info(M, &n, &nnz, &bs);
+    if (!rc) {
+        rp.resize(n + 1);
+        col.resize(nnz);
+        val.resize(nnz);
+        rc = ffgpu_matrix_csr(M, rp.data(), col.data(), val.data());
+    }
+    if (M) ffgpu_matrix_destroy(M);
+    if (S) ffgpu_space_destroy(S);
+    if (rc) ExecError((std::string("ffgpu assembly: ") + ffgpu_last_error()).c_str());
+    // FreeFEM's matrix object, as creationBlockOfMatrixToBilinearForm leaves it (problem.hpp:1663-1714)
+    A.A = 0;
+    A.Uh = Uh;
+    A.Vh = Uh;
+    HashMatrix<int, double> *H = new HashMatrix<int, double>(n, n, 0, 0);
+    H->set(n, n, 0, (size_t)nnz, rp.data(), col.data(), val.data(), 0, 1);
+    A.A.master(H);
+    return true;
+}
+
+template <class MMesh, class v_fes>
+struct GpuBilinear : public OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> {
+    typedef OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> Base;
+    typedef typename v_fes::pfes pfes;
+    typedef typename v_fes::FESpace FES;
+    class GOp : public Base::Op {
+       public:
+        GOp(Expression aa, Expression bb, int initt) : Base::Op(aa, bb, initt) {}
+        AnyType operator()(Stack stack) const {
+            const Call_FormBilinear<v_fes, v_fes> *b = this->b;
+            pfes *pUh = GetAny<pfes *>((*b->euh)(stack));
+            pfes *pVh = GetAny<pfes *>((*b->evh)(stack));
+            const FES *PUh = (FES *)**pUh, *PVh = (FES *)**pVh;
+            if (!PUh || PUh != PVh || isVF(b->largs)) return Base::Op::operator()(stack);
+            Data_Sparse_Solver ds;
+            ds.factorize = 0;
+            ds.initmat = true;
+            const int np = OpCall_FormBilinear_np::n_name_param - NB_NAME_PARM_HMAT;
+            SetEnd_Data_Sparse_Solver<double>(stack, ds, b->nargs, np);
+            Matrice_Creuse<double> &A(*GetAny<Matrice_Creuse<double> *>((*this->a)(stack)));
+            if (this->init) A.init();
+            if (!device_matrix<MMesh, FES>(stack, b->largs, *PUh, ds, A)) return Base::Op::operator()(stack);
+            A.pHM()->half = ds.sym;
+            SetSolver(stack, false, *A.A, ds);
+            return SetAny<Matrice_Creuse<double> *>(&A);
+        }
+    };
+    E_F0 *code(const basicAC_F0 &args) const {
+        return new GOp(to<Matrice_Creuse<double> *>(args[0]), args[1], this->init);
+    }
+    GpuBilinear(int initt) : Base(initt) { this->pref = 10; }
+};
+
 }  // namespace
 
 static void Load_Init() {
@@ -117,6 +481,10 @@ static void Load_Init() {
     Global.New("GPUCG", CConstant<std::string *>(&gpucg));
     Global.New("GPUGMRES", CConstant<std::string *>(&gpugmres));
     Global.New("GPUCGMIXED", CConstant<std::string *>(&gpumixed));
+    // device assembly behind `matrix A = a(Vh,Vh)` (lgfem.cpp:6669-6673, :6823-6826)
+    TheOperators->Add("=", new GpuBilinear<Mesh, v_fes>(0), new GpuBilinear<Mesh3, v_fes3>(0));
+    TheOperators->Add("<-", new GpuBilinear<Mesh, v_fes>(1));
+    TheOperators->Add("<-", new GpuBilinear<Mesh3, v_fes3>(1));
     if (verbosity > 1) std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED)" << std::endl;
 }
 

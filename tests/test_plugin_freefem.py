@@ -30,26 +30,141 @@ cout << "umax " << u[].max << endl;
 """
 
 
-def test_plugin_registers_solvers_and_refuses_cpu_fallback(tmp_path):
+@pytest.fixture(scope="module")
+def plugin(tmp_path_factory):
+    """The plugin compiled with FreeFEM's ff-c++ against this repository's libffgpu.so."""
     from ffgpu.build import build
     lib = build()
-    src = tmp_path / "ffgpu.cpp"
-    shutil.copy(os.path.join(REPO, "freefem-sources_gb300", "plugin", "ffgpu.cpp"), src)
+    d = tmp_path_factory.mktemp("plugin")
+    shutil.copy(os.path.join(REPO, "freefem-sources_gb300", "plugin", "ffgpu.cpp"), d / "ffgpu.cpp")
     r = subprocess.run([FF_CXX, "-auto", "ffgpu.cpp", "-I" + os.path.join(REPO, "include"), lib],
-                       cwd=tmp_path, capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0 and (tmp_path / "ffgpu.so").exists(), r.stdout + r.stderr
-    (tmp_path / "t.edp").write_text(SCRIPT % str(tmp_path / "ffgpu"))
+                       cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and (d / "ffgpu.so").exists(), r.stdout + r.stderr
     env = dict(os.environ, FF_LOADPATH=FF_LOADPATH,
                LD_LIBRARY_PATH=os.path.dirname(lib) + ":" + os.environ.get("LD_LIBRARY_PATH", ""))
-    r = subprocess.run([FF_BIN, "-nw", "t.edp", "-v", "2"], cwd=tmp_path, env=env, capture_output=True,
-                       text=True, timeout=300)
-    out = r.stdout + r.stderr
-    assert "load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED)" in out
+    return d, env
+
+
+def run_script(plugin, name, body, extra_env=None):
+    d, env = plugin
+    (d / name).write_text(('load "%s"\n' % str(d / "ffgpu")) + body)
+    r = subprocess.run([FF_BIN, "-nw", name, "-v", "2"], cwd=d, env=dict(env, **(extra_env or {})),
+                       capture_output=True, text=True, timeout=300)
+    return r, r.stdout + r.stderr
+
+
+def gpu_present():
     import torch
-    if torch.cuda.is_available():
+    return torch.cuda.is_available()
+
+
+def test_plugin_registers_solvers_and_refuses_cpu_fallback(plugin):
+    r, out = run_script(plugin, "t.edp", SCRIPT.split("\n", 2)[2])
+    assert "load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED)" in out
+    assert "ffgpu: device assembly P1 dim 2" in out
+    if gpu_present():
         assert r.returncode == 0 and "umax 0.07" in out, out[-2000:]
     else:
         assert r.returncode != 0
         assert "ffgpu: no usable CUDA device" in out
         # (-v 2 echoes the script, so look for the printed value, not the word)
         assert not any(line.startswith("umax ") for line in r.stdout.splitlines())
+
+
+P0_CUBE = r"""
+load "msh3"
+mesh3 Th=cube(3,3,3);
+fespace Vh(Th,P1); fespace Ph(Th,P0);
+Ph kappa; kappa = 1 + x + 2*y*y;
+Vh u,v;
+varf a(u,v)=int3d(Th)(kappa*(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v))) + on(1,2,3,4,5,6,u=0);
+real s=0; for (int k=0;k<Th.nt;k++) s += kappa[][k]*(k%7+1);
+cout.precision(17); cout << "ksum " << s << endl;
+matrix A=a(Vh,Vh);
+cout << "nnz " << A.nnz << endl;
+"""
+
+ELASTICITY = r"""
+load "msh3"
+mesh3 Th=cube(2,2,2);
+fespace Vh(Th,[P2,P2,P2]);
+Vh [u1,u2,u3],[v1,v2,v3];
+real E=1, nu=0.3; real mu=E/(2*(1+nu)); real lambda=E*nu/((1+nu)*(1-2*nu));
+real s2=sqrt(2.);
+macro epsilon(u1,u2,u3) [dx(u1),dy(u2),dz(u3),(dz(u2)+dy(u3))/s2,(dz(u1)+dx(u3))/s2,(dy(u1)+dx(u2))/s2] // EOM
+macro div(u1,u2,u3) (dx(u1)+dy(u2)+dz(u3)) // EOM
+varf a([u1,u2,u3],[v1,v2,v3])=int3d(Th)(lambda*div(u1,u2,u3)*div(v1,v2,v3)+2.*mu*(epsilon(u1,u2,u3)'*epsilon(v1,v2,v3))) + int3d(Th)(-1.*v3) + on(4,u1=0,u2=0,u3=0);
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10);
+cout << "nnz " << A.nnz << endl;
+"""
+
+
+def _dumped(d):
+    import numpy as np
+    return {k: np.fromfile(d / f"{k}.bin", dt) for k, dt in
+            [("coords", np.float64), ("elems", np.int32), ("dof", np.int32), ("belems", np.int32),
+             ("blabel", np.int32), ("kappa", np.float64)]}
+
+
+def test_device_assembly_hook_extracts_freefem_arrays(plugin, tmp_path):
+    """`matrix A = a(Vh,Vh)` on a recognised form goes to the device path; the arrays it hands
+    to the C ABI equal, bit for bit, this repository's FreeFEM-order mesh and DOF builders."""
+    import numpy as np
+    from ffgpu import mesh
+    from ffgpu.fespace import FESpace
+    d1 = tmp_path / "p0"
+    d1.mkdir()
+    r, out = run_script(plugin, "p0.edp", P0_CUBE, {"FFGPU_PLUGIN_DUMP": str(d1)})
+    ksum = [l for l in r.stdout.splitlines() if l.startswith("ksum ")][0].split()[1]
+    assert f"ffgpu: device assembly P1 dim 3 nt 162 ndof 64 kappa-check {ksum} mass 0" in out
+    a = _dumped(d1)
+    Th = mesh.cube(3)
+    Vh = FESpace(Th, "P1")
+    assert np.array_equal(a["coords"], Th.coords.ravel()) and np.array_equal(a["elems"], Th.elems.ravel())
+    assert np.array_equal(a["dof"], Vh.dof.ravel())
+    assert np.array_equal(a["belems"], Th.belems.ravel()) and np.array_equal(a["blabel"], Th.blabel)
+    bc = Th.coords[Th.elems].mean(axis=1)
+    assert np.abs(a["kappa"] - (1 + bc[:, 0] + 2 * bc[:, 1] ** 2)).max() <= 1e-15
+    d2 = tmp_path / "el"
+    d2.mkdir()
+    r, out = run_script(plugin, "el.edp", ELASTICITY, {"FFGPU_PLUGIN_DUMP": str(d2)})
+    assert "ffgpu: device assembly [P2,P2,P2] dim 3 nt 48 ndof 375 lambda 0.576923 mu 0.384615" in out
+    assert "components 7 labels 4" in out
+    a = _dumped(d2)
+    Th = mesh.cube(2)
+    assert np.array_equal(a["dof"], FESpace(Th, "P2vec").dof.ravel())
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+        assert not any(line.startswith("nnz ") for line in r.stdout.splitlines())
+
+
+def test_unsupported_forms_are_assembled_by_freefem(plugin):
+    body = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)((1+x*y)*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,2,3,4,u=0);
+matrix A=a(Vh,Vh);
+cout << "nnzA " << A.nnz << endl;
+fespace Wh(Th,P2);
+Wh w,z;
+varf b(w,z)=int2d(Th,qft=qf1pT)(dx(w)*dx(z)+dy(w)*dy(z)) + on(1,2,3,4,w=0);
+matrix B=b(Wh,Wh);
+cout << "nnzB " << B.nnz << endl;
+fespace Bh(Th,P1b);
+Bh p,q;
+varf c(p,q)=int2d(Th)(dx(p)*dx(q)+dy(p)*dy(q));
+matrix C=c(Bh,Bh);
+cout << "nnzC " << C.nnz << endl;
+varf e(u,v)=int2d(Th)(dx(u)*dy(v));
+matrix D=e(Vh,Vh);
+cout << "nnzD " << D.nnz << endl;
+"""
+    r, out = run_script(plugin, "fb.edp", body)
+    assert r.returncode == 0, out[-2000:]
+    for why in ("coefficient not constant on elements", "quadrature not exact for the form", "element type",
+                "mixed derivative term"):
+        assert f"ffgpu: form assembled by FreeFEM ({why})" in out
+    nnz = {l.split()[0]: int(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("nnz")}
+    # square(6) P1: 7 nv - 8 n - 6 entries
+    assert nnz["nnzA"] == 7 * 49 - 8 * 6 - 6 and nnz["nnzD"] == nnz["nnzA"]
