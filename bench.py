@@ -316,10 +316,11 @@ def run_gpu(args, rank, world):
     # written): 12 nnz + 4 (n+1) + 8 n + 8 n; the bytes the chosen layout actually streams
     # (block/sliced storage shares one column index per 3x3 block) are reported beside it
     spmv_bytes = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
+    col_bytes = 2 if (layout or "").startswith("sell32") and ffgpu.lib().ffgpu_matrix_spmv_layout(A.h, 3) else 4
     if bs == 3:
         stored = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
     else:
-        stored = 8 * nnz + (2 if layout == "sell32" else 4) * nnz + 4 * (nb + 1) + 8 * n + 8 * n
+        stored = 8 * nnz + col_bytes * nnz + 4 * (nb + 1) + 8 * n + 8 * n
     achieved = spmv_bytes / (spmv_avg * 1e-3) / 1e9
     peaks = {}
     try:

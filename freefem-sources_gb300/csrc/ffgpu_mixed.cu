@@ -40,7 +40,7 @@ struct InnerScalars {
 __device__ __noinline__ void ir_graph_stop(cudaGraphConditionalHandle cond) { cudaGraphSetConditional(cond, 0); }
 
 // inner K_a on the SELL-32 FP32 copy: q = A h and (h, q) -> rho
-template <int BS, bool C16, int ASSIGN>
+template <int BS, bool C16, int ASSIGN, bool DEEP>
 __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *__restrict__ val,
                                                        const float *__restrict__ h, float *__restrict__ q,
                                                        InnerScalars *ks, float *part) {
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *
     float hq = 0;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         float y[BS];
-        sell_row32<BS, C16>(S, val, h, L, sr, lane, a, y);
+        sell_row32<BS, C16, DEEP>(S, val, h, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -247,16 +247,22 @@ struct IRState {
     double *y = nullptr, *out3 = nullptr;
 };
 
-constexpr int kSellCode = 64;   // layout codes shared with the FP64 tuner: 64 + chunk assignment
+// layout codes shared with the FP64 tuner: 64 + chunk assignment + 2 * deep unroll
+constexpr int kSellCode = 64;
 
 static void *ir_ka_fn(const ffgpu_matrix *A, int kind) {
-    const int assign = kind >= kSellCode ? kind - kSellCode : kSellRanges;
-    void *t[3][3] = {{(void *)ir_ka<1, false, 0>, (void *)ir_ka<1, false, 1>, (void *)ir_ka<1, false, 2>},
-                     {(void *)ir_ka<1, true, 0>, (void *)ir_ka<1, true, 1>, (void *)ir_ka<1, true, 2>},
-                     {(void *)ir_ka<3, false, 0>, (void *)ir_ka<3, false, 1>, (void *)ir_ka<3, false, 2>}};
-    return t[A->bs == 3 ? 2 : (A->scol16 ? 1 : 0)][assign];
+    const int code = kind >= kSellCode ? kind - kSellCode : 0;
+    void *t[3][4] = {{(void *)ir_ka<1, false, 0, false>, (void *)ir_ka<1, false, 1, false>,
+                      (void *)ir_ka<1, false, 0, true>, (void *)ir_ka<1, false, 1, true>},
+                     {(void *)ir_ka<1, true, 0, false>, (void *)ir_ka<1, true, 1, false>,
+                      (void *)ir_ka<1, true, 0, true>, (void *)ir_ka<1, true, 1, true>},
+                     {(void *)ir_ka<3, false, 0, false>, (void *)ir_ka<3, false, 1, false>,
+                      (void *)ir_ka<3, false, 0, true>, (void *)ir_ka<3, false, 1, true>}};
+    return t[A->bs == 3 ? 2 : (A->scol16 ? 1 : 0)][code];
 }
-static bool ir_ranges(const ffgpu_matrix *A) { return A->sell32_kind - kSellCode == kSellRanges || !A->sell32_kind; }
+static bool ir_ranges(const ffgpu_matrix *A) {
+    return !A->sell32_kind || ((A->sell32_kind - kSellCode) & 1) == kSellRanges;
+}
 
 // `unroll` inner iterations (K_a K_b K_c) on stream s
 static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditionalHandle cond, int in_graph,
@@ -296,15 +302,15 @@ static int ir_tune(ffgpu_matrix *A, IRState &S) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int bestk = kSellCode + kSellRanges;
-    const int kinds[3] = {kSellCode + kSellRanges, kSellCode + kSellRotated, kSellCode + kSellStride};
-    const char *names[3] = {"ranges", "rotated", "stride"};
-    for (int kk = 0; kk < 3; ++kk) {
+    int bestk = kSellCode;
+    const int kinds[4] = {kSellCode, kSellCode + 1, kSellCode + 2, kSellCode + 3};
+    const char *names[4] = {"ranges", "rotated", "ranges deep", "rotated deep"};
+    for (int kk = 0; kk < 4; ++kk) {
         SellArgs sa = sell_args(A);
         const float *sv = A->sval32;
         void *ka = ir_ka_fn(A, kinds[kk]);
         const int g = resident_grid(ka, kMxWarps * 32);
-        if (kk == 0) FFGPU_TRY(sell_partition(A, g * kMxWarps, &sa.part));
+        if ((kk & 1) == kSellRanges) FFGPU_TRY(sell_partition(A, g * kMxWarps, &sa.part));
         float *part = (float *)ctx->d_part;
         void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
         cudaLaunchKernel(ka, g, kMxWarps * 32, aa, 0, s);

@@ -79,10 +79,8 @@ __device__ __forceinline__ float2 split_f64(double v) {
 // kSellRotated: pass k of warp w takes chunk k*nw + (w + 5k) mod nw -- the chunks in flight at
 //   a time stay one contiguous band of the matrix, and the rotation by an odd step walks every
 //   warp through all 32 positions of the degree-sorted windows.
-// kSellStride: pass k of warp w takes chunk k*nw + w (a band too; a warp always meets the same
-//   window position, which only costs where degrees vary inside windows).
-// The tuners time all three on the matrix.
-enum SellAssign { kSellRanges = 0, kSellRotated = 1, kSellStride = 2 };
+// The tuners time both, each with two unroll depths of the row loop (DEEP).
+enum SellAssign { kSellRanges = 0, kSellRotated = 1 };
 
 template <int ASSIGN>
 struct ChunkWalk {
@@ -99,9 +97,7 @@ struct ChunkWalk {
             c = at(0);
         }
     }
-    __device__ __forceinline__ int at(int kk) const {
-        return kk * nw + (ASSIGN == kSellRotated ? (w + 5 * kk) % nw : w);
-    }
+    __device__ __forceinline__ int at(int kk) const { return kk * nw + (w + 5 * kk) % nw; }
     // next chunk of this warp (>= ce when done)
     __device__ __forceinline__ int next() {
         if constexpr (ASSIGN == kSellRanges) return c + 1;
@@ -116,7 +112,7 @@ template <int ASSIGN, typename F>
 __device__ __forceinline__ void sell_for_chunks(const SellArgs &S, F &&body) {
     const int lane = threadIdx.x & 31;
     ChunkWalk<ASSIGN> it(S);
-    // the rotated and plain strides can land past the last chunk on a warp's final pass
+    // the rotated stride can land past the last chunk on a warp's final pass
     while (it.c < it.ce && it.c >= S.nchunk) it.advance(it.next());
     if (it.c >= it.ce) return;
     int a = __ldg(S.perm + (int64_t)it.c * 32 + lane), L = __ldg(S.len + it.c);
@@ -148,7 +144,7 @@ __device__ __forceinline__ int sell_col(const SellArgs &S, int64_t e, int ar) {
     return __ldcs(S.col + e);
 }
 
-template <int BS, bool C16>
+template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__restrict__ val,
                                            const double *__restrict__ x, int L, int64_t sr, int lane, int a,
                                            double *y) {
@@ -156,8 +152,8 @@ __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__re
     const int64_t ce = sr * 32 + lane;
     const double *v = val + sr * (BS * BS * 32) + lane;
     double s0 = 0, s1 = 0, s2 = 0;
-    // scalar rows: 16 slots in flight hide the column -> gather dependency; 3x3 blocks: 2
-    constexpr int UNR = BS == 1 ? 16 : 2;
+    // slots in flight (the column -> gather dependency): scalar rows 8 or 16, 3x3 blocks 2 or 4
+    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 4 : 2);
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
@@ -176,7 +172,7 @@ __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__re
     if (BS == 3) { y[1] = s1; y[2] = s2; }
 }
 
-template <int BS, bool C16>
+template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__restrict__ val,
                                           const float2 *__restrict__ x, int L, int64_t sr, int lane, int a,
                                           double *y) {
@@ -184,7 +180,7 @@ __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__res
     const int64_t ce = sr * 32 + lane;
     const float2 *v = val + sr * (BS * BS * 32) + lane;
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
-    constexpr int UNR = BS == 1 ? 16 : 2;
+    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 4 : 2);
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
@@ -206,7 +202,7 @@ __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__res
     }
 }
 
-template <int BS, bool C16>
+template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__restrict__ val,
                                            const float *__restrict__ x, int L, int64_t sr, int lane, int a,
                                            float *y) {
@@ -214,7 +210,7 @@ __device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__res
     const int64_t ce = sr * 32 + lane;
     const float *v = val + sr * (BS * BS * 32) + lane;
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    constexpr int UNR = BS == 1 ? 16 : 4;
+    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 8 : 4);
 #pragma unroll UNR
     for (int j = 0; j < L; ++j) {
         const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);

@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
 // ------------------------------------------------------------------ SELL-32 K_a
 // One block row per lane, one chunk of 32 rows per warp (resident grid, chunks strided over
 // warps).  FP64: AH = A H and (H, AH) -> rho; padding lanes (a < 0) write nothing.
-template <int BS, bool C16, int ASSIGN>
+template <int BS, bool C16, int ASSIGN, bool DEEP>
 __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const double *__restrict__ val,
                                                               const double *__restrict__ h, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
     double hq = 0;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double y[BS];
-        sell_row64<BS, C16>(S, val, h, L, sr, lane, a, y);
+        sell_row64<BS, C16, DEEP>(S, val, h, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
 }
 
 // double-float: AH = A H from the split H, (H, AH) in FP64
-template <int BS, bool C16, int ASSIGN>
+template <int BS, bool C16, int ASSIGN, bool DEEP>
 __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const float2 *__restrict__ val,
                                                                const float2 *__restrict__ hx,
                                                                const double *__restrict__ h, double *__restrict__ q,
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
     double hq = 0;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double y[BS];
-        sell_rowx<BS, C16>(S, val, hx, L, sr, lane, a, y);
+        sell_rowx<BS, C16, DEEP>(S, val, hx, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -413,13 +413,13 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
 }
 
 // y = A x (FP64)
-template <int BS, bool C16, int ASSIGN>
+template <int BS, bool C16, int ASSIGN, bool DEEP>
 __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const double *__restrict__ val,
                                                              const double *__restrict__ x, double *__restrict__ y) {
     const int lane = threadIdx.x & 31;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double r[BS];
-        sell_row64<BS, C16>(S, val, x, L, sr, lane, a, r);
+        sell_row64<BS, C16, DEEP>(S, val, x, L, sr, lane, a, r);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) y[(int64_t)BS * a + m] = r[m];
@@ -562,17 +562,22 @@ __global__ void transpose_kernel(int nb, int bs, const int32_t *brp, const int32
 }
 
 // ------------------------------------------------------------------ host side
-// tuner codes of the SELL-32 kernels (one row per lane), 64 + the chunk assignment
-// (sell_for_chunks); block CSR is coded by its lanes per row
+// tuner codes of the SELL-32 kernels (one row per lane): 64 + chunk assignment
+// (sell_for_chunks) + 2 * deep unroll; block CSR is coded by its lanes per row
 constexpr int kSellCode = 64;
-static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 3; }
+static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 4; }
+static int sell_assign(int T) { return (T - kSellCode) & 1; }
+static bool sell_deep(int T) { return (T - kSellCode) >> 1; }
 
-#define FFGPU_SELL_FN(K)                                                                           \
-    static void *K##_fn(int bs, bool c16, int assign) {                                           \
-        void *t[3][3] = {{(void *)K<1, false, 0>, (void *)K<1, false, 1>, (void *)K<1, false, 2>}, \
-                         {(void *)K<1, true, 0>, (void *)K<1, true, 1>, (void *)K<1, true, 2>},    \
-                         {(void *)K<3, false, 0>, (void *)K<3, false, 1>, (void *)K<3, false, 2>}}; \
-        return t[bs == 3 ? 2 : (c16 ? 1 : 0)][assign];                                             \
+#define FFGPU_SELL_FN(K)                                                                             \
+    static void *K##_fn(int bs, bool c16, int code) {                                               \
+        void *t[3][4] = {{(void *)K<1, false, 0, false>, (void *)K<1, false, 1, false>,               \
+                          (void *)K<1, false, 0, true>, (void *)K<1, false, 1, true>},                \
+                         {(void *)K<1, true, 0, false>, (void *)K<1, true, 1, false>,                 \
+                          (void *)K<1, true, 0, true>, (void *)K<1, true, 1, true>},                  \
+                         {(void *)K<3, false, 0, false>, (void *)K<3, false, 1, false>,               \
+                          (void *)K<3, false, 0, true>, (void *)K<3, false, 1, true>}};               \
+        return t[bs == 3 ? 2 : (c16 ? 1 : 0)][code - kSellCode];                                     \
     }
 FFGPU_SELL_FN(cg_ka_sell)
 FFGPU_SELL_FN(cg_kax_sell)
@@ -663,17 +668,16 @@ static int ka_setup(ffgpu_matrix *A, int mode, int trans, int T, const double *h
         FFGPU_TRY(sell_values(A, mode == 1 ? (trans ? kSellXT : kSellX) : (trans ? kSell64T : kSell64)));
         // the column format is known only once the layout exists
         const bool c16 = A->scol16 != nullptr;
-        const int assign = T - kSellCode;
-        const bool range = assign == kSellRanges;
+        const bool range = sell_assign(T) == kSellRanges;
         k.sl = sell_args(A);
         if (mode == 1) {
             k.vx = trans ? A->svalx_t : A->svalx;
-            k.fn = cg_kax_sell_fn(A->bs, c16, assign);
+            k.fn = cg_kax_sell_fn(A->bs, c16, T);
             k.args[0] = &k.sl; k.args[1] = &k.vx; k.args[2] = &k.hx; k.args[3] = &k.h; k.args[4] = &k.q;
             k.args[5] = &k.ks; k.args[6] = &k.part;
         } else {
             k.v64 = trans ? A->sval_t : A->sval;
-            k.fn = cg_ka_sell_fn(A->bs, c16, assign);
+            k.fn = cg_ka_sell_fn(A->bs, c16, T);
             k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.h; k.args[3] = &k.q; k.args[4] = &k.ks;
             k.args[5] = &k.part;
         }
@@ -715,8 +719,8 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     // FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row;
     // double-float: reductions are FP32, so wider lane groups
     const int S0 = kSellCode;
-    const int cands64[] = {S0 + kSellRanges, S0 + kSellRotated, S0 + kSellStride, 1, 2, 4, 8};
-    const int candsx[] = {S0 + kSellRanges, S0 + kSellRotated, S0 + kSellStride, 4, 8, 16, 32};
+    const int cands64[] = {S0, S0 + 1, S0 + 2, S0 + 3, 1, 2, 4, 8};
+    const int candsx[] = {S0, S0 + 1, S0 + 2, S0 + 3, 4, 8, 16, 32};
     const int *cands = mode == 1 ? candsx : cands64;
     const int64_t vs = vstride(A->n);
     double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
@@ -731,7 +735,7 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     cudaEventCreate(&e1);
     float best = 1e30f;
     int bestT = kSellCode;
-    for (int c = 0; c < 7; ++c) {
+    for (int c = 0; c < 8; ++c) {
         const int T = cands[c];
         KaCall k;
         FFGPU_TRY(ka_setup(A, mode, 0, T, x, y, k));
@@ -747,9 +751,9 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
         if (getenv("FFGPU_VERBOSE"))
             fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s %.4f ms\n", mode,
                     A->nb, (long long)A->nnzb,
-                    T == S0 + kSellRanges ? "sell32 ranges"
-                                          : (T == S0 + kSellRotated ? "sell32 rotated"
-                                                                    : (T == S0 + kSellStride ? "sell32 stride" : "bsr lanes")),
+                    is_sell(T) ? (sell_assign(T) == kSellRanges ? (sell_deep(T) ? "sell32 ranges deep" : "sell32 ranges")
+                                                                : (sell_deep(T) ? "sell32 rotated deep" : "sell32 rotated"))
+                               : "bsr lanes",
                     ms / 3);
         if (ms < best) { best = ms; bestT = T; }
     }
@@ -773,9 +777,9 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
     const double *sv = trans ? A->sval_t : A->sval;
     if (sv) {
         SellArgs sl = sell_args(A);
-        const int assign = is_sell(A->csr_lanes) ? A->csr_lanes - kSellCode : kSellRanges;
-        const bool range = assign == kSellRanges;
-        void *fn = spmv_sell_fn(A->bs, A->scol16 != nullptr, assign);
+        const int code = is_sell(A->csr_lanes) ? A->csr_lanes : kSellCode;
+        const bool range = sell_assign(code) == kSellRanges;
+        void *fn = spmv_sell_fn(A->bs, A->scol16 != nullptr, code);
         const int grid = resident_grid(fn, kSpmvWarps * 32);
         if (range) FFGPU_TRY(sell_partition(A, grid * kSpmvWarps, &sl.part));
         void *args[] = {&sl, &sv, &x, &y};
@@ -1243,6 +1247,7 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
 
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode) {
     if (!A) return 0;
+    if (mode == 3) return A->scol16 != nullptr;
     return mode == 2 ? A->sell32_kind : (mode == 1 ? A->csr_lanes_x : A->csr_lanes);
 }
 

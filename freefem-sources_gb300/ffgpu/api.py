@@ -297,10 +297,14 @@ class Matrix:
 
     def spmv_layout(self, mode=0):
         """The SpMV layout the tuner chose for mode 0 (FP64 CG), 1 (double-float CG) or 2 (FP32
-        inner solve): 'sell32' (chunk ranges), 'sell32-rot', 'sell32-stride', 'bsr/T' (T lanes per
-        block row) or None."""
+        inner solve): 'sell32' (chunk ranges) or 'sell32-rot', with '-deep' for the deeper unroll,
+        'bsr/T' (T lanes per block row) or None."""
         v = int(lib().ffgpu_matrix_spmv_layout(self.h, int(mode)))
-        return None if v <= 0 else {64: "sell32", 65: "sell32-rot", 66: "sell32-stride"}.get(v, f"bsr/{v}")
+        if v <= 0:
+            return None
+        if 64 <= v < 68:
+            return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + ("-deep" if v >= 66 else "")
+        return f"bsr/{v}"
 
     def mult(self, x, trans=False, out=None):
         if out is None:

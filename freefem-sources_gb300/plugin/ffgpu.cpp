@@ -177,6 +177,33 @@ static int op_index(int op, int d) {
 static void ref_points(R2 &a, R2 &b) { a = R2(1. / 3., 1. / 3.); b = R2(0.2, 0.3); }
 static void ref_points(R3 &a, R3 &b) { a = R3(0.25, 0.25, 0.25); b = R3(0.1, 0.2, 0.3); }
 
+// vertices of the reference simplex and barycentric coordinates of a reference point
+static int ref_vertices(R2 *v) { v[0] = R2(0, 0); v[1] = R2(1, 0); v[2] = R2(0, 1); return 3; }
+static int ref_vertices(R3 *v) { v[0] = R3(0, 0, 0); v[1] = R3(1, 0, 0); v[2] = R3(0, 1, 0); v[3] = R3(0, 0, 1); return 4; }
+static void barycentric(const R2 &p, double *l) { l[1] = p.x; l[2] = p.y; l[0] = 1 - p.x - p.y; }
+static void barycentric(const R3 &p, double *l) { l[1] = p.x; l[2] = p.y; l[3] = p.z; l[0] = 1 - p.x - p.y - p.z; }
+
+// true when the coefficient restricted to element K is linear: its values at two interior points
+// (ca at pa, cb at pb) are the barycentric combinations of its vertex values
+template <class Element, class FElement, class Rd>
+static bool linear_on_element(Stack stack, const C_F0 &coef, const Element &K, FElement &FK, const Rd &pa,
+                              const Rd &pb, double ca, double cb) {
+    Rd v[4];
+    double f[4], la[4], lb[4];
+    const int nv = ref_vertices(v);
+    double m = std::max(std::fabs(ca), std::fabs(cb));
+    for (int i = 0; i < nv; ++i) {
+        MeshPointStack(stack)->set(K(v[i]), v[i], FK);
+        f[i] = GetAny<double>(coef.eval(stack));
+        m = std::max(m, std::fabs(f[i]));
+    }
+    barycentric(pa, la);
+    barycentric(pb, lb);
+    double sa = 0, sb = 0;
+    for (int i = 0; i < nv; ++i) { sa += la[i] * f[i]; sb += lb[i] * f[i]; }
+    return std::fabs(sa - ca) <= 1e-13 * m && std::fabs(sb - cb) <= 1e-13 * m;
+}
+
 // quadrature exactness of a domain of integration
 static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).exact; }
 static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).exact; }
@@ -252,15 +279,19 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
                 else if (c != 0.0) { r.why = "mixed derivative term"; ok = false; }
                 continue;
             }
-            // coefficient depending on the point: it must be constant on every element (P0)
+            // coefficient depending on the point: constant on every element (P0), or -- for a P1
+            // stiffness term, whose gradients are constant -- linear on every element, where
+            // int_K k grad(phi_i).grad(phi_j) = |K| k(barycentre) grad(phi_i).grad(phi_j)
+            const bool linear_ok = r.fe == FFGPU_FE_P1 && pu == pv && pu > 0 && ex >= 1;
             for (int k = 0; k < nt; ++k) {
                 typename FES::FElement FK = Uh[k];
                 MeshPointStack(stack)->set(Th[k](pa), pa, FK);
                 const double ca = GetAny<double>(l->second.eval(stack));
                 MeshPointStack(stack)->set(Th[k](pb), pb, FK);
                 const double cb = GetAny<double>(l->second.eval(stack));
-                if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
-                    r.why = "coefficient not constant on elements"; ok = false; break;
+                if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb))) &&
+                    !(linear_ok && linear_on_element(stack, l->second, Th[k], FK, pa, pb, ca, cb))) {
+                    r.why = "coefficient not constant (or, for P1 stiffness, not linear) on elements"; ok = false; break;
                 }
                 if (pu == pv && pu > 0) kx[(size_t)k * (d + 1) + pu - 1] += ca;
                 else if (pu == 0 && pv == 0) kx[(size_t)k * (d + 1) + d] += ca;
@@ -470,6 +501,181 @@ struct GpuBilinear : public OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> 
     GpuBilinear(int initt) : Base(initt) { this->pref = 10; }
 };
 
+// ------------------------------------------------------------------ device linear form
+// `b = a(0, Vh)` for a recognised space: int(Th)(f*v) terms with f constant on elements (per
+// component for [P2,P2,P2]), exact quadrature, on(labels, u = constants).  Bilinear terms do not
+// contribute to b.  Anything else, and `b += a(0,Vh)`, is FreeFEM's own operator.
+struct RecognisedRhs {
+    int fe = 0;
+    std::vector<double> f;        // nt x ncomp
+    std::vector<int32_t> labels;
+    double g[3] = {0, 0, 0};      // on(...) values per component
+    int comp_mask = -1;
+    std::string why;
+};
+
+template <class MMesh, class FES>
+static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th, const FES &Uh, RecognisedRhs &r) {
+    typedef typename Dim<MMesh>::Rd Rd;
+    const int d = Dim<MMesh>::d;
+    r.fe = fe_kind(Uh);
+    if (!r.fe) { r.why = "element type"; return false; }
+    const int nc = r.fe == FFGPU_FE_P2VEC3 ? 3 : 1, nt = Th.nt;
+    r.f.assign((size_t)nt * nc, 0.0);
+    std::set<long> on;
+    FreeFempp::TypeVarForm<double> *tvf = FreeFempp::TypeVarForm<double>::Global;
+    MeshPoint mp = *MeshPointStack(stack);
+    Rd pa, pb;
+    ref_points(pa, pb);
+    bool ok = true;
+    for (list<C_F0>::const_iterator ii = largs.begin(); ok && ii != largs.end(); ++ii) {
+        aType t = ii->left();
+        Expression e = ii->LeftValue();
+        if (t == tvf->tFB) continue;   // bilinear terms: not part of b
+        if (t == tvf->tBC) {
+            const BC_set *bc = dynamic_cast<const BC_set *>(e);
+            int mask = 0;
+            for (size_t i = 0; ok && i < bc->bc.size(); ++i) {
+                const int c = bc->bc[i].first;
+                mask |= 1 << c;
+                if (!bc->bc[i].second->MeshIndependent()) { r.why = "on() value not constant"; ok = false; break; }
+                const double gv = GetAny<double>((*bc->bc[i].second)(stack));
+                if (r.comp_mask >= 0 && (r.comp_mask >> c & 1) && r.g[c] != gv) { r.why = "on() values differ"; ok = false; }
+                r.g[c] = gv;
+            }
+            if (r.comp_mask >= 0 && r.comp_mask != mask) { r.why = "on() with different components"; ok = false; }
+            r.comp_mask = mask;
+            Fem2D::Expandsetoflab(stack, *bc, on);
+            continue;
+        }
+        if (t != tvf->tFL) { r.why = "term kind"; ok = false; break; }
+        const FormLinear *lf = dynamic_cast<const FormLinear *>(e);
+        const CDomainOfIntegration &di = *lf->di;
+        if (di.d != d || di.dHat != d || !di.what.empty() || di.islevelset() || di.withmap()) {
+            r.why = "domain of integration"; ok = false; break;
+        }
+        if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { r.why = "integration mesh"; ok = false; break; }
+        if (exactness(stack, di, &Th) < (r.fe == FFGPU_FE_P1 ? 1 : 2)) { r.why = "quadrature not exact"; ok = false; break; }
+        const Ftest &ft = *lf->l;
+        for (Ftest::const_iterator l = ft.v.begin(); ok && l != ft.v.end(); ++l) {
+            const int jv = l->first.first, pv = op_index(l->first.second, d);
+            if (jv >= nc || pv != 0) { r.why = "operator"; ok = false; break; }
+            const bool constant = l->second.LeftValue()->MeshIndependent();
+            for (int k = 0; k < nt; ++k) {
+                typename FES::FElement FK = Uh[k];
+                MeshPointStack(stack)->set(Th[k](pa), pa, FK);
+                const double ca = GetAny<double>(l->second.eval(stack));
+                if (!constant) {
+                    MeshPointStack(stack)->set(Th[k](pb), pb, FK);
+                    const double cb = GetAny<double>(l->second.eval(stack));
+                    if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
+                        r.why = "source not constant on elements"; ok = false; break;
+                    }
+                }
+                r.f[(size_t)k * nc + jv] += ca;
+                if (constant && k == 0) {   // the same value everywhere
+                    for (int kk = 1; kk < nt; ++kk) r.f[(size_t)kk * nc + jv] += ca;
+                    break;
+                }
+            }
+        }
+    }
+    *MeshPointStack(stack) = mp;
+    if (!ok) return false;
+    r.labels.assign(on.begin(), on.end());
+    return true;
+}
+
+template <class MMesh, class FES>
+static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, double tgv, KN_<double> &out) {
+    const MMesh &Th = Uh.Th;
+    const int d = Dim<MMesh>::d;
+    RecognisedRhs r;
+    if (!recognise_rhs(stack, largs, Th, Uh, r)) {
+        if (verbosity > 1) std::cout << "  ffgpu: linear form assembled by FreeFEM (" << r.why << ")" << std::endl;
+        return false;
+    }
+    if (verbosity > 1) {
+        double fs = 0;
+        for (size_t k = 0; k < r.f.size(); ++k) fs += r.f[k] * (double)(k % 7 + 1);
+        std::cout << "  ffgpu: device linear form " << fe_name(r.fe) << " dim " << d << " f-check " << std::setprecision(17)
+                  << fs << " g " << r.g[0] << std::setprecision(6) << " tgv " << tgv << std::endl;
+    }
+    std::vector<double> X;
+    std::vector<int32_t> E, BE, BL;
+    mesh_arrays(Th, X, E, BE, BL);
+    const int ndofK = Uh[0].NbDoF(), nc = r.fe == FFGPU_FE_P2VEC3 ? 3 : 1;
+    std::vector<int32_t> dof((size_t)Th.nt * ndofK);
+    for (int k = 0; k < Th.nt; ++k) {
+        typename FES::FElement K = Uh[k];
+        for (int i = 0; i < ndofK; ++i) dof[(size_t)k * ndofK + i] = K(i);
+    }
+    ffgpu_ctx *ctx = context();
+    ffgpu_space *S = nullptr;
+    int rc = ffgpu_space_create(ctx, d, Th.nv, X.data(), Th.nt, E.data(), r.fe, ndofK, dof.data(), Uh.NbOfDF, &S);
+    if (!rc && !BL.empty()) rc = ffgpu_space_set_boundary(S, (int)BL.size(), BE.data(), BL.data());
+    std::vector<double> g;
+    if (!rc) {
+        ffgpu_varf v;
+        memset(&v, 0, sizeof(v));
+        v.form = nc == 3 ? FFGPU_FORM_ELASTICITY : FFGPU_FORM_DIFFUSION;
+        v.c_stiff = 1.0;
+        v.E = 1.0;
+        v.f = r.f.data();
+        ffgpu_bc bc;
+        memset(&bc, 0, sizeof(bc));
+        bc.tgv = tgv;
+        bc.nlabels = (int)r.labels.size();
+        bc.labels = r.labels.data();
+        bc.comp_mask = nc == 3 && r.comp_mask != 7 ? r.comp_mask : 0;
+        if (r.g[0] != 0 || r.g[1] != 0 || r.g[2] != 0) {
+            g.resize(Uh.NbOfDF);
+            for (int i = 0; i < Uh.NbOfDF; ++i) g[i] = r.g[i % nc];
+            bc.g = g.data();
+        }
+        rc = ffgpu_rhs_assemble(S, &v, r.labels.empty() ? nullptr : &bc, (double *)out);
+    }
+    if (S) ffgpu_space_destroy(S);
+    if (rc) ExecError((std::string("ffgpu linear form: ") + ffgpu_last_error()).c_str());
+    return true;
+}
+
+template <class MMesh, class v_fes>
+struct GpuLinear : public OpArraytoLinearForm<double, MMesh, v_fes> {
+    typedef OpArraytoLinearForm<double, MMesh, v_fes> Base;
+    typedef typename v_fes::FESpace FES;
+    class GOp : public Base::Op {
+       public:
+        GOp(Expression xx, Expression ll, bool isptr, bool init, bool zero) : Base::Op(xx, ll, isptr, init, zero) {}
+        AnyType operator()(Stack stack) const {
+            if (!this->zero) return Base::Op::operator()(stack);   // b += a(0,Vh)
+            v_fes *&pp = *GetAny<v_fes **>((*this->l->ppfes)(stack));
+            FES *pVh = *pp;
+            if (!pVh) return Base::Op::operator()(stack);
+            double tgv = ff_tgv;
+            if (this->l->nargs[0]) tgv = GetAny<double>((*this->l->nargs[0])(stack));
+            const long n = pVh->NbOfDF;
+            KN<double> *px = nullptr;
+            if (this->isptr) {
+                px = GetAny<KN<double> *>((*this->x)(stack));
+                if (this->init) px->init(n);
+                if (px->N() != n) px->resize(n);
+            }
+            KN_<double> xx(px ? *(KN_<double> *)px : GetAny<KN_<double> >((*this->x)(stack)));
+            if (xx.N() != n || xx.step != 1 || !device_rhs<MMesh, FES>(stack, this->l->largs, *pVh, tgv, xx))
+                return Base::Op::operator()(stack);
+            return SetAny<KN_<double> >(xx);
+        }
+    };
+    E_F0 *code(const basicAC_F0 &args) const {
+        if (this->isptr) return new GOp(to<KN<double> *>(args[0]), args[1], this->isptr, this->init, this->zero);
+        return new GOp(to<KN_<double> >(args[0]), args[1], this->isptr, this->init, this->zero);
+    }
+    GpuLinear(const basicForEachType *tt, bool isptrr, bool initt, bool zzero = 1) : Base(tt, isptrr, initt, zzero) {
+        this->pref = 10;
+    }
+};
+
 }  // namespace
 
 static void Load_Init() {
@@ -485,6 +691,11 @@ static void Load_Init() {
     TheOperators->Add("=", new GpuBilinear<Mesh, v_fes>(0), new GpuBilinear<Mesh3, v_fes3>(0));
     TheOperators->Add("<-", new GpuBilinear<Mesh, v_fes>(1));
     TheOperators->Add("<-", new GpuBilinear<Mesh3, v_fes3>(1));
+    // and the linear form `b = a(0,Vh)` (lgfem.cpp:6668-6688)
+    TheOperators->Add("=", new GpuLinear<Mesh, v_fes>(atype<KN_<double> >(), false, false),
+                      new GpuLinear<Mesh3, v_fes3>(atype<KN_<double> >(), false, false));
+    TheOperators->Add("<-", new GpuLinear<Mesh, v_fes>(atype<KN<double> *>(), true, true),
+                      new GpuLinear<Mesh3, v_fes3>(atype<KN<double> *>(), true, true));
     if (verbosity > 1) std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED)" << std::endl;
 }
 

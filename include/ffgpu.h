@@ -147,10 +147,11 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
 int ffgpu_matrix_destroy(ffgpu_matrix *A);
 int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_size);
 /* SpMV layout the solver's tuner chose for this matrix: mode 0 (FP64 CG), 1 (double-float CG)
- * or 2 (FP32 inner solve of ffgpu_solve_ir).  Returns 64/65/66 for the SELL-32 copy with
- * contiguous per-warp chunk ranges / a rotated chunk stride / a plain chunk stride, T in
- * {1,..,32} for block CSR with T lanes per block row, 0 before the first solve.  No FreeFEM
- * counterpart. */
+ * or 2 (FP32 inner solve of ffgpu_solve_ir).  Returns 64 + a + 2u for the SELL-32 copy, with
+ * a = 0 for contiguous per-warp chunk ranges or 1 for a rotated chunk stride and u = 1 for the
+ * deeper unroll of the row loop; T in {1,..,32} for block CSR with T lanes per block row; 0
+ * before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences.
+ * No FreeFEM counterpart. */
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
 /* [I,J,C] = A in sorted CSR form (HashMatrix::CSR / Sortij, HashMatrix.cpp:671-682,870-876) */
 int ffgpu_matrix_csr(const ffgpu_matrix *A, int32_t *rowptr, int32_t *col, double *val);

@@ -162,9 +162,50 @@ cout << "nnzD " << D.nnz << endl;
 """
     r, out = run_script(plugin, "fb.edp", body)
     assert r.returncode == 0, out[-2000:]
-    for why in ("coefficient not constant on elements", "quadrature not exact for the form", "element type",
-                "mixed derivative term"):
+    for why in ("coefficient not constant (or, for P1 stiffness, not linear) on elements",
+                "quadrature not exact for the form", "element type", "mixed derivative term"):
         assert f"ffgpu: form assembled by FreeFEM ({why})" in out
     nnz = {l.split()[0]: int(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("nnz")}
     # square(6) P1: 7 nv - 8 n - 6 entries
     assert nnz["nnzA"] == 7 * 49 - 8 * 6 - 6 and nnz["nnzD"] == nnz["nnzA"]
+
+
+def test_linear_form_hook(plugin):
+    """`b = a(0,Vh)`: a constant/P0 source with constant on() values goes to the device
+    (ffgpu_rhs_assemble); a point-dependent source is FreeFEM's own operator."""
+    body = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(x*y*v) + on(1,2,3,4,u=0);
+real[int] b=a(0,Vh);
+cout << "bsum " << b.sum << endl;
+varf a2(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(2.5*v) + on(1,3,u=1.5);
+real[int] b2=a2(0,Vh);
+cout << "b2sum " << b2.sum << endl;
+"""
+    r, out = run_script(plugin, "lf.edp", body)
+    assert "ffgpu: linear form assembled by FreeFEM (source not constant on elements)" in out
+    assert any(line.startswith("bsum ") for line in r.stdout.splitlines())
+    # 72 triangles, f = 2.5: sum_k 2.5 (k % 7 + 1) = 707.5
+    assert "ffgpu: device linear form P1 dim 2 f-check 707.5 g 1.5 tgv 1e+30" in out
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+
+
+def test_p1_stiffness_with_a_p1_coefficient(plugin):
+    """A coefficient linear on every element (a P1 function) in a P1 stiffness term: its mean
+    over the element is its barycentre value, exactly FreeFEM's P0 interpolation of it."""
+    body = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v, kap = 1 + x + 2*y;
+varf a(u,v)=int2d(Th)(kap*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,2,3,4,u=0);
+fespace Ph(Th,P0); Ph kb = 1 + x + 2*y;
+real s=0; for (int k=0;k<Th.nt;k++) s += kb[][k]*(k%7+1);
+cout.precision(17); cout << "ksum " << s << endl;
+matrix A=a(Vh,Vh);
+"""
+    r, out = run_script(plugin, "p1k.edp", body)
+    ksum = [l for l in r.stdout.splitlines() if l.startswith("ksum ")][0].split()[1]
+    assert f"ffgpu: device assembly P1 dim 2 nt 72 ndof 49 kappa-check {ksum} mass 0" in out
