@@ -293,34 +293,27 @@ def run_gpu(args, rank, world):
     rh = (b - r).cpu().numpy()
     mask = onbc.astype(bool)
     rel_res = float(np.linalg.norm(rh[~mask]) / np.linalg.norm(b.cpu().numpy()[~mask]))
-    # dominant kernel: the SpMV of the CG (K_a); timed alone on the library stream
-    nrep = 20
-    y = torch.empty_like(b)
-    A.mult(ub, out=y)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize(dev)
-    spmv_ms = []
-    for _ in range(nrep):
-        e0.record(stream)
-        A.mult(ub, out=y)
-        e1.record(stream)
-        e1.synchronize()
-        spmv_ms.append(e0.elapsed_time(e1))
-    spmv_avg = statistics.median(spmv_ms)
+    # dominant kernel: the SpMV of the CG (K_a, with its fused dot), in the layout the tuner
+    # chose, launched back to back on the library stream and timed there with CUDA events
+    # (each launch streams the whole matrix, larger than L2)
+    spmv_avg = A.time_spmv(0, 20)
     n, nnz, bs = A.n, A.nnz, A.block_size
     nnzb = nnz // (bs * bs)
     nb = n // bs
     layout = A.spmv_layout(0)
     # algorithmic bytes of one SpMV (CSR with FP64 values and int32 columns, x read once, y
     # written): 12 nnz + 4 (n+1) + 8 n + 8 n; the bytes the chosen layout actually streams
-    # (block/sliced storage shares one column index per 3x3 block) are reported beside it
+    # (one column index per 3x3 block, 16-bit column differences, SELL padding) beside it
     spmv_bytes = 12 * nnz + 4 * (n + 1) + 8 * n + 8 * n
-    col_bytes = 2 if (layout or "").startswith("sell32") and ffgpu.lib().ffgpu_matrix_spmv_layout(A.h, 3) else 4
-    if bs == 3:
-        stored = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
+    if (layout or "").startswith("sell32"):
+        lib = ffgpu.lib()
+        col_bytes = 2 if lib.ffgpu_matrix_spmv_layout(A.h, 3) else 4
+        ent = lib.ffgpu_matrix_spmv_layout(A.h, 4)
+        ent = ent if ent > 0 else nnzb
+        # per stored block entry: values + column; per row: permutation; x read, y written
+        stored = ent * (8 * bs * bs + col_bytes) + 4 * nb + 8 * n + 8 * n
     else:
-        stored = 8 * nnz + col_bytes * nnz + 4 * (nb + 1) + 8 * n + 8 * n
+        stored = 8 * nnz + 4 * nnzb + 4 * (nb + 1) + 8 * n + 8 * n
     achieved = spmv_bytes / (spmv_avg * 1e-3) / 1e9
     peaks = {}
     try:
@@ -357,12 +350,13 @@ def run_gpu(args, rank, world):
         def run_df():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
             A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
-            return A2.solve(b, spmv_mode=1), A2.stats.iterations, A2.spmv_layout(1)
-        (udf, itdf, lay), msdf = timed_variant(run_df, 2)
+            return A2.solve(b, spmv_mode=1), A2.stats.iterations, A2.spmv_layout(1), A2
+        (udf, itdf, lay, Adf), msdf = timed_variant(run_df, 2)
         variants["fp64_values_doublefloat_spmv"] = {
             "value": Vh.ndof / (msdf * 1e-3), "ms_per_step": msdf, "cg_iterations": itdf,
-            "spmv_layout": lay,
+            "spmv_layout": lay, "spmv_ms": Adf.time_spmv(1, 10),
             "rel_err_vs_fp64": float(torch.linalg.norm(udf - u_ref) / torch.linalg.norm(u_ref))}
+        del Adf
 
         def run_ir():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
@@ -373,13 +367,16 @@ def run_gpu(args, rank, world):
             ur = A2.solve_mixed(b, eps=cfg["eps"])
             t1.record(stream)
             t1.synchronize()
-            return ur, A2.stats.iterations, A2.stats.outer_iterations, A2.spmv_layout(2), t0.elapsed_time(t1)
-        (uir, itir, outir, lay32, solve_ir_ms), msir = timed_variant(run_ir, 1)
+            return (ur, A2.stats.iterations, A2.stats.outer_iterations, A2.spmv_layout(2), t0.elapsed_time(t1),
+                    A2)
+        (uir, itir, outir, lay32, solve_ir_ms, Air), msir = timed_variant(run_ir, 1)
         variants["mixed_fp32_inner_fp64_refinement"] = {
             "value": Vh.ndof / (msir * 1e-3), "ms_per_step": msir, "inner_iterations": itir,
-            "outer_iterations": outir, "spmv_layout": lay32, "solve_ms": solve_ir_ms,
+            "outer_iterations": outir, "spmv_layout": lay32, "spmv_ms": Air.time_spmv(2, 10),
+            "solve_ms": solve_ir_ms,
             "solve_speedup_vs_fp64": statistics.median(phase["solve"][-args.steps:]) / solve_ir_ms,
             "rel_err_vs_fp64": float(torch.linalg.norm(uir - u_ref) / torch.linalg.norm(u_ref))}
+        del Air
     # e2e: public API from host arrays (H2D of mesh/DOF table/BC mask, D2H of b and u)
     e2e_times = []
     bh = np.empty(Vh.ndof)

@@ -231,6 +231,8 @@ int sell_prepare(ffgpu_matrix *A);               // structure (once per pattern)
 int sell_partition(ffgpu_matrix *A, int nw, const int32_t **part);
 int sell_values(ffgpu_matrix *A, int kind);      // value array of one kind (once per numeric state)
 void sell_release_values(ffgpu_matrix *A);       // drop the value arrays (new numeric state)
+// mean time of nrep launches of the FP32 K_a of the mixed solve (after a mixed solve)
+int ir_time_ka(ffgpu_matrix *A, int nrep, float *ms);
 void sell_release(ffgpu_matrix *A);              // drop everything (matrix destruction)
 inline SellArgs sell_args(const ffgpu_matrix *A) {
     return SellArgs{A->nchunk, A->sperm, A->slen, A->soff, A->scol, A->scol16, nullptr};

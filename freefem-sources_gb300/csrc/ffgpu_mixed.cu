@@ -334,6 +334,51 @@ static int ir_tune(ffgpu_matrix *A, IRState &S) {
     return FFGPU_OK;
 }
 
+int ir_time_ka(ffgpu_matrix *A, int nrep, float *ms) {
+    FFGPU_CHECK(A->sell32_kind && A->sval32 && A->vec, FFGPU_EINVAL,
+                "ffgpu_matrix_time_spmv: run a mixed-precision solve first");
+    ffgpu_ctx *ctx = A->ctx;
+    cudaStream_t s = ctx->stream;
+    const int64_t vs = vstride(A->n);
+    // FP32 input and output vectors in the FP64 work slots 5 and 6 (n floats fit in n doubles)
+    float *h = (float *)(A->vec + 5 * vs), *q = (float *)(A->vec + 6 * vs);
+    InnerScalars *ks = nullptr;
+    FFGPU_CUDA(cudaMalloc((void **)&ks, sizeof(InnerScalars)));
+    FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(InnerScalars), s));
+    FFGPU_CUDA(cudaMemsetAsync(h, 0, sizeof(float) * A->n, s));
+    SellArgs sa = sell_args(A);
+    const float *sv = A->sval32;
+    void *ka = ir_ka_fn(A, A->sell32_kind);
+    const int g = resident_grid(ka, kMxWarps * 32);
+    int rc = FFGPU_OK;
+    if (ir_ranges(A)) rc = sell_partition(A, g * kMxWarps, &sa.part);
+    float t = 0;
+    if (!rc) {
+        float *part = (float *)ctx->d_part;
+        void *aa[] = {&sa, &sv, &h, &q, &ks, &part};
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaLaunchKernel(ka, g, kMxWarps * 32, aa, 0, s);
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < nrep; ++r) cudaLaunchKernel(ka, g, kMxWarps * 32, aa, 0, s);
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->launches += nrep + 1;
+        if (e != cudaSuccess) {
+            set_error("ffgpu_matrix_time_spmv: %s", cudaGetErrorString(e));
+            rc = FFGPU_ECUDA;
+        }
+    }
+    cudaFree(ks);
+    *ms = t / nrep;
+    return rc;
+}
+
 static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;

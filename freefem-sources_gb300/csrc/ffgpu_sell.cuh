@@ -135,15 +135,110 @@ __device__ __forceinline__ void sell_for_chunks(const SellArgs &S, F &&body) {
 }
 
 // ------------------------------------------------------------------ SELL-32 rows
-// One block row per lane: lane `lane` of chunk c holds row a (a < 0: padding lane, its
-// entries are zero blocks on column 0).  Entries are read in column order; matrix streams use
-// evict-first loads so that the gathered vector stays in L2.
+// Entries are read in column order; matrix streams use evict-first loads so that the gathered
+// vector stays in L2.
 template <bool C16>
 __device__ __forceinline__ int sell_col(const SellArgs &S, int64_t e, int ar) {
     if (C16) return ar + (int)__ldcs(S.col16 + e);
     return __ldcs(S.col + e);
 }
 
+// FP32 and double-float rows process entries in batches of B slots: all column, value and vector
+// loads of a batch are issued before its first product, so a lane keeps B independent gathers
+// in flight (a runtime-length loop unrolled B deep runs its remainder one dependent load at a
+// time, and most P1 chunks are shorter than 16 slots).  The last, partial batch of a chunk
+// loads only its `rem` slots (warp-uniform predicate) and applies exactly that many products
+// through a compile-time case chain, so the products and their order are those of the plain
+// j = 0..L-1 loop.
+struct AccF32 {
+    float s = 0.f;
+    __device__ __forceinline__ void fma_(float a, float x) { s = fmaf(a, x, s); }
+    __device__ __forceinline__ float get() const { return s; }
+};
+struct AccDF {
+    float S = 0.f, C = 0.f;
+    __device__ __forceinline__ void fma_(float2 a, float2 x) { df_fma(a, x, S, C); }
+    __device__ __forceinline__ double get() const { return (double)S + (double)C; }
+};
+
+template <typename V, int BS, int B>
+struct SellBatch {
+    V a[B][BS * BS];
+    V xv[B][BS];
+    template <bool C16, bool GUARD>
+    __device__ __forceinline__ void load(const SellArgs &S, const V *__restrict__ v, const V *__restrict__ x,
+                                         int64_t ce, int ar, int j, int rem) {
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            if (GUARD && u >= rem) continue;
+            const int col = sell_col<C16>(S, ce + (int64_t)(j + u) * 32, ar);
+            const V *w = v + (int64_t)(j + u) * (BS * BS * 32);
+#pragma unroll
+            for (int k = 0; k < BS * BS; ++k) a[u][k] = __ldcs(w + 32 * k);
+#pragma unroll
+            for (int m = 0; m < BS; ++m) xv[u][m] = __ldg(x + (int64_t)BS * col + m);
+        }
+    }
+    template <typename Acc>
+    __device__ __forceinline__ void apply(int u, Acc *acc) {
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+#pragma unroll
+            for (int m = 0; m < BS; ++m) acc[r].fma_(a[u][r * BS + m], xv[u][m]);
+    }
+};
+
+// applies slots 0..rem-1 of a partial batch (1 <= rem < K+1), each case fully unrolled
+template <int K>
+struct SellTail {
+    template <typename Bt, typename Acc>
+    __device__ __forceinline__ static void run(Bt &t, int rem, Acc *acc) {
+        if (rem == K) {
+#pragma unroll
+            for (int u = 0; u < K; ++u) t.apply(u, acc);
+        } else {
+            SellTail<K - 1>::run(t, rem, acc);
+        }
+    }
+};
+template <>
+struct SellTail<0> {
+    template <typename Bt, typename Acc>
+    __device__ __forceinline__ static void run(Bt &, int, Acc *) {}
+};
+
+// One block row per lane: lane `lane` of chunk c holds row a (a < 0: padding lane, its entries
+// are zero blocks on column 0), L slots starting at slot row sr.
+template <typename V, int BS, int B, bool C16, typename Acc>
+__device__ __forceinline__ void sell_row(const SellArgs &S, const V *__restrict__ val, const V *__restrict__ x,
+                                         int L, int64_t sr, int lane, int a, Acc *acc) {
+    const int ar = a < 0 ? 0 : a;
+    const int64_t ce = sr * 32 + lane;
+    const V *v = val + sr * (BS * BS * 32) + lane;
+    int j = 0;
+    for (; j + B <= L; j += B) {
+        SellBatch<V, BS, B> t;
+        t.template load<C16, false>(S, v, x, ce, ar, j, B);
+#pragma unroll
+        for (int u = 0; u < B; ++u) t.apply(u, acc);
+    }
+    const int rem = L - j;
+    if (rem > 0) {
+        SellBatch<V, BS, B> t;
+        t.template load<C16, true>(S, v, x, ce, ar, j, rem);
+        SellTail<B - 1>::run(t, rem, acc);
+    }
+}
+
+// batch depth: scalar rows 8 or 16 slots, 3x3 blocks 2 or 4 (FP32: 4 or 8)
+template <int BS, bool DEEP, bool F32 = false>
+struct SellDepth {
+    static constexpr int B = BS == 1 ? (DEEP ? 16 : 8) : (F32 ? (DEEP ? 8 : 4) : (DEEP ? 4 : 2));
+};
+
+// FP64 rows keep a plain loop unrolled UNR deep: the kernel is bound by the FP64 pipe, and the
+// compiler's software pipelining of the unrolled loop (loads of later slots under the FMAs of
+// earlier ones) measured faster than the batched form on both the P1 and the [P2]^3 matrices.
 template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__restrict__ val,
                                            const double *__restrict__ x, int L, int64_t sr, int lane, int a,
@@ -176,57 +271,20 @@ template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_rowx(const SellArgs &S, const float2 *__restrict__ val,
                                           const float2 *__restrict__ x, int L, int64_t sr, int lane, int a,
                                           double *y) {
-    const int ar = a < 0 ? 0 : a;
-    const int64_t ce = sr * 32 + lane;
-    const float2 *v = val + sr * (BS * BS * 32) + lane;
-    float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f, S2 = 0.f, C2 = 0.f;
-    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 4 : 2);
-#pragma unroll UNR
-    for (int j = 0; j < L; ++j) {
-        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
-        if (BS == 1) {
-            df_fma(__ldcs(v + (int64_t)j * 32), __ldg(x + col), S0, C0);
-        } else {
-            const float2 x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
-                         x2 = __ldg(x + 3 * (int64_t)col + 2);
-            const float2 *w = v + (int64_t)j * 288;
-            df_fma(__ldcs(w), x0, S0, C0); df_fma(__ldcs(w + 32), x1, S0, C0); df_fma(__ldcs(w + 64), x2, S0, C0);
-            df_fma(__ldcs(w + 96), x0, S1, C1); df_fma(__ldcs(w + 128), x1, S1, C1); df_fma(__ldcs(w + 160), x2, S1, C1);
-            df_fma(__ldcs(w + 192), x0, S2, C2); df_fma(__ldcs(w + 224), x1, S2, C2); df_fma(__ldcs(w + 256), x2, S2, C2);
-        }
-    }
-    y[0] = (double)S0 + (double)C0;
-    if (BS == 3) {
-        y[1] = (double)S1 + (double)C1;
-        y[2] = (double)S2 + (double)C2;
-    }
+    AccDF acc[BS];
+    sell_row<float2, BS, SellDepth<BS, DEEP>::B, C16>(S, val, x, L, sr, lane, a, acc);
+#pragma unroll
+    for (int m = 0; m < BS; ++m) y[m] = acc[m].get();
 }
 
 template <int BS, bool C16, bool DEEP>
 __device__ __forceinline__ void sell_row32(const SellArgs &S, const float *__restrict__ val,
                                            const float *__restrict__ x, int L, int64_t sr, int lane, int a,
                                            float *y) {
-    const int ar = a < 0 ? 0 : a;
-    const int64_t ce = sr * 32 + lane;
-    const float *v = val + sr * (BS * BS * 32) + lane;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 8 : 4);
-#pragma unroll UNR
-    for (int j = 0; j < L; ++j) {
-        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
-        if (BS == 1) {
-            s0 = fmaf(__ldcs(v + (int64_t)j * 32), __ldg(x + col), s0);
-        } else {
-            const float x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
-                        x2 = __ldg(x + 3 * (int64_t)col + 2);
-            const float *w = v + (int64_t)j * 288;
-            s0 = fmaf(__ldcs(w), x0, s0); s0 = fmaf(__ldcs(w + 32), x1, s0); s0 = fmaf(__ldcs(w + 64), x2, s0);
-            s1 = fmaf(__ldcs(w + 96), x0, s1); s1 = fmaf(__ldcs(w + 128), x1, s1); s1 = fmaf(__ldcs(w + 160), x2, s1);
-            s2 = fmaf(__ldcs(w + 192), x0, s2); s2 = fmaf(__ldcs(w + 224), x1, s2); s2 = fmaf(__ldcs(w + 256), x2, s2);
-        }
-    }
-    y[0] = s0;
-    if (BS == 3) { y[1] = s1; y[2] = s2; }
+    AccF32 acc[BS];
+    sell_row<float, BS, SellDepth<BS, DEEP, true>::B, C16>(S, val, x, L, sr, lane, a, acc);
+#pragma unroll
+    for (int m = 0; m < BS; ++m) y[m] = acc[m].get();
 }
 
 }  // namespace ffgpu

@@ -1248,7 +1248,46 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode) {
     if (!A) return 0;
     if (mode == 3) return A->scol16 != nullptr;
+    if (mode == 4) return A->nslot > 0 && A->nslot * 32 <= INT32_MAX ? (int)(A->nslot * 32) : (A->nslot ? -1 : 0);
     return mode == 2 ? A->sell32_kind : (mode == 1 ? A->csr_lanes_x : A->csr_lanes);
+}
+
+int ffgpu_matrix_time_spmv(ffgpu_matrix *A, int mode, int nrep, float *ms) {
+    FFGPU_CHECK(A && ms && nrep > 0 && mode >= 0 && mode <= 2, FFGPU_EINVAL,
+                "ffgpu_matrix_time_spmv: bad argument");
+    ffgpu_ctx *ctx = A->ctx;
+    FFGPU_CUDA(cudaSetDevice(ctx->device));
+    if (mode == 2) return ir_time_ka(A, nrep, ms);
+    const int T = mode == 1 ? A->csr_lanes_x : A->csr_lanes;
+    FFGPU_CHECK(A->vec && T > 0 && (mode == 0 || A->hx), FFGPU_EINVAL,
+                "ffgpu_matrix_time_spmv: solve the matrix in mode %d first", mode);
+    cudaStream_t s = ctx->stream;
+    const int64_t vs = vstride(A->n);
+    KaCall k;
+    // input: the staged solution of the last solve; output: the tuner's scratch vector
+    FFGPU_TRY(ka_setup(A, mode, 0, T, A->vec + 4 * vs, A->vec + 6 * vs, k));
+    // K_a returns at once when the Krylov scalars say the solve is done: clear them
+    FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
+    cudaEvent_t e0, e1;
+    FFGPU_CUDA(cudaEventCreate(&e0));
+    FFGPU_CUDA(cudaEventCreate(&e1));
+    k.launch(s);
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < nrep; ++r) k.launch(s);
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->launches += nrep + 1;
+    FFGPU_CUDA(e);
+    FFGPU_CUDA(cudaGetLastError());
+    // the fused dot left partial sums in the Krylov scalars: clear them as the tuner does
+    FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
+    FFGPU_CUDA(cudaStreamSynchronize(s));
+    *ms = t / nrep;
+    return FFGPU_OK;
 }
 
 int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans) {

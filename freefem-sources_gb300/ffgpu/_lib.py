@@ -23,6 +23,7 @@ EXPORTS = [
     "ffgpu_space_create", "ffgpu_space_destroy", "ffgpu_space_set_boundary", "ffgpu_space_bc_mask", "ffgpu_matrix_assemble", "ffgpu_matrix_reassemble",
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_spmv_layout",
+    "ffgpu_matrix_time_spmv",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
@@ -94,6 +95,7 @@ def lib():
         "ffgpu_matrix_destroy": (i32, [vp]),
         "ffgpu_matrix_info": (i32, [vp, P(i32), P(i64), P(i32)]),
         "ffgpu_matrix_spmv_layout": (i32, [vp, i32]),
+        "ffgpu_matrix_time_spmv": (i32, [vp, i32, i32, P(C.c_float)]),
         "ffgpu_matrix_csr": (i32, [vp, vp, vp, vp]),
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),

@@ -306,6 +306,13 @@ class Matrix:
             return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + ("-deep" if v >= 66 else "")
         return f"bsr/{v}"
 
+    def time_spmv(self, mode=0, nrep=20):
+        """Mean device time (ms) of nrep back-to-back launches of the solver's SpMV kernel for
+        mode 0/1/2 (see spmv_layout), CUDA events on the library stream; solve in that mode first."""
+        ms = C.c_float(0)
+        check(lib().ffgpu_matrix_time_spmv(self.h, int(mode), int(nrep), C.byref(ms)))
+        return float(ms.value)
+
     def mult(self, x, trans=False, out=None):
         if out is None:
             out = np.empty(self.n) if not hasattr(x, "data_ptr") else x.new_empty(self.n)

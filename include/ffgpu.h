@@ -150,9 +150,16 @@ int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_si
  * or 2 (FP32 inner solve of ffgpu_solve_ir).  Returns 64 + a + 2u for the SELL-32 copy, with
  * a = 0 for contiguous per-warp chunk ranges or 1 for a rotated chunk stride and u = 1 for the
  * deeper unroll of the row loop; T in {1,..,32} for block CSR with T lanes per block row; 0
- * before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences.
+ * before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences;
+ * mode 4: block entries the SELL copy stores, padding included (32 per slot; -1 past INT32_MAX).
  * No FreeFEM counterpart. */
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
+/* Average device time in ms of `nrep` back-to-back launches of the solver's SpMV kernel (K_a,
+ * with its fused dot product) for mode 0 (FP64 CG), 1 (double-float CG) or 2 (FP32 inner solve
+ * of ffgpu_solve_ir), in the layout the tuner chose, timed with CUDA events on the library
+ * stream.  The matrix must have been solved in that mode first.  Reads the last solution, writes
+ * only scratch vectors.  A measurement helper; no FreeFEM counterpart. */
+int ffgpu_matrix_time_spmv(ffgpu_matrix *A, int mode, int nrep, float *ms);
 /* [I,J,C] = A in sorted CSR form (HashMatrix::CSR / Sortij, HashMatrix.cpp:671-682,870-876) */
 int ffgpu_matrix_csr(const ffgpu_matrix *A, int32_t *rowptr, int32_t *col, double *val);
 
