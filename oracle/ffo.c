@@ -371,6 +371,109 @@ int ffo_rhs(double *b, int dim, int nt, const double *X, const int *elems, int n
     return 0;
 }
 
+/* ------------------------------------------------------------------ boundary terms
+ * One varf term on the boundary elements e whose label is one of labels[0..nlabels) (every
+ * boundary element when nlabels == 0), integrated on the edge/face bel_face[e] (the one
+ * opposite that local vertex) of the adjacent element bel_elem[e], in boundary-element order
+ * (the bedges / be(k) loops of AssembleBilinearForm and AssembleLinearForm,
+ * problem.cpp:1011-1019, 10722-10735):
+ *   hm != NULL: element matrix M(i,j) = sum_q (c coef_q) w_i w_j over every local i, j of the
+ *               element, per component for [P2,P2,P2], then A += M (Element_Op on an edge,
+ *               problem.cpp:6222-6262; on a face, problem.cpp:6516-6560);
+ *   b  != NULL: b(i) += coef_q g_c w_i for component c (Element_rhs on an edge,
+ *               problem.cpp:8612-8683; on a face, problem.cpp:8517-8580).
+ * 2D: 3-point Gauss-Legendre on the edge (QF_GaussLegendre3, QuadratureFormular.cpp:319-343),
+ *     coef = |E| a_q with E = Edge(ie), point PA s + PB (1 - s) where PA, PB are the reference
+ *     vertices VerticesOfTriangularEdge[ie] (fem.hpp:95,112).
+ * 3D: the 7-point T_5 rule on the face, coef = 0.5 |N| a_q with N = (P_f0 P_f2) x (P_f0 P_f1),
+ *     point KHat[f0] (1-x-y) + KHat[f1] x + KHat[f2] y, f = nvfaceTet[ie] (GenericMesh.hpp:272,
+ *     Mesh3dn.hpp:76, Mesh3dn.cpp:72).
+ * c (Robin coefficient) and g (source): per boundary element (nbe, resp. nbe*ncomp) or NULL,
+ * then the constants cconst / gconst[c]. */
+static const int tet_face[4][3] = {{3, 2, 1}, {0, 2, 3}, {3, 1, 0}, {0, 1, 2}};
+
+int ffo_bterm(void *hm, double *b, int dim, const double *X, const int *elems, int ndofK,
+              const int *dof, int fe, int nbe, const int *bel_elem, const int *bel_face,
+              const int *blabel, int nlabels, const int *labels, const double *cP, double cconst,
+              const double *gP, int ncomp, const double *gconst) {
+    ffo_hm *A = (ffo_hm *)hm;
+    const int nv = dim + 1, order = fe == 1 ? 1 : 2, ncp = fe == 3 ? 3 : 1;
+    double P[14 * 3], W[14];
+    int nq;
+    if (dim == 2) {
+        const double g1 = (1 - sqrt(3. / 5.)) / 2;
+        P[0] = 0.5; W[0] = 8. / 18.;
+        P[1] = g1; W[1] = 5. / 18.;
+        P[2] = 1 - g1; W[2] = 5. / 18.;
+        nq = 3;
+    } else {
+        nq = quad_rule(5, P, W);
+    }
+    const double hat2[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+    const double hat3[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    double *M = hm ? (double *)malloc(sizeof(double) * ndofK * ndofK) : NULL;
+    for (int e = 0; e < nbe; ++e) {
+        if (nlabels > 0) {
+            int hit = 0;
+            for (int k = 0; k < nlabels; ++k) hit |= blabel[e] == labels[k];
+            if (!hit) continue;
+        }
+        const int k = bel_elem[e], ie = bel_face[e];
+        const int *v = elems + (int64_t)k * nv;
+        const int *d = dof + (int64_t)k * ndofK;
+        double G[4][3] = {{0}};
+        if (M) memset(M, 0, sizeof(double) * ndofK * ndofK);
+        for (int q = 0; q < nq; ++q) {
+            double l[4], coef;
+            if (dim == 2) {
+                const double *p1 = X + 2 * v[tri_edge[ie][0]], *p2 = X + 2 * v[tri_edge[ie][1]];
+                const double ex = p2[0] - p1[0], ey = p2[1] - p1[1];
+                const double le = sqrt(ex * ex + ey * ey);
+                coef = le * W[q];
+                const double sa = P[q], sb = 1 - sa;
+                const double *PA = hat2[tri_edge[ie][0]], *PB = hat2[tri_edge[ie][1]];
+                const double x = PA[0] * sa + PB[0] * sb, y = PA[1] * sa + PB[1] * sb;
+                l[1] = x; l[2] = y; l[0] = 1 - x - y;
+            } else {
+                const int *f = tet_face[ie];
+                const double *a = X + 3 * v[f[0]], *p1 = X + 3 * v[f[1]], *p2 = X + 3 * v[f[2]];
+                const double u[3] = {p2[0] - a[0], p2[1] - a[1], p2[2] - a[2]};
+                const double w[3] = {p1[0] - a[0], p1[1] - a[1], p1[2] - a[2]};
+                const double N[3] = {u[1] * w[2] - u[2] * w[1], w[0] * u[2] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+                const double le = sqrt(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+                coef = le * W[q] * 0.5;
+                const double x = P[2 * q], y = P[2 * q + 1], s = 1 - x - y;
+                double pt[3];
+                for (int c = 0; c < 3; ++c) pt[c] = hat3[f[0]][c] * s + hat3[f[1]][c] * x + hat3[f[2]][c] * y;
+                l[1] = pt[0]; l[2] = pt[1]; l[3] = pt[2]; l[0] = 1. - (pt[0] + pt[1] + pt[2]);
+            }
+            double w[10], dw[10][3];
+            const int nb = basis(dim, order, l, G, w, dw);
+            if (M) {
+                const double c = cP ? cP[e] : cconst;
+                for (int cp = 0; cp < ncp; ++cp) {
+                    const double ccc = c * coef;
+                    for (int i = 0; i < nb; ++i)
+                        for (int j = 0; j < nb; ++j) M[(cp * nb + i) * ndofK + cp * nb + j] += ccc * w[i] * w[j];
+                }
+            }
+            if (b)
+                for (int i = 0; i < nb; ++i)
+                    for (int c = 0; c < ncomp; ++c) {
+                        const double gc = gP ? gP[(int64_t)e * ncomp + c] : gconst[c];
+                        if (gc == 0.0 && !gP) continue;
+                        b[d[c * nb + i]] += coef * gc * w[i];
+                    }
+        }
+        if (M)
+            for (int il = 0; il < ndofK; ++il)
+                for (int jl = 0; jl < ndofK; ++jl) *hm_npij(A, d[il], d[jl]) += M[il * ndofK + jl];
+    }
+    free(M);
+    (void)nv;
+    return 0;
+}
+
 /* SetBC (HashMatrix.cpp:1195-1238) with the rhs of AssembleBC (problem.cpp:9937,10020):
  *   tgv > 0: diagonal := tgv on marked rows, b_i = tgv g_i;
  *   tgv < 0: b_i = g_i; marked rows get diagonal 1 (0 if tgv <= -10) and zero off-diagonals

@@ -55,6 +55,9 @@ def lib():
         L.ffo_rhs.argtypes = [_dp, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int, C.c_int,
                               C.c_void_p, C.c_int, _dp]
         L.ffo_setbc.argtypes = [C.c_void_p, C.c_void_p, _bp, C.c_void_p, C.c_double]
+        L.ffo_bterm.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
+                                C.c_int, _ip, _ip, _ip, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                C.c_void_p, C.c_int, _dp]
         L.ffo_cg.restype = C.c_int
         L.ffo_cg.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_double,
                              C.POINTER(C.c_int), _dp]
@@ -179,6 +182,62 @@ def rhs(Th, Vh, f=1.0, quad=None):
     L.ffo_rhs(b, dim, Th.nt, np.ascontiguousarray(Th.coords), np.ascontiguousarray(Th.elems, np.int32),
               Vh.ndofK, np.ascontiguousarray(Vh.dof, np.int32), fe, int(quad), _ptr(fP0), nc, fconst)
     return b
+
+
+def boundary_adjacency(Th):
+    """(element, local edge/face) of every boundary element: the element whose edge/face
+    opposite local vertex f has the boundary element's vertices (the smallest element index if
+    two do).  Independent numpy restatement of Mesh::BoundaryElement."""
+    dim = Th.dim
+    faces = [[1, 2], [2, 0], [0, 1]] if dim == 2 else [[3, 2, 1], [0, 2, 3], [3, 1, 0], [0, 1, 2]]
+    el = np.asarray(Th.elems, np.int64)
+    fv = np.sort(el[:, faces], axis=2).reshape(-1, dim)          # (nt*(dim+1), dim)
+    bv = np.sort(np.asarray(Th.belems, np.int64), axis=1)
+    nv = int(Th.nv)
+    key = fv[:, 0]
+    bkey = bv[:, 0]
+    for c in range(1, dim):
+        key = key * nv + fv[:, c]
+        bkey = bkey * nv + bv[:, c]
+    order = np.argsort(key, kind="stable")                         # stable: smallest element first
+    pos = np.searchsorted(key[order], bkey)
+    if np.any(pos >= key.size) or np.any(key[order][np.minimum(pos, key.size - 1)] != bkey):
+        raise ValueError("boundary element without an adjacent element")
+    idx = order[pos]
+    return (idx // (dim + 1)).astype(np.int32), (idx % (dim + 1)).astype(np.int32)
+
+
+def bterm(Th, Vh, labels=(), robin=None, g=None, A: HashMatrix | None = None, b=None, adj=None):
+    """One boundary term on the boundary elements carrying one of `labels` (all when empty):
+    robin (scalar or per boundary element) adds robin*u.v to A, g (scalar, per-component tuple
+    or per boundary element [x ncomp]) adds g.v to b."""
+    L = lib()
+    bel_elem, bel_face = boundary_adjacency(Th) if adj is None else adj
+    nc = 3 if Vh.kind == "P2vec" else 1
+    fe = {"P1": 1, "P2": 2, "P2vec": 3}[Vh.kind]
+    lab = np.ascontiguousarray(labels, np.int32)
+    cP, cc = None, 0.0
+    if robin is not None:
+        if np.isscalar(robin):
+            cc = float(robin)
+        else:
+            cP = np.ascontiguousarray(robin, np.float64)
+    gP, gconst = None, np.zeros(3)
+    if g is not None:
+        if np.isscalar(g):
+            gconst[0] = float(g)
+        else:
+            ga = np.asarray(g, np.float64)
+            if ga.ndim == 1 and ga.size == nc and ga.size != Th.nbe:
+                gconst[:nc] = ga
+            else:
+                gP = np.ascontiguousarray(ga.reshape(Th.nbe, nc))
+    L.ffo_bterm(A.h if (A is not None and robin is not None) else None,
+                _ptr(b) if (b is not None and g is not None) else None, Th.dim,
+                np.ascontiguousarray(Th.coords, np.float64), np.ascontiguousarray(Th.elems, np.int32),
+                Vh.ndofK, np.ascontiguousarray(Vh.dof, np.int32), fe, Th.nbe, bel_elem, bel_face,
+                np.ascontiguousarray(Th.blabel, np.int32), lab.size, _ptr(lab) if lab.size else None,
+                _ptr(cP), cc, _ptr(gP), nc, gconst)
 
 
 def setbc(A: HashMatrix, b, onbc, g=None, tgv=1e30):

@@ -287,6 +287,66 @@ for (int k=0;k<Th.nv;k++) cout << "G uT " << u[][k] << endl;
     return body, {"kappa.txt": kap}
 
 
+BT_VARF2 = {
+    "P1": "int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int1d(Th,3)(2.5*u*v) + int2d(Th)(1.*v) + int1d(Th,2)(gk*v) + int1d(Th,3)(-0.75*v) + on(1,4,u=0)",
+}
+BT_VARF3 = ("int3d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v)) + int2d(Th,2)(2.*u*v) + int3d(Th)(1.*v) "
+            "+ int2d(Th,1,3)(gk*v) + int2d(Th,6)(0.5*v) + on(4,u=0)")
+
+
+def case_bterms(kind, dims, seed):
+    """Boundary terms: Robin c*u*v and Neumann g*v on labelled boundary edges/faces (int1d in 2D,
+    int2d on the boundary in 3D), g a constant or a P0 function (value of the adjacent element),
+    next to the volume terms and on(...)."""
+    rng = np.random.default_rng(seed)
+    dim = len(dims)
+    nt = 2 * dims[0] * dims[1] if dim == 2 else 6 * dims[0] * dims[1] * dims[2]
+    gk = rng.uniform(0.5, 2.0, nt)
+    if dim == 2:
+        head = f"mesh Th=square({dims[0]},{dims[1]});\n"
+        dump = DUMP_MESH2
+    else:
+        head = f'load "msh3"\nmesh3 Th=cube({dims[0]},{dims[1]},{dims[2]});\n'
+        dump = DUMP_MESH3
+    if kind == "P2vec":
+        body = HEAD + head + """
+fespace Vh(Th,[P2,P2,P2]); fespace Ph(Th,P0);
+""" + read_vec_edp("gka", "gk.txt", "Th.nt") + """
+Ph gk; gk[]=gka;
+Vh [u1,u2,u3],[v1,v2,v3];
+real E=1, nu=0.3; real mu=E/(2*(1+nu)); real lambda=E*nu/((1+nu)*(1-2*nu));
+real s2=sqrt(2.);
+macro epsilon(u1,u2,u3) [dx(u1),dy(u2),dz(u3),(dz(u2)+dy(u3))/s2,(dz(u1)+dx(u3))/s2,(dy(u1)+dx(u2))/s2] // EOM
+macro div(u1,u2,u3) (dx(u1)+dy(u2)+dz(u3)) // EOM
+varf a([u1,u2,u3],[v1,v2,v3])=int3d(Th)(lambda*div(u1,u2,u3)*div(v1,v2,v3)+2.*mu*(epsilon(u1,u2,u3)'*epsilon(v1,v2,v3)))
+  + int2d(Th,6)(0.1*(u1*v1+u2*v2+u3*v3)) + int3d(Th)(-1.*v3) + int2d(Th,2)(0.25*v1-0.5*v3) + on(4,u1=0,u2=0,u3=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u1[]=0; u1[]=A^-1*b;
+cout << "S nit " << nit << endl;
+for (int k=0;k<Th.nt;k++) cout << "G p0dof " << Ph(k,0) << endl;
+""" + dump + DUMP_DOF + DUMP_A + \
+            "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u1[][k] << endl;\n"
+        return body, {"gk.txt": gk}
+    varf = BT_VARF2["P1"] if dim == 2 else BT_VARF3
+    body = HEAD + head + f"""
+fespace Vh(Th,{kind}); fespace Ph(Th,P0);
+""" + read_vec_edp("gka", "gk.txt", "Th.nt") + f"""
+Ph gk; gk[]=gka;
+Vh u,v;
+varf a(u,v)={varf};
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+for (int k=0;k<Th.nt;k++) cout << "G p0dof " << Ph(k,0) << endl;
+""" + dump + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {"gk.txt": gk}
+
+
 CASES = {
     "p1sq_n2": lambda: case_p1_square(2),
     "p1sq_n5": lambda: case_p1_square(5),
@@ -309,6 +369,11 @@ CASES = {
     "p1sq_n6_tgvp": lambda: case_p1_square_tgv(6, 1e30, "CG"),
     "adj_p1_n8": lambda: case_adjoint_p1(8, seed=31),
     "heat_p1_n6": lambda: case_heat_p1(6, 10, 1e-2, seed=41),
+    "bt_p1sq_6x5": lambda: case_bterms("P1", (6, 5), seed=51),
+    "bt_p2sq_5x4": lambda: case_bterms("P2", (5, 4), seed=52),
+    "bt_p1cube_3x3x2": lambda: case_bterms("P1", (3, 3, 2), seed=53),
+    "bt_p2cube_2x2x2": lambda: case_bterms("P2", (2, 2, 2), seed=54),
+    "bt_p2el_2x2x2": lambda: case_bterms("P2vec", (2, 2, 2), seed=55),
 }
 
 

@@ -68,3 +68,31 @@ def value_errors(v, ref, rowptr):
     den = np.maximum(a, 1e-3 * s[rows])
     den = np.where(den == 0, 1.0, den)
     return np.abs(v - ref) / den
+
+
+# Boundary-term cases (tests/golden/make_golden.py: case_bterms): volume terms as the other
+# cases, then the boundary terms in varf order.  "gk" = the P0 function of the fixture, taken
+# on each boundary element from its adjacent element.
+BT_CASES = {
+    "bt_p1sq_6x5": dict(kind="P1", dims=(6, 5), on=(1, 4), robin=[((3,), 2.5)],
+                        neumann=[((2,), "gk"), ((3,), -0.75)]),
+    "bt_p2sq_5x4": dict(kind="P2", dims=(5, 4), on=(1, 4), robin=[((3,), 2.5)],
+                        neumann=[((2,), "gk"), ((3,), -0.75)]),
+    "bt_p1cube_3x3x2": dict(kind="P1", dims=(3, 3, 2), on=(4,), robin=[((2,), 2.0)],
+                            neumann=[((1, 3), "gk"), ((6,), 0.5)]),
+    "bt_p2cube_2x2x2": dict(kind="P2", dims=(2, 2, 2), on=(4,), robin=[((2,), 2.0)],
+                            neumann=[((1, 3), "gk"), ((6,), 0.5)]),
+    "bt_p2el_2x2x2": dict(kind="P2vec", dims=(2, 2, 2), on=(4,), robin=[((6,), 0.1)],
+                          neumann=[((2,), (0.25, 0.0, -0.5))]),
+}
+
+
+def bt_case(name):
+    """-> dict(Th, kind, d, sc, spec, gk_elem): gk_elem[k] = the P0 value on element k."""
+    d, sc = load(name)
+    spec = BT_CASES[name]
+    dims = spec["dims"]
+    Th = mesh.square(*dims) if len(dims) == 2 else mesh.cube(*dims)
+    gk_elem = d["in_gk"][d["g_p0dof"].astype(np.int64)]
+    return dict(name=name, d=d, sc=sc, spec=spec, Th=Th, kind=spec["kind"], gk_elem=gk_elem,
+                dof=d["dof"] if spec["kind"] == "P2" and len(dims) == 2 else None)
