@@ -382,6 +382,9 @@ struct FillArgs {
     double tgv;
     int max_deg;
     int *status;
+    // boundary terms (NULL bptr: none): node -> codes b*NN + il, element vectors / matrices
+    const int32_t *bptr, *blist, *bel_elem;
+    const double *brhs, *bmat;
 };
 
 // FE: 1 = P1 scalar, 2 = P2 scalar, 3 = [P2]^3 elasticity
@@ -490,6 +493,25 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
             racc = r;   // lanes < BS: component `lane`
         }
         __syncwarp();
+        // ---- boundary terms, boundary element by boundary element, after the volume sum
+        if (A.bptr) {
+            const int p1 = A.bptr[a + 1];
+            for (int p = A.bptr[a]; p < p1; ++p) {
+                const int code = A.blist[p];
+                const int bb = code / NN, il = code - bb * NN;
+                if (A.bmat && A.val && lane < NN) {
+                    const int cn = A.nodes[(int64_t)A.bel_elem[bb] * NN + lane];
+                    const int rk = find_sorted(cols, deg, cn);
+                    const double m = A.bmat[((int64_t)bb * NN + il) * NN + lane];
+                    if (rk < 0) dev_fail(A.status, kDevNotFound);
+                    else
+#pragma unroll
+                        for (int c = 0; c < BS; ++c) acc[rk * BS2 + c * BS + c] += m;
+                }
+                if (A.brhs && A.rhs && lane < BS) racc += A.brhs[((int64_t)bb * BS + lane) * NN + il];
+                __syncwarp();
+            }
+        }
         // ---- Dirichlet rows (tgv > 0): diagonal := tgv, rhs := tgv * g
         int self = find_sorted(cols, deg, a);
         if (self < 0) { if (lane == 0) dev_fail(A.status, kDevNotFound); continue; }
@@ -536,7 +558,8 @@ template <int DIM, int FE>
 __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *inc_elem,
                            const uint8_t *inc_loc, const double *geo, const double *fP0,
                            double f0, double f1, double f2, const uint8_t *onbc, const double *g,
-                           double tgv, double *rhs) {
+                           double tgv, double *rhs, const int32_t *bptr, const int32_t *blist,
+                           const double *brhs) {
     constexpr int BS = FE == 3 ? 3 : 1;
     // same association as the fill kernel's fused linear form: element p of the node goes to
     // partial p % SLOTS, partials summed in order
@@ -564,6 +587,12 @@ __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *in
     double s = part[0];
 #pragma unroll
     for (int sl = 1; sl < SLOTS; ++sl) s += part[sl];
+    if (bptr)   // boundary terms, in boundary-element order, after the volume terms
+        for (int p = bptr[a]; p < bptr[a + 1]; ++p) {
+            const int code = blist[p];
+            const int bb = code / NN, il = code - bb * NN;
+            s += brhs[((int64_t)bb * BS + c) * NN + il];
+        }
     if (onbc && onbc[t]) s = (tgv > 0 ? tgv : 1.0) * (g ? g[t] : 0.0);
     rhs[t] = s;
 }
@@ -776,7 +805,12 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     }
     fa.onbc = mask; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
-    FFGPU_TRY(fill_launch(S, fa));
+    BoundaryTerms bt;
+    FFGPU_TRY(boundary_prepare(S, v, rh.d != nullptr, true, bt));
+    fa.bptr = bt.ptr; fa.blist = bt.list; fa.bel_elem = bt.bel_elem; fa.brhs = bt.rhs; fa.bmat = bt.mat;
+    const int frc = fill_launch(S, fa);
+    boundary_release(S, bt);
+    FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish(ctx->stream));
     // the solver data of a previous numeric state are stale; so is a cached CG graph, which
@@ -879,6 +913,7 @@ int ffgpu_space_destroy(ffgpu_space *S) {
     cudaFree(S->coords); cudaFree(S->elems); cudaFree(S->nodes);
     cudaFree(S->inc_ptr); cudaFree(S->inc_elem); cudaFree(S->inc_loc);
     cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
+    cudaFree(S->bel_elem); cudaFree(S->bel_face);
     delete S;
     return FFGPU_OK;
 }
@@ -890,7 +925,8 @@ int ffgpu_space_set_boundary(ffgpu_space *S, int nbe, const int32_t *belems, con
     cudaStream_t s = ctx->stream;
     const int bdim = S->dim;   // vertices per boundary element
     cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
-    S->belems = S->blabel = S->bv_ptr = S->bv_elem = nullptr;
+    cudaFree(S->bel_elem); cudaFree(S->bel_face);
+    S->belems = S->blabel = S->bv_ptr = S->bv_elem = S->bel_elem = S->bel_face = nullptr;
     S->vmark = nullptr;
     S->nbe = nbe;
     int32_t *cnt = nullptr;
@@ -1023,10 +1059,12 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
             if (!rc) rc = space_bc_mask_device(S, bc->nlabels, bc->labels, bc->comp_mask, lmask);
             mask = lmask;
         }
+        BoundaryTerms bt;
+        if (!rc) rc = boundary_prepare(S, v, true, false, bt);
         if (!rc) {
             void (*k)(int, const int32_t *, const int32_t *, const uint8_t *, const double *,
                       const double *, double, double, double, const uint8_t *, const double *,
-                      double, double *) = nullptr;
+                      double, double *, const int32_t *, const int32_t *, const double *) = nullptr;
             if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = rhs_kernel<2, 1>;
             if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = rhs_kernel<3, 1>;
             if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = rhs_kernel<2, 2>;
@@ -1034,9 +1072,10 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
             if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) k = rhs_kernel<3, 3>;
             k<<<grid_for((int64_t)S->ndof, 256), 256, 0, s>>>(
                 S->nnodes, S->inc_ptr, S->inc_elem, S->inc_loc, geo, fP0.d, v->f_const[0],
-                v->f_const[1], v->f_const[2], mask, gv.d, bc ? bc->tgv : 0.0, rh.d);
+                v->f_const[1], v->f_const[2], mask, gv.d, bc ? bc->tgv : 0.0, rh.d, bt.ptr, bt.list, bt.rhs);
             rc = launch_check(ctx, "rhs_kernel");
         }
+        boundary_release(S, bt);
         if (!rc) rc = rh.finish(s);
         if (lmask) cudaFreeAsync(lmask, s);
     }

@@ -94,6 +94,8 @@ struct ffgpu_space {
     int nbe;
     int32_t *belems, *blabel, *bv_ptr, *bv_elem;
     uint8_t *vmark;       // scratch: vertex on a selected boundary element (nv)
+    // adjacent element and its local edge/face of each boundary element (boundary terms)
+    int32_t *bel_elem, *bel_face;
 };
 
 struct ffgpu_matrix {
@@ -212,6 +214,18 @@ int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n);  //
 int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
 // order[0..n): indices sorted by decreasing key (0 <= key <= maxkey), ties by increasing index
 int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order);
+// Boundary terms of a varf prepared for one assembly call (ffgpu_boundary.cu): for every node
+// the (boundary element, local node) codes b*nn + il touching it, ascending, and per boundary
+// element its element vector (nn*bs, component-major) and Robin element matrix (nn*nn).
+struct BoundaryTerms {
+    const int32_t *ptr = nullptr;    // nnodes + 1
+    const int32_t *list = nullptr;
+    const double *rhs = nullptr;     // NULL: no linear boundary term
+    const double *mat = nullptr;     // NULL: no Robin term
+    const int32_t *bel_elem = nullptr;
+};
+int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool want_mat, BoundaryTerms &bt);
+void boundary_release(ffgpu_space *S, BoundaryTerms &bt);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 

@@ -4,10 +4,10 @@ See ``api`` for the FreeFEM-shaped interface and include/ffgpu.h for the C ABI.
 """
 from .mesh import Mesh, square, cube, movemesh, jittered_square
 from .fespace import FESpace
-from .api import (DeviceSpace, Matrix, VarForm, context, fespace, kernel_launches, matrix, stream_handle,
+from .api import (BoundaryTerm, DeviceSpace, Matrix, VarForm, context, fespace, kernel_launches, matrix, stream_handle,
                   matrix_from_csr, rhs, varf_diffusion, varf_elasticity)
 from ._lib import FFGPUError, lib
 
 __all__ = ["Mesh", "square", "cube", "movemesh", "jittered_square", "FESpace", "DeviceSpace",
-           "Matrix", "VarForm", "context", "fespace", "kernel_launches", "matrix",
+           "BoundaryTerm", "Matrix", "VarForm", "context", "fespace", "kernel_launches", "matrix",
            "matrix_from_csr", "rhs", "varf_diffusion", "varf_elasticity", "FFGPUError", "lib"]

@@ -32,10 +32,16 @@ EXPORTS = [
 ]
 
 
+class BTerm(C.Structure):
+    _fields_ = [("nlabels", C.c_int), ("labels", C.c_void_p), ("robin", C.c_void_p),
+                ("robin_const", C.c_double), ("g", C.c_void_p), ("g_const", C.c_double * 3)]
+
+
 class Varf(C.Structure):
     _fields_ = [("form", C.c_int), ("kappa", C.c_void_p), ("c_stiff", C.c_double),
                 ("c_mass", C.c_double), ("E", C.c_double), ("nu", C.c_double),
-                ("f", C.c_void_p), ("f_const", C.c_double * 3)]
+                ("f", C.c_void_p), ("f_const", C.c_double * 3), ("nbterms", C.c_int),
+                ("bterms", C.c_void_p)]
 
 
 class BC(C.Structure):

@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BC, SolverParams, SolverStats, Varf, check, lib
+from ._lib import BC, BTerm, SolverParams, SolverStats, Varf, check, lib
 from .fespace import FESpace
 from .mesh import Mesh
 
@@ -111,8 +111,20 @@ class DeviceSpace:
 
 
 @dataclass
+class BoundaryTerm:
+    """int1d(Th, labels)(robin*u*v + g*v) in 2D, int2d(Th, labels)(...) on the boundary faces in
+    3D (labels empty: the whole boundary).  robin: scalar or per boundary element (nbe); g:
+    scalar, per-component tuple, or per boundary element (nbe[, ncomp]).  For [P2,P2,P2] the
+    Robin term is robin*(u1*v1+u2*v2+u3*v3)."""
+
+    labels: tuple = ()
+    robin: object = 0.0
+    g: object = 0.0
+
+
+@dataclass
 class VarForm:
-    """A varf of the supported family (P0 coefficients, constant or P0 sources)."""
+    """A varf of the supported family (P0 coefficients, constant or P0 sources, boundary terms)."""
 
     form: int = _lib.FORM_DIFFUSION
     kappa: object = None          # P0 coefficient (nt) or None
@@ -125,6 +137,7 @@ class VarForm:
     g: object = None              # Dirichlet values per DOF (None = 0)
     components: tuple | None = None
     tgv: float = 1e30
+    bterms: tuple = ()            # BoundaryTerm, in varf order
     _keep: list = field(default_factory=list)
 
     def c_varf(self, Vh: FESpace) -> Varf:
@@ -155,6 +168,46 @@ class VarForm:
                 fa = np.ascontiguousarray(fa.reshape(Vh.Th.nt, nc))
                 self._keep.append(fa)
                 v.f = _ptr(fa).value
+        v.nbterms = 0
+        v.bterms = None
+        if self.bterms:
+            nc = 3 if Vh.kind == "P2vec" else 1
+            nbe = Vh.Th.nbe
+            arr = (BTerm * len(self.bterms))()
+            for t, bt in enumerate(self.bterms):
+                T = arr[t]
+                lab = np.ascontiguousarray(np.atleast_1d(np.asarray(bt.labels, np.int32)), np.int32)
+                self._keep.append(lab)
+                T.nlabels = lab.size
+                T.labels = _ptr(lab).value if lab.size else None
+                T.robin = None
+                T.robin_const = 0.0
+                if np.isscalar(bt.robin):
+                    T.robin_const = float(bt.robin)
+                else:
+                    r = bt.robin if hasattr(bt.robin, "data_ptr") else np.ascontiguousarray(bt.robin, np.float64)
+                    if r.size != nbe:
+                        raise ValueError("BoundaryTerm.robin: one value per boundary element expected")
+                    self._keep.append(r)
+                    T.robin = _ptr(r).value
+                T.g = None
+                if np.isscalar(bt.g):
+                    T.g_const[0] = float(bt.g)
+                elif hasattr(bt.g, "data_ptr"):
+                    self._keep.append(bt.g)
+                    T.g = _ptr(bt.g).value
+                else:
+                    ga = np.asarray(bt.g, np.float64)
+                    if ga.ndim == 1 and ga.size == nc and ga.size != nbe:
+                        for c in range(nc):
+                            T.g_const[c] = ga[c]
+                    else:
+                        ga = np.ascontiguousarray(ga.reshape(nbe, nc))
+                        self._keep.append(ga)
+                        T.g = _ptr(ga).value
+            self._keep.append(arr)
+            v.nbterms = len(self.bterms)
+            v.bterms = C.cast(arr, C.c_void_p).value
         return v
 
     def c_bc(self, Vh: FESpace, device_marking: bool = False) -> BC:
@@ -188,16 +241,21 @@ class VarForm:
         return bc
 
 
-def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tgv=1e30) -> VarForm:
-    """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v) + on(on, u=g)."""
+def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tgv=1e30,
+                   bterms=()) -> VarForm:
+    """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v)
+    + the boundary terms (BoundaryTerm: robin*u*v + g*v on labelled boundary edges/faces)
+    + on(on, u=g)."""
     return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
-                   c_stiff=c_stiff, tgv=tgv)
+                   c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms))
 
 
-def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30) -> VarForm:
-    """varf a([u],[v]) = int(lambda div u div v + 2mu eps(u):eps(v)) + int(f.v) + on(on, u=0)."""
+def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30,
+                    bterms=()) -> VarForm:
+    """varf a([u],[v]) = int(lambda div u div v + 2mu eps(u):eps(v)) + int(f.v)
+    + the boundary terms (tractions g.v, Robin robin*u.v) + on(on, u=0)."""
     return VarForm(form=_lib.FORM_ELASTICITY, E=E, nu=nu, f=f, on=tuple(on), components=components,
-                   tgv=tgv)
+                   tgv=tgv, bterms=tuple(bterms))
 
 
 class Matrix:

@@ -38,10 +38,30 @@ typedef struct ffgpu_ctx ffgpu_ctx;
 typedef struct ffgpu_space ffgpu_space;
 typedef struct ffgpu_matrix ffgpu_matrix;
 
+/* One boundary term of a varf: int1d(Th, labels)(...) in 2D, int2d(Th, labels)(...) on the
+ * boundary faces in 3D, on the space's boundary elements (ffgpu_space_set_boundary) whose label
+ * is one of labels[0..nlabels) (nlabels = 0: every boundary element).  Each is integrated on the
+ * edge/face of its adjacent element as FreeFEM's Element_Op / Element_rhs on a boundary edge or
+ * face do (problem.cpp:6222-6262, 6516-6560, 8517-8580, 8612-8683): 3-point Gauss-Legendre on
+ * an edge, the 7-point degree-5 rule on a face.
+ *   robin: coefficient of u.v (of u_c v_c for every component c of [P2,P2,P2]), per boundary
+ *          element (length nbe) or NULL, then robin_const (0 = no matrix term);
+ *   g:     source of the linear term g.v per boundary element and component (nbe*ncomp) or
+ *          NULL, then g_const[c].  Like f, it enters b = a(0,Vh) with a plus sign. */
+typedef struct {
+    int nlabels;
+    const int32_t *labels;
+    const double *robin;
+    double robin_const;
+    const double *g;
+    double g_const[3];
+} ffgpu_bterm;
+
 /* varf description.  kappa: P0 coefficient per element (length nt) or NULL (= 1);
  * the stiffness term is c_stiff*kappa_e, the mass term c_mass (0 = none).
  * Elasticity uses E and nu (mu = E/(2(1+nu)), lambda = E nu/((1+nu)(1-2nu))).
- * f: P0 source per element and component (nt*ncomp) or NULL, then f_const[c] applies. */
+ * f: P0 source per element and component (nt*ncomp) or NULL, then f_const[c] applies.
+ * bterms[0..nbterms): boundary terms, added after the volume terms and before on(...). */
 typedef struct {
     int form;
     const double *kappa;
@@ -49,6 +69,8 @@ typedef struct {
     double E, nu;
     const double *f;
     double f_const[3];
+    int nbterms;
+    const ffgpu_bterm *bterms;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or
