@@ -29,9 +29,11 @@
 #include "ff++.hpp"
 #include "ffgpu.h"
 
-// label set of an on(...) condition (defined in FreeFEM, lgfem.cpp:7792)
+// label sets of an on(...) condition and of a domain of integration (defined in FreeFEM,
+// lgfem.cpp:7792, 7809)
 namespace Fem2D {
 void Expandsetoflab(Stack stack, const BC_set &bc, set<long> &setoflab);
+void Expandsetoflab(Stack stack, const CDomainOfIntegration &di, set<int> &setoflab, bool &all);
 }
 
 namespace {
@@ -129,7 +131,11 @@ template <> const int SolverGpu<kMixed>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 //     element) and m constant;
 //   3D [P2,P2,P2]:            int3d(Th)(lambda*div(u)*div(v) + 2*mu*(eps(u):eps(v)))
 //     + on(labels, ...) with constant lambda, mu (any way of writing it whose terms add up
-//     to the isotropic tensor).
+//     to the isotropic tensor);
+//   both with boundary terms int1d(Th, labels)(c*u*v) in 2D / int2d(Th, labels)(c*u*v) on a
+//     3D mesh (c*(u1*v1+u2*v2+u3*v3) for [P2,P2,P2]), c constant on every boundary element,
+//     and, in the linear form, int1d / int2d(Th, labels)(g*v) with g constant on every
+//     boundary element (boundary quadrature exact for the term).
 // The device matrix is built by ffgpu_matrix_assemble (pattern, values and tgv rows) and
 // handed to FreeFEM as its HashMatrix (sorted CSR, HashMatrix::set).
 
@@ -137,12 +143,21 @@ template <class MMesh> struct Dim;
 template <> struct Dim<Mesh> { static const int d = 2; typedef R2 Rd; };
 template <> struct Dim<Mesh3> { static const int d = 3; typedef R3 Rd; };
 
+// One boundary term of the device's kind: labels (empty: the whole boundary) and, per boundary
+// element, the coefficient of u.v (Robin) or of v_c (source) -- constant on every boundary element.
+struct BoundaryRec {
+    std::vector<int32_t> labels;
+    std::vector<double> robin;   // nbe, empty: none
+    std::vector<double> g;       // nbe * ncomp, empty: none
+};
+
 struct Recognised {
     int fe = 0, form = FFGPU_FORM_DIFFUSION;
     std::vector<double> kappa;
     double c_mass = 0, lam = 0, mu = 0, tgv = 1e30;
     int comp_mask = -1;   // components constrained by on(...) (-1: no on)
     std::vector<int32_t> labels;
+    std::vector<BoundaryRec> bterms;   // Robin terms, in varf order
     std::string why;
 };
 
@@ -204,9 +219,144 @@ static bool linear_on_element(Stack stack, const C_F0 &coef, const Element &K, F
     return std::fabs(sa - ca) <= 1e-13 * m && std::fabs(sb - cb) <= 1e-13 * m;
 }
 
-// quadrature exactness of a domain of integration
+// quadrature exactness of a domain of integration (volume, boundary)
 static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).exact; }
 static int exactness(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).exact; }
+static int bexactness(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIE(s).exact; }
+static int bexactness(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIT(s).exact; }
+
+// int2d(Th) in 2D / int3d(Th) in 3D over the whole mesh; int1d(Th, labels) in 2D / int2d(Th,
+// labels) on a 3D mesh: its boundary (CDomainOfIntegration kinds, problem.hpp:313)
+static bool volume_domain(const CDomainOfIntegration &di, int d) {
+    return di.kind == (d == 2 ? CDomainOfIntegration::int2d : CDomainOfIntegration::int3d) && di.d == d &&
+           di.dHat == d && di.what.empty() && !di.islevelset() && !di.withmap();
+}
+static bool boundary_domain(const CDomainOfIntegration &di, int d) {
+    return di.kind == (d == 2 ? CDomainOfIntegration::int1d : CDomainOfIntegration::int2d) && di.d == d &&
+           di.dHat == d && !di.islevelset() && !di.withmap();
+}
+
+// boundary elements in FreeFEM's order, their labels, adjacent element and local edge/face
+static int nb_boundary(const Mesh &Th) { return Th.neb; }
+static int nb_boundary(const Mesh3 &Th) { return Th.nbe; }
+static int boundary_label(const Mesh &Th, int e) { return Th.bedges[e].lab; }
+static int boundary_label(const Mesh3 &Th, int e) { return Th.be(e).lab; }
+// two points of edge/face ie in reference coordinates and the outward unit normal, as
+// Element_rhs places its quadrature points there (problem.cpp:8645-8652, 8543-8548)
+static void boundary_points(const Mesh::Element &T, int ie, R2 *P, R2 &N) {
+    const R2 PA(TriangleHat[VerticesOfTriangularEdge[ie][0]]), PB(TriangleHat[VerticesOfTriangularEdge[ie][1]]);
+    P[0] = PA * 0.5 + PB * 0.5;
+    P[1] = PA * 0.3 + PB * 0.7;
+    const R2 E = T.Edge(ie);
+    N = R2(E.y, -E.x) / sqrt((E, E));
+}
+static void boundary_points(const Mesh3::Element &T, int ie, R3 *P, R3 &N) {
+    P[0] = T.PBord(ie, R2(1. / 3., 1. / 3.));
+    P[1] = T.PBord(ie, R2(0.2, 0.3));
+    N = T.N(ie);
+    N /= N.norme();
+}
+
+// Values of `coef` on the boundary elements of `di` (others 0); false when it is not constant
+// on one of them.
+template <class MMesh, class FES>
+static bool boundary_values(Stack stack, const MMesh &Th, const FES &Uh, const std::set<int> &labs, bool all,
+                            const C_F0 &coef, std::vector<double> &out, int stride, int comp) {
+    typedef typename Dim<MMesh>::Rd Rd;
+    const bool constant = coef.LeftValue()->MeshIndependent();
+    const int nbe = nb_boundary(Th);
+    for (int e = 0; e < nbe; ++e) {
+        const int lab = boundary_label(Th, e);
+        if (!all && !labs.count(lab)) continue;
+        int ie;
+        const int k = Th.BoundaryElement(e, ie);
+        typename FES::FElement FK = Uh[k];
+        Rd P[2], N;
+        boundary_points(Th[k], ie, P, N);
+        MeshPointStack(stack)->set(Th[k](P[0]), P[0], FK, lab, N, ie);
+        const double ca = GetAny<double>(coef.eval(stack));
+        if (!constant) {
+            MeshPointStack(stack)->set(Th[k](P[1]), P[1], FK, lab, N, ie);
+            const double cb = GetAny<double>(coef.eval(stack));
+            if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) return false;
+        }
+        out[(size_t)e * stride + comp] += ca;
+    }
+    return true;
+}
+
+// Label set and quadrature check of a boundary domain, shared by the two readers below.
+template <class MMesh>
+static bool boundary_domain_labels(Stack stack, const MMesh &Th, const CDomainOfIntegration &di, int degree,
+                                   std::set<int> &labs, bool &all, BoundaryRec &r, std::string &why) {
+    if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { why = "integration mesh"; return false; }
+    if (bexactness(stack, di, &Th) < degree) { why = "boundary quadrature not exact"; return false; }
+    all = true;
+    Fem2D::Expandsetoflab(stack, di, labs, all);
+    if (!all) r.labels.assign(labs.begin(), labs.end());
+    return true;
+}
+
+// A boundary FormBilinear: Robin sum over the components of c u_j v_j, the same c for every
+// component; r.robin per boundary element.
+template <class MMesh, class FES>
+static bool read_boundary_bilinear(Stack stack, const MMesh &Th, const FES &Uh, const CDomainOfIntegration &di,
+                                   const BilinearOperator &op, int fe, BoundaryRec &r, std::string &why) {
+    const int d = Dim<MMesh>::d, nc = fe == FFGPU_FE_P2VEC3 ? 3 : 1, order = fe == FFGPU_FE_P1 ? 1 : 2;
+    std::set<int> labs;
+    bool all;
+    if (!boundary_domain_labels(stack, Th, di, 2 * order, labs, all, r, why)) return false;
+    const int nbe = nb_boundary(Th);
+    std::vector<double> per((size_t)nbe * nc, 0.0);
+    for (BilinearOperator::const_iterator l = op.v.begin(); l != op.v.end(); ++l) {
+        const int ju = l->first.first.first, jv = l->first.second.first;
+        if (ju != jv || ju >= nc || op_index(l->first.first.second, d) != 0 || op_index(l->first.second.second, d) != 0) {
+            why = "boundary term other than c*u*v"; return false;
+        }
+        if (!boundary_values(stack, Th, Uh, labs, all, l->second, per, nc, ju)) {
+            why = "boundary coefficient not constant on boundary elements"; return false;
+        }
+    }
+    r.robin.assign(nbe, 0.0);
+    for (int e = 0; e < nbe; ++e) {
+        for (int c = 1; c < nc; ++c)
+            if (per[(size_t)e * nc + c] != per[(size_t)e * nc]) { why = "Robin coefficients differ between components"; return false; }
+        r.robin[e] = per[(size_t)e * nc];
+    }
+    return true;
+}
+
+// A boundary FormLinear: sources g_j v_j; r.g per boundary element and component.
+template <class MMesh, class FES>
+static bool read_boundary_linear(Stack stack, const MMesh &Th, const FES &Uh, const CDomainOfIntegration &di,
+                                 const Ftest &ft, int fe, BoundaryRec &r, std::string &why) {
+    const int d = Dim<MMesh>::d, nc = fe == FFGPU_FE_P2VEC3 ? 3 : 1, order = fe == FFGPU_FE_P1 ? 1 : 2;
+    std::set<int> labs;
+    bool all;
+    if (!boundary_domain_labels(stack, Th, di, order, labs, all, r, why)) return false;
+    r.g.assign((size_t)nb_boundary(Th) * nc, 0.0);
+    for (Ftest::const_iterator l = ft.v.begin(); l != ft.v.end(); ++l) {
+        const int jv = l->first.first;
+        if (jv >= nc || op_index(l->first.second, d) != 0) { why = "boundary term other than g*v"; return false; }
+        if (!boundary_values(stack, Th, Uh, labs, all, l->second, r.g, nc, jv)) {
+            why = "boundary source not constant on boundary elements"; return false;
+        }
+    }
+    return true;
+}
+
+// the C ABI's view of the recognised boundary terms
+static std::vector<ffgpu_bterm> c_bterms(const std::vector<BoundaryRec> &bt) {
+    std::vector<ffgpu_bterm> out(bt.size());
+    for (size_t t = 0; t < bt.size(); ++t) {
+        memset(&out[t], 0, sizeof(ffgpu_bterm));
+        out[t].nlabels = (int)bt[t].labels.size();
+        out[t].labels = bt[t].labels.empty() ? nullptr : bt[t].labels.data();
+        out[t].robin = bt[t].robin.empty() ? nullptr : bt[t].robin.data();
+        out[t].g = bt[t].g.empty() ? nullptr : bt[t].g.data();
+    }
+    return out;
+}
 
 // Reads the form's terms.  Returns true when the device can assemble it; r.why otherwise.
 template <class MMesh, class FES>
@@ -247,9 +397,13 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
         if (t != tvf->tFB) { r.why = "term kind"; ok = false; break; }
         const FormBilinear *bf = dynamic_cast<const FormBilinear *>(e);
         const CDomainOfIntegration &di = *bf->di;
-        if (di.d != d || di.dHat != d || !di.what.empty() || di.islevelset() || di.withmap()) {
-            r.why = "domain of integration"; ok = false; break;
+        if (boundary_domain(di, d)) {
+            BoundaryRec br;
+            if (!read_boundary_bilinear(stack, Th, Uh, di, *bf->b, r.fe, br, r.why)) { ok = false; break; }
+            r.bterms.push_back(br);
+            continue;
         }
+        if (!volume_domain(di, d)) { r.why = "domain of integration"; ok = false; break; }
         if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { r.why = "integration mesh"; ok = false; break; }
         const int ex = exactness(stack, di, &Th);
         const BilinearOperator &op = *bf->b;
@@ -397,6 +551,13 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         else std::cout << " kappa-check " << std::setprecision(17) << ksum << " mass " << r.c_mass;
         std::cout << " tgv " << ds.tgv << " components " << r.comp_mask << " labels";
         for (size_t i = 0; i < r.labels.size(); ++i) std::cout << " " << r.labels[i];
+        for (size_t t = 0; t < r.bterms.size(); ++t) {
+            double rs = 0;
+            for (size_t e = 0; e < r.bterms[t].robin.size(); ++e) rs += r.bterms[t].robin[e] * (double)(e % 7 + 1);
+            std::cout << " | robin-check " << std::setprecision(17) << rs << " on";
+            if (r.bterms[t].labels.empty()) std::cout << " all";
+            for (size_t i = 0; i < r.bterms[t].labels.size(); ++i) std::cout << " " << r.bterms[t].labels[i];
+        }
         std::cout << std::setprecision(6) << std::endl;
     }
     std::vector<double> X;
@@ -418,6 +579,8 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         dump(p + "/belems.bin", BE.data(), BE.size() * sizeof(int32_t));
         dump(p + "/blabel.bin", BL.data(), BL.size() * sizeof(int32_t));
         dump(p + "/kappa.bin", r.kappa.data(), r.kappa.size() * sizeof(double));
+        for (size_t t = 0; t < r.bterms.size(); ++t)
+            dump(p + "/robin" + std::to_string(t) + ".bin", r.bterms[t].robin.data(), r.bterms[t].robin.size() * sizeof(double));
     }
     ffgpu_ctx *ctx = context();
     ffgpu_space *S = nullptr;
@@ -436,6 +599,9 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
             v.kappa = r.kappa.data();
             v.c_mass = r.c_mass;
         }
+        const std::vector<ffgpu_bterm> bt = c_bterms(r.bterms);
+        v.nbterms = (int)bt.size();
+        v.bterms = bt.empty() ? nullptr : bt.data();
         ffgpu_bc bc;
         memset(&bc, 0, sizeof(bc));
         bc.tgv = ds.tgv;
@@ -509,6 +675,7 @@ struct RecognisedRhs {
     int fe = 0;
     std::vector<double> f;        // nt x ncomp
     std::vector<int32_t> labels;
+    std::vector<BoundaryRec> bterms;   // boundary sources, in varf order
     double g[3] = {0, 0, 0};      // on(...) values per component
     int comp_mask = -1;
     std::string why;
@@ -551,9 +718,13 @@ static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th,
         if (t != tvf->tFL) { r.why = "term kind"; ok = false; break; }
         const FormLinear *lf = dynamic_cast<const FormLinear *>(e);
         const CDomainOfIntegration &di = *lf->di;
-        if (di.d != d || di.dHat != d || !di.what.empty() || di.islevelset() || di.withmap()) {
-            r.why = "domain of integration"; ok = false; break;
+        if (boundary_domain(di, d)) {
+            BoundaryRec br;
+            if (!read_boundary_linear(stack, Th, Uh, di, *lf->l, r.fe, br, r.why)) { ok = false; break; }
+            r.bterms.push_back(br);
+            continue;
         }
+        if (!volume_domain(di, d)) { r.why = "domain of integration"; ok = false; break; }
         if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { r.why = "integration mesh"; ok = false; break; }
         if (exactness(stack, di, &Th) < (r.fe == FFGPU_FE_P1 ? 1 : 2)) { r.why = "quadrature not exact"; ok = false; break; }
         const Ftest &ft = *lf->l;
@@ -599,7 +770,15 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
         double fs = 0;
         for (size_t k = 0; k < r.f.size(); ++k) fs += r.f[k] * (double)(k % 7 + 1);
         std::cout << "  ffgpu: device linear form " << fe_name(r.fe) << " dim " << d << " f-check " << std::setprecision(17)
-                  << fs << " g " << r.g[0] << std::setprecision(6) << " tgv " << tgv << std::endl;
+                  << fs << " g " << r.g[0] << std::setprecision(6) << " tgv " << tgv;
+        for (size_t t = 0; t < r.bterms.size(); ++t) {
+            double gs = 0;
+            for (size_t e = 0; e < r.bterms[t].g.size(); ++e) gs += r.bterms[t].g[e] * (double)(e % 7 + 1);
+            std::cout << " | g-check " << std::setprecision(17) << gs << std::setprecision(6) << " on";
+            if (r.bterms[t].labels.empty()) std::cout << " all";
+            for (size_t i = 0; i < r.bterms[t].labels.size(); ++i) std::cout << " " << r.bterms[t].labels[i];
+        }
+        std::cout << std::endl;
     }
     std::vector<double> X;
     std::vector<int32_t> E, BE, BL;
@@ -622,6 +801,9 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
         v.c_stiff = 1.0;
         v.E = 1.0;
         v.f = r.f.data();
+        const std::vector<ffgpu_bterm> bt = c_bterms(r.bterms);
+        v.nbterms = (int)bt.size();
+        v.bterms = bt.empty() ? nullptr : bt.data();
         ffgpu_bc bc;
         memset(&bc, 0, sizeof(bc));
         bc.tgv = tgv;

@@ -209,3 +209,77 @@ matrix A=a(Vh,Vh);
     r, out = run_script(plugin, "p1k.edp", body)
     ksum = [l for l in r.stdout.splitlines() if l.startswith("ksum ")][0].split()[1]
     assert f"ffgpu: device assembly P1 dim 2 nt 72 ndof 49 kappa-check {ksum} mass 0" in out
+
+
+def test_boundary_terms_in_the_device_hook(plugin, tmp_path):
+    """int1d / boundary int2d terms: Robin c*u*v into the device matrix, g*v into the device
+    linear form, per boundary element in FreeFEM's boundary order (checksums below); terms the
+    device does not assemble stay FreeFEM's."""
+    import numpy as np
+    from ffgpu import mesh
+    body = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int1d(Th,3)(2.5*u*v) + int2d(Th)(1.*v) + int1d(Th,2)((1+y)*v) + on(1,4,u=0);
+matrix A=a(Vh,Vh);
+"""
+    d1 = tmp_path / "bt"
+    d1.mkdir()
+    r, out = run_script(plugin, "bt.edp", body, {"FFGPU_PLUGIN_DUMP": str(d1)})
+    Th = mesh.square(6)
+    w = np.arange(Th.nbe) % 7 + 1
+    rob = np.where(Th.blabel == 3, 2.5, 0.0)
+    assert f"| robin-check {'%.17g' % (rob * w).sum()} on 3" in out, out[-3000:]
+    assert np.array_equal(np.fromfile(d1 / "robin0.bin", np.float64), rob)
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+    # the linear form: g = 1 + y is not constant on the right edges -> FreeFEM; 1 + x is
+    body2 = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(1.*v) + int1d(Th,2)((1+y)*v) + on(1,4,u=0);
+real[int] b=a(0,Vh);
+varf a2(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(1.*v) + int1d(Th,2)((1+x)*v) + int1d(Th,3)((2+y)*v) + on(1,4,u=0);
+real[int] b2=a2(0,Vh);
+"""
+    r, out = run_script(plugin, "bt2.edp", body2)
+    assert "ffgpu: linear form assembled by FreeFEM (boundary source not constant on boundary elements)" in out
+    # right edges (x = 1): 1 + x = 2; top edges (y = 1): 2 + y = 3
+    g2 = np.where(Th.blabel == 2, 2.0, 0.0)
+    g3 = np.where(Th.blabel == 3, 3.0, 0.0)
+    assert (f"| g-check {'%.17g' % (g2 * w).sum()} on 2 | g-check {'%.17g' % (g3 * w).sum()} on 3" in out), out[-3000:]
+
+
+def test_boundary_terms_3d_and_rejections(plugin):
+    import numpy as np
+    from ffgpu import mesh
+    body = r"""
+load "msh3"
+mesh3 Th=cube(3,3,2);
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)=int3d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v)) + int2d(Th,2)(2.*u*v) + on(4,u=0);
+matrix A=a(Vh,Vh);
+"""
+    r, out = run_script(plugin, "bt3.edp", body)
+    Th = mesh.cube(3, 3, 2)
+    w = np.arange(Th.nbe) % 7 + 1
+    rob = np.where(Th.blabel == 2, 2.0, 0.0)
+    assert "ffgpu: device assembly P2 dim 3" in out and f"| robin-check {'%.17g' % (rob * w).sum()} on 2" in out
+    body2 = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int1d(Th,2)(dx(u)*v) + on(1,4,u=0);
+matrix A=a(Vh,Vh);
+cout << "nnzA " << A.nnz << endl;
+varf a2(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int1d(Th,2,qfe=qf1pE)(u*v) + on(1,4,u=0);
+matrix A2=a2(Vh,Vh);
+cout << "nnzA2 " << A2.nnz << endl;
+"""
+    r, out = run_script(plugin, "bt4.edp", body2)
+    assert r.returncode == 0, out[-2000:]
+    assert "ffgpu: form assembled by FreeFEM (boundary term other than c*u*v)" in out
+    assert "ffgpu: form assembled by FreeFEM (boundary quadrature not exact)" in out
