@@ -24,6 +24,8 @@ EXPORTS = [
     "ffgpu_rhs_assemble", "ffgpu_matrix_from_csr", "ffgpu_matrix_destroy", "ffgpu_matrix_info",
     "ffgpu_matrix_spmv_layout",
     "ffgpu_matrix_time_spmv",
+    "ffgpu_matrix_text_read",
+    "ffgpu_matrix_text_write",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
@@ -102,6 +104,8 @@ def lib():
         "ffgpu_matrix_info": (i32, [vp, P(i32), P(i64), P(i32)]),
         "ffgpu_matrix_spmv_layout": (i32, [vp, i32]),
         "ffgpu_matrix_time_spmv": (i32, [vp, i32, i32, P(C.c_float)]),
+        "ffgpu_matrix_text_read": (i32, [C.c_char_p, P(i32), P(i32), P(i64), P(i32), vp, vp, vp]),
+        "ffgpu_matrix_text_write": (i32, [C.c_char_p, i32, i32, i32, i32, vp, vp, vp]),
         "ffgpu_matrix_csr": (i32, [vp, vp, vp, vp]),
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),

@@ -364,6 +364,11 @@ class Matrix:
             return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + ("-deep" if v >= 66 else "")
         return f"bsr/{v}"
 
+    def save(self, path, format="coo"):
+        """``ofstream f(path); f << A;``: FreeFEM's text form of the matrix (sorted)."""
+        rp, cl, vl = self.csr()
+        write_matrix_text(path, rp, cl, vl, format=format)
+
     def time_spmv(self, mode=0, nrep=20):
         """Mean device time (ms) of nrep back-to-back launches of the solver's SpMV kernel for
         mode 0/1/2 (see spmv_layout), CUDA events on the library stream; solve in that mode first."""
@@ -423,6 +428,70 @@ def rhs(varf: VarForm, Vh, out=None, device=0):
     bc = varf.c_bc(V, device_marking=space.has_boundary)
     check(lib().ffgpu_rhs_assemble(space.h, C.byref(v), C.byref(bc), _ptr(out)))
     return out
+
+
+# ------------------------------------------------------------------ FreeFEM's text forms
+_TEXT_FORMATS = {"coo": 0, "morse": 1}
+
+
+def read_matrix_text(path):
+    """``matrix A; ifstream f(path); f >> A;``: FreeFEM's "(COO)" or "(Morse)" text form ->
+    (n, m, half, rowptr, col, val), sorted CSR (a repeated entry keeps its last value)."""
+    n, m, half = C.c_int(), C.c_int(), C.c_int()
+    nnz = C.c_int64()
+    bp = str(path).encode()
+    check(lib().ffgpu_matrix_text_read(bp, C.byref(n), C.byref(m), C.byref(nnz), C.byref(half),
+                                       None, None, None))
+    rp = np.empty(n.value + 1, np.int32)
+    cl = np.empty(nnz.value, np.int32)
+    vl = np.empty(nnz.value, np.float64)
+    check(lib().ffgpu_matrix_text_read(bp, C.byref(n), C.byref(m), C.byref(nnz), C.byref(half),
+                                       _ptr(rp), _ptr(cl), _ptr(vl)))
+    return n.value, m.value, half.value, rp, cl, vl
+
+
+def write_matrix_text(path, rowptr, col, val, m=None, half=0, format="coo"):
+    """``ofstream f(path); f << A;`` for a sorted CSR: format "coo" (FreeFEM's default print of
+    a sorted matrix) or "morse"."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    cl = np.ascontiguousarray(col, np.int32)
+    vl = np.ascontiguousarray(val, np.float64)
+    n = rp.size - 1
+    check(lib().ffgpu_matrix_text_write(str(path).encode(), _TEXT_FORMATS[format], n,
+                                        n if m is None else int(m), int(half), _ptr(rp), _ptr(cl), _ptr(vl)))
+
+
+def read_vector_text(path):
+    """``real[int] b(n); ifstream f(path); f >> b;`` (RNM_tpl.hpp:112-125): the length, then the
+    values."""
+    with open(path) as f:
+        tok = f.read().split()
+    n = int(tok[0])
+    if len(tok) < n + 1:
+        raise ValueError(f"{path}: {len(tok) - 1} values for a vector of length {n}")
+    return np.array([float(t) for t in tok[1:n + 1]])
+
+
+def write_vector_text(path, v, digits=17):
+    """``ofstream f(path); f << b;`` (RNM_tpl.hpp:100-110: the length, then five values per
+    line); `digits` significant digits (FreeFEM writes at least 10)."""
+    v = np.asarray(v, np.float64)
+    parts = [f"{v.size}\t\n\t"]
+    for i, x in enumerate(v):
+        x = 0.0 if abs(x) < 1e-305 else float(x)
+        parts.append(f"{x:3.{digits}g}" + ("\n\t" if i % 5 == 4 else "\t"))
+    with open(path, "w") as f:
+        f.write("".join(parts) + "\n")
+
+
+def matrix_from_file(path, solver="CG", eps=1e-6, tgv=1e30, device=0) -> Matrix:
+    """A matrix FreeFEM wrote (``f << A``) loaded into the device solver."""
+    n, m, half, rp, cl, vl = read_matrix_text(path)
+    if n != m:
+        raise ValueError(f"{path}: {n} x {m} matrix, the solvers need a square one")
+    if half:
+        raise ValueError(f"{path}: half (symmetric) storage; the device path keeps full storage")
+    return matrix_from_csr(rp, cl, vl, solver=solver, eps=eps, tgv=tgv, device=device)
 
 
 def matrix_from_csr(rowptr, col, val, solver="CG", eps=1e-6, tgv=1e30, device=0) -> Matrix:

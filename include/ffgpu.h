@@ -163,6 +163,20 @@ int ffgpu_matrix_reassemble(ffgpu_matrix *A, const ffgpu_varf *varf, const ffgpu
  * (src/fflib/problem.hpp:1351-1388, src/fflib/problem.cpp:7839-7911,10555). */
 int ffgpu_rhs_assemble(ffgpu_space *space, const ffgpu_varf *varf, const ffgpu_bc *bc,
                        double *rhs);
+/* FreeFEM's sparse-matrix text forms, host only (no device, no context):
+ * ffgpu_matrix_text_read replaces HashMatrix(istream&) (HashMatrix.cpp:137-214, `f >> A`):
+ * reads the "(COO)" form FreeFEM prints by default and the "(Morse)" CSR form; entries are
+ * assigned (a repeated (i, j) keeps its last value); returns the sorted CSR.  Call with
+ * rowptr == NULL for n, m, nnz, half, then with rowptr[n+1], col[nnz], val[nnz].
+ * ffgpu_matrix_text_write replaces operator<<(ostream&, HashMatrix) (HashMatrix.hpp:484-520,
+ * `f << A` and solve(..., save=)) for a sorted CSR: FFGPU_TEXT_COO (0-based, as FreeFEM prints
+ * a sorted matrix) or FFGPU_TEXT_MORSE (1-based), values at 20 significant digits. */
+#define FFGPU_TEXT_COO 0
+#define FFGPU_TEXT_MORSE 1
+int ffgpu_matrix_text_read(const char *path, int *n, int *m, int64_t *nnz, int *half, int32_t *rowptr,
+                           int32_t *col, double *val);
+int ffgpu_matrix_text_write(const char *path, int format, int n, int m, int half, const int32_t *rowptr,
+                            const int32_t *col, const double *val);
 /* matrix from a sorted CSR (the addsolver path: HashMatrix::CSR, HashMatrix.cpp:859-867) */
 int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *rowptr,
                           const int32_t *col, const double *val, ffgpu_matrix **out);

@@ -287,6 +287,22 @@ for (int k=0;k<Th.nv;k++) cout << "G uT " << u[][k] << endl;
     return body, {"kappa.txt": kap}
 
 
+def case_text_io(n):
+    """FreeFEM's own text forms of a matrix and a vector (``f << A``, ``f << b``) next to the
+    sorted COO and the values, for the readers of those forms."""
+    body = HEAD + f"""
+mesh Th=square({n},{n});
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)((1+x)*v) + on(1,2,u=0);
+matrix A=a(Vh,Vh);
+real[int] b=a(0,Vh);
+{{ ofstream f("A_coo.txt"); f << A; }}
+{{ ofstream f("b.txt"); f << b; }}
+""" + DUMP_A + "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << b[k] << endl;\n"
+    return body, {}
+
+
 BT_VARF2 = {
     "P1": "int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int1d(Th,3)(2.5*u*v) + int2d(Th)(1.*v) + int1d(Th,2)(gk*v) + int1d(Th,3)(-0.75*v) + on(1,4,u=0)",
 }
@@ -369,6 +385,7 @@ CASES = {
     "p1sq_n6_tgvp": lambda: case_p1_square_tgv(6, 1e30, "CG"),
     "adj_p1_n8": lambda: case_adjoint_p1(8, seed=31),
     "heat_p1_n6": lambda: case_heat_p1(6, 10, 1e-2, seed=41),
+    "io_p1sq_n4": lambda: case_text_io(4),
     "bt_p1sq_6x5": lambda: case_bterms("P1", (6, 5), seed=51),
     "bt_p2sq_5x4": lambda: case_bterms("P2", (5, 4), seed=52),
     "bt_p1cube_3x3x2": lambda: case_bterms("P1", (3, 3, 2), seed=53),
@@ -435,6 +452,10 @@ def run_case(name: str) -> None:
         if p.returncode != 0:
             raise RuntimeError(f"{name}: FreeFEM failed\n{p.stdout[-2000:]}\n{p.stderr[-2000:]}")
         res = parse(p.stdout)
+        for fn in ("A_coo.txt", "b.txt"):
+            if os.path.exists(os.path.join(td, fn)):
+                with open(os.path.join(td, fn)) as f:
+                    res["text_" + fn.split(".")[0]] = np.array(f.read())
         for fn, arr in files.items():
             res["in_" + fn.split(".")[0]] = np.asarray(arr, dtype=np.float64)
         res["edp"] = np.array(body)

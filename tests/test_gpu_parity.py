@@ -342,3 +342,25 @@ def test_bad_inputs_rejected_on_host_or_device():
         ffgpu.DeviceSpace(Vh, dof=bad)
     with pytest.raises(ffgpu.FFGPUError):
         ffgpu.matrix(ffgpu.varf_elasticity(f=1.0, on=(1,)), Vh)   # elasticity on a scalar space
+
+
+def test_matrix_from_freefem_text_file_and_save(tmp_path):
+    """A matrix in FreeFEM's text form (f << A) solved on the device; a device matrix saved in
+    that form reads back unchanged."""
+    d, sc = load("p1sq_n16")
+    n = d["b"].size
+    rp = np.concatenate([[0], np.cumsum(np.bincount(d["I"], minlength=n))]).astype(np.int32)
+    p = tmp_path / "A.txt"
+    ffgpu.write_matrix_text(p, rp, d["J"], d["C"])
+    A = ffgpu.matrix_from_file(p, eps=1e-10)
+    u = A.solve(d["b"])
+    assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
+    assert abs(A.stats.iterations - int(sc["nit"])) <= 2
+    c = case("p2el_n2")
+    Vh = FESpace(c["Th"], c["kind"])
+    B = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10)
+    for fmt in ("coo", "morse"):
+        B.save(tmp_path / f"B_{fmt}.txt", format=fmt)
+        n2, m2, half, rp2, cl2, vl2 = ffgpu.read_matrix_text(tmp_path / f"B_{fmt}.txt")
+        rpb, clb, vlb = B.csr()
+        assert np.array_equal(rp2, rpb) and np.array_equal(cl2, clb) and np.array_equal(vl2, vlb)
