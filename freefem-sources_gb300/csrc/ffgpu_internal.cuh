@@ -211,6 +211,8 @@ struct DevOut {
 int check_device_status(ffgpu_ctx *ctx, const char *where);
 int launch_check(ffgpu_ctx *ctx, const char *what);
 int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n);  // exclusive, out[n]=total
+// status kBadIndex when an element lists a vertex outside [0, nv) (ffgpu_assembly.cu)
+__global__ void check_elems_kernel(const int32_t *elems, int64_t m, int nv, int *status);
 int device_max_i32(ffgpu_ctx *ctx, const int32_t *in, int n, int *host_max);
 // order[0..n): indices sorted by decreasing key (0 <= key <= maxkey), ties by increasing index
 int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxkey, int32_t *order);

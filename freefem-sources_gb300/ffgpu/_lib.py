@@ -26,6 +26,9 @@ EXPORTS = [
     "ffgpu_matrix_time_spmv",
     "ffgpu_matrix_text_read",
     "ffgpu_matrix_text_write",
+    "ffgpu_mesh_sizes",
+    "ffgpu_mesh_build",
+    "ffgpu_number_p2",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
@@ -106,6 +109,9 @@ def lib():
         "ffgpu_matrix_time_spmv": (i32, [vp, i32, i32, P(C.c_float)]),
         "ffgpu_matrix_text_read": (i32, [C.c_char_p, P(i32), P(i32), P(i64), P(i32), vp, vp, vp]),
         "ffgpu_matrix_text_write": (i32, [C.c_char_p, i32, i32, i32, i32, vp, vp, vp]),
+        "ffgpu_mesh_sizes": (i32, [i32, i32, i32, i32, P(i32), P(i32), P(i32)]),
+        "ffgpu_mesh_build": (i32, [vp, i32, i32, i32, i32, vp, vp, vp, vp]),
+        "ffgpu_number_p2": (i32, [vp, i32, i32, vp, vp, P(i32)]),
         "ffgpu_matrix_csr": (i32, [vp, vp, vp, vp]),
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),

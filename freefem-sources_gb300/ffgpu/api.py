@@ -430,6 +430,79 @@ def rhs(varf: VarForm, Vh, out=None, device=0):
     return out
 
 
+# ------------------------------------------------------------------ meshes and numbering on the device
+class _DeviceMeshInfo:
+    """Sizes of a mesh whose arrays live on the GPU (what DeviceSpace and VarForm read)."""
+
+    def __init__(self, dim, nv, nt, nbe):
+        self.dim, self.nv, self.nt, self.nbe = dim, nv, nt, nbe
+
+
+class _DeviceSpaceInfo:
+    """FE-space metadata of a device-built space (kind, element code, DOFs)."""
+
+    def __init__(self, Th, kind, ndof):
+        self.Th, self.kind = Th, kind
+        self.fe = {"P1": 1, "P2": 2, "P2vec": 3}[kind]
+        self.bs = 3 if kind == "P2vec" else 1
+        nn = Th.dim + 1 if kind == "P1" else (10 if Th.dim == 3 else 6)
+        self.ndofK = nn * self.bs
+        self.ndof = ndof
+
+
+def device_mesh(dim, nx, ny=None, nz=None, device=0):
+    """FreeFEM's square(nx, ny) (dim 2) or cube(nx, ny, nz) (dim 3) built on the GPU: a dict of
+    torch tensors on the device (coords, elems, belems, blabel) and the sizes."""
+    import torch
+    ny = nx if ny is None else ny
+    nz = (nx if nz is None else nz) if dim == 3 else 0
+    nv, nt, nbe = C.c_int(), C.c_int(), C.c_int()
+    check(lib().ffgpu_mesh_sizes(dim, nx, ny, nz, C.byref(nv), C.byref(nt), C.byref(nbe)))
+    dev = torch.device("cuda", device)
+    X = torch.empty((nv.value, dim), dtype=torch.float64, device=dev)
+    E = torch.empty((nt.value, dim + 1), dtype=torch.int32, device=dev)
+    BE = torch.empty((nbe.value, dim), dtype=torch.int32, device=dev)
+    BL = torch.empty(nbe.value, dtype=torch.int32, device=dev)
+    check(lib().ffgpu_mesh_build(context(device), dim, nx, ny, nz, _ptr(X), _ptr(E), _ptr(BE), _ptr(BL)))
+    return dict(dim=dim, nv=nv.value, nt=nt.value, nbe=nbe.value, coords=X, elems=E, belems=BE, blabel=BL)
+
+
+def number_p2(elems, nv, device=0):
+    """FreeFEM's first-encounter P2 node table of a tetrahedral mesh, computed on the GPU:
+    (nodes (nt, 10) int32 on the device, node count)."""
+    import torch
+    E = elems if hasattr(elems, "data_ptr") else torch.as_tensor(np.ascontiguousarray(elems, np.int32),
+                                                                  device=torch.device("cuda", device))
+    nt = E.shape[0]
+    nodes = torch.empty((nt, 10), dtype=torch.int32, device=E.device)
+    nn = C.c_int()
+    check(lib().ffgpu_number_p2(context(device), int(nv), nt, _ptr(E), _ptr(nodes), C.byref(nn)))
+    return nodes, nn.value
+
+
+def device_space(kind, dim, nx, ny=None, nz=None, device=0):
+    """``fespace Vh(square(...)/cube(...), kind)`` with the mesh, the DOF numbering and the space
+    built on the GPU (no host arrays): a DeviceSpace for ffgpu.matrix / ffgpu.rhs."""
+    import torch
+    m = device_mesh(dim, nx, ny, nz, device)
+    Th = _DeviceMeshInfo(dim, m["nv"], m["nt"], m["nbe"])
+    if kind == "P1":
+        dof, ndof = m["elems"], m["nv"]
+    elif dim == 3 and kind in ("P2", "P2vec"):
+        nodes, nn = number_p2(m["elems"], m["nv"], device)
+        if kind == "P2":
+            dof, ndof = nodes, nn
+        else:
+            n3 = 3 * nodes
+            dof, ndof = torch.cat([n3, n3 + 1, n3 + 2], dim=1).contiguous(), 3 * nn
+    else:
+        raise NotImplementedError("on the device: P1 (2D, 3D), P2 and [P2,P2,P2] on tetrahedra")
+    S = DeviceSpace(_DeviceSpaceInfo(Th, kind, ndof), device=device, coords=m["coords"], elems=m["elems"],
+                    dof=dof, belems=m["belems"], blabel=m["blabel"])
+    S.arrays = dict(m, dof=dof)
+    return S
+
+
 # ------------------------------------------------------------------ FreeFEM's text forms
 _TEXT_FORMATS = {"coo": 0, "morse": 1}
 

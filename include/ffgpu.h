@@ -146,6 +146,21 @@ int ffgpu_space_set_boundary(ffgpu_space *space, int nbe, const int32_t *belems,
 int ffgpu_space_bc_mask(ffgpu_space *space, int nlabels, const int32_t *labels, int comp_mask,
                         uint8_t *onbc);
 
+/* FreeFEM's structured meshes on [0,1]^dim, built on the device into caller arrays (host or
+ * device): square(nx, ny) (Carre_, src/fflib/lgmesh.cpp:1229-1384) for dim 2 and
+ * cube(nx, ny, nz) (BuildCube, src/fflib/msh3.cpp:7879-8132, 6 tetrahedra per hexahedron) for
+ * dim 3, with FreeFEM's vertex, element and boundary-element order and labels.
+ * coords[nv*dim], elems[nt*(dim+1)], belems[nbe*dim], blabel[nbe]; sizes from ffgpu_mesh_sizes. */
+int ffgpu_mesh_sizes(int dim, int nx, int ny, int nz, int *nv, int *nt, int *nbe);
+int ffgpu_mesh_build(ffgpu_ctx *ctx, int dim, int nx, int ny, int nz, double *coords, int32_t *elems,
+                     int32_t *belems, int32_t *blabel);
+/* P2 node table of a tetrahedral mesh on the device (host or device arrays): FreeFEM's
+ * first-encounter numbering over the element slots (4 vertices, then the edges
+ * 01 02 03 12 13 23) of GenericMesh::BuildDFNumbering (src/femlib/GenericMesh.hpp:1878-1929).
+ * nodes[nt*10]; *nnodes = the node count.  (2D P2 spaces are Gibbs-renumbered by FreeFEM,
+ * gibbs.cpp:1094: pass FreeFEM's table.) */
+int ffgpu_number_p2(ffgpu_ctx *ctx, int nv, int nt, const int32_t *elems, int32_t *nodes, int *nnodes);
+
 /* ------------------------------------------------------------------ assembly
  * matrix A = a(Vh,Vh, ...): replaces OpMatrixtoBilinearForm::Op::operator() /
  * AssembleBilinearForm / HashMatrix::operator+= / AssembleBC+SetBC
