@@ -255,6 +255,9 @@ inline SellArgs sell_args(const ffgpu_matrix *A) {
 }
 // Persistent grid of a kernel: resident blocks per SM (occupancy calculator) x SMs
 int resident_grid(const void *kernel, int threads, size_t smem = 0);
+// the resident grid capped to `need` blocks: small problems get fewer, fuller blocks and a
+// shorter cross-block reduction
+int sized_grid(const void *kernel, int threads, int64_t need, size_t smem = 0);
 
 // matrix-level operations shared by the solvers
 int matrix_prepare_solver(ffgpu_matrix *A);

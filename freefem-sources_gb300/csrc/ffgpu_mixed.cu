@@ -260,6 +260,13 @@ static void *ir_ka_fn(const ffgpu_matrix *A, int kind) {
                       (void *)ir_ka<3, false, 0, true>, (void *)ir_ka<3, false, 1, true>}};
     return t[A->bs == 3 ? 2 : (A->scol16 ? 1 : 0)][code];
 }
+// grids: the FP32 K_a by the chunks it has to take, the vector kernels by the n/4 float4 quads
+static int ir_ka_grid(const ffgpu_matrix *A, const void *ka) {
+    return sized_grid(ka, kMxWarps * 32, ((int64_t)A->nchunk + kMxWarps - 1) / kMxWarps);
+}
+static int ir_vec_grid(const void *k, int n) {
+    return min(4096, sized_grid(k, kMxThreads, ((int64_t)n / 4 + kMxThreads - 1) / kMxThreads));
+}
 static bool ir_ranges(const ffgpu_matrix *A) {
     return !A->sell32_kind || ((A->sell32_kind - kSellCode) & 1) == kSellRanges;
 }
@@ -270,10 +277,10 @@ static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditional
     SellArgs sa = sell_args(A);
     const float *sv = A->sval32;
     void *ka = ir_ka_fn(A, A->sell32_kind);
-    const int gka = resident_grid(ka, kMxWarps * 32);
+    const int gka = ir_ka_grid(A, ka);
     if (ir_ranges(A)) FFGPU_TRY(sell_partition(A, gka * kMxWarps, &sa.part));
-    const int gkb = min(4096, resident_grid((const void *)ir_kb, kMxThreads));
-    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
+    const int gkb = ir_vec_grid((const void *)ir_kb, A->n);
+    const int gkc = ir_vec_grid((const void *)ir_kc, A->n);
     float *part = (float *)A->ctx->d_part;
     int n = A->n;
     for (int u = 0; u < unroll; ++u) {
@@ -309,7 +316,7 @@ static int ir_tune(ffgpu_matrix *A, IRState &S) {
         SellArgs sa = sell_args(A);
         const float *sv = A->sval32;
         void *ka = ir_ka_fn(A, kinds[kk]);
-        const int g = resident_grid(ka, kMxWarps * 32);
+        const int g = ir_ka_grid(A, ka);
         if ((kk & 1) == kSellRanges) FFGPU_TRY(sell_partition(A, g * kMxWarps, &sa.part));
         float *part = (float *)ctx->d_part;
         void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
@@ -349,7 +356,7 @@ int ir_time_ka(ffgpu_matrix *A, int nrep, float *ms) {
     SellArgs sa = sell_args(A);
     const float *sv = A->sval32;
     void *ka = ir_ka_fn(A, A->sell32_kind);
-    const int g = resident_grid(ka, kMxWarps * 32);
+    const int g = ir_ka_grid(A, ka);
     int rc = FFGPU_OK;
     if (ir_ranges(A)) rc = sell_partition(A, g * kMxWarps, &sa.part);
     float t = 0;
@@ -385,7 +392,7 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     // the warp partition is built before the capture starts (no allocation inside a capture)
     if (ir_ranges(A)) {
         const int32_t *part = nullptr;
-        FFGPU_TRY(sell_partition(A, resident_grid(ir_ka_fn(A, A->sell32_kind), kMxWarps * 32) * kMxWarps, &part));
+        FFGPU_TRY(sell_partition(A, ir_ka_grid(A, ir_ka_fn(A, A->sell32_kind)) * kMxWarps, &part));
     }
     cudaGraph_t graph, body;
     FFGPU_CUDA(cudaGraphCreate(&graph, 0));
@@ -482,7 +489,7 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     bool keep = prm->restart_inner == 0;
     float eps_in = (float)(prm->eps_inner > 0 ? prm->eps_inner : (keep ? 1e-2 : 1e-5));
     int first_its = -1;
-    const int gkc = min(4096, resident_grid((const void *)ir_kc, kMxThreads));
+    const int gkc = ir_vec_grid((const void *)ir_kc, n);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -18,6 +18,8 @@
 // matrix bandwidth allows (2 instead of 4 bytes per entry).
 #include <string.h>
 
+#include <algorithm>
+
 #include "ffgpu_internal.cuh"
 
 namespace ffgpu {
@@ -157,6 +159,11 @@ int resident_grid(const void *kernel, int threads, size_t smem) {
         per_sm < 1)
         per_sm = 1;
     return per_sm * kNumSM;
+}
+
+int sized_grid(const void *kernel, int threads, int64_t need, size_t smem) {
+    const int64_t g = resident_grid(kernel, threads, smem);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, need));
 }
 
 int sell_prepare(ffgpu_matrix *A) {

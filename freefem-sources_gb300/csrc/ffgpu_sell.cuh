@@ -236,35 +236,51 @@ struct SellDepth {
     static constexpr int B = BS == 1 ? (DEEP ? 16 : 8) : (F32 ? (DEEP ? 8 : 4) : (DEEP ? 4 : 2));
 };
 
-// FP64 rows keep a plain loop unrolled UNR deep: the kernel is bound by the FP64 pipe, and the
-// compiler's software pipelining of the unrolled loop (loads of later slots under the FMAs of
-// earlier ones) measured faster than the batched form on both the P1 and the [P2]^3 matrices.
-template <int BS, bool C16, bool DEEP>
+// FP64 rows: LOOP 0/1 keep a plain loop unrolled UNR deep -- the large FP64 kernels are bound by
+// the FP64 pipe, and the compiler's software pipelining of the unrolled loop (loads of later
+// slots under the FMAs of earlier ones) measured faster there than the batched form; LOOP 2/3
+// use the batched form (B = 8/16 slots, 2/4 blocks), which wins where latency, not the FP64
+// pipe, sets the time (small matrices, short rows).  The tuner times all four.
+struct AccF64 {
+    double s = 0;
+    __device__ __forceinline__ void fma_(double a, double x) { s = fma(a, x, s); }
+    __device__ __forceinline__ double get() const { return s; }
+};
+
+template <int BS, bool C16, int LOOP>
 __device__ __forceinline__ void sell_row64(const SellArgs &S, const double *__restrict__ val,
                                            const double *__restrict__ x, int L, int64_t sr, int lane, int a,
                                            double *y) {
-    const int ar = a < 0 ? 0 : a;
-    const int64_t ce = sr * 32 + lane;
-    const double *v = val + sr * (BS * BS * 32) + lane;
-    double s0 = 0, s1 = 0, s2 = 0;
-    // slots in flight (the column -> gather dependency): scalar rows 8 or 16, 3x3 blocks 2 or 4
-    constexpr int UNR = BS == 1 ? (DEEP ? 16 : 8) : (DEEP ? 4 : 2);
+    if constexpr (LOOP >= 2) {
+        AccF64 acc[BS];
+        sell_row<double, BS, SellDepth<BS, LOOP == 3>::B, C16>(S, val, x, L, sr, lane, a, acc);
+#pragma unroll
+        for (int m = 0; m < BS; ++m) y[m] = acc[m].get();
+        return;
+    } else {
+        const int ar = a < 0 ? 0 : a;
+        const int64_t ce = sr * 32 + lane;
+        const double *v = val + sr * (BS * BS * 32) + lane;
+        double s0 = 0, s1 = 0, s2 = 0;
+        // slots in flight (the column -> gather dependency): scalar rows 8 or 16, 3x3 blocks 2 or 4
+        constexpr int UNR = BS == 1 ? (LOOP ? 16 : 8) : (LOOP ? 4 : 2);
 #pragma unroll UNR
-    for (int j = 0; j < L; ++j) {
-        const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
-        if (BS == 1) {
-            s0 = fma(__ldcs(v + (int64_t)j * 32), __ldg(x + col), s0);
-        } else {
-            const double x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
-                         x2 = __ldg(x + 3 * (int64_t)col + 2);
-            const double *w = v + (int64_t)j * 288;
-            s0 = fma(__ldcs(w), x0, s0); s0 = fma(__ldcs(w + 32), x1, s0); s0 = fma(__ldcs(w + 64), x2, s0);
-            s1 = fma(__ldcs(w + 96), x0, s1); s1 = fma(__ldcs(w + 128), x1, s1); s1 = fma(__ldcs(w + 160), x2, s1);
-            s2 = fma(__ldcs(w + 192), x0, s2); s2 = fma(__ldcs(w + 224), x1, s2); s2 = fma(__ldcs(w + 256), x2, s2);
+        for (int j = 0; j < L; ++j) {
+            const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
+            if (BS == 1) {
+                s0 = fma(__ldcs(v + (int64_t)j * 32), __ldg(x + col), s0);
+            } else {
+                const double x0 = __ldg(x + 3 * (int64_t)col), x1 = __ldg(x + 3 * (int64_t)col + 1),
+                             x2 = __ldg(x + 3 * (int64_t)col + 2);
+                const double *w = v + (int64_t)j * 288;
+                s0 = fma(__ldcs(w), x0, s0); s0 = fma(__ldcs(w + 32), x1, s0); s0 = fma(__ldcs(w + 64), x2, s0);
+                s1 = fma(__ldcs(w + 96), x0, s1); s1 = fma(__ldcs(w + 128), x1, s1); s1 = fma(__ldcs(w + 160), x2, s1);
+                s2 = fma(__ldcs(w + 192), x0, s2); s2 = fma(__ldcs(w + 224), x1, s2); s2 = fma(__ldcs(w + 256), x2, s2);
+            }
         }
+        y[0] = s0;
+        if (BS == 3) { y[1] = s1; y[2] = s2; }
     }
-    y[0] = s0;
-    if (BS == 3) { y[1] = s1; y[2] = s2; }
 }
 
 template <int BS, bool C16, bool DEEP>

@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
 // ------------------------------------------------------------------ SELL-32 K_a
 // One block row per lane, one chunk of 32 rows per warp (resident grid, chunks strided over
 // warps).  FP64: AH = A H and (H, AH) -> rho; padding lanes (a < 0) write nothing.
-template <int BS, bool C16, int ASSIGN, bool DEEP>
+template <int BS, bool C16, int ASSIGN, int LOOP>
 __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const double *__restrict__ val,
                                                               const double *__restrict__ h, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
     double hq = 0;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double y[BS];
-        sell_row64<BS, C16, DEEP>(S, val, h, L, sr, lane, a, y);
+        sell_row64<BS, C16, LOOP>(S, val, h, L, sr, lane, a, y);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) {
@@ -413,13 +413,13 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
 }
 
 // y = A x (FP64)
-template <int BS, bool C16, int ASSIGN, bool DEEP>
+template <int BS, bool C16, int ASSIGN, int LOOP>
 __global__ void __launch_bounds__(kSpmvWarps * 32) spmv_sell(SellArgs S, const double *__restrict__ val,
                                                              const double *__restrict__ x, double *__restrict__ y) {
     const int lane = threadIdx.x & 31;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
         double r[BS];
-        sell_row64<BS, C16, DEEP>(S, val, x, L, sr, lane, a, r);
+        sell_row64<BS, C16, LOOP>(S, val, x, L, sr, lane, a, r);
         if (a >= 0) {
 #pragma unroll
             for (int m = 0; m < BS; ++m) y[(int64_t)BS * a + m] = r[m];
@@ -565,9 +565,17 @@ __global__ void transpose_kernel(int nb, int bs, const int32_t *brp, const int32
 // tuner codes of the SELL-32 kernels (one row per lane): 64 + chunk assignment
 // (sell_for_chunks) + 2 * deep unroll; block CSR is coded by its lanes per row
 constexpr int kSellCode = 64;
-static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 4; }
+// SELL codes: kSellCode + assign + 2 * loop; loop 0/1: unrolled row loop (plain, deep), 2/3
+// (FP64 kernels only): batched row loop (plain, deep)
+static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 8; }
 static int sell_assign(int T) { return (T - kSellCode) & 1; }
-static bool sell_deep(int T) { return (T - kSellCode) >> 1; }
+static int sell_loop(int T) { return (T - kSellCode) >> 1; }
+static const char *sell_name(int T) {
+    static const char *names[8] = {"sell32 ranges", "sell32 rotated", "sell32 ranges deep", "sell32 rotated deep",
+                                   "sell32 ranges batch", "sell32 rotated batch", "sell32 ranges batch deep",
+                                   "sell32 rotated batch deep"};
+    return names[T - kSellCode];
+}
 
 #define FFGPU_SELL_FN(K)                                                                             \
     static void *K##_fn(int bs, bool c16, int code) {                                               \
@@ -579,10 +587,25 @@ static bool sell_deep(int T) { return (T - kSellCode) >> 1; }
                           (void *)K<3, false, 0, true>, (void *)K<3, false, 1, true>}};               \
         return t[bs == 3 ? 2 : (c16 ? 1 : 0)][code - kSellCode];                                     \
     }
-FFGPU_SELL_FN(cg_ka_sell)
 FFGPU_SELL_FN(cg_kax_sell)
-FFGPU_SELL_FN(spmv_sell)
 #undef FFGPU_SELL_FN
+// FP64 kernels: the four row loops
+#define FFGPU_SELL64_FN(K)                                                                           \
+    static void *K##_fn(int bs, bool c16, int code) {                                               \
+        void *t[3][8] = {{(void *)K<1, false, 0, 0>, (void *)K<1, false, 1, 0>, (void *)K<1, false, 0, 1>,   \
+                          (void *)K<1, false, 1, 1>, (void *)K<1, false, 0, 2>, (void *)K<1, false, 1, 2>,   \
+                          (void *)K<1, false, 0, 3>, (void *)K<1, false, 1, 3>},                          \
+                         {(void *)K<1, true, 0, 0>, (void *)K<1, true, 1, 0>, (void *)K<1, true, 0, 1>,      \
+                          (void *)K<1, true, 1, 1>, (void *)K<1, true, 0, 2>, (void *)K<1, true, 1, 2>,      \
+                          (void *)K<1, true, 0, 3>, (void *)K<1, true, 1, 3>},                            \
+                         {(void *)K<3, false, 0, 0>, (void *)K<3, false, 1, 0>, (void *)K<3, false, 0, 1>,   \
+                          (void *)K<3, false, 1, 1>, (void *)K<3, false, 0, 2>, (void *)K<3, false, 1, 2>,   \
+                          (void *)K<3, false, 0, 3>, (void *)K<3, false, 1, 3>}};                         \
+        return t[bs == 3 ? 2 : (c16 ? 1 : 0)][code - kSellCode];                                     \
+    }
+FFGPU_SELL64_FN(cg_ka_sell)
+FFGPU_SELL64_FN(spmv_sell)
+#undef FFGPU_SELL64_FN
 
 // lanes per block row of the block-CSR kernels
 static int pick_lanes(const ffgpu_matrix *A) {
@@ -681,7 +704,7 @@ static int ka_setup(ffgpu_matrix *A, int mode, int trans, int T, const double *h
             k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.h; k.args[3] = &k.q; k.args[4] = &k.ks;
             k.args[5] = &k.part;
         }
-        k.grid = resident_grid(k.fn, kSpmvWarps * 32);
+        k.grid = sized_grid(k.fn, kSpmvWarps * 32, ((int64_t)A->nchunk + kSpmvWarps - 1) / kSpmvWarps);
         if (range) FFGPU_TRY(sell_partition(A, k.grid * kSpmvWarps, &k.sl.part));
         return FFGPU_OK;
     }
@@ -719,9 +742,10 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     // FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row;
     // double-float: reductions are FP32, so wider lane groups
     const int S0 = kSellCode;
-    const int cands64[] = {S0, S0 + 1, S0 + 2, S0 + 3, 1, 2, 4, 8};
+    const int cands64[] = {S0, S0 + 1, S0 + 2, S0 + 3, S0 + 4, S0 + 5, S0 + 6, S0 + 7, 1, 2, 4, 8};
     const int candsx[] = {S0, S0 + 1, S0 + 2, S0 + 3, 4, 8, 16, 32};
     const int *cands = mode == 1 ? candsx : cands64;
+    const int ncand = mode == 1 ? 8 : 12;
     const int64_t vs = vstride(A->n);
     double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
     cudaStream_t s = ctx->stream;
@@ -735,7 +759,7 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     cudaEventCreate(&e1);
     float best = 1e30f;
     int bestT = kSellCode;
-    for (int c = 0; c < 8; ++c) {
+    for (int c = 0; c < ncand; ++c) {
         const int T = cands[c];
         KaCall k;
         FFGPU_TRY(ka_setup(A, mode, 0, T, x, y, k));
@@ -751,9 +775,7 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
         if (getenv("FFGPU_VERBOSE"))
             fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s %.4f ms\n", mode,
                     A->nb, (long long)A->nnzb,
-                    is_sell(T) ? (sell_assign(T) == kSellRanges ? (sell_deep(T) ? "sell32 ranges deep" : "sell32 ranges")
-                                                                : (sell_deep(T) ? "sell32 rotated deep" : "sell32 rotated"))
-                               : "bsr lanes",
+                    is_sell(T) ? sell_name(T) : "bsr lanes",
                     ms / 3);
         if (ms < best) { best = ms; bestT = T; }
     }
@@ -780,7 +802,7 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
         const int code = is_sell(A->csr_lanes) ? A->csr_lanes : kSellCode;
         const bool range = sell_assign(code) == kSellRanges;
         void *fn = spmv_sell_fn(A->bs, A->scol16 != nullptr, code);
-        const int grid = resident_grid(fn, kSpmvWarps * 32);
+        const int grid = sized_grid(fn, kSpmvWarps * 32, ((int64_t)A->nchunk + kSpmvWarps - 1) / kSpmvWarps);
         if (range) FFGPU_TRY(sell_partition(A, grid * kSpmvWarps, &sl.part));
         void *args[] = {&sl, &sv, &x, &y};
         FFGPU_CUDA(cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, st));
@@ -857,16 +879,17 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
     return launch_check(ctx, "jacobi");
 }
 
-static int vec_grid_kb() {
+// grids of K_b / K_c: resident, at most 4096 blocks, no more than the n/2 double2 pairs need
+static int vec_grid_kb(int n) {
     static int g = 0;
     if (!g) g = min(4096, resident_grid((const void *)cg_kb, kVecThreads));
-    return g;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, ((int64_t)n / 2 + kVecThreads - 1) / kVecThreads));
 }
-static int vec_grid_kc() {
+static int vec_grid_kc(int n) {
     static int g = 0;
     if (!g) g = min(4096, max(resident_grid((const void *)cg_kc_t<false>, kVecThreads),
                               resident_grid((const void *)cg_kc_t<true>, kVecThreads)));
-    return g;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, ((int64_t)n / 2 + kVecThreads - 1) / kVecThreads));
 }
 
 // One CG iteration (K_a K_b K_c) on stream s.
@@ -874,11 +897,11 @@ static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h
                     float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
                     cudaStream_t s) {
     ka.launch(s);
-    cg_kb<<<vec_grid_kb(), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, in_graph);
+    cg_kb<<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, in_graph);
     if (mode == 1)
-        cg_kc_t<true><<<vec_grid_kc(), kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
+        cg_kc_t<true><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
     else
-        cg_kc_t<false><<<vec_grid_kc(), kVecThreads, 0, s>>>(n, g, h, nullptr, dinv, ks, part);
+        cg_kc_t<false><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, nullptr, dinv, ks, part);
 }
 
 // Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }].
@@ -889,8 +912,8 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     cudaStream_t s = ctx->stream;
     KaCall ka;
     FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
-    vec_grid_kb();
-    vec_grid_kc();
+    vec_grid_kb(A->n);
+    vec_grid_kc(A->n);
     cudaGraph_t graph, body;
     FFGPU_CUDA(cudaGraphCreate(&graph, 0));
     cudaGraphConditionalHandle cond;

@@ -355,13 +355,14 @@ class Matrix:
 
     def spmv_layout(self, mode=0):
         """The SpMV layout the tuner chose for mode 0 (FP64 CG), 1 (double-float CG) or 2 (FP32
-        inner solve): 'sell32' (chunk ranges) or 'sell32-rot', with '-deep' for the deeper unroll,
-        'bsr/T' (T lanes per block row) or None."""
+        inner solve): 'sell32' (chunk ranges) or 'sell32-rot', with '-deep' for the deeper unroll and
+        '-batch' / '-batch-deep' for the batched row loop, 'bsr/T' (T lanes per block row) or None."""
         v = int(lib().ffgpu_matrix_spmv_layout(self.h, int(mode)))
         if v <= 0:
             return None
-        if 64 <= v < 68:
-            return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + ("-deep" if v >= 66 else "")
+        if 64 <= v < 72:
+            loop = ["", "-deep", "-batch", "-batch-deep"][(v - 64) >> 1]
+            return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + loop
         return f"bsr/{v}"
 
     def save(self, path, format="coo"):

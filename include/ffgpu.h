@@ -199,9 +199,9 @@ int ffgpu_matrix_destroy(ffgpu_matrix *A);
 int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_size);
 /* SpMV layout the solver's tuner chose for this matrix: mode 0 (FP64 CG), 1 (double-float CG)
  * or 2 (FP32 inner solve of ffgpu_solve_ir).  Returns 64 + a + 2u for the SELL-32 copy, with
- * a = 0 for contiguous per-warp chunk ranges or 1 for a rotated chunk stride and u = 1 for the
- * deeper unroll of the row loop; T in {1,..,32} for block CSR with T lanes per block row; 0
- * before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences;
+ * a = 0 for contiguous per-warp chunk ranges or 1 for a rotated chunk stride, and the row loop
+ * u = 0 unrolled, 1 unrolled deeper, 2 batched, 3 batched deeper (2 and 3: FP64 only); T in
+ * {1,..,32} for block CSR with T lanes per block row; 0 before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences;
  * mode 4: block entries the SELL copy stores, padding included (32 per slot; -1 past INT32_MAX).
  * No FreeFEM counterpart. */
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
