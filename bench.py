@@ -215,6 +215,34 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ GPU arm
+# ------------------------------------------------------------------ replicas across ranks
+# One process per GPU (torchrun); no data-path collective: every rank assembles and solves its
+# own problem(s), the timings are bracketed by barriers and reduced by MAX, and the value counts
+# the DOFs of all ranks.
+def dist_max(values, world, device):
+    """Element-wise max over ranks of a list of timings (identity on one rank)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def dist_sum(values, world, device):
+    """Element-wise sum over ranks (the units all ranks processed)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    return t.tolist()
+
+
+def rank_device(rank, world):
+    return 0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank))
+
+
 def run_gpu(args, rank, world):
     import numpy as np
     import torch
@@ -223,7 +251,7 @@ def run_gpu(args, rank, world):
     build()
     cfgname = args.config
     cfg = CONFIGS[cfgname]
-    dev = 0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank))
+    dev = rank_device(rank, world)
     torch.cuda.set_device(dev)
     Th, Vh, a, _ = build_problem(cfg)
     ctx = ffgpu.context(dev)
@@ -394,10 +422,7 @@ def run_gpu(args, rank, world):
     # max over ranks
     t_step = total_ms / args.steps
     t_e2e = sum(e2e_times) / len(e2e_times)
-    if world > 1:
-        tt = torch.tensor([t_step, t_e2e], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step, t_e2e = tt.tolist()
+    t_step, t_e2e = dist_max([t_step, t_e2e], world, torch.device("cuda", dev))
     value = world * Vh.ndof / (t_step * 1e-3)
     e2e_value = world * Vh.ndof / (t_e2e * 1e-3)
     out = {
@@ -470,9 +495,11 @@ def profile_case(kind, n, iters, spmv_mode):
         del A, S
 
 
-def run_adjoint(args):
+def run_adjoint(args, rank=0, world=1):
     """dL/dkappa by the adjoint (forward CG, transpose CG, sensitivity kernel) on the device;
-    the heat variant with checkpoint-and-recompute; FD check on seeded elements."""
+    the heat variant with checkpoint-and-recompute; FD check on seeded elements.  A step is one
+    gradient evaluation (L, dL/dkappa, dL/df at kappa = 1, its forward solve included); on N
+    ranks every rank evaluates its own replica (weak scaling, no collective on the data path)."""
     import numpy as np
     import torch
     import ffgpu
@@ -484,13 +511,15 @@ def run_adjoint(args):
     n = cfg["mesh"][1]
     Th = ffgpu.square(n)
     Vh = FESpace(Th, "P1")
-    dev = torch.device("cuda", 0)
-    ffgpu.context(0)
-    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(0), device=0)
+    di = rank_device(rank, world)
+    dev = torch.device("cuda", di)
+    torch.cuda.set_device(dev)
+    ffgpu.context(di)
+    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(di), device=dev)
     cells = gaussian_field(n, cfg["ell"], cfg["sigma"], cfg["seed"])
     k_true = torch.from_numpy(np.exp(np.repeat(cells, 2))).to(dev)      # both triangles of a cell
     ones = torch.ones(Th.nt, dtype=torch.float64, device=dev)
-    P = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"])
+    P = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"], device=di)
     u_true = P.solve(k_true, 1.0)
     rng = np.random.Generator(np.random.PCG64(cfg["seed"] + 1))
     rms = float(torch.sqrt(torch.mean(u_true * u_true)))
@@ -500,29 +529,41 @@ def run_adjoint(args):
     def ev():
         return torch.cuda.Event(enable_timing=True)
 
-    fwd_ms, grad_ms = [], []
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        P.value_and_grad(kappa, 1.0, u_obs)
+    # the timed steps: K gradient evaluations between barriers
+    barrier()
+    l0 = ffgpu.kernel_launches(di)
     clocks = ClockSampler()
-    for k in range(args.warmup + args.steps):
-        if k == args.warmup:
-            l0 = ffgpu.kernel_launches()
-            clocks.start()
-        e0, e1, e2 = ev(), ev(), ev()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        u = P.solve(kappa, 1.0)
-        e1.record(stream)
-        it_fwd = P.A.stats.iterations
+    clocks.start()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(args.steps):
         L, gk, gf, u2, lam = P.value_and_grad(kappa, 1.0, u_obs)
-        e2.record(stream)
-        e2.synchronize()
-        if k >= args.warmup:
-            fwd_ms.append(e0.elapsed_time(e1))
-            grad_ms.append(e1.elapsed_time(e2))
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
     clk = clocks.stop()
-    launches = (ffgpu.kernel_launches() - l0) // args.steps
+    launches = ffgpu.kernel_launches(di) - l0
     it_adj = P.A.stats.iterations
+    t_grad = e0.elapsed_time(e1) / args.steps
+    # the forward solve alone, for the gradient / forward cost ratio
+    fwd_ms = []
+    for _ in range(args.steps):
+        f0, f1 = ev(), ev()
+        torch.cuda.synchronize(dev)
+        f0.record(stream)
+        P.solve(kappa, 1.0)
+        f1.record(stream)
+        f1.synchronize()
+        fwd_ms.append(f0.elapsed_time(f1))
+    it_fwd = P.A.stats.iterations
     t_fwd = statistics.median(fwd_ms)
-    t_grad = statistics.median(grad_ms)
     # central FD on seeded elements (host path of the same library), outside the timed region
     ek = rng.choice(Th.nt, size=cfg["nfd"], replace=False)
     gk_h = gk.cpu().numpy()
@@ -531,7 +572,7 @@ def run_adjoint(args):
     fd_err = float((np.abs(fd - gk_h[ek]) / np.maximum(np.abs(gk_h[ek]), floor)).max())
     # heat variant: forward alone, then forward + checkpointed backward
     H = adjoint.HeatProblem(Vh, dt=cfg["heat_dt"], nsteps=cfg["heat_steps"], on=cfg["on"],
-                            checkpoint=cfg["heat_checkpoint"], eps=cfg["eps"])
+                            checkpoint=cfg["heat_checkpoint"], eps=cfg["eps"], device=di)
     uN, _ = H.forward(k_true, 1.0, keep_checkpoints=False)
     h_obs = uN + cfg["noise"] * float(torch.sqrt(torch.mean(uN * uN))) * torch.from_numpy(
         rng.standard_normal(Vh.ndof)).to(dev)
@@ -549,7 +590,7 @@ def run_adjoint(args):
             hf.append((t1 - t0) * 1e3)
             hg.append((t2 - t1) * 1e3)
     # e2e: the same gradient from host arrays through the public API
-    P2 = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"])
+    P2 = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"], device=di)
     uo_h = u_obs.cpu().numpy()
     e2e = []
     for k in range(1 + args.steps):
@@ -558,9 +599,12 @@ def run_adjoint(args):
         if k >= 1:
             e2e.append((time.perf_counter() - t0) * 1e3)
     t_e2e = statistics.median(e2e)
-    value = Vh.ndof / (t_grad * 1e-3)
+    t_grad, t_e2e = dist_max([t_grad, t_e2e], world, dev)
+    if rank != 0:
+        return None
+    value = world * Vh.ndof / (t_grad * 1e-3)
     cb, _ = (None, None) if args.no_cpu_baseline else cpu_baseline(args.config, procs=1)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_grad, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": args.config, "mesh": f"square({n})", "fe": "P1", "ndof": Vh.ndof,
@@ -575,17 +619,20 @@ def run_adjoint(args):
                                "gradient_over_forward": statistics.median(hg) / statistics.median(hf),
                                "solves_gradient": H.solves},
                       "l2": "working set below L2 (square(512)); timing is of repeated gradients"},
-           "e2e": {"value": Vh.ndof / (t_e2e * 1e-3), "unit": UNIT,
+           "e2e": {"value": world * Vh.ndof / (t_e2e * 1e-3), "unit": UNIT,
                    "h2d_bytes_per_step": int(2 * Th.nt * 8 + Vh.ndof * 8),
                    "d2h_bytes_per_step": int(2 * Th.nt * 8 + 2 * Vh.ndof * 8), "ms_per_step": t_e2e},
-           "gpu_launches": int(launches) * args.steps, "clocks": clk, "roofline": None}
+           "gpu_launches": int(launches), "clocks": clk, "roofline": None,
+           "roofline_note": "square(512): matrix and vectors stay in L2 between kernels; no HBM roofline"}
     if cb:
         out["cpu_baseline"] = cb
     print(json.dumps(out))
 
 
-def run_batch(args):
-    """Batched independent problems: one assembly pass and one persistent solve per step."""
+def run_batch(args, rank=0, world=1):
+    """Batched independent problems: one assembly pass and one persistent solve per step.  On
+    N ranks every rank solves its own batch of the same size (seed + rank): weak scaling, no
+    collective on the data path; value = the DOFs of all ranks / the slowest rank's time."""
     import numpy as np
     import torch
     import ffgpu
@@ -593,22 +640,30 @@ def run_batch(args):
     from ffgpu.build import build
     build()
     cfg = CONFIGS[args.config]
-    meshes, kappas, Ns = batch.c5_meshes(cfg["nprob"], cfg["nmin"], cfg["nmax"], seed=cfg["seed"])
+    di = rank_device(rank, world)
+    dev = torch.device("cuda", di)
+    torch.cuda.set_device(dev)
+    meshes, kappas, Ns = batch.c5_meshes(cfg["nprob"], cfg["nmin"], cfg["nmax"], seed=cfg["seed"] + rank)
     ndof = int(sum(m.nv for m in meshes))
-    ffgpu.context(0)
-    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(0), device=0)
-    B = batch.Batch(meshes)
-    kap = torch.from_numpy(np.concatenate(kappas)).cuda()
-    x = torch.zeros(ndof, dtype=torch.float64, device="cuda")
+    ffgpu.context(di)
+    stream = torch.cuda.ExternalStream(ffgpu.stream_handle(di), device=dev)
+    B = batch.Batch(meshes, device=di)
+    kap = torch.from_numpy(np.concatenate(kappas)).to(dev)
+    x = torch.zeros(ndof, dtype=torch.float64, device=dev)
 
     def step():
         B.assemble(kap, f=1.0)
         return B.solve(eps=cfg["eps"], out=x)
 
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
     for _ in range(args.warmup):
         step()
-    torch.cuda.synchronize()
-    l0 = ffgpu.kernel_launches()
+    barrier()
+    l0 = ffgpu.kernel_launches(di)
     clocks = ClockSampler()
     clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -618,9 +673,12 @@ def run_batch(args):
         step()
     e1.record(stream)
     e1.synchronize()
+    barrier()
     clk = clocks.stop()
-    launches = ffgpu.kernel_launches() - l0
+    launches = ffgpu.kernel_launches(di) - l0
     ms = e0.elapsed_time(e1) / args.steps
+    ms, = dist_max([ms], world, dev)
+    ndof_all, = dist_sum([ndof], world, dev)
     solve_ms = B.stats.elapsed_ms
     nt_, lanes, tms = B.tuned()
     # accuracy against the FP64 oracle on a sample of problems
@@ -639,13 +697,17 @@ def run_batch(args):
         uo, it, r, _ = ffo.cg(A, bo, eps=1e-10)
         errs.append(float(np.linalg.norm(xs[p] - uo) / np.linalg.norm(uo)))
     # e2e from host arrays
+    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        B2 = batch.Batch(meshes)
+        B2 = batch.Batch(meshes, device=di)
         B2.assemble(kappas, f=1.0)
         xh = B2.solve(eps=cfg["eps"])
         B2.close()
     t_e2e = (time.perf_counter() - t0) * 1e3 / args.steps
+    t_e2e, = dist_max([t_e2e], world, dev)
+    if rank != 0:
+        return None
     h2d = sum(m.coords.nbytes + m.elems.nbytes for m in meshes) + sum(k.nbytes for k in kappas) + ndof
     # CPU: the oracle (single core) on 16 sampled problems, FP64 CG to the same eps
     t0 = time.perf_counter()
@@ -661,21 +723,23 @@ def run_batch(args):
     cpu_v = nd / (time.perf_counter() - t0)
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(REPO, "MEASURED_PEAKS.json")) else {}
-    out = {"metric": METRIC, "value": ndof / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+    out = {"metric": METRIC, "value": ndof_all / (ms * 1e-3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
            "config": {"workload": args.config, "nprob": len(meshes), "ndof": ndof,
+                      "parallelism": f"{world} ranks, one batch each" if world > 1 else "single GPU",
                       "N_range": [int(Ns.min()), int(Ns.max())], "eps": cfg["eps"],
                       "solve_ms": solve_ms, "inner_iterations_total": int(B.stats.iterations),
                       "max_outer": int(B.stats.outer_iterations), "tuned_cta_threads": nt_,
                       "tuned_lanes_per_row": lanes, "rel_err_vs_fp64_oracle_max": max(errs),
                       "l2": "working set %.0f MB" % ((ndof * 7 * 12) / 1e6)},
-           "e2e": {"value": ndof / (t_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "e2e": {"value": ndof_all / (t_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(ndof * 8), "ms_per_step": t_e2e},
            "gpu_launches": int(launches), "clocks": clk,
            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                             "sample": "16 of the batch's problems, oracle FP64 CG, single core"},
-           "roofline": None, "peak_hbm_gbs": peaks.get("hbm_gbs")}
+           "roofline": None, "peak_hbm_gbs": peaks.get("hbm_gbs"),
+           "roofline_note": "one persistent launch over 1024 small problems (each CTA's problem in L1/L2)"}
     print(json.dumps(out))
 
 
@@ -700,13 +764,18 @@ def main():
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    if CONFIGS[args.config].get("batch") and args.impl != "reference":
-        if rank == 0:
-            run_batch(args)
-        return
-    if CONFIGS[args.config].get("adjoint") and args.impl != "reference":
-        if rank == 0:
-            run_adjoint(args)
+    special = CONFIGS[args.config].get("batch") or CONFIGS[args.config].get("adjoint")
+    if special and args.impl != "reference":
+        if world > 1:
+            import torch
+            torch.distributed.init_process_group("nccl")
+        if CONFIGS[args.config].get("batch"):
+            run_batch(args, rank, world)
+        else:
+            run_adjoint(args, rank, world)
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
         return
     if args.impl == "reference":
         if rank != 0:
