@@ -128,7 +128,8 @@ template <> const int SolverGpu<kMixed>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 // terms -- is assembled by FreeFEM's own operator, unchanged.
 //   scalar P1 / P2 (2D, 3D):  int(Th)(k*(grad u . grad v) [+ m*u*v]) + on(labels, u = ...)
 //     with k piecewise constant (a P0 function, a constant, any expression constant per
-//     element) and m constant;
+//     element) -- for P1 any expression, as its quadrature-rule average per element -- and m
+//     constant;
 //   3D [P2,P2,P2]:            int3d(Th)(lambda*div(u)*div(v) + 2*mu*(eps(u):eps(v)))
 //     + on(labels, ...) with constant lambda, mu (any way of writing it whose terms add up
 //     to the isotropic tensor);
@@ -192,31 +193,33 @@ static int op_index(int op, int d) {
 static void ref_points(R2 &a, R2 &b) { a = R2(1. / 3., 1. / 3.); b = R2(0.2, 0.3); }
 static void ref_points(R3 &a, R3 &b) { a = R3(0.25, 0.25, 0.25); b = R3(0.1, 0.2, 0.3); }
 
-// vertices of the reference simplex and barycentric coordinates of a reference point
-static int ref_vertices(R2 *v) { v[0] = R2(0, 0); v[1] = R2(1, 0); v[2] = R2(0, 1); return 3; }
-static int ref_vertices(R3 *v) { v[0] = R3(0, 0, 0); v[1] = R3(1, 0, 0); v[2] = R3(0, 1, 0); v[3] = R3(0, 0, 1); return 4; }
-static void barycentric(const R2 &p, double *l) { l[1] = p.x; l[2] = p.y; l[0] = 1 - p.x - p.y; }
-static void barycentric(const R3 &p, double *l) { l[1] = p.x; l[2] = p.y; l[3] = p.z; l[0] = 1 - p.x - p.y - p.z; }
-
-// true when the coefficient restricted to element K is linear: its values at two interior points
-// (ca at pa, cb at pb) are the barycentric combinations of its vertex values
-template <class Element, class FElement, class Rd>
-static bool linear_on_element(Stack stack, const C_F0 &coef, const Element &K, FElement &FK, const Rd &pa,
-                              const Rd &pb, double ca, double cb) {
-    Rd v[4];
-    double f[4], la[4], lb[4];
-    const int nv = ref_vertices(v);
-    double m = std::max(std::fabs(ca), std::fabs(cb));
-    for (int i = 0; i < nv; ++i) {
-        MeshPointStack(stack)->set(K(v[i]), v[i], FK);
-        f[i] = GetAny<double>(coef.eval(stack));
-        m = std::max(m, std::fabs(f[i]));
+// the element average of a coefficient by the domain's own quadrature rule,
+// sum_q a_q c(x_q) (weights relative to the element measure, problem.cpp:6096-6100): for a P1
+// stiffness term, whose gradients are constant, int_K c grad(phi_i).grad(phi_j) as FreeFEM
+// forms it is |K| (sum_q a_q c_q) grad(phi_i).grad(phi_j)
+template <class FElement>
+static double rule_average(Stack stack, const C_F0 &coef, const Mesh::Element &K, FElement &FK,
+                           const CDomainOfIntegration &di) {
+    const QuadratureFormular &FI = di.FIT(stack);
+    double s = 0;
+    for (int q = 0; q < FI.n; ++q) {
+        const R2 P(FI[q].x, FI[q].y);
+        MeshPointStack(stack)->set(K(P), P, FK);
+        s += FI[q].a * GetAny<double>(coef.eval(stack));
     }
-    barycentric(pa, la);
-    barycentric(pb, lb);
-    double sa = 0, sb = 0;
-    for (int i = 0; i < nv; ++i) { sa += la[i] * f[i]; sb += lb[i] * f[i]; }
-    return std::fabs(sa - ca) <= 1e-13 * m && std::fabs(sb - cb) <= 1e-13 * m;
+    return s;
+}
+template <class FElement>
+static double rule_average(Stack stack, const C_F0 &coef, const Mesh3::Element &K, FElement &FK,
+                           const CDomainOfIntegration &di) {
+    const GQuadratureFormular<R3> &FI = di.FIV(stack);
+    double s = 0;
+    for (int q = 0; q < FI.n; ++q) {
+        const R3 P(FI[q].x, FI[q].y, FI[q].z);
+        MeshPointStack(stack)->set(K(P), P, FK);
+        s += FI[q].a * GetAny<double>(coef.eval(stack));
+    }
+    return s;
 }
 
 // quadrature exactness of a domain of integration (volume, boundary)
@@ -433,19 +436,21 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
                 else if (c != 0.0) { r.why = "mixed derivative term"; ok = false; }
                 continue;
             }
-            // coefficient depending on the point: constant on every element (P0), or -- for a P1
-            // stiffness term, whose gradients are constant -- linear on every element, where
-            // int_K k grad(phi_i).grad(phi_j) = |K| k(barycentre) grad(phi_i).grad(phi_j)
-            const bool linear_ok = r.fe == FFGPU_FE_P1 && pu == pv && pu > 0 && ex >= 1;
+            // coefficient depending on the point.  A P1 stiffness term takes any coefficient,
+            // as its average by the form's own quadrature rule (the gradients are constant on
+            // the element); other terms need it constant on every element (P0)
+            const bool p1_stiff = r.fe == FFGPU_FE_P1 && pu == pv && pu > 0;
             for (int k = 0; k < nt; ++k) {
                 typename FES::FElement FK = Uh[k];
                 MeshPointStack(stack)->set(Th[k](pa), pa, FK);
-                const double ca = GetAny<double>(l->second.eval(stack));
+                double ca = GetAny<double>(l->second.eval(stack));
                 MeshPointStack(stack)->set(Th[k](pb), pb, FK);
                 const double cb = GetAny<double>(l->second.eval(stack));
-                if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb))) &&
-                    !(linear_ok && linear_on_element(stack, l->second, Th[k], FK, pa, pb, ca, cb))) {
-                    r.why = "coefficient not constant (or, for P1 stiffness, not linear) on elements"; ok = false; break;
+                if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
+                    if (!p1_stiff) {
+                        r.why = "coefficient not constant on elements (a P1 stiffness term takes any)"; ok = false; break;
+                    }
+                    ca = rule_average(stack, l->second, Th[k], FK, di);
                 }
                 if (pu == pv && pu > 0) kx[(size_t)k * (d + 1) + pu - 1] += ca;
                 else if (pu == 0 && pv == 0) kx[(size_t)k * (d + 1) + d] += ca;

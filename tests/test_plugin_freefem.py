@@ -143,7 +143,7 @@ def test_unsupported_forms_are_assembled_by_freefem(plugin):
 mesh Th=square(6,6);
 fespace Vh(Th,P1);
 Vh u,v;
-varf a(u,v)=int2d(Th)((1+x*y)*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,2,3,4,u=0);
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v) + (1+x*y)*u*v) + on(1,2,3,4,u=0);
 matrix A=a(Vh,Vh);
 cout << "nnzA " << A.nnz << endl;
 fespace Wh(Th,P2);
@@ -162,7 +162,7 @@ cout << "nnzD " << D.nnz << endl;
 """
     r, out = run_script(plugin, "fb.edp", body)
     assert r.returncode == 0, out[-2000:]
-    for why in ("coefficient not constant (or, for P1 stiffness, not linear) on elements",
+    for why in ("coefficient not constant on elements (a P1 stiffness term takes any)",
                 "quadrature not exact for the form", "element type", "mixed derivative term"):
         assert f"ffgpu: form assembled by FreeFEM ({why})" in out
     nnz = {l.split()[0]: int(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("nnz")}
@@ -207,8 +207,38 @@ cout.precision(17); cout << "ksum " << s << endl;
 matrix A=a(Vh,Vh);
 """
     r, out = run_script(plugin, "p1k.edp", body)
-    ksum = [l for l in r.stdout.splitlines() if l.startswith("ksum ")][0].split()[1]
-    assert f"ffgpu: device assembly P1 dim 2 nt 72 ndof 49 kappa-check {ksum} mass 0" in out
+    ksum = float([l for l in r.stdout.splitlines() if l.startswith("ksum ")][0].split()[1])
+    line = [l for l in out.splitlines() if "ffgpu: device assembly P1 dim 2 nt 72 ndof 49 kappa-check" in l][0]
+    assert abs(float(line.split("kappa-check ")[1].split()[0]) - ksum) <= 1e-13 * abs(ksum)
+
+
+def test_p1_stiffness_with_any_coefficient_uses_the_rule_average(plugin, tmp_path):
+    """A P1 stiffness coefficient of any form (here exp(x+y)) enters as its average by the
+    form's quadrature rule (default T_5 on triangles), exactly the weighted sum FreeFEM forms."""
+    import numpy as np
+    from ffgpu import mesh
+    body = r"""
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(exp(x+y)*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,2,3,4,u=0);
+matrix A=a(Vh,Vh);
+"""
+    d1 = tmp_path / "ek"
+    d1.mkdir()
+    r, out = run_script(plugin, "ek.edp", body, {"FFGPU_PLUGIN_DUMP": str(d1)})
+    assert "ffgpu: device assembly P1 dim 2 nt 72" in out, out[-2000:]
+    kap = np.fromfile(d1 / "kappa.bin", np.float64)
+    Th = mesh.square(6)
+    s15 = np.sqrt(15.0)
+    t, r1, s1, u1, v1 = 1 / 3, (6 - s15) / 21, (9 + 2 * s15) / 21, (6 + s15) / 21, (9 - 2 * s15) / 21
+    P = np.array([[t, t], [r1, r1], [r1, s1], [s1, r1], [u1, u1], [u1, v1], [v1, u1]])
+    W = np.array([0.225] + [(155 - s15) / 1200] * 3 + [(155 + s15) / 1200] * 3)
+    X = Th.coords[Th.elems]                                  # (nt, 3, 2)
+    lam = np.stack([1 - P[:, 0] - P[:, 1], P[:, 0], P[:, 1]], axis=1)   # (7, 3)
+    xq = np.einsum("qi,kid->kqd", lam, X)
+    want = (np.exp(xq[..., 0] + xq[..., 1]) * W).sum(axis=1)
+    assert np.abs(kap - want).max() <= 1e-14 * want.max()
 
 
 def test_boundary_terms_in_the_device_hook(plugin, tmp_path):
