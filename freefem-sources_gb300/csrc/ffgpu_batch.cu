@@ -17,6 +17,8 @@
 
 #include "ffgpu_internal.cuh"
 
+#include <new>
+
 extern "C" int ffgpu_matrix_to_f32(ffgpu_matrix *A);
 
 namespace ffgpu {
@@ -259,8 +261,21 @@ static int batch_graph(ffgpu_batch *B, int cand) {
 
 extern "C" {
 
+static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int32_t *nt, const double *coords,
+                        const int32_t *elems, ffgpu_batch **out);
+
 int ffgpu_batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int32_t *nt, const double *coords,
                        const int32_t *elems, ffgpu_batch **out) {
+    try {
+        return batch_create(ctx, nprob, nv, nt, coords, elems, out);
+    } catch (const std::bad_alloc &) {
+        set_error("ffgpu_batch_create: out of host memory");
+        return FFGPU_ENOMEM;
+    }
+}
+
+static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int32_t *nt, const double *coords,
+                        const int32_t *elems, ffgpu_batch **out) {
     FFGPU_CHECK(ctx && out && nv && nt && coords && elems && nprob > 0, FFGPU_EINVAL,
                 "ffgpu_batch_create: bad argument");
     FFGPU_CUDA(cudaSetDevice(ctx->device));

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -62,7 +63,7 @@ int parse_matrix_text(const char *path, int &n, int &m, int &half, std::vector<T
         set_error("%s: not a FreeFEM matrix (no '(Morse)' or '(COO)' header)", path);
         return FFGPU_EINVAL;
     }
-    if (!rc && (n < 0 || m < 0 || nnz < 0 || n > INT32_MAX - 1)) rc = FFGPU_EINVAL;
+    if (!rc && (n < 0 || m < 0 || nnz < 0 || n > INT32_MAX - 1 || nnz > INT32_MAX)) rc = FFGPU_EINVAL;
     if (rc) { fclose(f); set_error("%s: bad size line", path); return rc; }
     t.clear();
     t.reserve((size_t)nnz);
@@ -109,7 +110,12 @@ int ffgpu_matrix_text_read(const char *path, int *n, int *m, int64_t *nnz, int *
     FFGPU_CHECK(path && n && m && nnz && half, FFGPU_EINVAL, "ffgpu_matrix_text_read: NULL argument");
     std::vector<Triple> t;
     int nn = 0, mm = 0, hh = 0;
-    FFGPU_TRY(parse_matrix_text(path, nn, mm, hh, t));
+    try {
+        FFGPU_TRY(parse_matrix_text(path, nn, mm, hh, t));
+    } catch (const std::bad_alloc &) {
+        set_error("%s: out of host memory", path);
+        return FFGPU_ENOMEM;
+    }
     *n = nn; *m = mm; *half = hh;
     *nnz = (int64_t)t.size();
     if (!rowptr) return FFGPU_OK;
