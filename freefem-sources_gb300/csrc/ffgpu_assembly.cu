@@ -226,6 +226,24 @@ struct P2Basis {
 //   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J    (rank 3)
 // The I type is the same on every lane of a warp (a row's node is either a vertex or an edge
 // of all its elements); the J side is evaluated without branches.
+// P2 mass matrix of the element, int_K phi_i phi_j = |K| kP2Mass*[i][j] / den (exact integrals
+// of the degree-4 products of the vertex functions l(2l-1) and edge functions 4 l_p l_q,
+// int_K l^a = |K| d! prod a_i! / (d + |a|)!), local order as the P2 basis above
+__device__ __constant__ signed char kP2Mass2[6][6] = {{6, -1, -1, -4, 0, 0},  {-1, 6, -1, 0, -4, 0},
+                                                     {-1, -1, 6, 0, 0, -4},  {-4, 0, 0, 32, 16, 16},
+                                                     {0, -4, 0, 16, 32, 16}, {0, 0, -4, 16, 16, 32}};
+__device__ __constant__ signed char kP2Mass3[10][10] = {
+    {6, 1, 1, 1, -4, -4, -4, -6, -6, -6},   {1, 6, 1, 1, -4, -6, -6, -4, -4, -6},
+    {1, 1, 6, 1, -6, -4, -6, -4, -6, -4},   {1, 1, 1, 6, -6, -6, -4, -6, -4, -4},
+    {-4, -4, -6, -6, 32, 16, 16, 16, 16, 8}, {-4, -6, -4, -6, 16, 32, 16, 16, 8, 16},
+    {-4, -6, -6, -4, 16, 16, 32, 8, 16, 16}, {-6, -4, -4, -6, 16, 16, 8, 32, 16, 16},
+    {-6, -4, -6, -4, 16, 8, 16, 16, 32, 16}, {-6, -6, -4, -4, 8, 16, 16, 16, 16, 32}};
+
+template <int DIM>
+__device__ __forceinline__ double p2_mass(int i, int j) {
+    return DIM == 3 ? kP2Mass3[i][j] * (1.0 / 420.0) : kP2Mass2[i][j] * (1.0 / 180.0);
+}
+
 template <int DIM>
 struct P2Pair {
     V3 u0, w0, u1, w1, u2, w2;
@@ -450,6 +468,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     const double m = meas * mfac;
                     if (FE == 2) {
                         v[0] = kap * m * P.trace();
+                        if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
                     } else {
                         const double tr = P.trace();
 #pragma unroll
@@ -756,8 +775,6 @@ static int varf_check(const ffgpu_space *S, const ffgpu_varf *v) {
     else
         FFGPU_CHECK(v->form == FFGPU_FORM_DIFFUSION && S->fe != FFGPU_FE_P2VEC3, FFGPU_EINVAL,
                     "unsupported form %d for this space", v->form);
-    FFGPU_CHECK(!(S->fe == FFGPU_FE_P2 && v->c_mass != 0.0), FFGPU_EINVAL,
-                "P2 mass term is not supported on the device path");
     return FFGPU_OK;
 }
 

@@ -195,6 +195,30 @@ cout << "S nit " << nit << endl;
     return body, {}
 
 
+def case_p2_mass(dim, n):
+    """P2 stiffness plus a mass term 2.5*u*v (default quadrature, exact for the degree-4 mass)."""
+    if dim == 3:
+        head = f'load "msh3"\nmesh3 Th=cube({n},{n},{n});\n'
+        form = "int3d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v)+2.5*u*v) + int3d(Th)(1.*v) + on(1,2,3,4,5,6,u=0)"
+        dump = DUMP_MESH3
+    else:
+        head = f"mesh Th=square({n},{n});\n"
+        form = "int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+2.5*u*v) + int2d(Th)(1.*v) + on(1,2,3,4,u=0)"
+        dump = DUMP_MESH2
+    body = HEAD + head + f"""
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)={form};
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + dump + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
 def case_p2_square_scalar(n):
     """2D P2: FreeFEM renumbers the P2 nodes (Gibbs); the fixture carries its DOF table."""
     body = HEAD + f"""
@@ -386,6 +410,8 @@ CASES = {
     "adj_p1_n8": lambda: case_adjoint_p1(8, seed=31),
     "heat_p1_n6": lambda: case_heat_p1(6, 10, 1e-2, seed=41),
     "io_p1sq_n4": lambda: case_text_io(4),
+    "p2cubem_n2": lambda: case_p2_mass(3, 2),
+    "p2sqm_n4": lambda: case_p2_mass(2, 4),
     "bt_p1sq_6x5": lambda: case_bterms("P1", (6, 5), seed=51),
     "bt_p2sq_5x4": lambda: case_bterms("P2", (5, 4), seed=52),
     "bt_p1cube_3x3x2": lambda: case_bterms("P1", (3, 3, 2), seed=53),

@@ -45,6 +45,12 @@ def case(name):
     elif name.startswith("p2sq_"):
         n = int(name.split("_")[1][1:])
         c.update(Th=mesh.square(n), kind="P2", labels=(1, 2, 3, 4), dof=d["dof"])
+    elif name.startswith("p2cubem_"):
+        n = int(name.split("_")[1][1:])
+        c.update(Th=mesh.cube(n), kind="P2", labels=(1, 2, 3, 4, 5, 6), mass=2.5)
+    elif name.startswith("p2sqm_"):
+        n = int(name.split("_")[1][1:])
+        c.update(Th=mesh.square(n), kind="P2", labels=(1, 2, 3, 4), dof=d["dof"], mass=2.5)
     else:
         raise KeyError(name)
     return c
@@ -52,7 +58,7 @@ def case(name):
 
 MATRIX_CASES = ["p1sq_n2", "p1sq_n5", "p1sq_n16", "p1sq_7x3", "p1sq_n8_T5", "p1sq_n12_gmres",
                 "p1sqk_n8_jit", "p1sqk_n6", "p1cubek_n2", "p1cubek_n4", "p2cube_n2", "p2el_n1",
-                "p2el_n2", "p2el_3x2x1", "p2sq_n4"]
+                "p2el_n2", "p2el_3x2x1", "p2sq_n4", "p2cubem_n2", "p2sqm_n4"]
 
 
 def value_errors(v, ref, rowptr):

@@ -33,7 +33,7 @@ def _lib_built():
 def gpu_varf(c):
     if c["form"] == "elasticity":
         return ffgpu.varf_elasticity(E=1.0, nu=0.3, f=c["f"], on=c["labels"])
-    return ffgpu.varf_diffusion(kappa=c["kappa"], f=c["f"], on=c["labels"])
+    return ffgpu.varf_diffusion(kappa=c["kappa"], f=c["f"], on=c["labels"], c_mass=c.get("mass", 0.0))
 
 
 @pytest.mark.parametrize("name", MATRIX_CASES)
@@ -63,7 +63,7 @@ def test_transpose_mult_and_solve_against_oracle(name):
     c = case(name)
     Th = c["Th"]
     Vh = FESpace(Th, c["kind"], c.get("dof"))
-    Ao = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"])
+    Ao = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"], mass=c.get("mass", 0.0))
     bo = ffo.rhs(Th, Vh, f=c["f"], quad=c["quad"])
     ffo.setbc(Ao, bo, Vh.on(c["labels"]))
     A = ffgpu.matrix(gpu_varf(c), Vh, eps=1e-10)

@@ -14,7 +14,7 @@ from golden_cases import MATRIX_CASES, case, load, value_errors
 def oracle_system(c):
     Th = c["Th"]
     Vh = FESpace(Th, c["kind"], c.get("dof"))
-    A = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"])
+    A = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"], mass=c.get("mass", 0.0))
     b = ffo.rhs(Th, Vh, f=c["f"], quad=c["quad"])
     on = Vh.on(c["labels"], c["components"])
     ffo.setbc(A, b, on)
@@ -56,7 +56,7 @@ def test_oracle_matrix_rhs_solution(name):
 
 
 def test_oracle_scalar_cases_bit_exact():
-    for name in ["p1sq_n16", "p1sqk_n8_jit", "p1cubek_n4", "p2cube_n2"]:
+    for name in ["p1sq_n16", "p1sqk_n8_jit", "p1cubek_n4", "p2cube_n2", "p2cubem_n2", "p2sqm_n4"]:
         c = case(name)
         d = c["d"]
         Vh, A, b, on = oracle_system(c)
@@ -94,7 +94,7 @@ def test_oracle_against_freefem_hashmatrix_and_cg(name):
     Vh = FESpace(Th, c["kind"], c.get("dof"))
     I, J, V = ffo.element_contributions(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"])
     R = ffo.RefHashMatrix(Vh.ndof, I, J, V)
-    A = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"])
+    A = ffo.assemble(Th, Vh, form=c["form"], kappa=c["kappa"], quad=c["quad"], mass=c.get("mass", 0.0))
     b = ffo.rhs(Th, Vh, f=c["f"], quad=c["quad"])
     on = Vh.on(c["labels"], c["components"])
     R.setbc(on)
