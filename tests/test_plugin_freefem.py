@@ -313,3 +313,17 @@ cout << "nnzA2 " << A2.nnz << endl;
     assert r.returncode == 0, out[-2000:]
     assert "ffgpu: form assembled by FreeFEM (boundary term other than c*u*v)" in out
     assert "ffgpu: form assembled by FreeFEM (boundary quadrature not exact)" in out
+
+
+def test_p2_with_a_mass_term_goes_to_the_device(plugin):
+    body = r"""
+mesh Th=square(5,5);
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+2.5*u*v) + on(1,2,3,4,u=0);
+matrix A=a(Vh,Vh);
+"""
+    r, out = run_script(plugin, "p2m.edp", body)
+    assert "ffgpu: device assembly P2 dim 2 nt 50" in out and " mass 2.5 " in out, out[-2000:]
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
