@@ -450,10 +450,25 @@ def run_gpu(args, rank, world):
                      "stored_bytes_per_launch": stored,
                      "frac_of_stored_bytes": stored / (spmv_avg * 1e-3) / 1e9 / peak,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "assembly_roofline": assembly_roofline(Th, Vh, cfg, statistics.median(phase["assemble"][-args.steps:]), peak),
         "clocks": clk,
         "variants": variants,
     }
     return out
+
+
+def assembly_roofline(Th, Vh, cfg, ms, peak):
+    """The assembly (pattern + values + RHS + on()) against the algorithmic bytes of an
+    element-scatter assembly, per element with k local DOFs: connectivity 4k, coordinates
+    8 d (d+1), coefficient 8, element -> nonzero map 4 k^2, values 8 k^2, plus the RHS 8 n."""
+    d = Th.dim
+    k = Vh.ndofK
+    bytes_ = Th.nt * (4 * k + 8 * d * (d + 1) + 8 + 12 * k * k) + 8 * Vh.ndof
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    return {"bound": "fp64 / latency (per-row gather, no scatter)", "achieved": gbs, "peak": peak, "unit": "GB/s",
+            "frac": gbs / peak, "bytes": int(bytes_), "ms": ms,
+            "note": "the device writes each nonzero once (row gather), not once per element contribution: "
+                    "the scatter formula's bytes are not what it moves"}
 
 
 def profile_case(kind, n, iters, spmv_mode):
