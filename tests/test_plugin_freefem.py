@@ -327,3 +327,37 @@ matrix A=a(Vh,Vh);
     assert "ffgpu: device assembly P2 dim 2 nt 50" in out and " mass 2.5 " in out, out[-2000:]
     if not gpu_present():
         assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+
+
+def test_solve_and_problem_statements_use_the_gpu_solver(plugin):
+    """solve / problem with solver=GPUCG go to the registered device solver (FreeFEM assembles
+    the problem form itself); set(A, solver=GPUCG) rebinds a matrix to it."""
+    body = r"""
+mesh Th=square(10,10);
+fespace Vh(Th,P1);
+Vh u,v;
+solve pb(u,v,solver=GPUCG,eps=1e-10)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) - int2d(Th)(1.*v) + on(1,2,3,4,u=0);
+cout << "umax " << u[].max << endl;
+"""
+    r, out = run_script(plugin, "sv.edp", body)
+    if gpu_present():
+        assert r.returncode == 0 and "umax " in r.stdout, out[-2000:]
+    else:
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out, out[-2000:]
+        assert not any(line.startswith("umax ") for line in r.stdout.splitlines())
+    body2 = r"""
+mesh Th=square(10,10);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(1.*v) + on(1,2,3,4,u=0);
+matrix A=a(Vh,Vh);
+set(A,solver=GPUCG,eps=1e-10);
+real[int] b=a(0,Vh);
+u[]=A^-1*b;
+cout << "umax " << u[].max << endl;
+"""
+    r, out = run_script(plugin, "st.edp", body2)
+    if gpu_present():
+        assert r.returncode == 0 and "umax " in r.stdout, out[-2000:]
+    else:
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out, out[-2000:]
