@@ -220,12 +220,6 @@ struct P2Basis {
     __device__ __forceinline__ double d2() const { return vtx ? 0.0 : 4.0; }
 };
 
-// The 3x3 matrix (1/m) int_K d_a(phi_I) d_b(phi_J) = sum_c C_I[c]_a C_J[c]_b + S_I,a S_J,b as a sum
-// of at most three outer products u_k (x) w_k:
-//   I vertex i:   u = g_i,  w = 4 C_J[i] - (d-2) S_J                    (rank 1)
-//   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J    (rank 3)
-// The I type is the same on every lane of a warp (a row's node is either a vertex or an edge
-// of all its elements); the J side is evaluated without branches.
 // P2 mass matrix of the element, int_K phi_i phi_j = |K| kP2Mass*[i][j] / den (exact integrals
 // of the degree-4 products of the vertex functions l(2l-1) and edge functions 4 l_p l_q,
 // int_K l^a = |K| d! prod a_i! / (d + |a|)!), local order as the P2 basis above
@@ -244,6 +238,12 @@ __device__ __forceinline__ double p2_mass(int i, int j) {
     return DIM == 3 ? kP2Mass3[i][j] * (1.0 / 420.0) : kP2Mass2[i][j] * (1.0 / 180.0);
 }
 
+// The 3x3 matrix (1/m) int_K d_a(phi_I) d_b(phi_J) = sum_c C_I[c]_a C_J[c]_b + S_I,a S_J,b as a sum
+// of at most three outer products u_k (x) w_k:
+//   I vertex i:   u = g_i,  w = 4 C_J[i] - (d-2) S_J                    (rank 1)
+//   I edge (p,q): 4 g_q (x) C_J[p] + 4 g_p (x) C_J[q] + S_I (x) S_J    (rank 3)
+// The I type is the same on every lane of a warp (a row's node is either a vertex or an edge
+// of all its elements); the J side is evaluated without branches.
 template <int DIM>
 struct P2Pair {
     V3 u0, w0, u1, w1, u2, w2;
