@@ -185,6 +185,17 @@ class ClockSampler:
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+            return
+        # nvidia-smi's start-up (NVML initialisation) stalls CUDA calls of this process for tens of
+        # milliseconds: the timed region starts once the sampler has written its first line
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.p.poll() is None:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.01)
 
     def stop(self):
         if not self.p:

@@ -802,7 +802,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     FFGPU_TRY(fP0.err); FFGPU_TRY(onbc.err); FFGPU_TRY(gv.err); FFGPU_TRY(rh.err);
     const uint8_t *mask = onbc.d;
     if (bc && !bc->onbc && bc->nlabels > 0) {
-        if (!M->bcmask) FFGPU_CUDA(cudaMalloc((void **)&M->bcmask, S->ndof));
+        if (!M->bcmask) FFGPU_CUDA(dalloc(ctx, (void **)&M->bcmask, S->ndof));
         FFGPU_TRY(space_bc_mask_device(S, bc->nlabels, bc->labels, bc->comp_mask, M->bcmask));
         mask = M->bcmask;
     }
@@ -833,10 +833,10 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     // the solver data of a previous numeric state are stale; so is a cached CG graph, which
     // holds the addresses of the derived value arrays
     M->ntgv = -1;
-    if (M->val_t) { cudaFree(M->val_t); M->val_t = nullptr; }
-    if (M->val32) { cudaFree(M->val32); M->val32 = nullptr; }
-    if (M->valx) { cudaFree(M->valx); M->valx = nullptr; }
-    if (M->valx_t) { cudaFree(M->valx_t); M->valx_t = nullptr; }
+    if (M->val_t) { dfree(ctx, M->val_t); M->val_t = nullptr; }
+    if (M->val32) { dfree(ctx, M->val32); M->val32 = nullptr; }
+    if (M->valx) { dfree(ctx, M->valx); M->valx = nullptr; }
+    if (M->valx_t) { dfree(ctx, M->valx_t); M->valx_t = nullptr; }
     sell_release_values(M);
     if (M->cg_exec) { cudaGraphExecDestroy(M->cg_exec); M->cg_exec = nullptr; }
     return FFGPU_OK;
@@ -871,13 +871,13 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
         DevIn<int32_t> E(elems, (size_t)nt * nvk, s);
         DevIn<int32_t> D(dof, (size_t)nt * ndofK, s);
         if (X.err || E.err || D.err) { rc = X.err ? X.err : (E.err ? E.err : D.err); goto fail; }
-        if (cudaMalloc((void **)&S->coords, sizeof(double) * nv * dim) ||
-            cudaMalloc((void **)&S->elems, sizeof(int32_t) * nt * nvk) ||
-            cudaMalloc((void **)&S->nodes, sizeof(int32_t) * m) ||
-            cudaMalloc((void **)&S->inc_ptr, sizeof(int32_t) * (S->nnodes + 1)) ||
-            cudaMalloc((void **)&S->inc_elem, sizeof(int32_t) * m) ||
-            cudaMalloc((void **)&S->inc_loc, m) ||
-            cudaMalloc((void **)&cnt, sizeof(int32_t) * (S->nnodes + 1))) {
+        if (dalloc(ctx, (void **)&S->coords, sizeof(double) * nv * dim) ||
+            dalloc(ctx, (void **)&S->elems, sizeof(int32_t) * nt * nvk) ||
+            dalloc(ctx, (void **)&S->nodes, sizeof(int32_t) * m) ||
+            dalloc(ctx, (void **)&S->inc_ptr, sizeof(int32_t) * (S->nnodes + 1)) ||
+            dalloc(ctx, (void **)&S->inc_elem, sizeof(int32_t) * m) ||
+            dalloc(ctx, (void **)&S->inc_loc, m) ||
+            dalloc(ctx, (void **)&cnt, sizeof(int32_t) * (S->nnodes + 1))) {
             set_error("ffgpu_space_create: device allocation failed");
             rc = FFGPU_ENOMEM; goto fail;
         }
@@ -919,7 +919,7 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
     *out = S;
     return FFGPU_OK;
 fail:
-    if (cnt) cudaFree(cnt);
+    if (cnt) dfree(ctx, cnt);
     ffgpu_space_destroy(S);
     return rc;
 }
@@ -927,10 +927,10 @@ fail:
 int ffgpu_space_destroy(ffgpu_space *S) {
     if (!S) return FFGPU_OK;
     cudaStreamSynchronize(S->ctx->stream);
-    cudaFree(S->coords); cudaFree(S->elems); cudaFree(S->nodes);
-    cudaFree(S->inc_ptr); cudaFree(S->inc_elem); cudaFree(S->inc_loc);
-    cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
-    cudaFree(S->bel_elem); cudaFree(S->bel_face);
+    dfree(S->ctx, S->coords); dfree(S->ctx, S->elems); dfree(S->ctx, S->nodes);
+    dfree(S->ctx, S->inc_ptr); dfree(S->ctx, S->inc_elem); dfree(S->ctx, S->inc_loc);
+    dfree(S->ctx, S->belems); dfree(S->ctx, S->blabel); dfree(S->ctx, S->bv_ptr); dfree(S->ctx, S->bv_elem); dfree(S->ctx, S->vmark);
+    dfree(S->ctx, S->bel_elem); dfree(S->ctx, S->bel_face);
     delete S;
     return FFGPU_OK;
 }
@@ -941,20 +941,20 @@ int ffgpu_space_set_boundary(ffgpu_space *S, int nbe, const int32_t *belems, con
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const int bdim = S->dim;   // vertices per boundary element
-    cudaFree(S->belems); cudaFree(S->blabel); cudaFree(S->bv_ptr); cudaFree(S->bv_elem); cudaFree(S->vmark);
-    cudaFree(S->bel_elem); cudaFree(S->bel_face);
+    dfree(ctx, S->belems); dfree(ctx, S->blabel); dfree(ctx, S->bv_ptr); dfree(ctx, S->bv_elem); dfree(ctx, S->vmark);
+    dfree(ctx, S->bel_elem); dfree(ctx, S->bel_face);
     S->belems = S->blabel = S->bv_ptr = S->bv_elem = S->bel_elem = S->bel_face = nullptr;
     S->vmark = nullptr;
     S->nbe = nbe;
     int32_t *cnt = nullptr;
-    if (cudaMalloc((void **)&S->belems, sizeof(int32_t) * nbe * bdim) ||
-        cudaMalloc((void **)&S->blabel, sizeof(int32_t) * nbe) ||
-        cudaMalloc((void **)&S->bv_ptr, sizeof(int32_t) * (S->nv + 1)) ||
-        cudaMalloc((void **)&S->bv_elem, sizeof(int32_t) * nbe * bdim) ||
-        cudaMalloc((void **)&S->vmark, S->nv) ||
-        cudaMalloc((void **)&cnt, sizeof(int32_t) * (S->nv + 1))) {
+    if (dalloc(ctx, (void **)&S->belems, sizeof(int32_t) * nbe * bdim) ||
+        dalloc(ctx, (void **)&S->blabel, sizeof(int32_t) * nbe) ||
+        dalloc(ctx, (void **)&S->bv_ptr, sizeof(int32_t) * (S->nv + 1)) ||
+        dalloc(ctx, (void **)&S->bv_elem, sizeof(int32_t) * nbe * bdim) ||
+        dalloc(ctx, (void **)&S->vmark, S->nv) ||
+        dalloc(ctx, (void **)&cnt, sizeof(int32_t) * (S->nv + 1))) {
         set_error("ffgpu_space_set_boundary: device allocation failed");
-        cudaFree(cnt);
+        dfree(ctx, cnt);
         return FFGPU_ENOMEM;
     }
     FFGPU_CUDA(cudaMemcpyAsync(S->belems, belems, sizeof(int32_t) * nbe * bdim, cudaMemcpyDefault, s));
@@ -1005,9 +1005,9 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     M->ntgv = -1; M->csr_lanes = 0;
     int rc = FFGPU_OK;
     int32_t *deg = nullptr;
-    if (cudaMalloc((void **)&M->browptr, sizeof(int32_t) * (M->nb + 1)) ||
-        cudaMalloc((void **)&deg, sizeof(int32_t) * (M->nb + 1)) ||
-        cudaMalloc((void **)&M->geo, sizeof(double) * kGeoStride * S->nt)) {
+    if (dalloc(ctx, (void **)&M->browptr, sizeof(int32_t) * (M->nb + 1)) ||
+        dalloc(ctx, (void **)&deg, sizeof(int32_t) * (M->nb + 1)) ||
+        dalloc(ctx, (void **)&M->geo, sizeof(double) * kGeoStride * S->nt)) {
         set_error("ffgpu_matrix_assemble: device allocation failed");
         rc = FFGPU_ENOMEM; goto fail;
     }
@@ -1019,7 +1019,7 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     if ((rc = device_max_i32(ctx, deg, M->nb, &M->max_deg))) goto fail;
     if ((rc = device_scan_i32(ctx, deg, M->browptr, M->nb))) goto fail;
     // SpMV row order: block rows grouped by degree so that the lanes of a warp share trip counts
-    if (cudaMalloc((void **)&M->rowperm, sizeof(int32_t) * M->nb)) {
+    if (dalloc(ctx, (void **)&M->rowperm, sizeof(int32_t) * M->nb)) {
         set_error("ffgpu_matrix_assemble: device allocation failed");
         rc = FFGPU_ENOMEM; goto fail;
     }
@@ -1033,9 +1033,9 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     }
     cudaFreeAsync(deg, s);
     deg = nullptr;
-    if (cudaMalloc((void **)&M->bcol, sizeof(int32_t) * M->nnzb) ||
-        cudaMalloc((void **)&M->diagpos, sizeof(int32_t) * M->nb) ||
-        cudaMalloc((void **)&M->val, sizeof(double) * M->nnz)) {
+    if (dalloc(ctx, (void **)&M->bcol, sizeof(int32_t) * M->nnzb) ||
+        dalloc(ctx, (void **)&M->diagpos, sizeof(int32_t) * M->nb) ||
+        dalloc(ctx, (void **)&M->val, sizeof(double) * M->nnz)) {
         set_error("ffgpu_matrix_assemble: allocation of %lld values failed", (long long)M->nnz);
         rc = FFGPU_ENOMEM; goto fail;
     }
@@ -1043,7 +1043,7 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
     *out = M;
     return FFGPU_OK;
 fail:
-    if (deg) cudaFree(deg);
+    if (deg) dfree(ctx, deg);
     ffgpu_matrix_destroy(M);
     return rc;
 }
@@ -1110,10 +1110,10 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
     ffgpu_matrix *M = new ffgpu_matrix();
     memset(M, 0, sizeof(*M));
     M->ctx = ctx; M->bs = 1; M->nb = n; M->n = n; M->nnzb = nnz; M->nnz = nnz; M->ntgv = -1;
-    if (cudaMalloc((void **)&M->browptr, sizeof(int32_t) * (n + 1)) ||
-        cudaMalloc((void **)&M->bcol, sizeof(int32_t) * nnz) ||
-        cudaMalloc((void **)&M->diagpos, sizeof(int32_t) * n) ||
-        cudaMalloc((void **)&M->val, sizeof(double) * nnz)) {
+    if (dalloc(ctx, (void **)&M->browptr, sizeof(int32_t) * (n + 1)) ||
+        dalloc(ctx, (void **)&M->bcol, sizeof(int32_t) * nnz) ||
+        dalloc(ctx, (void **)&M->diagpos, sizeof(int32_t) * n) ||
+        dalloc(ctx, (void **)&M->val, sizeof(double) * nnz)) {
         set_error("ffgpu_matrix_from_csr: device allocation failed");
         ffgpu_matrix_destroy(M);
         return FFGPU_ENOMEM;
@@ -1136,7 +1136,7 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
         row_degree_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, deg);
         int rc = launch_check(ctx, "row_degree");
         if (!rc) rc = device_max_i32(ctx, deg, n, &M->max_deg);
-        if (!rc && cudaMalloc((void **)&M->rowperm, sizeof(int32_t) * n)) { set_error("allocation failed"); rc = FFGPU_ENOMEM; }
+        if (!rc && dalloc(ctx, (void **)&M->rowperm, sizeof(int32_t) * n)) { set_error("allocation failed"); rc = FFGPU_ENOMEM; }
         if (!rc) rc = device_order_by_key_desc(ctx, deg, n, M->max_deg, M->rowperm);
         cudaFreeAsync(deg, s);
         if (rc) { ffgpu_matrix_destroy(M); return rc; }
@@ -1152,10 +1152,10 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     if (!M) return FFGPU_OK;
     cudaStreamSynchronize(M->ctx->stream);
     if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
-    cudaFree(M->browptr); cudaFree(M->bcol); cudaFree(M->diagpos); cudaFree(M->rowperm); cudaFree(M->val);
-    cudaFree(M->geo); cudaFree(M->bcmask);
-    cudaFree(M->diag_inv); cudaFree(M->wcl); cudaFree(M->vec); cudaFree(M->val_t);
-    cudaFree(M->val32); cudaFree(M->valx); cudaFree(M->valx_t); cudaFree(M->hx); cudaFree(M->ks);
+    dfree(M->ctx, M->browptr); dfree(M->ctx, M->bcol); dfree(M->ctx, M->diagpos); dfree(M->ctx, M->rowperm); dfree(M->ctx, M->val);
+    dfree(M->ctx, M->geo); dfree(M->ctx, M->bcmask);
+    dfree(M->ctx, M->diag_inv); dfree(M->ctx, M->wcl); dfree(M->ctx, M->vec); dfree(M->ctx, M->val_t);
+    dfree(M->ctx, M->val32); dfree(M->ctx, M->valx); dfree(M->ctx, M->valx_t); dfree(M->ctx, M->hx); dfree(M->ctx, M->ks);
     sell_release(M);
     delete M;
     return FFGPU_OK;

@@ -248,9 +248,9 @@ static int boundary_adjacency(ffgpu_space *S) {
     if (S->bel_elem) return FFGPU_OK;
     ffgpu_ctx *ctx = S->ctx;
     cudaStream_t s = ctx->stream;
-    if (cudaMalloc((void **)&S->bel_elem, sizeof(int32_t) * S->nbe) ||
-        cudaMalloc((void **)&S->bel_face, sizeof(int32_t) * S->nbe)) {
-        cudaFree(S->bel_elem); cudaFree(S->bel_face);
+    if (dalloc(ctx, (void **)&S->bel_elem, sizeof(int32_t) * S->nbe) ||
+        dalloc(ctx, (void **)&S->bel_face, sizeof(int32_t) * S->nbe)) {
+        dfree(ctx, S->bel_elem); dfree(ctx, S->bel_face);
         S->bel_elem = S->bel_face = nullptr;
         set_error("boundary terms: device allocation failed");
         return FFGPU_ENOMEM;
@@ -270,7 +270,7 @@ static int boundary_adjacency(ffgpu_space *S) {
     FFGPU_TRY(launch_check(ctx, "badj_check"));
     const int rc = check_device_status(ctx, "boundary terms (a boundary element has no adjacent element)");
     if (rc) {
-        cudaFree(S->bel_elem); cudaFree(S->bel_face);
+        dfree(ctx, S->bel_elem); dfree(ctx, S->bel_face);
         S->bel_elem = S->bel_face = nullptr;
     }
     return rc;

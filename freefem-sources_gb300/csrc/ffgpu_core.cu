@@ -249,12 +249,20 @@ int ffgpu_ctx_create(int device, ffgpu_ctx **out) {
     ffgpu_ctx *c = new ffgpu_ctx();
     memset(c, 0, sizeof(*c));
     c->device = device;
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    uint64_t keep = UINT64_MAX;  // freed blocks stay mapped for the next object of the context
+    if (cudaMemPoolCreate(&c->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc((void **)&c->d_part, sizeof(double) * 8192) != cudaSuccess ||
         cudaMalloc((void **)&c->d_status, sizeof(int) * 4) != cudaSuccess ||
         cudaMalloc((void **)&c->d_ticket, sizeof(unsigned int) * 16) != cudaSuccess ||
         cudaMalloc((void **)&c->d_iscratch, sizeof(int) * 16) != cudaSuccess) {
         set_error("ffgpu_ctx_create: CUDA setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (c->pool) cudaMemPoolDestroy(c->pool);
         delete c;
         return FFGPU_ECUDA;
     }
@@ -273,6 +281,8 @@ int ffgpu_ctx_destroy(ffgpu_ctx *c) {
     cudaFree(c->d_ticket);
     cudaFree(c->d_iscratch);
     cudaStreamDestroy(c->stream);
+    // blocks of objects still alive are released when those objects free them
+    cudaMemPoolDestroy(c->pool);
     delete c;
     return FFGPU_OK;
 }

@@ -67,6 +67,7 @@ struct ffgpu_ctx_impl;
 struct ffgpu_ctx {
     int device;
     cudaStream_t stream;
+    cudaMemPool_t pool;         // the context's buffers: stream-ordered, kept mapped between objects
     int64_t launches;
     double *d_part;             // reduction partials [kRedBlocks * 4]
     int *d_status;              // DevStatus word
@@ -207,6 +208,16 @@ struct DevOut {
     }
     ~DevOut() { if (owned && d) cudaFreeAsync(d, st); }
 };
+
+// Buffers of spaces, matrices and solver state come from the context's memory pool in the order of
+// its stream: rebuilding a matrix of the same size reuses mapped memory, with no device-wide
+// synchronisation of cudaMalloc/cudaFree.  Every user of these buffers runs on ctx->stream.
+inline cudaError_t dalloc(ffgpu_ctx *ctx, void **p, size_t bytes) {
+    return cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream);
+}
+inline void dfree(ffgpu_ctx *ctx, void *p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
 
 int check_device_status(ffgpu_ctx *ctx, const char *where);
 int launch_check(ffgpu_ctx *ctx, const char *what);

@@ -350,7 +350,7 @@ int ir_time_ka(ffgpu_matrix *A, int nrep, float *ms) {
     // FP32 input and output vectors in the FP64 work slots 5 and 6 (n floats fit in n doubles)
     float *h = (float *)(A->vec + 5 * vs), *q = (float *)(A->vec + 6 * vs);
     InnerScalars *ks = nullptr;
-    FFGPU_CUDA(cudaMalloc((void **)&ks, sizeof(InnerScalars)));
+    FFGPU_CUDA(dalloc(ctx, (void **)&ks, sizeof(InnerScalars)));
     FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(InnerScalars), s));
     FFGPU_CUDA(cudaMemsetAsync(h, 0, sizeof(float) * A->n, s));
     SellArgs sa = sell_args(A);
@@ -381,7 +381,7 @@ int ir_time_ka(ffgpu_matrix *A, int nrep, float *ms) {
             rc = FFGPU_ECUDA;
         }
     }
-    cudaFree(ks);
+    dfree(ctx, ks);
     *ms = t / nrep;
     return rc;
 }
@@ -440,7 +440,7 @@ int ffgpu_matrix_to_f32(ffgpu_matrix *A) {
     if (A->val32) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
-    FFGPU_CUDA(cudaMalloc((void **)&A->val32, sizeof(float) * A->nnz));
+    FFGPU_CUDA(dalloc(ctx, (void **)&A->val32, sizeof(float) * A->nnz));
     to_f32_kernel<<<kMxVecBlocks * 4, kMxThreads, 0, ctx->stream>>>(A->nnz, A->val, A->val32);
     return launch_check(ctx, "to_f32");
 }

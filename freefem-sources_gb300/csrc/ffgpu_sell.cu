@@ -144,8 +144,8 @@ int sell_partition(ffgpu_matrix *A, int nw, const int32_t **part) {
         if (A->spart[i] && A->spart_nw[i] == nw) { *part = A->spart[i]; return FFGPU_OK; }
     int slot = 0;
     while (slot < 4 && A->spart[slot]) ++slot;
-    if (slot == 4) { cudaFree(A->spart[3]); A->spart[3] = nullptr; slot = 3; }
-    FFGPU_CUDA(cudaMalloc((void **)&A->spart[slot], sizeof(int32_t) * ((size_t)nw + 1)));
+    if (slot == 4) { dfree(A->ctx, A->spart[3]); A->spart[3] = nullptr; slot = 3; }
+    FFGPU_CUDA(dalloc(A->ctx, (void **)&A->spart[slot], sizeof(int32_t) * ((size_t)nw + 1)));
     A->spart_nw[slot] = nw;
     sell_part_kernel<<<(nw + 256) / 256, 256, 0, A->ctx->stream>>>(A->nchunk, A->soff, nw, A->spart[slot]);
     FFGPU_TRY(launch_check(A->ctx, "sell_partition"));
@@ -175,9 +175,9 @@ int sell_prepare(ffgpu_matrix *A) {
     const int nwin = (nb + kSellWin - 1) / kSellWin;
     const int nchunk = (nb + 31) / 32;
     A->nchunk = nchunk;
-    FFGPU_CUDA(cudaMalloc((void **)&A->sperm, sizeof(int32_t) * (size_t)nwin * kSellWin));
-    FFGPU_CUDA(cudaMalloc((void **)&A->slen, sizeof(int32_t) * ((size_t)nchunk + 1)));
-    FFGPU_CUDA(cudaMalloc((void **)&A->soff, sizeof(int32_t) * ((size_t)nchunk + 1)));
+    FFGPU_CUDA(dalloc(ctx, (void **)&A->sperm, sizeof(int32_t) * (size_t)nwin * kSellWin));
+    FFGPU_CUDA(dalloc(ctx, (void **)&A->slen, sizeof(int32_t) * ((size_t)nchunk + 1)));
+    FFGPU_CUDA(dalloc(ctx, (void **)&A->soff, sizeof(int32_t) * ((size_t)nchunk + 1)));
     sell_sort_kernel<<<nwin, kSellWin, 0, s>>>(nb, A->browptr, A->sperm);
     FFGPU_TRY(launch_check(ctx, "sell_sort"));
     sell_len_kernel<<<(nchunk + 255) / 256, 256, 0, s>>>(nchunk, A->sperm, A->browptr, A->slen);
@@ -203,11 +203,11 @@ int sell_prepare(ffgpu_matrix *A) {
     const int64_t thr = (int64_t)nchunk * 32;
     const int grid = (int)((thr + 255) / 256);
     if (c16) {
-        FFGPU_CUDA(cudaMalloc((void **)&A->scol16, sizeof(int16_t) * (size_t)ent));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->scol16, sizeof(int16_t) * (size_t)ent));
         sell_col_kernel<true><<<grid, 256, 0, s>>>(nchunk, A->sperm, A->slen, A->soff, A->browptr, A->bcol,
                                                    nullptr, A->scol16);
     } else {
-        FFGPU_CUDA(cudaMalloc((void **)&A->scol, sizeof(int32_t) * (size_t)ent));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->scol, sizeof(int32_t) * (size_t)ent));
         sell_col_kernel<false><<<grid, 256, 0, s>>>(nchunk, A->sperm, A->slen, A->soff, A->browptr, A->bcol,
                                                     A->scol, nullptr);
     }
@@ -219,7 +219,7 @@ static int sell_fill(ffgpu_matrix *A, const double *src, Out **dst) {
     if (*dst) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
     const int64_t ent = A->nslot * 32 * A->bs * A->bs;
-    FFGPU_CUDA(cudaMalloc((void **)dst, sizeof(Out) * (size_t)ent));
+    FFGPU_CUDA(dalloc(ctx, (void **)dst, sizeof(Out) * (size_t)ent));
     const int64_t thr = (int64_t)A->nchunk * 32;
     const int grid = (int)((thr + 255) / 256);
     if (A->bs == 3)
@@ -245,12 +245,12 @@ int sell_values(ffgpu_matrix *A, int kind) {
 
 void sell_release(ffgpu_matrix *A) {
     sell_release_values(A);
-    cudaFree(A->sperm); cudaFree(A->slen); cudaFree(A->soff); cudaFree(A->scol); cudaFree(A->scol16);
-    for (int i = 0; i < 4; ++i) cudaFree(A->spart[i]);
+    dfree(A->ctx, A->sperm); dfree(A->ctx, A->slen); dfree(A->ctx, A->soff); dfree(A->ctx, A->scol); dfree(A->ctx, A->scol16);
+    for (int i = 0; i < 4; ++i) dfree(A->ctx, A->spart[i]);
 }
 
 void sell_release_values(ffgpu_matrix *A) {
-    cudaFree(A->sval); cudaFree(A->sval_t); cudaFree(A->svalx); cudaFree(A->svalx_t); cudaFree(A->sval32);
+    dfree(A->ctx, A->sval); dfree(A->ctx, A->sval_t); dfree(A->ctx, A->svalx); dfree(A->ctx, A->svalx_t); dfree(A->ctx, A->sval32);
     A->sval = A->sval_t = nullptr;
     A->svalx = A->svalx_t = nullptr;
     A->sval32 = nullptr;

@@ -749,7 +749,7 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     const int64_t vs = vstride(A->n);
     double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
     cudaStream_t s = ctx->stream;
-    if (mode == 1 && !A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vs));
+    if (mode == 1 && !A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vs));
     FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
     if (mode == 1) FFGPU_CUDA(cudaMemsetAsync(A->hx, 0, sizeof(float2) * A->n, s));
     KrylovScalars *ks = A->ks;
@@ -784,11 +784,11 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
     FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
     FFGPU_CUDA(cudaStreamSynchronize(s));
     if (is_sell(bestT)) {
-        if (mode == 1) { cudaFree(A->valx); A->valx = nullptr; }
+        if (mode == 1) { dfree(ctx, A->valx); A->valx = nullptr; }
     } else if (mode == 1) {
-        cudaFree(A->svalx); A->svalx = nullptr;
+        dfree(ctx, A->svalx); A->svalx = nullptr;
     } else {
-        cudaFree(A->sval); A->sval = nullptr;
+        dfree(ctx, A->sval); A->sval = nullptr;
     }
     *slot = bestT;
     if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT, mode};
@@ -819,11 +819,11 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t st
 
 int matrix_prepare_split(ffgpu_matrix *A, int trans) {
     ffgpu_ctx *ctx = A->ctx;
-    if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vstride(A->n)));
+    if (!A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vstride(A->n)));
     float2 **dst = trans ? &A->valx_t : &A->valx;
     if (*dst) return FFGPU_OK;
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
-    FFGPU_CUDA(cudaMalloc((void **)dst, sizeof(float2) * A->nnz));
+    FFGPU_CUDA(dalloc(ctx, (void **)dst, sizeof(float2) * A->nnz));
     split_kernel<<<8 * kNumSM, 256, 0, ctx->stream>>>(A->nnz, trans ? A->val_t : A->val, *dst);
     return launch_check(ctx, "split");
 }
@@ -831,7 +831,7 @@ int matrix_prepare_split(ffgpu_matrix *A, int trans) {
 int matrix_prepare_transpose(ffgpu_matrix *A) {
     if (A->val_t) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
-    FFGPU_CUDA(cudaMalloc((void **)&A->val_t, sizeof(double) * A->nnz));
+    FFGPU_CUDA(dalloc(ctx, (void **)&A->val_t, sizeof(double) * A->nnz));
     transpose_kernel<<<(A->nb + 127) / 128, 128, 0, ctx->stream>>>(A->nb, A->bs, A->browptr, A->bcol, A->val,
                                                                    A->val_t, ctx->d_status);
     FFGPU_TRY(launch_check(ctx, "transpose"));
@@ -843,10 +843,10 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
     cudaStream_t s = ctx->stream;
     int64_t n = A->n;
     if (!A->vec) {
-        FFGPU_CUDA(cudaMalloc((void **)&A->vec, sizeof(double) * vstride(n) * 8));
-        FFGPU_CUDA(cudaMalloc((void **)&A->diag_inv, sizeof(double) * vstride(n)));
-        FFGPU_CUDA(cudaMalloc((void **)&A->wcl, n));
-        FFGPU_CUDA(cudaMalloc((void **)&A->ks, sizeof(KrylovScalars)));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->vec, sizeof(double) * vstride(n) * 8));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->diag_inv, sizeof(double) * vstride(n)));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->wcl, n));
+        FFGPU_CUDA(dalloc(ctx, (void **)&A->ks, sizeof(KrylovScalars)));
         FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
     }
     FFGPU_TRY(tune_lanes(A, 0));
@@ -969,7 +969,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
     const int mode = prm->spmv_mode == 1 ? 1 : 0;
     if (mode == 1) {
-        if (!A->hx) FFGPU_CUDA(cudaMalloc((void **)&A->hx, sizeof(float2) * vs));
+        if (!A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vs));
         FFGPU_TRY(tune_lanes(A, 1));
     }
     FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
