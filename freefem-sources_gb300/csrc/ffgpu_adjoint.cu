@@ -74,8 +74,8 @@ int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     FFGPU_TRY(matrix_prepare_solver(A));   // tgv rows as the solver sees them
-    DevIn<double> ud(u, S->ndof, s), ld(lambda, S->ndof, s);
-    DevOut<double> gk(grad_kappa, grad_kappa ? S->nt : 0, s, false), gf(grad_f, grad_f ? S->nt : 0, s, false);
+    DevIn<double> ud(u, S->ndof, ctx), ld(lambda, S->ndof, ctx);
+    DevOut<double> gk(grad_kappa, grad_kappa ? S->nt : 0, ctx, false), gf(grad_f, grad_f ? S->nt : 0, ctx, false);
     FFGPU_TRY(ud.err); FFGPU_TRY(ld.err); FFGPU_TRY(gk.err); FFGPU_TRY(gf.err);
     const uint8_t *wcl = A->ntgv > 0 ? A->wcl : nullptr;
     int grid = (S->nt + 255) / 256;
@@ -84,8 +84,8 @@ int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *
     else
         sensitivity_kernel<3><<<grid, 256, 0, s>>>(S->nt, S->nodes, A->geo, c_stiff, ud.d, ld.d, wcl, gk.d, gf.d);
     FFGPU_TRY(launch_check(ctx, "sensitivity"));
-    FFGPU_TRY(gk.finish(s));
-    FFGPU_TRY(gf.finish(s));
+    FFGPU_TRY(gk.finish());
+    FFGPU_TRY(gf.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }

@@ -724,7 +724,7 @@ int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int
     FFGPU_CHECK(nlabels > 0 && nlabels <= 64 && labels, FFGPU_EINVAL, "on(labels): 1..64 labels expected");
     ffgpu_ctx *ctx = S->ctx;
     cudaStream_t s = ctx->stream;
-    DevIn<int32_t> lab(labels, nlabels, s);
+    DevIn<int32_t> lab(labels, nlabels, ctx);
     FFGPU_TRY(lab.err);
     FFGPU_CUDA(cudaMemsetAsync(S->vmark, 0, S->nv, s));
     FFGPU_CUDA(cudaMemsetAsync(onbc, 0, S->ndof, s));
@@ -780,7 +780,7 @@ static int varf_check(const ffgpu_space *S, const ffgpu_varf *v) {
 
 static int run_geometry(ffgpu_space *S, const ffgpu_varf *v, double *geo) {
     ffgpu_ctx *ctx = S->ctx;
-    DevIn<double> kap(v->kappa, v->kappa ? S->nt : 0, ctx->stream);
+    DevIn<double> kap(v->kappa, v->kappa ? S->nt : 0, ctx);
     FFGPU_TRY(kap.err);
     double cs = v->form == FFGPU_FORM_DIFFUSION ? v->c_stiff : 1.0;
     geometry_kernel<<<grid_for(S->nt, 256), 256, 0, ctx->stream>>>(S->coords, S->elems, S->nt, S->dim,
@@ -795,10 +795,10 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     FFGPU_TRY(varf_check(S, v));
     FFGPU_TRY(run_geometry(S, v, M->geo));
     int bs = S->bs;
-    DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * bs : 0, ctx->stream);
-    DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, ctx->stream);
-    DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, ctx->stream);
-    DevOut<double> rh(rhs, rhs ? S->ndof : 0, ctx->stream, false);
+    DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * bs : 0, ctx);
+    DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, ctx);
+    DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, ctx);
+    DevOut<double> rh(rhs, rhs ? S->ndof : 0, ctx, false);
     FFGPU_TRY(fP0.err); FFGPU_TRY(onbc.err); FFGPU_TRY(gv.err); FFGPU_TRY(rh.err);
     const uint8_t *mask = onbc.d;
     if (bc && !bc->onbc && bc->nlabels > 0) {
@@ -829,7 +829,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     boundary_release(S, bt);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
-    FFGPU_TRY(rh.finish(ctx->stream));
+    FFGPU_TRY(rh.finish());
     // the solver data of a previous numeric state are stale; so is a cached CG graph, which
     // holds the addresses of the derived value arrays
     M->ntgv = -1;
@@ -847,7 +847,10 @@ extern "C" {
 int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, int nt,
                        const int32_t *elems, int fe, int ndofK, const int32_t *dof, int ndof,
                        ffgpu_space **out) {
-    FFGPU_CHECK(ctx && out && coords && elems && dof, FFGPU_EINVAL, "ffgpu_space_create: NULL argument");
+    FFGPU_CHECK(ctx && out && coords && elems && (dof || fe == FFGPU_FE_P1), FFGPU_EINVAL,
+                "ffgpu_space_create: NULL argument");
+    FFGPU_CHECK(dof || ndof == nv, FFGPU_EINVAL,
+                "ffgpu_space_create: P1 without a DOF table needs ndof == nv (got %d, nv %d)", ndof, nv);
     FFGPU_CHECK(dim == 2 || dim == 3, FFGPU_EINVAL, "dim must be 2 or 3");
     FFGPU_CHECK(nv > 0 && nt > 0 && ndof > 0, FFGPU_EINVAL, "empty mesh or space");
     int nvk = dim + 1, nn, bs;
@@ -867,10 +870,8 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
     int rc = FFGPU_OK;
     int32_t *cnt = nullptr;
     {
-        DevIn<double> X(coords, (size_t)nv * dim, s);
-        DevIn<int32_t> E(elems, (size_t)nt * nvk, s);
-        DevIn<int32_t> D(dof, (size_t)nt * ndofK, s);
-        if (X.err || E.err || D.err) { rc = X.err ? X.err : (E.err ? E.err : D.err); goto fail; }
+        DevIn<int32_t> D(dof, dof ? (size_t)nt * ndofK : 0, ctx);   // NULL (P1): the vertices
+        if (D.err) { rc = D.err; goto fail; }
         if (dalloc(ctx, (void **)&S->coords, sizeof(double) * nv * dim) ||
             dalloc(ctx, (void **)&S->elems, sizeof(int32_t) * nt * nvk) ||
             dalloc(ctx, (void **)&S->nodes, sizeof(int32_t) * m) ||
@@ -881,11 +882,16 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
             set_error("ffgpu_space_create: device allocation failed");
             rc = FFGPU_ENOMEM; goto fail;
         }
-        cudaMemcpyAsync(S->coords, X.d, sizeof(double) * nv * dim, cudaMemcpyDeviceToDevice, s);
-        cudaMemcpyAsync(S->elems, E.d, sizeof(int32_t) * nt * nvk, cudaMemcpyDeviceToDevice, s);
+        // host or device arrays, copied straight into the space's own buffers
+        if (cudaMemcpyAsync(S->coords, coords, sizeof(double) * nv * dim, cudaMemcpyDefault, s) ||
+            cudaMemcpyAsync(S->elems, elems, sizeof(int32_t) * nt * nvk, cudaMemcpyDefault, s)) {
+            set_error("ffgpu_space_create: copy of the mesh failed");
+            rc = FFGPU_ECUDA; goto fail;
+        }
         check_elems_kernel<<<grid_for((int64_t)nt * nvk, 256), 256, 0, s>>>(S->elems, (int64_t)nt * nvk, nv, ctx->d_status);
         if ((rc = launch_check(ctx, "check_elems"))) goto fail;
-        build_nodes_kernel<<<grid_for(m, 256), 256, 0, s>>>(D.d, nt, ndofK, nn, bs, ndof, S->nodes, ctx->d_status);
+        build_nodes_kernel<<<grid_for(m, 256), 256, 0, s>>>(dof ? D.d : S->elems, nt, ndofK, nn, bs, ndof,
+                                                            S->nodes, ctx->d_status);
         if ((rc = launch_check(ctx, "build_nodes"))) goto fail;
         if ((rc = check_device_status(ctx, "ffgpu_space_create"))) goto fail;
     }
@@ -910,7 +916,7 @@ int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, in
             S->inc_ptr, S->nnodes, S->max_inc, S->inc_elem, S->inc_loc);
         if ((rc = launch_check(ctx, "inc_sort"))) goto fail;
     }
-    cudaFreeAsync(cnt, s);
+    dfree(ctx, cnt);
     cnt = nullptr;
     if (cudaStreamSynchronize(s) != cudaSuccess) {
         set_error("ffgpu_space_create: %s", cudaGetErrorString(cudaGetLastError()));
@@ -975,7 +981,7 @@ int ffgpu_space_set_boundary(ffgpu_space *S, int nbe, const int32_t *belems, con
                                                                          S->bv_elem);
         rc = launch_check(ctx, "bfill");
     }
-    cudaFreeAsync(cnt, s);
+    dfree(ctx, cnt);
     if (!rc && cudaStreamSynchronize(s) != cudaSuccess) { set_error("ffgpu_space_set_boundary failed"); rc = FFGPU_ECUDA; }
     return rc;
 }
@@ -984,10 +990,10 @@ int ffgpu_space_bc_mask(ffgpu_space *S, int nlabels, const int32_t *labels, int 
     FFGPU_CHECK(S && onbc, FFGPU_EINVAL, "ffgpu_space_bc_mask: NULL argument");
     cudaStream_t s = S->ctx->stream;
     FFGPU_CUDA(cudaSetDevice(S->ctx->device));
-    DevOut<uint8_t> m(onbc, S->ndof, s, false);
+    DevOut<uint8_t> m(onbc, S->ndof, S->ctx, false);
     FFGPU_TRY(m.err);
     FFGPU_TRY(space_bc_mask_device(S, nlabels, labels, comp_mask, m.d));
-    FFGPU_TRY(m.finish(s));
+    FFGPU_TRY(m.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }
@@ -1031,7 +1037,7 @@ int ffgpu_matrix_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *b
         M->nnzb = nnzb;
         M->nnz = M->nnzb * M->bs * M->bs;
     }
-    cudaFreeAsync(deg, s);
+    dfree(ctx, deg);
     deg = nullptr;
     if (dalloc(ctx, (void **)&M->bcol, sizeof(int32_t) * M->nnzb) ||
         dalloc(ctx, (void **)&M->diagpos, sizeof(int32_t) * M->nb) ||
@@ -1061,18 +1067,18 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
     cudaStream_t s = ctx->stream;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     double *geo = nullptr;
-    FFGPU_CUDA(cudaMallocAsync((void **)&geo, sizeof(double) * kGeoStride * S->nt, s));
+    FFGPU_CUDA(dalloc(ctx, (void **)&geo, sizeof(double) * kGeoStride * S->nt));
     int rc = run_geometry(S, v, geo);
     {
-        DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * S->bs : 0, s);
-        DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, s);
-        DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, s);
-        DevOut<double> rh(rhs, S->ndof, s, false);
+        DevIn<double> fP0(v->f, v->f ? (size_t)S->nt * S->bs : 0, ctx);
+        DevIn<uint8_t> onbc(bc ? bc->onbc : nullptr, bc && bc->onbc ? S->ndof : 0, ctx);
+        DevIn<double> gv(bc ? bc->g : nullptr, bc && bc->g ? S->ndof : 0, ctx);
+        DevOut<double> rh(rhs, S->ndof, ctx, false);
         if (!rc) rc = fP0.err ? fP0.err : (onbc.err ? onbc.err : (gv.err ? gv.err : rh.err));
         uint8_t *lmask = nullptr;
         const uint8_t *mask = onbc.d;
         if (!rc && bc && !bc->onbc && bc->nlabels > 0) {
-            if (cudaMallocAsync((void **)&lmask, S->ndof, s) != cudaSuccess) rc = FFGPU_ENOMEM;
+            if (dalloc(ctx, (void **)&lmask, S->ndof) != cudaSuccess) rc = FFGPU_ENOMEM;
             if (!rc) rc = space_bc_mask_device(S, bc->nlabels, bc->labels, bc->comp_mask, lmask);
             mask = lmask;
         }
@@ -1093,10 +1099,10 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
             rc = launch_check(ctx, "rhs_kernel");
         }
         boundary_release(S, bt);
-        if (!rc) rc = rh.finish(s);
-        if (lmask) cudaFreeAsync(lmask, s);
+        if (!rc) rc = rh.finish();
+        if (lmask) dfree(ctx, lmask);
     }
-    cudaFreeAsync(geo, s);
+    dfree(ctx, geo);
     cudaStreamSynchronize(s);
     return rc;
 }
@@ -1132,13 +1138,13 @@ int ffgpu_matrix_from_csr(ffgpu_ctx *ctx, int n, int64_t nnz, const int32_t *row
             return FFGPU_EINVAL;
         }
         int32_t *deg = nullptr;
-        FFGPU_CUDA(cudaMallocAsync((void **)&deg, sizeof(int32_t) * n, s));
+        FFGPU_CUDA(dalloc(ctx, (void **)&deg, sizeof(int32_t) * n));
         row_degree_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, deg);
         int rc = launch_check(ctx, "row_degree");
         if (!rc) rc = device_max_i32(ctx, deg, n, &M->max_deg);
         if (!rc && dalloc(ctx, (void **)&M->rowperm, sizeof(int32_t) * n)) { set_error("allocation failed"); rc = FFGPU_ENOMEM; }
         if (!rc) rc = device_order_by_key_desc(ctx, deg, n, M->max_deg, M->rowperm);
-        cudaFreeAsync(deg, s);
+        dfree(ctx, deg);
         if (rc) { ffgpu_matrix_destroy(M); return rc; }
     }
     diagpos_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, M->browptr, M->bcol, M->diagpos);
@@ -1174,14 +1180,14 @@ int ffgpu_matrix_csr(const ffgpu_matrix *M, int32_t *rowptr, int32_t *col, doubl
     ffgpu_ctx *ctx = M->ctx;
     cudaStream_t s = ctx->stream;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
-    DevOut<int32_t> rp(rowptr, M->n + 1, s, false);
-    DevOut<int32_t> cl(col, M->nnz, s, false);
-    DevOut<double> vl(val, M->nnz, s, false);
+    DevOut<int32_t> rp(rowptr, M->n + 1, ctx, false);
+    DevOut<int32_t> cl(col, M->nnz, ctx, false);
+    DevOut<double> vl(val, M->nnz, ctx, false);
     FFGPU_TRY(rp.err); FFGPU_TRY(cl.err); FFGPU_TRY(vl.err);
     export_csr_kernel<<<grid_for(M->nb, 128), 128, 0, s>>>(M->nb, M->bs, M->browptr, M->bcol, M->val,
                                                             rp.d, cl.d, vl.d);
     FFGPU_TRY(launch_check(ctx, "export_csr"));
-    FFGPU_TRY(rp.finish(s)); FFGPU_TRY(cl.finish(s)); FFGPU_TRY(vl.finish(s));
+    FFGPU_TRY(rp.finish()); FFGPU_TRY(cl.finish()); FFGPU_TRY(vl.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }

@@ -356,7 +356,7 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const int NV = B->A->n;
-    DevOut<double> xd(x, NV, s, false);
+    DevOut<double> xd(x, NV, ctx, false);
     FFGPU_TRY(xd.err);
     BatchArgs &a = B->args;
     bool changed = a.x != xd.d || a.eps != prm->eps ||
@@ -402,7 +402,7 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
     FFGPU_CUDA(cudaGraphLaunch(B->exec, s));
     cudaEventRecord(e1, s);
     ctx->launches += 2;
-    FFGPU_TRY(xd.finish(s));
+    FFGPU_TRY(xd.finish());
     FFGPU_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);

@@ -305,15 +305,15 @@ int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool wa
     int32_t *ptr = nullptr, *list = nullptr, *cnt = nullptr;
     double *brhs = nullptr, *bmat = nullptr;
     auto fail = [&](int rc) {
-        cudaFreeAsync(bsel, s); cudaFreeAsync(ptr, s); cudaFreeAsync(list, s); cudaFreeAsync(cnt, s);
-        cudaFreeAsync(brhs, s); cudaFreeAsync(bmat, s);
+        dfree(ctx, bsel); dfree(ctx, ptr); dfree(ctx, list); dfree(ctx, cnt);
+        dfree(ctx, brhs); dfree(ctx, bmat);
         return rc;
     };
-    if (cudaMallocAsync((void **)&bsel, nbe, s) || cudaMallocAsync((void **)&ptr, sizeof(int32_t) * (S->nnodes + 1), s) ||
-        cudaMallocAsync((void **)&cnt, sizeof(int32_t) * (S->nnodes + 1), s) ||
-        cudaMallocAsync((void **)&list, sizeof(int32_t) * (size_t)nbe * nn, s) ||
-        (want_rhs && cudaMallocAsync((void **)&brhs, sizeof(double) * (size_t)nbe * nn * bsz, s)) ||
-        (want_mat && cudaMallocAsync((void **)&bmat, sizeof(double) * (size_t)nbe * nn * nn, s))) {
+    if (dalloc(ctx, (void **)&bsel, nbe) || dalloc(ctx, (void **)&ptr, sizeof(int32_t) * (S->nnodes + 1)) ||
+        dalloc(ctx, (void **)&cnt, sizeof(int32_t) * (S->nnodes + 1)) ||
+        dalloc(ctx, (void **)&list, sizeof(int32_t) * (size_t)nbe * nn) ||
+        (want_rhs && dalloc(ctx, (void **)&brhs, sizeof(double) * (size_t)nbe * nn * bsz)) ||
+        (want_mat && dalloc(ctx, (void **)&bmat, sizeof(double) * (size_t)nbe * nn * nn))) {
         set_error("boundary terms: device allocation failed");
         return fail(FFGPU_ENOMEM);
     }
@@ -322,9 +322,9 @@ int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool wa
     if (bmat) cudaMemsetAsync(bmat, 0, sizeof(double) * (size_t)nbe * nn * nn, s);
     for (int t = 0; t < v->nbterms; ++t) {
         const ffgpu_bterm &T = v->bterms[t];
-        DevIn<int32_t> lab(T.labels, T.nlabels, s);
-        DevIn<double> rob(T.robin, T.robin ? nbe : 0, s);
-        DevIn<double> gg(T.g, T.g ? (size_t)nbe * bsz : 0, s);
+        DevIn<int32_t> lab(T.labels, T.nlabels, ctx);
+        DevIn<double> rob(T.robin, T.robin ? nbe : 0, ctx);
+        DevIn<double> gg(T.g, T.g ? (size_t)nbe * bsz : 0, ctx);
         if (lab.err || rob.err || gg.err) return fail(lab.err ? lab.err : (rob.err ? rob.err : gg.err));
         BTermArgs a;
         memset(&a, 0, sizeof(a));
@@ -358,18 +358,18 @@ int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool wa
         rc = launch_check(ctx, "bnode_sort");
     }
     if (rc) return fail(rc);
-    cudaFreeAsync(cnt, s);
-    cudaFreeAsync(bsel, s);
+    dfree(ctx, cnt);
+    dfree(ctx, bsel);
     bt.ptr = ptr; bt.list = list; bt.rhs = brhs; bt.mat = bmat; bt.bel_elem = S->bel_elem;
     return FFGPU_OK;
 }
 
 void boundary_release(ffgpu_space *S, BoundaryTerms &bt) {
-    cudaStream_t s = S->ctx->stream;
-    if (bt.ptr) cudaFreeAsync((void *)bt.ptr, s);
-    if (bt.list) cudaFreeAsync((void *)bt.list, s);
-    if (bt.rhs) cudaFreeAsync((void *)bt.rhs, s);
-    if (bt.mat) cudaFreeAsync((void *)bt.mat, s);
+    ffgpu_ctx *ctx = S->ctx;
+    if (bt.ptr) dfree(ctx, (void *)bt.ptr);
+    if (bt.list) dfree(ctx, (void *)bt.list);
+    if (bt.rhs) dfree(ctx, (void *)bt.rhs);
+    if (bt.mat) dfree(ctx, (void *)bt.mat);
     bt = BoundaryTerms{};
 }
 

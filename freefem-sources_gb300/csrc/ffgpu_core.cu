@@ -137,7 +137,7 @@ int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n) {
         return FFGPU_OK;
     }
     int32_t *tot = nullptr;
-    FFGPU_CUDA(cudaMallocAsync((void **)&tot, sizeof(int32_t) * (nb + 1), ctx->stream));
+    FFGPU_CUDA(dalloc(ctx, (void **)&tot, sizeof(int32_t) * (nb + 1)));
     scan_tile_totals<<<nb, kScanThreads, 0, ctx->stream>>>(in, n, tot);
     int r = launch_check(ctx, "scan_tile_totals");
     if (r == FFGPU_OK) {
@@ -148,7 +148,7 @@ int device_scan_i32(ffgpu_ctx *ctx, const int32_t *in, int32_t *out, int n) {
         scan_tiles<<<nb, kScanThreads, 0, ctx->stream>>>(in, n, tot, out);
         r = launch_check(ctx, "scan_tiles");
     }
-    cudaFreeAsync(tot, ctx->stream);
+    dfree(ctx, tot);
     return r;
 }
 
@@ -218,7 +218,7 @@ int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxk
     int64_t m = (int64_t)K * ntiles;
     FFGPU_CHECK(m < (int64_t)1 << 30, FFGPU_EINVAL, "row ordering: %d keys x %d tiles too large", K, ntiles);
     int32_t *hist = nullptr;
-    FFGPU_CUDA(cudaMallocAsync((void **)&hist, sizeof(int32_t) * (2 * m + 1), ctx->stream));
+    FFGPU_CUDA(dalloc(ctx, (void **)&hist, sizeof(int32_t) * (2 * m + 1)));
     int32_t *off = hist + m;
     size_t smem = sizeof(int) * K;
     order_hist_kernel<<<ntiles, 1024, smem, ctx->stream>>>(key, n, maxkey, ntiles, hist);
@@ -228,7 +228,7 @@ int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxk
         order_place_kernel<<<ntiles, 32, smem, ctx->stream>>>(key, n, maxkey, ntiles, off, order);
         r = launch_check(ctx, "order_place");
     }
-    cudaFreeAsync(hist, ctx->stream);
+    dfree(ctx, hist);
     return r;
 }
 

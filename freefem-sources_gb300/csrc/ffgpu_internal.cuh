@@ -154,61 +154,6 @@ namespace ffgpu {
 // -------------------------------------------------------------------- host helpers
 bool is_device_ptr(const void *p);
 
-// A view of a caller array on the device: copies host data in on construction when needed.
-template <typename T>
-struct DevIn {
-    const T *d = nullptr;
-    T *owned = nullptr;
-    int err = FFGPU_OK;
-    cudaStream_t st;
-    DevIn(const T *p, size_t n, cudaStream_t s) : st(s) {
-        if (!p || n == 0) { d = nullptr; return; }
-        if (is_device_ptr(p)) { d = p; return; }
-        if (cudaMallocAsync((void **)&owned, n * sizeof(T), s) != cudaSuccess) {
-            set_error("device allocation of %zu bytes failed", n * sizeof(T));
-            err = FFGPU_ENOMEM; return;
-        }
-        if (cudaMemcpyAsync(owned, p, n * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            set_error("host to device copy failed"); err = FFGPU_ECUDA; return;
-        }
-        d = owned;
-    }
-    ~DevIn() { if (owned) cudaFreeAsync(owned, st); }
-};
-
-// A device buffer standing in for a caller output array; copied back by finish().
-template <typename T>
-struct DevOut {
-    T *user = nullptr, *d = nullptr;
-    bool owned = false;
-    size_t n = 0;
-    int err = FFGPU_OK;
-    cudaStream_t st;
-    DevOut(T *p, size_t nn, cudaStream_t s, bool copy_in) : user(p), n(nn), st(s) {
-        if (!p || n == 0) return;
-        if (is_device_ptr(p)) { d = p; return; }
-        owned = true;
-        if (cudaMallocAsync((void **)&d, n * sizeof(T), s) != cudaSuccess) {
-            set_error("device allocation of %zu bytes failed", n * sizeof(T));
-            err = FFGPU_ENOMEM; d = nullptr; return;
-        }
-        if (copy_in &&
-            cudaMemcpyAsync(d, p, n * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            set_error("host to device copy failed"); err = FFGPU_ECUDA;
-        }
-    }
-    int finish(cudaStream_t s) {
-        if (owned && d) {
-            if (cudaMemcpyAsync(user, d, n * sizeof(T), cudaMemcpyDeviceToHost, s) != cudaSuccess) {
-                set_error("device to host copy failed"); return FFGPU_ECUDA;
-            }
-            if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("stream sync failed"); return FFGPU_ECUDA; }
-        }
-        return FFGPU_OK;
-    }
-    ~DevOut() { if (owned && d) cudaFreeAsync(d, st); }
-};
-
 // Buffers of spaces, matrices and solver state come from the context's memory pool in the order of
 // its stream: rebuilding a matrix of the same size reuses mapped memory, with no device-wide
 // synchronisation of cudaMalloc/cudaFree.  Every user of these buffers runs on ctx->stream.
@@ -218,6 +163,63 @@ inline cudaError_t dalloc(ffgpu_ctx *ctx, void **p, size_t bytes) {
 inline void dfree(ffgpu_ctx *ctx, void *p) {
     if (p) cudaFreeAsync(p, ctx->stream);
 }
+
+// A view of a caller array on the device: copies host data in on construction when needed.
+template <typename T>
+struct DevIn {
+    const T *d = nullptr;
+    T *owned = nullptr;
+    int err = FFGPU_OK;
+    ffgpu_ctx *ctx;
+    DevIn(const T *p, size_t n, ffgpu_ctx *c) : ctx(c) {
+        if (!p || n == 0) { d = nullptr; return; }
+        if (is_device_ptr(p)) { d = p; return; }
+        if (dalloc(ctx, (void **)&owned, n * sizeof(T)) != cudaSuccess) {
+            set_error("device allocation of %zu bytes failed", n * sizeof(T));
+            err = FFGPU_ENOMEM; owned = nullptr; return;
+        }
+        if (cudaMemcpyAsync(owned, p, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
+            set_error("host to device copy failed"); err = FFGPU_ECUDA; return;
+        }
+        d = owned;
+    }
+    ~DevIn() { dfree(ctx, owned); }
+};
+
+// A device buffer standing in for a caller output array; copied back by finish().
+template <typename T>
+struct DevOut {
+    T *user = nullptr, *d = nullptr;
+    bool owned = false;
+    size_t n = 0;
+    int err = FFGPU_OK;
+    ffgpu_ctx *ctx;
+    DevOut(T *p, size_t nn, ffgpu_ctx *c, bool copy_in) : user(p), n(nn), ctx(c) {
+        if (!p || n == 0) return;
+        if (is_device_ptr(p)) { d = p; return; }
+        owned = true;
+        if (dalloc(ctx, (void **)&d, n * sizeof(T)) != cudaSuccess) {
+            set_error("device allocation of %zu bytes failed", n * sizeof(T));
+            err = FFGPU_ENOMEM; d = nullptr; return;
+        }
+        if (copy_in &&
+            cudaMemcpyAsync(d, p, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
+            set_error("host to device copy failed"); err = FFGPU_ECUDA;
+        }
+    }
+    int finish() {
+        if (owned && d) {
+            if (cudaMemcpyAsync(user, d, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) {
+                set_error("device to host copy failed"); return FFGPU_ECUDA;
+            }
+            if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+                set_error("stream sync failed"); return FFGPU_ECUDA;
+            }
+        }
+        return FFGPU_OK;
+    }
+    ~DevOut() { if (owned) dfree(ctx, d); }
+};
 
 int check_device_status(ffgpu_ctx *ctx, const char *where);
 int launch_check(ffgpu_ctx *ctx, const char *what);

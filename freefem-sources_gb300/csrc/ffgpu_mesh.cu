@@ -214,10 +214,10 @@ int ffgpu_mesh_build(ffgpu_ctx *ctx, int dim, int nx, int ny, int nz, double *co
     FFGPU_TRY(ffgpu_mesh_sizes(dim, nx, ny, nz, &nv, &nt, &nbe));
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    DevOut<double> X(coords, (size_t)nv * dim, s, false);
-    DevOut<int32_t> E(elems, (size_t)nt * (dim + 1), s, false);
-    DevOut<int32_t> BE(belems, (size_t)nbe * dim, s, false);
-    DevOut<int32_t> BL(blabel, (size_t)nbe, s, false);
+    DevOut<double> X(coords, (size_t)nv * dim, ctx, false);
+    DevOut<int32_t> E(elems, (size_t)nt * (dim + 1), ctx, false);
+    DevOut<int32_t> BE(belems, (size_t)nbe * dim, ctx, false);
+    DevOut<int32_t> BL(blabel, (size_t)nbe, ctx, false);
     FFGPU_TRY(X.err); FFGPU_TRY(E.err); FFGPU_TRY(BE.err); FFGPU_TRY(BL.err);
     if (dim == 2) {
         const int64_t m = std::max<int64_t>(nv, std::max<int64_t>((int64_t)nx * ny, nbe));
@@ -231,9 +231,9 @@ int ffgpu_mesh_build(ffgpu_ctx *ctx, int dim, int nx, int ny, int nz, double *co
         FFGPU_TRY(launch_check(ctx, "cube_tets"));
         int32_t *flag = nullptr, *pos = nullptr;
         const int64_t ns = (int64_t)nt * 4;
-        if (cudaMallocAsync((void **)&flag, sizeof(int32_t) * (ns + 1), s) ||
-            cudaMallocAsync((void **)&pos, sizeof(int32_t) * (ns + 1), s)) {
-            cudaFreeAsync(flag, s);
+        if (dalloc(ctx, (void **)&flag, sizeof(int32_t) * (ns + 1)) ||
+            dalloc(ctx, (void **)&pos, sizeof(int32_t) * (ns + 1))) {
+            dfree(ctx, flag);
             set_error("ffgpu_mesh_build: device allocation failed");
             return FFGPU_ENOMEM;
         }
@@ -250,11 +250,11 @@ int ffgpu_mesh_build(ffgpu_ctx *ctx, int dim, int nx, int ny, int nz, double *co
             cube_bfill_kernel<<<grid_n(ns, 256), 256, 0, s>>>(D, nt, pos, BE.d, BL.d);
             rc = launch_check(ctx, "cube_bfill");
         }
-        cudaFreeAsync(flag, s);
-        cudaFreeAsync(pos, s);
+        dfree(ctx, flag);
+        dfree(ctx, pos);
         FFGPU_TRY(rc);
     }
-    FFGPU_TRY(X.finish(s)); FFGPU_TRY(E.finish(s)); FFGPU_TRY(BE.finish(s)); FFGPU_TRY(BL.finish(s));
+    FFGPU_TRY(X.finish()); FFGPU_TRY(E.finish()); FFGPU_TRY(BE.finish()); FFGPU_TRY(BL.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }
@@ -264,18 +264,18 @@ int ffgpu_number_p2(ffgpu_ctx *ctx, int nv, int nt, const int32_t *elems, int32_
     FFGPU_CHECK((int64_t)nt * 10 < INT32_MAX, FFGPU_EINVAL, "ffgpu_number_p2: mesh too large");
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    DevIn<int32_t> E(elems, (size_t)nt * 4, s);
-    DevOut<int32_t> N(nodes, (size_t)nt * 10, s, false);
+    DevIn<int32_t> E(elems, (size_t)nt * 4, ctx);
+    DevOut<int32_t> N(nodes, (size_t)nt * 10, ctx, false);
     FFGPU_TRY(E.err); FFGPU_TRY(N.err);
     const int64_t n4 = (int64_t)nt * 4, n10 = (int64_t)nt * 10;
     int32_t *cnt = nullptr, *ptr = nullptr, *list = nullptr, *first = nullptr, *prim = nullptr, *rank = nullptr;
     int rc = FFGPU_OK;
-    if (cudaMallocAsync((void **)&cnt, sizeof(int32_t) * (nv + 1), s) ||
-        cudaMallocAsync((void **)&ptr, sizeof(int32_t) * (nv + 1), s) ||
-        cudaMallocAsync((void **)&list, sizeof(int32_t) * n4, s) ||
-        cudaMallocAsync((void **)&first, sizeof(int32_t) * n10, s) ||
-        cudaMallocAsync((void **)&prim, sizeof(int32_t) * (n10 + 1), s) ||
-        cudaMallocAsync((void **)&rank, sizeof(int32_t) * (n10 + 1), s)) {
+    if (dalloc(ctx, (void **)&cnt, sizeof(int32_t) * (nv + 1)) ||
+        dalloc(ctx, (void **)&ptr, sizeof(int32_t) * (nv + 1)) ||
+        dalloc(ctx, (void **)&list, sizeof(int32_t) * n4) ||
+        dalloc(ctx, (void **)&first, sizeof(int32_t) * n10) ||
+        dalloc(ctx, (void **)&prim, sizeof(int32_t) * (n10 + 1)) ||
+        dalloc(ctx, (void **)&rank, sizeof(int32_t) * (n10 + 1))) {
         set_error("ffgpu_number_p2: device allocation failed");
         rc = FFGPU_ENOMEM;
     }
@@ -313,9 +313,9 @@ int ffgpu_number_p2(ffgpu_ctx *ctx, int nv, int nt, const int32_t *elems, int32_
     int total = 0;
     if (!rc && cudaMemcpyAsync(&total, rank + n10, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
         rc = FFGPU_ECUDA;
-    if (!rc) rc = N.finish(s);
-    cudaFreeAsync(cnt, s); cudaFreeAsync(ptr, s); cudaFreeAsync(list, s);
-    cudaFreeAsync(first, s); cudaFreeAsync(prim, s); cudaFreeAsync(rank, s);
+    if (!rc) rc = N.finish();
+    dfree(ctx, cnt); dfree(ctx, ptr); dfree(ctx, list);
+    dfree(ctx, first); dfree(ctx, prim); dfree(ctx, rank);
     if (!rc && cudaStreamSynchronize(s) != cudaSuccess) { set_error("ffgpu_number_p2 failed"); rc = FFGPU_ECUDA; }
     if (!rc) *nnodes = total;
     return rc;

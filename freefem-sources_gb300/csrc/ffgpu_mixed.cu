@@ -422,11 +422,11 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
     return FFGPU_OK;
 }
 
-static void ir_free(IRState &S, cudaStream_t s) {
+static void ir_free(IRState &S, ffgpu_ctx *ctx) {
     if (S.exec) cudaGraphExecDestroy(S.exec);
-    cudaFreeAsync(S.g, s);
-    cudaFreeAsync(S.ks, s);
-    cudaFreeAsync(S.y, s);
+    dfree(ctx, S.g);
+    dfree(ctx, S.ks);
+    dfree(ctx, S.y);
 }
 
 }  // namespace ffgpu
@@ -454,17 +454,17 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     const int n = A->n;
     FFGPU_TRY(matrix_prepare_solver(A));
     FFGPU_TRY(sell_values(A, kSell32));
-    DevIn<double> bd(b, n, s);
-    DevOut<double> xd(x, n, s, true);
+    DevIn<double> bd(b, n, ctx);
+    DevOut<double> xd(x, n, ctx, true);
     FFGPU_TRY(bd.err);
     FFGPU_TRY(xd.err);
     IRState S;
     const int64_t vs = vstride(n);
-    if (cudaMallocAsync((void **)&S.g, sizeof(float) * (size_t)vs * 5, s) != cudaSuccess ||
-        cudaMallocAsync((void **)&S.ks, sizeof(InnerScalars), s) != cudaSuccess ||
-        cudaMallocAsync((void **)&S.y, sizeof(double) * ((size_t)n + 8), s) != cudaSuccess) {
+    if (dalloc(ctx, (void **)&S.g, sizeof(float) * (size_t)vs * 5) != cudaSuccess ||
+        dalloc(ctx, (void **)&S.ks, sizeof(InnerScalars)) != cudaSuccess ||
+        dalloc(ctx, (void **)&S.y, sizeof(double) * ((size_t)n + 8)) != cudaSuccess) {
         set_error("ffgpu_solve_ir: device allocation failed");
-        ir_free(S, s);
+        ir_free(S, ctx);
         return FFGPU_ENOMEM;
     }
     S.h = S.g + vs; S.q = S.g + 2 * vs; S.d = S.g + 3 * vs; S.dinv = S.g + 4 * vs;
@@ -476,7 +476,7 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     const bool host_loop = ge && ge[0] == '0';
     int rc = ir_tune(A, S);
     if (!rc && !host_loop) rc = ir_build_graph(A, S, unroll);
-    if (rc) { ir_free(S, s); return rc; }
+    if (rc) { ir_free(S, ctx); return rc; }
     const double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
     const int itmax_in = prm->itmax_inner > 0 ? prm->itmax_inner : n;
     const int max_outer = prm->max_outer > 0 ? prm->max_outer : 30;
@@ -564,9 +564,9 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    ir_free(S, s);
+    ir_free(S, ctx);
     if (rc) return rc;
-    FFGPU_TRY(xd.finish(s));
+    FFGPU_TRY(xd.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     if (stats) {
         memset(stats, 0, sizeof(*stats));

@@ -190,12 +190,12 @@ int sell_prepare(ffgpu_matrix *A) {
     bool c16 = false;
     if (A->bs == 1) {
         int32_t *band = nullptr;
-        FFGPU_CUDA(cudaMallocAsync((void **)&band, sizeof(int32_t) * (size_t)nb, s));
+        FFGPU_CUDA(dalloc(ctx, (void **)&band, sizeof(int32_t) * (size_t)nb));
         sell_band_kernel<<<(nb + 255) / 256, 256, 0, s>>>(nb, A->browptr, A->bcol, band);
         int rc = launch_check(ctx, "sell_band");
         int bw = 0;
         if (!rc) rc = device_max_i32(ctx, band, nb, &bw);
-        cudaFreeAsync(band, s);
+        dfree(ctx, band);
         FFGPU_TRY(rc);
         c16 = bw < 32768;
     }

@@ -1121,11 +1121,11 @@ static int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, con
     const int G = kVecBlocks, TB = kVecThreads;
     double *V = nullptr, *Vp = nullptr, *dev = nullptr;
     size_t ld = m + 1;
-    FFGPU_CUDA(cudaMallocAsync((void **)&V, sizeof(double) * (size_t)n * (m + 1), s));
-    FFGPU_CUDA(cudaMallocAsync((void **)&Vp, sizeof(double) * (size_t)n * (m + 1), s));
+    FFGPU_CUDA(dalloc(ctx, (void **)&V, sizeof(double) * (size_t)n * (m + 1)));
+    FFGPU_CUDA(dalloc(ctx, (void **)&Vp, sizeof(double) * (size_t)n * (m + 1)));
     // device scalars: Hn[(m+2) x (m+1)], rot0, rot1, g, y, dotv, relres
     size_t nsc = (size_t)(m + 2) * ld + 4 * (m + 2) + 8;
-    FFGPU_CUDA(cudaMallocAsync((void **)&dev, sizeof(double) * nsc, s));
+    FFGPU_CUDA(dalloc(ctx, (void **)&dev, sizeof(double) * nsc));
     FFGPU_CUDA(cudaMemsetAsync(dev, 0, sizeof(double) * nsc, s));
     double *Hn = dev, *rot0 = Hn + (size_t)(m + 2) * ld, *rot1 = rot0 + (m + 2), *gv = rot1 + (m + 2);
     double *y = gv + (m + 2), *dotv = y + (m + 2), *relres_d = dotv + 2;
@@ -1196,9 +1196,9 @@ static int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, con
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFreeAsync(V, s);
-    cudaFreeAsync(Vp, s);
-    cudaFreeAsync(dev, s);
+    dfree(ctx, V);
+    dfree(ctx, Vp);
+    dfree(ctx, dev);
     cudaStreamSynchronize(s);
     if (rc) return rc;
     if (st) {
@@ -1226,8 +1226,8 @@ static int solve_many(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
     int64_t n = A->n;
     FFGPU_TRY(matrix_prepare_solver(A));
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
-    DevIn<double> bd(b, (size_t)n * nrhs, s);
-    DevOut<double> xd(x, (size_t)n * nrhs, s, true);
+    DevIn<double> bd(b, (size_t)n * nrhs, ctx);
+    DevOut<double> xd(x, (size_t)n * nrhs, ctx, true);
     FFGPU_TRY(bd.err);
     FFGPU_TRY(xd.err);
     ffgpu_solver_stats acc;
@@ -1242,7 +1242,7 @@ static int solve_many(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
         total_it += one.iterations;
         acc.elapsed_ms += one.elapsed_ms;
     }
-    FFGPU_TRY(xd.finish(s));
+    FFGPU_TRY(xd.finish());
     if (stats) {
         *stats = one;
         stats->iterations = nrhs == 1 ? one.iterations : total_it;
@@ -1318,12 +1318,12 @@ int ffgpu_matrix_mult(ffgpu_matrix *A, const double *x, double *y, int trans) {
     ffgpu_ctx *ctx = A->ctx;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    DevIn<double> xd(x, A->n, s);
-    DevOut<double> yd(y, A->n, s, false);
+    DevIn<double> xd(x, A->n, ctx);
+    DevOut<double> yd(y, A->n, ctx, false);
     FFGPU_TRY(xd.err);
     FFGPU_TRY(yd.err);
     FFGPU_TRY(spmv(A, xd.d, yd.d, trans, s));
-    FFGPU_TRY(yd.finish(s));
+    FFGPU_TRY(yd.finish());
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }

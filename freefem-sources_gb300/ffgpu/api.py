@@ -76,7 +76,8 @@ class DeviceSpace:
         self._keep = []
         X = coords if coords is not None else np.ascontiguousarray(Th.coords, np.float64)
         E = elems if elems is not None else np.ascontiguousarray(Th.elems, np.int32)
-        D = dof if dof is not None else np.ascontiguousarray(Vh.dof, np.int32)
+        # P1 DOFs are the vertices (FreeFEM's P1 numbering): no DOF table crosses to the device
+        D = dof if dof is not None else (None if Vh.kind == "P1" else np.ascontiguousarray(Vh.dof, np.int32))
         self._keep += [X, E, D]
         h = C.c_void_p()
         check(lib().ffgpu_space_create(context(device), Th.dim, Th.nv, _ptr(X), Th.nt, _ptr(E),

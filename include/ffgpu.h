@@ -134,6 +134,8 @@ void *ffgpu_ctx_stream(const ffgpu_ctx *ctx);
  * coords: nv*dim doubles; elems: nt*(dim+1) vertex indices (mesh order);
  * dof: nt*ndofK global DOF numbers, FreeFEM's Vh(k,i) (FESpacen.hpp:651-662), where for
  * FFGPU_FE_P2VEC3 local DOF c*10+i is component c of scalar node i (dof = 3*node + c).
+ * dof may be NULL for FFGPU_FE_P1 with ndof == nv: the DOFs are then the vertices, FreeFEM's
+ * P1 numbering without periodic conditions (FESpace.cpp:698-701, GenericMesh.hpp:1760-1764).
  * Builds the node->element incidence on the device. */
 int ffgpu_space_create(ffgpu_ctx *ctx, int dim, int nv, const double *coords, int nt,
                        const int32_t *elems, int fe, int ndofK, const int32_t *dof, int ndof,

@@ -250,6 +250,29 @@ def test_device_resident_inputs_torch():
     assert np.linalg.norm(uh - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"])
 
 
+def test_p1_space_without_dof_table_equals_explicit_table():
+    """A P1 space created with no DOF table (its DOFs are the vertices) assembles the same
+    matrix and right-hand side, bit for bit, as one given FreeFEM's table explicitly."""
+    import torch
+    Th = mesh.cube(6)
+    Vh = FESpace(Th, "P1")
+    kappa = np.exp(np.random.Generator(np.random.PCG64(5)).standard_normal(Th.nt))
+    a = ffgpu.varf_diffusion(kappa=kappa, f=1.0, on=(1, 3))
+    S0 = ffgpu.DeviceSpace(Vh)                                        # no table crosses
+    S1 = ffgpu.DeviceSpace(Vh, dof=np.ascontiguousarray(Vh.dof))      # FreeFEM's table
+    E = torch.from_numpy(Th.elems).cuda()
+    S2 = ffgpu.DeviceSpace(Vh, elems=E)                               # device mesh, no table
+    out = []
+    for S in (S0, S1, S2):
+        b = np.empty(Vh.ndof)
+        A = ffgpu.matrix(a, S, rhs_out=b)
+        rp, cl, v = A.csr()
+        out.append((rp, cl, v, b))
+    for rp, cl, v, b in out[1:]:
+        assert np.array_equal(rp, out[0][0]) and np.array_equal(cl, out[0][1])
+        assert np.array_equal(v, out[0][2]) and np.array_equal(b, out[0][3])
+
+
 def test_full_size_2d_poisson_known_answers():
     """square(256,256) P1 Poisson, qf2pT (the CPU-runnable headline case): nnz formula
     7 nv - 8 n - 6 = 460289, FreeFEM's recorded umax 0.0736705 and ||u|| 10.5628 (532 CG
