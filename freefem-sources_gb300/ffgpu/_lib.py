@@ -28,7 +28,7 @@ EXPORTS = [
     "ffgpu_matrix_text_write",
     "ffgpu_mesh_sizes",
     "ffgpu_mesh_build",
-    "ffgpu_number_p2",
+    "ffgpu_number_p2", "ffgpu_number_p2_2d", "ffgpu_gibbs_renumber",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc",
@@ -112,6 +112,8 @@ def lib():
         "ffgpu_mesh_sizes": (i32, [i32, i32, i32, i32, P(i32), P(i32), P(i32)]),
         "ffgpu_mesh_build": (i32, [vp, i32, i32, i32, i32, vp, vp, vp, vp]),
         "ffgpu_number_p2": (i32, [vp, i32, i32, vp, vp, P(i32)]),
+        "ffgpu_number_p2_2d": (i32, [i32, i32, vp, vp, P(i32)]),
+        "ffgpu_gibbs_renumber": (i32, [i64, vp, vp, vp, P(i64), P(i64)]),
         "ffgpu_matrix_csr": (i32, [vp, vp, vp, vp]),
         "ffgpu_matrix_mult": (i32, [vp, vp, vp, i32]),
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),

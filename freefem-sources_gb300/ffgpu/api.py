@@ -482,6 +482,16 @@ def number_p2(elems, nv, device=0):
     return nodes, nn.value
 
 
+def number_p2_2d(elems, nv):
+    """FreeFEM's P2 node table of a triangular mesh (host arrays): vertex nodes, edge nodes by
+    first encounter, then FreeFEM's Gibbs renumbering -> (nodes (nt, 6) int32, node count)."""
+    E = np.ascontiguousarray(elems, np.int32)
+    nodes = np.empty((E.shape[0], 6), np.int32)
+    nn = C.c_int()
+    check(lib().ffgpu_number_p2_2d(int(nv), E.shape[0], _ptr(E), _ptr(nodes), C.byref(nn)))
+    return nodes, nn.value
+
+
 def device_space(kind, dim, nx, ny=None, nz=None, device=0):
     """``fespace Vh(square(...)/cube(...), kind)`` with the mesh, the DOF numbering and the space
     built on the GPU (no host arrays): a DeviceSpace for ffgpu.matrix / ffgpu.rhs."""
@@ -497,8 +507,12 @@ def device_space(kind, dim, nx, ny=None, nz=None, device=0):
         else:
             n3 = 3 * nodes
             dof, ndof = torch.cat([n3, n3 + 1, n3 + 2], dim=1).contiguous(), 3 * nn
+    elif dim == 2 and kind == "P2":
+        # FreeFEM's Gibbs renumbering is a sequential graph algorithm: it runs on the host
+        nodes, ndof = number_p2_2d(m["elems"].cpu().numpy(), m["nv"])
+        dof = torch.from_numpy(nodes).to(m["elems"].device)
     else:
-        raise NotImplementedError("on the device: P1 (2D, 3D), P2 and [P2,P2,P2] on tetrahedra")
+        raise NotImplementedError("on the device: P1, P2 (2D, 3D) and [P2,P2,P2] on tetrahedra")
     S = DeviceSpace(_DeviceSpaceInfo(Th, kind, ndof), device=device, coords=m["coords"], elems=m["elems"],
                     dof=dof, belems=m["belems"], blabel=m["blabel"])
     S.arrays = dict(m, dof=dof)

@@ -8,8 +8,9 @@
   (``GenericMesh::BuildDFNumbering``, src/femlib/GenericMesh.hpp:1878-1929).
 * [P2,P2,P2] on tetrahedra: DOF = 3*node + component (FESpacen.hpp:582,656-657); the local
   DOF c*10 + i of an element is component c of its local node i, as ``Vh(k, i)`` lists them.
-* P2 on triangles: FreeFEM renumbers the nodes (Gibbs, ``gibbs.cpp:1094``); pass FreeFEM's
-  own table as ``dof=`` for that space.
+* P2 on triangles: vertex nodes, edge nodes by first encounter, then FreeFEM's Gibbs profile
+  renumbering (``FESpace.cpp:623-877``, ``gibbs.cpp:1094-1166``), computed by the library's
+  host routine ``ffgpu_number_p2_2d``; ``dof=`` still takes a table given by FreeFEM.
 
 ``on(labels)`` returns the DOF mask of ``on(labels, u=...)``: the DOFs of the boundary
 elements carrying one of the labels (AssembleBC, src/fflib/problem.cpp:9881-10034).
@@ -69,8 +70,10 @@ class FESpace:
             elif Th.dim == 3:
                 self.nodes, nn = first_encounter_nodes(Th)
             else:
-                raise NotImplementedError(
-                    "2D P2 numbering follows FreeFEM's Gibbs renumbering: pass FreeFEM's Vh(k,i) as dof=")
+                if kind == "P2vec":
+                    raise NotImplementedError("[P2,P2,P2] is provided on tetrahedra")
+                from .api import number_p2_2d
+                self.nodes, nn = number_p2_2d(Th.elems, Th.nv)
             if kind == "P2":
                 self.dof = self.nodes
                 self.ndof = nn

@@ -159,9 +159,23 @@ int ffgpu_mesh_build(ffgpu_ctx *ctx, int dim, int nx, int ny, int nz, double *co
 /* P2 node table of a tetrahedral mesh on the device (host or device arrays): FreeFEM's
  * first-encounter numbering over the element slots (4 vertices, then the edges
  * 01 02 03 12 13 23) of GenericMesh::BuildDFNumbering (src/femlib/GenericMesh.hpp:1878-1929).
- * nodes[nt*10]; *nnodes = the node count.  (2D P2 spaces are Gibbs-renumbered by FreeFEM,
- * gibbs.cpp:1094: pass FreeFEM's table.) */
+ * nodes[nt*10]; *nnodes = the node count.  (2D P2: ffgpu_number_p2_2d.) */
 int ffgpu_number_p2(ffgpu_ctx *ctx, int nv, int nt, const int32_t *elems, int32_t *nodes, int *nnodes);
+/* P2 node table of a triangular mesh (host code, host arrays), FreeFEM's two steps:
+ * ConstructDataFElement::Make (src/femlib/FESpace.cpp:623-877) -- node of vertex v = v, then
+ * edge nodes nv, nv+1, ... by first encounter over (triangle, local edge j = the edge opposite
+ * vertex j) -- and FESpace::renum (src/femlib/gibbs.cpp:1094-1166), the Gibbs profile
+ * renumbering of the node graph, kept when the profile does not grow.
+ * elems[nt*3]; nodes[nt*6] out (3 vertices, then the edges opposite vertices 0, 1, 2, as
+ * FreeFEM's Vh(k,i) lists the DOFs of scalar P2); *nnodes = nv + number of edges. */
+int ffgpu_number_p2_2d(int nv, int nt, const int32_t *elems, int32_t *nodes, int *nnodes);
+/* The Gibbs renumbering alone (gibbsa_, src/femlib/gibbs.cpp:209-433) on a graph in 1-based
+ * CSR form: vertex i (1..n) has the neighbours vois[ptvois[i-1]-1 .. ptvois[i]-2], 1-based,
+ * ptvois[0] = 1 (the lists are sorted in place by degree).  r[i-1] = new 1-based number of
+ * vertex i; *pfold, *pfnew = the profiles before and after (the new numbering is what FreeFEM
+ * applies when *pfnew <= *pfold). */
+int ffgpu_gibbs_renumber(int64_t n, const int64_t *ptvois, int64_t *vois, int64_t *r, int64_t *pfold,
+                         int64_t *pfnew);
 
 /* ------------------------------------------------------------------ assembly
  * matrix A = a(Vh,Vh, ...): replaces OpMatrixtoBilinearForm::Op::operator() /

@@ -1,7 +1,7 @@
 // ref_driver.cpp -- extern "C" driver around FreeFEM's own HashMatrix and Krylov solvers.
 //
-// TEST INFRASTRUCTURE ONLY.  Linked with src/femlib/HashMatrix.cpp and src/femlib/CG.cpp
-// compiled unmodified from the FreeFEM sources (recipe: oracle/Makefile, target `ref`);
+// TEST INFRASTRUCTURE ONLY.  Linked with src/femlib/HashMatrix.cpp, src/femlib/CG.cpp and
+// src/femlib/gibbs.cpp compiled unmodified from the FreeFEM sources (recipe: oracle/Makefile, target `ref`);
 // the result lives in oracle/_ref/ and is never shipped.  It pins the C restatement in
 // oracle/ffo.c: same hash-matrix pattern and COO order, same SetBC, same CG and fgmres.
 //
@@ -50,7 +50,19 @@ struct RefJacobi : CGMatVirt<int, double> {
   }
 };
 
+// FreeFEM's Gibbs renumbering (src/femlib/gibbs.cpp:209, `integer` = long there).
+int gibbsa_(long *n, long *ptvois, long *vois, long *r, long *m, long *nv, long *nx, long *ny, long *nn,
+            long *w1, long *w2, long *pfold, long *pfnew, long *impre, long *nfout);
+
 extern "C" {
+
+// gibbsa_ with the work arrays FESpace::renum gives it (gibbs.cpp:1131-1142)
+int ref_gibbs(long n, long *ptvois, long *vois, long *r, long *pfold, long *pfnew) {
+  std::vector<long> m(n + 1), nv(2 * (n + 1)), nx(n + 1), ny(n + 1), nn(n + 1), w1(n + 1), w2(n + 1);
+  long impre = 0, nfout = 6;
+  return gibbsa_(&n, ptvois, vois, r, m.data(), nv.data(), nx.data(), ny.data(), nn.data(), w1.data(),
+                 w2.data(), pfold, pfnew, &impre, &nfout);
+}
 
 void *ref_hm_new(int n) { return new HM(n, n, 0, 0); }
 void ref_hm_free(void *h) { delete (HM *)h; }

@@ -236,6 +236,24 @@ cout << "S nit " << nit << endl;
     return body, {}
 
 
+P2NUM_MESHES = {
+    # structured, unstructured (Delaunay), with a hole, two components, a truncated square
+    "sq7x3": "mesh Th=square(7,3);",
+    "disk": "border C(t=0,2*pi){x=cos(t);y=sin(t);label=1;}\nmesh Th=buildmesh(C(24));",
+    "annulus": ("border a(t=0,2*pi){x=2*cos(t);y=2*sin(t);label=1;}\n"
+                "border c(t=0,2*pi){x=cos(t);y=sin(t);label=2;}\nmesh Th=buildmesh(a(30)+c(-15));"),
+    "two": "mesh Th1=square(3,3);\nmesh Th2=square(2,4,[x+2,y]);\nmesh Th=Th1+Th2;",
+    "lshape": "mesh Th=trunc(square(8,8),(x<0.5)|(y<0.5));",
+    "disk80": "border C(t=0,2*pi){x=cos(t);y=sin(t);label=1;}\nmesh Th=buildmesh(C(80));",
+}
+
+
+def case_p2_numbering(which):
+    """FreeFEM's 2D P2 DOF table (ConstructDataFElement::Make + Gibbs renumbering) on a mesh."""
+    body = HEAD + P2NUM_MESHES[which] + "\nfespace Vh(Th,P2);\n" + DUMP_MESH2 + DUMP_DOF
+    return body, {}
+
+
 def case_adjoint_p1(n, seed):
     """FP64 adjoint of L = 1/2 (u-uobs)' M (u-uobs) for -div(kappa grad u) = f, written as
     a FreeFEM script: forward CG solve, transpose solve A'^-1, P0 sensitivities by a varf."""
@@ -403,6 +421,7 @@ CASES = {
     "p2el_n2": lambda: case_p2_elasticity(2, 2, 2),
     "p2el_3x2x1": lambda: case_p2_elasticity(3, 2, 1),
     "p2sq_n4": lambda: case_p2_square_scalar(4),
+    **{f"p2num_{w}": (lambda w=w: case_p2_numbering(w)) for w in P2NUM_MESHES},
     "p1sq_n6_tgvm1": lambda: case_p1_square_tgv(6, -1, "GMRES"),
     "p1sq_n6_tgvm2": lambda: case_p1_square_tgv(6, -2, "CG"),
     "p1sq_n6_tgvm3": lambda: case_p1_square_tgv(6, -3, "GMRES"),

@@ -55,7 +55,8 @@ def test_device_p2_numbering_on_a_shuffled_mesh():
     assert nn == nref and np.array_equal(nodes.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("kind,dims", [("P1", (9, 7)), ("P1", (4, 3, 3)), ("P2", (3, 3, 2)), ("P2vec", (2, 2, 3))])
+@pytest.mark.parametrize("kind,dims", [("P1", (9, 7)), ("P1", (4, 3, 3)), ("P2", (3, 3, 2)), ("P2vec", (2, 2, 3)),
+                                       ("P2", (6, 5))])
 def test_device_built_space_assembles_the_same_matrix(kind, dims):
     S = ffgpu.device_space(kind, len(dims), *dims)
     Th = mesh.square(*dims) if len(dims) == 2 else mesh.cube(*dims)
@@ -73,6 +74,15 @@ def test_device_built_space_assembles_the_same_matrix(kind, dims):
     assert np.array_equal(b1, b2)
 
 
-def test_2d_p2_numbering_is_refused():
-    with pytest.raises(NotImplementedError):
-        ffgpu.device_space("P2", 2, 4, 4)
+def test_2d_p2_device_space_matches_freefem():
+    """square(4) P2: mesh on the device, FreeFEM's Gibbs numbering on the host; the assembled
+    matrix equals FreeFEM's own (pattern exact, values within 1e-12)."""
+    from golden_cases import load, value_errors
+    d, _ = load("p2sq_n4")
+    S = ffgpu.device_space("P2", 2, 4, 4)
+    assert np.array_equal(S.arrays["dof"].cpu().numpy(), d["dof"])
+    A = ffgpu.matrix(ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4)), S, eps=1e-10)
+    I, J, V = A.coo()
+    assert np.array_equal(I, d["I"]) and np.array_equal(J, d["J"])
+    rowptr = A.csr()[0]
+    assert value_errors(V, d["C"], rowptr).max() <= 1e-12
