@@ -19,8 +19,6 @@
 
 namespace ffgpu {
 
-constexpr int kGeoStride = 16;   // doubles per element: meas, kappa, -, -, G[4][3]
-
 // ------------------------------------------------------------------ small device utils
 template <typename T>
 __device__ void warp_bitonic_sort(T *s, int P) {
@@ -392,6 +390,7 @@ struct FillArgs {
     double *val;              // NULL: no matrix (linear form only)
     double *rhs;              // NULL: no linear form
     const double *fP0;        // nt*bs or NULL
+    const double *fint;       // element vectors of a source at quadrature points, or NULL
     double f0, f1, f2;
     double c_mass;
     double lam, mu;           // elasticity
@@ -493,7 +492,8 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                 const int ee = A.inc_elem[t], ll = A.inc_loc[t];
                 const double meas = A.geo[(int64_t)ee * kGeoStride];
                 const double f = A.fP0 ? A.fP0[(int64_t)ee * BS + lb] : (lb == 0 ? A.f0 : (lb == 1 ? A.f1 : A.f2));
-                racc += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
+                racc += A.fint ? A.fint[((int64_t)ee * NN + ll) * BS + lb]
+                               : meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
             }
             __syncwarp();
         }
@@ -576,7 +576,8 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
 template <int DIM, int FE>
 __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *inc_elem,
                            const uint8_t *inc_loc, const double *geo, const double *fP0,
-                           double f0, double f1, double f2, const uint8_t *onbc, const double *g,
+                           const double *fint, double f0, double f1, double f2, const uint8_t *onbc,
+                           const double *g,
                            double tgv, double *rhs, const int32_t *bptr, const int32_t *blist,
                            const double *brhs) {
     constexpr int BS = FE == 3 ? 3 : 1;
@@ -599,7 +600,8 @@ __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *in
                 int e = inc_elem[p], l = inc_loc[p];
                 double meas = geo[(int64_t)e * kGeoStride];
                 double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
-                part[sl] += meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
+                part[sl] += fint ? fint[((int64_t)e * NN + l) * BS + c]
+                                 : meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
             }
         }
     }
@@ -822,11 +824,17 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     }
     fa.onbc = mask; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
+    double *fint = nullptr;
+    if (rh.d) FFGPU_TRY(source_prepare(S, v, M->geo, &fint));
+    fa.fint = fint;
     BoundaryTerms bt;
-    FFGPU_TRY(boundary_prepare(S, v, rh.d != nullptr, true, bt));
-    fa.bptr = bt.ptr; fa.blist = bt.list; fa.bel_elem = bt.bel_elem; fa.brhs = bt.rhs; fa.bmat = bt.mat;
-    const int frc = fill_launch(S, fa);
-    boundary_release(S, bt);
+    int frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
+    if (!frc) {
+        fa.bptr = bt.ptr; fa.blist = bt.list; fa.bel_elem = bt.bel_elem; fa.brhs = bt.rhs; fa.bmat = bt.mat;
+        frc = fill_launch(S, fa);
+        boundary_release(S, bt);
+    }
+    dfree(ctx, fint);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish());
@@ -1083,22 +1091,26 @@ int ffgpu_rhs_assemble(ffgpu_space *S, const ffgpu_varf *v, const ffgpu_bc *bc, 
             mask = lmask;
         }
         BoundaryTerms bt;
+        double *fint = nullptr;
+        if (!rc) rc = source_prepare(S, v, geo, &fint);
         if (!rc) rc = boundary_prepare(S, v, true, false, bt);
         if (!rc) {
             void (*k)(int, const int32_t *, const int32_t *, const uint8_t *, const double *,
-                      const double *, double, double, double, const uint8_t *, const double *,
-                      double, double *, const int32_t *, const int32_t *, const double *) = nullptr;
+                      const double *, const double *, double, double, double, const uint8_t *,
+                      const double *, double, double *, const int32_t *, const int32_t *,
+                      const double *) = nullptr;
             if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = rhs_kernel<2, 1>;
             if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = rhs_kernel<3, 1>;
             if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = rhs_kernel<2, 2>;
             if (S->dim == 3 && S->fe == FFGPU_FE_P2) k = rhs_kernel<3, 2>;
             if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) k = rhs_kernel<3, 3>;
             k<<<grid_for((int64_t)S->ndof, 256), 256, 0, s>>>(
-                S->nnodes, S->inc_ptr, S->inc_elem, S->inc_loc, geo, fP0.d, v->f_const[0],
+                S->nnodes, S->inc_ptr, S->inc_elem, S->inc_loc, geo, fP0.d, fint, v->f_const[0],
                 v->f_const[1], v->f_const[2], mask, gv.d, bc ? bc->tgv : 0.0, rh.d, bt.ptr, bt.list, bt.rhs);
             rc = launch_check(ctx, "rhs_kernel");
         }
         boundary_release(S, bt);
+        dfree(ctx, fint);
         if (!rc) rc = rh.finish();
         if (lmask) dfree(ctx, lmask);
     }

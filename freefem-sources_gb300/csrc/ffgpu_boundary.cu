@@ -106,6 +106,35 @@ __device__ __forceinline__ void basis_values(const double *l, double *w) {
     }
 }
 
+// One thread per element: the element vector of a source given at quadrature points,
+// |K| sum_q w_q f_q,c phi_i(lambda_q) (Element_rhs: problem.cpp:7839-7911, 7917-7990)
+template <int DIM, int NN, int BS>
+__global__ void source_qp_kernel(int nt, int nqp, const double *__restrict__ lam, const double *__restrict__ w,
+                                 const double *__restrict__ fqp, const double *__restrict__ geo,
+                                 double *__restrict__ fint) {
+    constexpr int NV = DIM + 1;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= nt) return;
+    double s[NN * BS];
+#pragma unroll
+    for (int i = 0; i < NN * BS; ++i) s[i] = 0.0;
+    for (int q = 0; q < nqp; ++q) {
+        double l[NV], phi[NN];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) l[i] = lam[q * NV + i];
+        basis_values<DIM, NN>(l, phi);
+#pragma unroll
+        for (int c = 0; c < BS; ++c) {
+            const double wf = w[q] * fqp[(e * nqp + q) * BS + c];
+#pragma unroll
+            for (int i = 0; i < NN; ++i) s[i * BS + c] += wf * phi[i];
+        }
+    }
+    const double meas = geo[e * kGeoStride];
+#pragma unroll
+    for (int i = 0; i < NN * BS; ++i) fint[e * NN * BS + i] = meas * s[i];
+}
+
 // One thread per boundary element: the element vector and Robin matrix of one term.
 template <int DIM, int NN, int BS>
 __global__ void bterm_kernel(BTermArgs A) {
@@ -362,6 +391,30 @@ int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool wa
     dfree(ctx, bsel);
     bt.ptr = ptr; bt.list = list; bt.rhs = brhs; bt.mat = bmat; bt.bel_elem = S->bel_elem;
     return FFGPU_OK;
+}
+
+int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **fint) {
+    *fint = nullptr;
+    if (!v || !v->f_qp) return FFGPU_OK;
+    FFGPU_CHECK(v->nqp > 0 && v->nqp <= 64 && v->qp_lambda && v->qp_weight, FFGPU_EINVAL,
+                "source at quadrature points: 1..64 points with coordinates and weights expected (nqp %d)", v->nqp);
+    ffgpu_ctx *ctx = S->ctx;
+    const int nv = S->dim + 1, nn = S->nn, bs = S->bs;
+    DevIn<double> lam(v->qp_lambda, (size_t)v->nqp * nv, ctx), w(v->qp_weight, v->nqp, ctx);
+    DevIn<double> fq(v->f_qp, (size_t)S->nt * v->nqp * bs, ctx);
+    FFGPU_TRY(lam.err); FFGPU_TRY(w.err); FFGPU_TRY(fq.err);
+    FFGPU_CUDA(dalloc(ctx, (void **)fint, sizeof(double) * (size_t)S->nt * nn * bs));
+    void (*k)(int, int, const double *, const double *, const double *, const double *, double *) = nullptr;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = source_qp_kernel<2, 3, 1>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = source_qp_kernel<3, 4, 1>;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = source_qp_kernel<2, 6, 1>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2) k = source_qp_kernel<3, 10, 1>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2VEC3) k = source_qp_kernel<3, 10, 3>;
+    FFGPU_CHECK(k, FFGPU_EINVAL, "source at quadrature points: unsupported element");
+    k<<<(int)((S->nt + 127) / 128), 128, 0, ctx->stream>>>(S->nt, v->nqp, lam.d, w.d, fq.d, geo, *fint);
+    const int rc = launch_check(ctx, "source_qp");
+    if (rc) { dfree(ctx, *fint); *fint = nullptr; }
+    return rc;
 }
 
 void boundary_release(ffgpu_space *S, BoundaryTerms &bt) {

@@ -232,6 +232,8 @@ int device_order_by_key_desc(ffgpu_ctx *ctx, const int32_t *key, int n, int maxk
 // Boundary terms of a varf prepared for one assembly call (ffgpu_boundary.cu): for every node
 // the (boundary element, local node) codes b*nn + il touching it, ascending, and per boundary
 // element its element vector (nn*bs, component-major) and Robin element matrix (nn*nn).
+constexpr int kGeoStride = 16;   // element geometry: doubles per element: meas, kappa, -, -, G[4][3]
+
 struct BoundaryTerms {
     const int32_t *ptr = nullptr;    // nnodes + 1
     const int32_t *list = nullptr;
@@ -241,6 +243,10 @@ struct BoundaryTerms {
 };
 int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool want_mat, BoundaryTerms &bt);
 void boundary_release(ffgpu_space *S, BoundaryTerms &bt);
+// Element vectors of a source given at quadrature points (ffgpu_varf.f_qp), for the linear
+// form: *fint = nt * nn * bs values |K| sum_q w_q f_q phi_i(lambda_q) ((e*nn + i)*bs + c), or
+// NULL when the varf has none.  geo: the element geometry (measure first).
+int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **fint);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 

@@ -22,7 +22,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib
+from . import _lib, quadrature
 from ._lib import BC, BTerm, SolverParams, SolverStats, Varf, check, lib
 from .fespace import FESpace
 from .mesh import Mesh
@@ -133,7 +133,11 @@ class VarForm:
     c_mass: float = 0.0
     E: float = 1.0
     nu: float = 0.3
-    f: object = 1.0               # scalar, per-component tuple, or P0 array (nt[, ncomp])
+    f: object = 1.0               # scalar, per-component tuple, P0 array (nt[, ncomp]), or a
+                                  # function of the coordinates, f(x, y[, z]) (a tuple of
+                                  # ncomp values for [P2,P2,P2]), taken at the rule's points
+    quad: str | None = None       # rule for a function source: qf2pT, qf5pT, tet2, tet5
+                                  # (None: FreeFEM's default, qf5pT / tet5)
     on: tuple = ()                # boundary labels of on(..., u=g)
     g: object = None              # Dirichlet values per DOF (None = 0)
     components: tuple | None = None
@@ -154,7 +158,11 @@ class VarForm:
             self._keep.append(k)
             v.kappa = _ptr(k).value
         v.f = None
-        if np.isscalar(self.f):
+        v.nqp = 0
+        v.qp_lambda = v.qp_weight = v.f_qp = None
+        if callable(self.f):
+            self._source_at_points(v, Vh)
+        elif np.isscalar(self.f):
             v.f_const[0] = float(self.f)
         elif hasattr(self.f, "data_ptr"):
             v.f = _ptr(self.f).value
@@ -211,6 +219,29 @@ class VarForm:
             v.bterms = C.cast(arr, C.c_void_p).value
         return v
 
+    def _source_at_points(self, v: Varf, Vh: FESpace) -> None:
+        """f(x, y[, z]) at the quadrature points of every element, as Element_rhs takes it."""
+        Th = Vh.Th
+        if not hasattr(Th, "coords"):
+            raise ValueError("a function source needs the mesh coordinates on the host")
+        lam, w = quadrature.rule(self.quad, Th.dim)
+        xq = quadrature.points(Th.coords, Th.elems, lam)
+        val = self.f(*[xq[..., d] for d in range(Th.dim)])
+        nc = 3 if Vh.kind == "P2vec" else 1
+        shape = (Th.nt, lam.shape[0])
+        if nc == 1:
+            fq = np.broadcast_to(np.asarray(val, np.float64), shape)[..., None]
+        else:
+            if len(val) != 3:
+                raise ValueError("[P2,P2,P2]: the source function returns three components")
+            fq = np.stack([np.broadcast_to(np.asarray(c, np.float64), shape) for c in val], axis=-1)
+        fq = np.ascontiguousarray(fq)
+        self._keep += [lam, w, fq]
+        v.nqp = lam.shape[0]
+        v.qp_lambda = _ptr(lam).value
+        v.qp_weight = _ptr(w).value
+        v.f_qp = _ptr(fq).value
+
     def c_bc(self, Vh: FESpace, device_marking: bool = False) -> BC:
         """on(labels): with device_marking the assembly marks the DOFs on the device from the
         space's boundary elements; otherwise the host mask FESpace.on is passed."""
@@ -243,20 +274,21 @@ class VarForm:
 
 
 def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tgv=1e30,
-                   bterms=()) -> VarForm:
+                   bterms=(), quad=None) -> VarForm:
     """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v)
     + the boundary terms (BoundaryTerm: robin*u*v + g*v on labelled boundary edges/faces)
-    + on(on, u=g)."""
+    + on(on, u=g).  f may be a function f(x, y[, z]), taken at the points of `quad`."""
     return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
-                   c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms))
+                   c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms), quad=quad)
 
 
 def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30,
-                    bterms=()) -> VarForm:
+                    bterms=(), quad=None) -> VarForm:
     """varf a([u],[v]) = int(lambda div u div v + 2mu eps(u):eps(v)) + int(f.v)
-    + the boundary terms (tractions g.v, Robin robin*u.v) + on(on, u=0)."""
+    + the boundary terms (tractions g.v, Robin robin*u.v) + on(on, u=0).  f may be a function
+    f(x, y, z) returning three components, taken at the points of `quad`."""
     return VarForm(form=_lib.FORM_ELASTICITY, E=E, nu=nu, f=f, on=tuple(on), components=components,
-                   tgv=tgv, bterms=tuple(bterms))
+                   tgv=tgv, bterms=tuple(bterms), quad=quad)
 
 
 class Matrix:

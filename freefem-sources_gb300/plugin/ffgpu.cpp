@@ -679,12 +679,79 @@ struct GpuBilinear : public OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> 
 struct RecognisedRhs {
     int fe = 0;
     std::vector<double> f;        // nt x ncomp
+    // sources that are not constant on elements: values at the points of the rule
+    int nqp = 0;
+    std::vector<double> lam, w;   // nqp x (dim+1) barycentric coordinates, weights
+    std::vector<double> fqp;      // (nt x nqp) x ncomp
     std::vector<int32_t> labels;
     std::vector<BoundaryRec> bterms;   // boundary sources, in varf order
     double g[3] = {0, 0, 0};      // on(...) values per component
     int comp_mask = -1;
     std::string why;
 };
+
+// the volume rule of `di`: size, point q (reference coordinates) and its weight
+static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).n; }
+static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).n; }
+static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R2 &P, double &w) {
+    const QuadratureFormular &FI = di.FIT(s);
+    P = R2(FI[q].x, FI[q].y);
+    w = FI[q].a;
+}
+static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R3 &P, double &w) {
+    const GQuadratureFormular<R3> &FI = di.FIV(s);
+    P = R3(FI[q].x, FI[q].y, FI[q].z);
+    w = FI[q].a;
+}
+static void barycentric(const R2 &P, double *l) { l[0] = 1. - P.x - P.y; l[1] = P.x; l[2] = P.y; }
+static void barycentric(const R3 &P, double *l) { l[0] = 1. - P.x - P.y - P.z; l[1] = P.x; l[2] = P.y; l[3] = P.z; }
+
+// Every volume source term taken at the points of its rule, as Element_rhs takes it
+// (problem.cpp:7839-7911, 7917-7990), summed per (element, point, component); the terms must
+// share one rule.  The device integrates the values with the rule's weights.
+template <class MMesh, class FES>
+static bool rhs_at_points(Stack stack, const list<C_F0> &largs, const MMesh &Th, const FES &Uh, RecognisedRhs &r) {
+    typedef typename Dim<MMesh>::Rd Rd;
+    const int d = Dim<MMesh>::d, nc = r.fe == FFGPU_FE_P2VEC3 ? 3 : 1, nt = Th.nt;
+    FreeFempp::TypeVarForm<double> *tvf = FreeFempp::TypeVarForm<double>::Global;
+    r.nqp = 0;
+    for (list<C_F0>::const_iterator ii = largs.begin(); ii != largs.end(); ++ii) {
+        if (ii->left() != tvf->tFL) continue;
+        const FormLinear *lf = dynamic_cast<const FormLinear *>(ii->LeftValue());
+        const CDomainOfIntegration &di = *lf->di;
+        if (!volume_domain(di, d)) continue;   // boundary sources: per boundary element
+        const int nq = rule_size(stack, di, &Th);
+        std::vector<Rd> P(nq);
+        std::vector<double> lam((size_t)nq * (d + 1)), w(nq);
+        for (int q = 0; q < nq; ++q) {
+            rule_point(stack, di, q, P[q], w[q]);
+            barycentric(P[q], &lam[(size_t)q * (d + 1)]);
+        }
+        if (r.nqp == 0) {
+            if (nq < 1 || nq > 64) { r.why = "quadrature rule size"; return false; }
+            r.nqp = nq;
+            r.lam = lam;
+            r.w = w;
+            r.fqp.assign((size_t)nt * nq * nc, 0.0);
+        } else if (lam != r.lam || w != r.w) {
+            r.why = "volume sources with different quadrature rules";
+            return false;
+        }
+        const Ftest &ft = *lf->l;
+        for (Ftest::const_iterator l = ft.v.begin(); l != ft.v.end(); ++l) {
+            const int jv = l->first.first;
+            for (int k = 0; k < nt; ++k) {
+                typename FES::FElement FK = Uh[k];
+                for (int q = 0; q < nq; ++q) {
+                    MeshPointStack(stack)->set(Th[k](P[q]), P[q], FK);
+                    r.fqp[((size_t)k * nq + q) * nc + jv] += GetAny<double>(l->second.eval(stack));
+                }
+            }
+        }
+    }
+    r.f.assign(r.f.size(), 0.0);
+    return true;
+}
 
 template <class MMesh, class FES>
 static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th, const FES &Uh, RecognisedRhs &r) {
@@ -699,7 +766,7 @@ static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th,
     MeshPoint mp = *MeshPointStack(stack);
     Rd pa, pb;
     ref_points(pa, pb);
-    bool ok = true;
+    bool ok = true, at_points = false;
     for (list<C_F0>::const_iterator ii = largs.begin(); ok && ii != largs.end(); ++ii) {
         aType t = ii->left();
         Expression e = ii->LeftValue();
@@ -731,13 +798,14 @@ static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th,
         }
         if (!volume_domain(di, d)) { r.why = "domain of integration"; ok = false; break; }
         if (GetAny<const MMesh *>((*di.Th)(stack)) != &Th) { r.why = "integration mesh"; ok = false; break; }
-        if (exactness(stack, di, &Th) < (r.fe == FFGPU_FE_P1 ? 1 : 2)) { r.why = "quadrature not exact"; ok = false; break; }
+        // a rule that does not integrate the basis exactly: the values at its points
+        if (exactness(stack, di, &Th) < (r.fe == FFGPU_FE_P1 ? 1 : 2)) at_points = true;
         const Ftest &ft = *lf->l;
         for (Ftest::const_iterator l = ft.v.begin(); ok && l != ft.v.end(); ++l) {
             const int jv = l->first.first, pv = op_index(l->first.second, d);
             if (jv >= nc || pv != 0) { r.why = "operator"; ok = false; break; }
             const bool constant = l->second.LeftValue()->MeshIndependent();
-            for (int k = 0; k < nt; ++k) {
+            for (int k = 0; !at_points && k < nt; ++k) {
                 typename FES::FElement FK = Uh[k];
                 MeshPointStack(stack)->set(Th[k](pa), pa, FK);
                 const double ca = GetAny<double>(l->second.eval(stack));
@@ -745,7 +813,8 @@ static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th,
                     MeshPointStack(stack)->set(Th[k](pb), pb, FK);
                     const double cb = GetAny<double>(l->second.eval(stack));
                     if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
-                        r.why = "source not constant on elements"; ok = false; break;
+                        at_points = true;   // a function of the point: the rule's points
+                        break;
                     }
                 }
                 r.f[(size_t)k * nc + jv] += ca;
@@ -756,6 +825,7 @@ static bool recognise_rhs(Stack stack, const list<C_F0> &largs, const MMesh &Th,
             }
         }
     }
+    if (ok && at_points) ok = rhs_at_points(stack, largs, Th, Uh, r);
     *MeshPointStack(stack) = mp;
     if (!ok) return false;
     r.labels.assign(on.begin(), on.end());
@@ -776,6 +846,11 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
         for (size_t k = 0; k < r.f.size(); ++k) fs += r.f[k] * (double)(k % 7 + 1);
         std::cout << "  ffgpu: device linear form " << fe_name(r.fe) << " dim " << d << " f-check " << std::setprecision(17)
                   << fs << " g " << r.g[0] << std::setprecision(6) << " tgv " << tgv;
+        if (r.nqp) {
+            double qs = 0;
+            for (size_t k = 0; k < r.fqp.size(); ++k) qs += r.fqp[k] * (double)(k % 7 + 1);
+            std::cout << " | at " << r.nqp << " points, fq-check " << std::setprecision(17) << qs << std::setprecision(6);
+        }
         for (size_t t = 0; t < r.bterms.size(); ++t) {
             double gs = 0;
             for (size_t e = 0; e < r.bterms[t].g.size(); ++e) gs += r.bterms[t].g[e] * (double)(e % 7 + 1);
@@ -789,6 +864,14 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
     std::vector<int32_t> E, BE, BL;
     mesh_arrays(Th, X, E, BE, BL);
     const int ndofK = Uh[0].NbDoF(), nc = r.fe == FFGPU_FE_P2VEC3 ? 3 : 1;
+    if (const char *dir = getenv("FFGPU_PLUGIN_DUMP")) {
+        const std::string p(dir);
+        dump(p + "/rhs_coords.bin", X.data(), X.size() * sizeof(double));
+        dump(p + "/rhs_elems.bin", E.data(), E.size() * sizeof(int32_t));
+        dump(p + "/rhs_fqp.bin", r.fqp.data(), r.fqp.size() * sizeof(double));
+        dump(p + "/rhs_lambda.bin", r.lam.data(), r.lam.size() * sizeof(double));
+        dump(p + "/rhs_weight.bin", r.w.data(), r.w.size() * sizeof(double));
+    }
     std::vector<int32_t> dof((size_t)Th.nt * ndofK);
     for (int k = 0; k < Th.nt; ++k) {
         typename FES::FElement K = Uh[k];
@@ -806,6 +889,12 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
         v.c_stiff = 1.0;
         v.E = 1.0;
         v.f = r.f.data();
+        if (r.nqp) {
+            v.nqp = r.nqp;
+            v.qp_lambda = r.lam.data();
+            v.qp_weight = r.w.data();
+            v.f_qp = r.fqp.data();
+        }
         const std::vector<ffgpu_bterm> bt = c_bterms(r.bterms);
         v.nbterms = (int)bt.size();
         v.bterms = bt.empty() ? nullptr : bt.data();

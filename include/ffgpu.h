@@ -61,7 +61,12 @@ typedef struct {
  * the stiffness term is c_stiff*kappa_e, the mass term c_mass (0 = none).
  * Elasticity uses E and nu (mu = E/(2(1+nu)), lambda = E nu/((1+nu)(1-2nu))).
  * f: P0 source per element and component (nt*ncomp) or NULL, then f_const[c] applies.
- * bterms[0..nbterms): boundary terms, added after the volume terms and before on(...). */
+ * bterms[0..nbterms): boundary terms, added after the volume terms and before on(...).
+ * f_qp: a source of any form, given by its values at the points of a quadrature rule, as
+ *   Element_rhs evaluates it (problem.cpp:7839-7911, 2D; 7917-7990, 3D): f_qp[(k*nqp + q)*ncomp
+ *   + c] at the point of barycentric coordinates qp_lambda[q*(dim+1) .. +dim] of element k, the
+ *   rule's weights qp_weight[q] relative to the element measure (nqp <= 64).  When non-NULL it
+ *   replaces f and f_const: b_i += |K| sum_q qp_weight[q] f_q phi_i(lambda_q). */
 typedef struct {
     int form;
     const double *kappa;
@@ -71,6 +76,10 @@ typedef struct {
     double f_const[3];
     int nbterms;
     const ffgpu_bterm *bterms;
+    int nqp;
+    const double *qp_lambda;
+    const double *qp_weight;
+    const double *f_qp;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or

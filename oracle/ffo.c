@@ -180,6 +180,9 @@ static int quad_rule(int id, double *P, double *W) {
     return 0;
 }
 
+/* the points (reference coordinates, dim per point) and weights of rule `id`; returns nq */
+int ffo_quad_points(int id, double *P, double *W) { return quad_rule(id, P, W); }
+
 /* ------------------------------------------------------------------ basis */
 static const int tet_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 static const int tri_edge[3][2] = {{1, 2}, {2, 0}, {0, 1}};
@@ -345,8 +348,12 @@ void ffo_element_matrix(int dim, const double *X, const int *elems, int k, int n
 }
 
 /* linear form: b[dof] += |K| w_q f_c phi_i  (f P0 per element and component, or constant) */
+/* fqp (or NULL): the source at the rule's points, fqp[(k*nq + q)*ncomp + c], in place of
+ * fP0 / fconst -- a source that is any function of the coordinates, as Element_rhs takes it
+ * (problem.cpp:7839-7911, 7917-7990) */
 int ffo_rhs(double *b, int dim, int nt, const double *X, const int *elems, int ndofK,
-            const int *dof, int fe, int quad, const double *fP0, int ncomp, const double *fconst) {
+            const int *dof, int fe, int quad, const double *fP0, int ncomp, const double *fconst,
+            const double *fqp) {
     int nv = dim + 1, order = fe == 1 ? 1 : 2;
     double P[14 * 3], W[14];
     int nq = quad_rule(quad, P, W);
@@ -362,8 +369,9 @@ int ffo_rhs(double *b, int dim, int nt, const double *X, const int *elems, int n
             double coef = mes * W[q];
             int nb = basis(dim, order, l, G, w, dw);
             for (int c = 0; c < ncomp; ++c) {
-                double fc = fP0 ? fP0[(int64_t)k * ncomp + c] : fconst[c];
-                if (fc == 0.0 && !fP0) continue;
+                double fc = fqp ? fqp[((int64_t)k * nq + q) * ncomp + c]
+                                : (fP0 ? fP0[(int64_t)k * ncomp + c] : fconst[c]);
+                if (fc == 0.0 && !fP0 && !fqp) continue;
                 for (int i = 0; i < nb; ++i) b[d[c * nb + i]] += coef * fc * w[i];
             }
         }

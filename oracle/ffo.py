@@ -53,7 +53,9 @@ def lib():
         L.ffo_element_matrix.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp]
         L.ffo_rhs.argtypes = [_dp, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int, C.c_int,
-                              C.c_void_p, C.c_int, _dp]
+                              C.c_void_p, C.c_int, _dp, C.c_void_p]
+        L.ffo_quad_points.restype = C.c_int
+        L.ffo_quad_points.argtypes = [C.c_int, _dp, _dp]
         L.ffo_setbc.argtypes = [C.c_void_p, C.c_void_p, _bp, C.c_void_p, C.c_double]
         L.ffo_bterm.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
                                 C.c_int, _ip, _ip, _ip, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
@@ -159,7 +161,9 @@ def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad
 
 
 def rhs(Th, Vh, f=1.0, quad=None):
-    """real[int] b = a(0,Vh) for int(f . v); f scalar, per-component tuple, or P0 array (nt[,nc])."""
+    """real[int] b = a(0,Vh) for int(f . v); f scalar, per-component tuple, P0 array (nt[,nc]),
+    or a function f(x, y[, z]) (a tuple of components for [P2,P2,P2]) taken at the rule's
+    points, mapped as K(P) = sum_i lambda_i X_i."""
     L = lib()
     dim = Th.dim
     if quad is None:
@@ -171,7 +175,22 @@ def rhs(Th, Vh, f=1.0, quad=None):
     fe = {"P1": 1, "P2": 2, "P2vec": 3}[Vh.kind]
     fconst = np.zeros(3)
     fP0 = None
-    if np.isscalar(f):
+    fqp = None
+    if callable(f):
+        P, W = np.zeros(14 * 3), np.zeros(14)
+        nq = L.ffo_quad_points(int(quad), P, W)
+        P = P[:nq * dim].reshape(nq, dim)
+        X = Th.coords[Th.elems]                                   # (nt, dim+1, dim)
+        xq = X[:, None, 0, :] * (1.0 - P.sum(axis=1))[None, :, None]
+        for i in range(dim):
+            xq = xq + X[:, None, i + 1, :] * P[None, :, i, None]
+        val = f(*[xq[..., d] for d in range(dim)])
+        if nc == 1:
+            fqp = np.broadcast_to(np.asarray(val, np.float64), (Th.nt, nq))[..., None]
+        else:
+            fqp = np.stack([np.broadcast_to(np.asarray(c, np.float64), (Th.nt, nq)) for c in val], axis=-1)
+        fqp = np.ascontiguousarray(fqp)
+    elif np.isscalar(f):
         fconst[0] = f
     else:
         fa = np.asarray(f, np.float64)
@@ -180,7 +199,8 @@ def rhs(Th, Vh, f=1.0, quad=None):
         else:
             fP0 = np.ascontiguousarray(fa.reshape(Th.nt, nc))
     L.ffo_rhs(b, dim, Th.nt, np.ascontiguousarray(Th.coords), np.ascontiguousarray(Th.elems, np.int32),
-              Vh.ndofK, np.ascontiguousarray(Vh.dof, np.int32), fe, int(quad), _ptr(fP0), nc, fconst)
+              Vh.ndofK, np.ascontiguousarray(Vh.dof, np.int32), fe, int(quad), _ptr(fP0), nc, fconst,
+              _ptr(fqp))
     return b
 
 

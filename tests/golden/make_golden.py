@@ -254,6 +254,41 @@ def case_p2_numbering(which):
     return body, {}
 
 
+# sources given as functions of the coordinates (taken at the points of the form's rule)
+SOURCE_CASES = {
+    "sq_p1": ("mesh Th=square(6,5);", "P1", "int2d(Th)", "sin(3*x)*cos(2*y)+x*y", None),
+    "sq_p1_qf2": ("mesh Th=square(5,4);", "P1", "int2d(Th,qft=qf2pT)", "exp(x)*(1+y*y)", None),
+    "sq_p2": ("mesh Th=square(4,3);", "P2", "int2d(Th)", "exp(x)*y-cos(5*y)", None),
+    "cube_p1": ("mesh3 Th=cube(3,2,2);", "P1", "int3d(Th)", "x*y*z+sin(2*z)", None),
+    "cube_p2": ("mesh3 Th=cube(2,2,1);", "P2", "int3d(Th)", "cos(x+2*y)*z", None),
+    "cube_el": ("mesh3 Th=cube(2,1,1);", "P2vec", "int3d(Th)", None, ("x", "y*z", "-1+x*x")),
+}
+
+
+def case_source_function(which):
+    """b = a(0,Vh) for a source that is a function of the coordinates: FreeFEM evaluates it at
+    the points of the rule (Element_rhs)."""
+    mesh_line, kind, dom, f, fv = SOURCE_CASES[which]
+    dump = DUMP_MESH3 if "mesh3" in mesh_line else DUMP_MESH2
+    if kind == "P2vec":
+        body = HEAD + "load \"msh3\"\n" + mesh_line + f"""
+fespace Vh(Th,[P2,P2,P2]);
+Vh [u1,u2,u3],[v1,v2,v3];
+varf a([u1,u2,u3],[v1,v2,v3])={dom}(({fv[0]})*v1+({fv[1]})*v2+({fv[2]})*v3);
+real[int] b=a(0,Vh);
+"""
+    else:
+        load = "load \"msh3\"\n" if "mesh3" in mesh_line else ""
+        body = HEAD + load + mesh_line + f"""
+fespace Vh(Th,{kind});
+Vh u,v;
+varf a(u,v)={dom}(({f})*v);
+real[int] b=a(0,Vh);
+"""
+    body += dump + DUMP_DOF + "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" 0\" << endl;\n"
+    return body, {}
+
+
 def case_adjoint_p1(n, seed):
     """FP64 adjoint of L = 1/2 (u-uobs)' M (u-uobs) for -div(kappa grad u) = f, written as
     a FreeFEM script: forward CG solve, transpose solve A'^-1, P0 sensitivities by a varf."""
@@ -422,6 +457,7 @@ CASES = {
     "p2el_3x2x1": lambda: case_p2_elasticity(3, 2, 1),
     "p2sq_n4": lambda: case_p2_square_scalar(4),
     **{f"p2num_{w}": (lambda w=w: case_p2_numbering(w)) for w in P2NUM_MESHES},
+    **{f"src_{w}": (lambda w=w: case_source_function(w)) for w in SOURCE_CASES},
     "p1sq_n6_tgvm1": lambda: case_p1_square_tgv(6, -1, "GMRES"),
     "p1sq_n6_tgvm2": lambda: case_p1_square_tgv(6, -2, "CG"),
     "p1sq_n6_tgvm3": lambda: case_p1_square_tgv(6, -3, "GMRES"),

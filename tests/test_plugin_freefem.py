@@ -7,6 +7,7 @@ import os
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -172,12 +173,12 @@ cout << "nnzD " << D.nnz << endl;
 
 def test_linear_form_hook(plugin):
     """`b = a(0,Vh)`: a constant/P0 source with constant on() values goes to the device
-    (ffgpu_rhs_assemble); a point-dependent source is FreeFEM's own operator."""
+    (ffgpu_rhs_assemble); a source with an operator on v is FreeFEM's own operator."""
     body = r"""
 mesh Th=square(6,6);
 fespace Vh(Th,P1);
 Vh u,v;
-varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(x*y*v) + on(1,2,3,4,u=0);
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(x*dx(v)) + on(1,2,3,4,u=0);
 real[int] b=a(0,Vh);
 cout << "bsum " << b.sum << endl;
 varf a2(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(2.5*v) + on(1,3,u=1.5);
@@ -185,12 +186,67 @@ real[int] b2=a2(0,Vh);
 cout << "b2sum " << b2.sum << endl;
 """
     r, out = run_script(plugin, "lf.edp", body)
-    assert "ffgpu: linear form assembled by FreeFEM (source not constant on elements)" in out
+    assert "ffgpu: linear form assembled by FreeFEM (operator)" in out
     assert any(line.startswith("bsum ") for line in r.stdout.splitlines())
     # 72 triangles, f = 2.5: sum_k 2.5 (k % 7 + 1) = 707.5
     assert "ffgpu: device linear form P1 dim 2 f-check 707.5 g 1.5 tgv 1e+30" in out
     if not gpu_present():
         assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_function_sources_go_to_the_device_at_the_rule_points(plugin, tmp_path, dim):
+    """A source that is a function of the point is handed to the device by its values at the
+    points of the form's rule, evaluated by FreeFEM itself (checked against the same function
+    at the dumped points); volume sources with different rules stay FreeFEM's."""
+    if dim == 2:
+        body = r"""
+mesh Th=square(5,4);
+fespace Vh(Th,P2);
+Vh u,v;
+varf a(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(sin(3*x)*y*v) + int2d(Th)(0.5*v) + on(1,u=0);
+real[int] b=a(0,Vh);
+"""
+        f = lambda x, y: np.sin(3 * x) * y + 0.5
+    else:
+        body = r"""
+load "msh3"
+mesh3 Th=cube(3,2,2);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int3d(Th)(dx(u)*dx(v)+dy(u)*dy(v)+dz(u)*dz(v)) + int3d(Th)(x*exp(z)*v) + on(1,u=0);
+real[int] b=a(0,Vh);
+"""
+        f = lambda x, y, z: x * np.exp(z)
+    d1 = tmp_path / "src"
+    d1.mkdir()
+    r, out = run_script(plugin, "fs.edp", body, {"FFGPU_PLUGIN_DUMP": str(d1)})
+    nq = 7 if dim == 2 else 14
+    assert f"at {nq} points, fq-check" in out
+    X = np.fromfile(d1 / "rhs_coords.bin", np.float64).reshape(-1, dim)
+    E = np.fromfile(d1 / "rhs_elems.bin", np.int32).reshape(-1, dim + 1)
+    lam = np.fromfile(d1 / "rhs_lambda.bin", np.float64).reshape(nq, dim + 1)
+    w = np.fromfile(d1 / "rhs_weight.bin", np.float64)
+    fq = np.fromfile(d1 / "rhs_fqp.bin", np.float64).reshape(E.shape[0], nq)
+    from ffgpu import quadrature
+    lam_ref, w_ref = quadrature.rule(None, dim)          # FreeFEM's default rule
+    assert np.allclose(lam, lam_ref, rtol=0, atol=1e-15) and np.allclose(w, w_ref, rtol=0, atol=1e-15)
+    xq = quadrature.points(X, E, lam)
+    ref = f(*[xq[..., k] for k in range(dim)])
+    assert np.max(np.abs(fq - ref)) <= 1e-14 * np.max(np.abs(ref))
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+    body2 = r"""
+mesh Th=square(4,4);
+fespace Vh(Th,P1);
+Vh u,v;
+varf a(u,v)=int2d(Th,qft=qf2pT)(x*v) + int2d(Th)(y*v);
+real[int] b=a(0,Vh);
+cout << "bsum " << b.sum << endl;
+"""
+    r, out = run_script(plugin, "fs2.edp", body2)
+    assert "ffgpu: linear form assembled by FreeFEM (volume sources with different quadrature rules)" in out
+    assert any(line.startswith("bsum ") for line in r.stdout.splitlines())
 
 
 def test_p1_stiffness_with_a_p1_coefficient(plugin):
