@@ -492,8 +492,11 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                 const int ee = A.inc_elem[t], ll = A.inc_loc[t];
                 const double meas = A.geo[(int64_t)ee * kGeoStride];
                 const double f = A.fP0 ? A.fP0[(int64_t)ee * BS + lb] : (lb == 0 ? A.f0 : (lb == 1 ? A.f1 : A.f2));
-                racc += A.fint ? A.fint[((int64_t)ee * NN + ll) * BS + lb]
-                               : meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, ll));
+                // explicit roundings: the linear-form-only kernel forms the same sums bit for bit
+                const double add = A.fint ? A.fint[((int64_t)ee * NN + ll) * BS + lb]
+                                          : __dmul_rn(__dmul_rn(meas, f), FE == 1 ? 1.0 / (DIM + 1)
+                                                                                  : basis_integral<DIM, 2>(1.0, ll));
+                racc = __dadd_rn(racc, add);
             }
             __syncwarp();
         }
@@ -600,8 +603,10 @@ __global__ void rhs_kernel(int nnodes, const int32_t *inc_ptr, const int32_t *in
                 int e = inc_elem[p], l = inc_loc[p];
                 double meas = geo[(int64_t)e * kGeoStride];
                 double f = fP0 ? fP0[(int64_t)e * BS + c] : (c == 0 ? f0 : (c == 1 ? f1 : f2));
-                part[sl] += fint ? fint[((int64_t)e * NN + l) * BS + c]
-                                 : meas * f * (FE == 1 ? 1.0 / (DIM + 1) : basis_integral<DIM, 2>(1.0, l));
+                const double add = fint ? fint[((int64_t)e * NN + l) * BS + c]
+                                        : __dmul_rn(__dmul_rn(meas, f), FE == 1 ? 1.0 / (DIM + 1)
+                                                                                : basis_integral<DIM, 2>(1.0, l));
+                part[sl] = __dadd_rn(part[sl], add);
             }
         }
     }
