@@ -391,6 +391,7 @@ struct FillArgs {
     double *rhs;              // NULL: no linear form
     const double *fP0;        // nt*bs or NULL
     const double *fint;       // element vectors of a source at quadrature points, or NULL
+    const double *mloc;       // element mass matrices of a coefficient at quadrature points, or NULL
     double f0, f1, f2;
     double c_mass;
     double lam, mu;           // elasticity
@@ -423,7 +424,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
     int *cols = (int *)sh_raw + w * kCandMax;
     double *acc = (double *)((int *)sh_raw + warps * kCandMax) + (int64_t)w * SLOTS * A.max_deg * BS2;
     const double mfac = DIM == 3 ? 1.0 / 20.0 : 1.0 / 12.0;
-    const bool has_mass = A.c_mass != 0.0;
+    const bool has_mass = A.c_mass != 0.0 && !A.mloc;
 
     for (int a = blockIdx.x * warps + w; a < A.nnodes; a += gridDim.x * warps) {
         int deg = gather_row(a, A.inc_ptr, A.inc_elem, A.nodes, NN, cols, A.status);
@@ -461,6 +462,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     for (int d = 0; d < DIM; ++d) s += __ldg(G + 3 * la + d) * __ldg(G + 3 * lb + d);
                     double val = kap * meas * s;
                     if (has_mass) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
+                    if (A.mloc) val += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     v[0] = val;
                 } else {
                     const P2Pair<DIM> P(G, la, lb);
@@ -468,6 +470,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     if (FE == 2) {
                         v[0] = kap * m * P.trace();
                         if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
+                        if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     } else {
                         const double tr = P.trace();
 #pragma unroll
@@ -829,17 +832,21 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     }
     fa.onbc = mask; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
-    double *fint = nullptr;
+    double *fint = nullptr, *mloc = nullptr;
     if (rh.d) FFGPU_TRY(source_prepare(S, v, M->geo, &fint));
+    int frc = mass_prepare(S, v, M->geo, &mloc);
+    if (frc) { dfree(ctx, fint); return frc; }
     fa.fint = fint;
+    fa.mloc = mloc;
     BoundaryTerms bt;
-    int frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
+    frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
     if (!frc) {
         fa.bptr = bt.ptr; fa.blist = bt.list; fa.bel_elem = bt.bel_elem; fa.brhs = bt.rhs; fa.bmat = bt.mat;
         frc = fill_launch(S, fa);
         boundary_release(S, bt);
     }
     dfree(ctx, fint);
+    dfree(ctx, mloc);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish());

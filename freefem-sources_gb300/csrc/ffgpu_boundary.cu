@@ -135,6 +135,39 @@ __global__ void source_qp_kernel(int nt, int nqp, const double *__restrict__ lam
     for (int i = 0; i < NN * BS; ++i) fint[e * NN * BS + i] = meas * s[i];
 }
 
+// One thread per element: the mass matrix of a coefficient given at quadrature points,
+// |K| sum_q w_q c_q phi_i(lambda_q) phi_j(lambda_q) (Element_Op: problem.cpp:6063-6160, 6337-6437)
+template <int DIM, int NN>
+__global__ void mass_qp_kernel(int nt, int nqp, const double *__restrict__ lam, const double *__restrict__ w,
+                               const double *__restrict__ cqp, const double *__restrict__ geo,
+                               double *__restrict__ mloc) {
+    constexpr int NV = DIM + 1;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= nt) return;
+    double m[NN * (NN + 1) / 2];
+#pragma unroll
+    for (int i = 0; i < NN * (NN + 1) / 2; ++i) m[i] = 0.0;
+    for (int q = 0; q < nqp; ++q) {
+        double l[NV], phi[NN];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) l[i] = lam[q * NV + i];
+        basis_values<DIM, NN>(l, phi);
+        const double wc = w[q] * cqp[e * nqp + q];
+        int p = 0;
+#pragma unroll
+        for (int i = 0; i < NN; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j) m[p++] += wc * phi[i] * phi[j];
+    }
+    const double meas = geo[e * kGeoStride];
+    double *out = mloc + e * NN * NN;
+    int p = 0;
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j, ++p) out[i * NN + j] = out[j * NN + i] = meas * m[p];
+}
+
 // One thread per boundary element: the element vector and Robin matrix of one term.
 template <int DIM, int NN, int BS>
 __global__ void bterm_kernel(BTermArgs A) {
@@ -414,6 +447,31 @@ int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, doubl
     k<<<(int)((S->nt + 127) / 128), 128, 0, ctx->stream>>>(S->nt, v->nqp, lam.d, w.d, fq.d, geo, *fint);
     const int rc = launch_check(ctx, "source_qp");
     if (rc) { dfree(ctx, *fint); *fint = nullptr; }
+    return rc;
+}
+
+int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **mloc) {
+    *mloc = nullptr;
+    if (!v || !v->mass_qp) return FFGPU_OK;
+    FFGPU_CHECK(v->form == FFGPU_FORM_DIFFUSION && S->bs == 1, FFGPU_EINVAL,
+                "a mass coefficient at quadrature points needs the scalar diffusion form");
+    FFGPU_CHECK(v->nqp > 0 && v->nqp <= 64 && v->qp_lambda && v->qp_weight, FFGPU_EINVAL,
+                "mass at quadrature points: 1..64 points with coordinates and weights expected (nqp %d)", v->nqp);
+    ffgpu_ctx *ctx = S->ctx;
+    const int nv = S->dim + 1, nn = S->nn;
+    DevIn<double> lam(v->qp_lambda, (size_t)v->nqp * nv, ctx), w(v->qp_weight, v->nqp, ctx);
+    DevIn<double> cq(v->mass_qp, (size_t)S->nt * v->nqp, ctx);
+    FFGPU_TRY(lam.err); FFGPU_TRY(w.err); FFGPU_TRY(cq.err);
+    FFGPU_CUDA(dalloc(ctx, (void **)mloc, sizeof(double) * (size_t)S->nt * nn * nn));
+    void (*k)(int, int, const double *, const double *, const double *, const double *, double *) = nullptr;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = mass_qp_kernel<2, 3>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = mass_qp_kernel<3, 4>;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = mass_qp_kernel<2, 6>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2) k = mass_qp_kernel<3, 10>;
+    FFGPU_CHECK(k, FFGPU_EINVAL, "mass at quadrature points: unsupported element");
+    k<<<(int)((S->nt + 127) / 128), 128, 0, ctx->stream>>>(S->nt, v->nqp, lam.d, w.d, cq.d, geo, *mloc);
+    const int rc = launch_check(ctx, "mass_qp");
+    if (rc) { dfree(ctx, *mloc); *mloc = nullptr; }
     return rc;
 }
 

@@ -247,6 +247,9 @@ void boundary_release(ffgpu_space *S, BoundaryTerms &bt);
 // form: *fint = nt * nn * bs values |K| sum_q w_q f_q phi_i(lambda_q) ((e*nn + i)*bs + c), or
 // NULL when the varf has none.  geo: the element geometry (measure first).
 int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **fint);
+// Element mass matrices of a coefficient given at quadrature points (ffgpu_varf.mass_qp):
+// *mloc = nt * nn * nn values |K| sum_q w_q c_q phi_i phi_j ((e*nn + i)*nn + j), or NULL.
+int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **mloc);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 

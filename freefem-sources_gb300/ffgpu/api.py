@@ -149,7 +149,8 @@ class VarForm:
         v = Varf()
         v.form = self.form
         v.c_stiff = self.c_stiff
-        v.c_mass = self.c_mass
+        v.c_mass = 0.0 if callable(self.c_mass) else self.c_mass
+        v.mass_qp = None
         v.E = self.E
         v.nu = self.nu
         v.kappa = None
@@ -160,6 +161,8 @@ class VarForm:
         v.f = None
         v.nqp = 0
         v.qp_lambda = v.qp_weight = v.f_qp = None
+        if callable(self.c_mass):
+            self._mass_at_points(v, Vh)
         if callable(self.f):
             self._source_at_points(v, Vh)
         elif np.isscalar(self.f):
@@ -219,13 +222,32 @@ class VarForm:
             v.bterms = C.cast(arr, C.c_void_p).value
         return v
 
+    def _rule_points(self, v: Varf, Vh: FESpace):
+        """The rule (set once in v) and the physical points of every element."""
+        Th = Vh.Th
+        if not hasattr(Th, "coords"):
+            raise ValueError("a coefficient or source function needs the mesh coordinates on the host")
+        lam, w = quadrature.rule(self.quad, Th.dim)
+        self._keep += [lam, w]
+        v.nqp = lam.shape[0]
+        v.qp_lambda = _ptr(lam).value
+        v.qp_weight = _ptr(w).value
+        return lam, quadrature.points(Th.coords, Th.elems, lam)
+
+    def _mass_at_points(self, v: Varf, Vh: FESpace) -> None:
+        """c(x, y[, z]) of the c*u*v term at the quadrature points, as Element_Op takes it."""
+        if self.form != _lib.FORM_DIFFUSION:
+            raise ValueError("a mass coefficient function needs the diffusion form")
+        lam, xq = self._rule_points(v, Vh)
+        val = self.c_mass(*[xq[..., d] for d in range(Vh.Th.dim)])
+        cq = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64), xq.shape[:2]))
+        self._keep.append(cq)
+        v.mass_qp = _ptr(cq).value
+
     def _source_at_points(self, v: Varf, Vh: FESpace) -> None:
         """f(x, y[, z]) at the quadrature points of every element, as Element_rhs takes it."""
         Th = Vh.Th
-        if not hasattr(Th, "coords"):
-            raise ValueError("a function source needs the mesh coordinates on the host")
-        lam, w = quadrature.rule(self.quad, Th.dim)
-        xq = quadrature.points(Th.coords, Th.elems, lam)
+        lam, xq = self._rule_points(v, Vh)
         val = self.f(*[xq[..., d] for d in range(Th.dim)])
         nc = 3 if Vh.kind == "P2vec" else 1
         shape = (Th.nt, lam.shape[0])
@@ -236,10 +258,7 @@ class VarForm:
                 raise ValueError("[P2,P2,P2]: the source function returns three components")
             fq = np.stack([np.broadcast_to(np.asarray(c, np.float64), shape) for c in val], axis=-1)
         fq = np.ascontiguousarray(fq)
-        self._keep += [lam, w, fq]
-        v.nqp = lam.shape[0]
-        v.qp_lambda = _ptr(lam).value
-        v.qp_weight = _ptr(w).value
+        self._keep.append(fq)
         v.f_qp = _ptr(fq).value
 
     def c_bc(self, Vh: FESpace, device_marking: bool = False) -> BC:
@@ -277,7 +296,8 @@ def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tg
                    bterms=(), quad=None) -> VarForm:
     """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v)
     + the boundary terms (BoundaryTerm: robin*u*v + g*v on labelled boundary edges/faces)
-    + on(on, u=g).  f may be a function f(x, y[, z]), taken at the points of `quad`."""
+    + on(on, u=g).  f and c_mass may be functions of the coordinates, f(x, y[, z]), taken at
+    the points of `quad`."""
     return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
                    c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms), quad=quad)
 

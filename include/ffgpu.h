@@ -80,6 +80,11 @@ typedef struct {
     const double *qp_lambda;
     const double *qp_weight;
     const double *f_qp;
+    /* mass_qp: the coefficient of u*v (diffusion form) at the points of the same rule,
+     * mass_qp[k*nqp + q]; when non-NULL it replaces c_mass: the element matrix gains
+     * |K| sum_q qp_weight[q] c_q phi_i(lambda_q) phi_j(lambda_q) (Element_Op,
+     * problem.cpp:6063-6160, 6337-6437). */
+    const double *mass_qp;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or

@@ -244,7 +244,8 @@ static int basis(int dim, int order, const double *l, double G[4][3], double *w,
  *       1 = linear elasticity lambda div u div v + 2 mu eps(u):eps(v)  (P2 vector, 3D)
  * fe:   1 = P1, 2 = P2 scalar, 3 = [P2,P2,P2] (local DOF = comp*10 + node)
  * coef: P0 coefficient per element or NULL (then c0 = 1 multiplies the stiffness)
- * mass: coefficient of u*v (0 = none), P0 per element `mcoef` or constant `mass`
+ * mass: constant coefficient of u*v (0 = none), or mqp: its values at the rule's points,
+ *       mqp[k*nq + q] (a coefficient that is any function of the point, as Element_Op takes it)
  */
 typedef struct {
     int dim, nt, ndofK, fe, form, quad;
@@ -252,6 +253,7 @@ typedef struct {
     const int *elems, *dof;
     const double *coef;
     double E, nu, mass;
+    const double *mqp;
 } ffo_form;
 
 static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = test */) {
@@ -279,8 +281,8 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
                 for (int i = 0; i < nb; ++i)
                     for (int j = 0; j < nb; ++j) M[i * nd + j] += ccc * dw[i][d] * dw[j][d];
             }
-            if (F->mass != 0.0) {
-                double ccc = F->mass * coef;
+            if (F->mass != 0.0 || F->mqp) {
+                double ccc = (F->mqp ? F->mqp[(int64_t)k * nq + q] : F->mass) * coef;
                 for (int i = 0; i < nb; ++i)
                     for (int j = 0; j < nb; ++j) M[i * nd + j] += ccc * w[i] * w[j];
             }
@@ -325,9 +327,9 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
 /* assemble the bilinear form into the hash matrix, element by element (insertion order) */
 int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, int ndofK,
                  const int *dof, int fe, int form, int quad, const double *coef, double E,
-                 double nu, double mass) {
+                 double nu, double mass, const double *mqp) {
     ffo_hm *A = (ffo_hm *)hm;
-    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass};
+    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass, mqp};
     double *M = (double *)malloc(sizeof(double) * ndofK * ndofK);
     for (int k = 0; k < nt; ++k) {
         elem_matrix(&F, k, M);
@@ -343,7 +345,7 @@ int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, i
 void ffo_element_matrix(int dim, const double *X, const int *elems, int k, int ndofK, int fe,
                         int form, int quad, const double *coef, double E, double nu,
                         double mass, double *M) {
-    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass};
+    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass, 0};
     elem_matrix(&F, k, M);
 }
 

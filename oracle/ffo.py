@@ -49,7 +49,8 @@ def lib():
         L.ffo_hm_coo.argtypes = [C.c_void_p, _ip, _ip, _dp]
         L.ffo_hm_csr.argtypes = [C.c_void_p, _ip, _ip, _dp]
         L.ffo_assemble.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
-                                   C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double]
+                                   C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                   C.c_void_p]
         L.ffo_element_matrix.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp]
         L.ffo_rhs.argtypes = [_dp, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int, C.c_int,
@@ -136,9 +137,24 @@ class HashMatrix:
         return y
 
 
+def points_values(Th, quad, fn):
+    """fn(x, y[, z]) at the points of oracle rule `quad` of every element -> (nt, nq[, ...])."""
+    L = lib()
+    dim = Th.dim
+    P, W = np.zeros(14 * 3), np.zeros(14)
+    nq = L.ffo_quad_points(int(quad), P, W)
+    P = P[:nq * dim].reshape(nq, dim)
+    X = Th.coords[Th.elems]                                   # (nt, dim+1, dim)
+    xq = X[:, None, 0, :] * (1.0 - P.sum(axis=1))[None, :, None]
+    for i in range(dim):
+        xq = xq + X[:, None, i + 1, :] * P[None, :, i, None]
+    return fn(*[xq[..., d] for d in range(dim)]), nq
+
+
 def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad=None,
              c_stiff=1.0):
-    """matrix A = a(Vh,Vh) of the oracle (no BC).  Returns a HashMatrix."""
+    """matrix A = a(Vh,Vh) of the oracle (no BC).  Returns a HashMatrix.  mass: constant, or a
+    function c(x, y[, z]) taken at the rule's points."""
     L = lib()
     dim = Th.dim
     if quad is None:
@@ -154,9 +170,14 @@ def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad
     if kappa is not None or c_stiff != 1.0:
         coef = np.ascontiguousarray(
             (np.ones(Th.nt) if kappa is None else np.asarray(kappa, np.float64)) * c_stiff)
+    mqp = None
+    if callable(mass):
+        val, nq = points_values(Th, quad, mass)
+        mqp = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64), (Th.nt, nq)))
+        mass = 0.0
     L.ffo_assemble(A.h, dim, Th.nt, X, el, Vh.ndofK, dof, fe, 1 if form == "elasticity" else 0,
-                   int(quad), _ptr(coef), float(E), float(nu), float(mass))
-    A._keep = coef
+                   int(quad), _ptr(coef), float(E), float(nu), float(mass), _ptr(mqp))
+    A._keep = (coef, mqp)
     return A
 
 
@@ -177,14 +198,7 @@ def rhs(Th, Vh, f=1.0, quad=None):
     fP0 = None
     fqp = None
     if callable(f):
-        P, W = np.zeros(14 * 3), np.zeros(14)
-        nq = L.ffo_quad_points(int(quad), P, W)
-        P = P[:nq * dim].reshape(nq, dim)
-        X = Th.coords[Th.elems]                                   # (nt, dim+1, dim)
-        xq = X[:, None, 0, :] * (1.0 - P.sum(axis=1))[None, :, None]
-        for i in range(dim):
-            xq = xq + X[:, None, i + 1, :] * P[None, :, i, None]
-        val = f(*[xq[..., d] for d in range(dim)])
+        val, nq = points_values(Th, quad, f)
         if nc == 1:
             fqp = np.broadcast_to(np.asarray(val, np.float64), (Th.nt, nq))[..., None]
         else:

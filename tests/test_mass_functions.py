@@ -1,0 +1,67 @@
+"""Mass coefficients that are functions of the point: int(Th)(c(x,y[,z]) * u * v).
+
+FreeFEM takes c at the points of the form's rule (Element_Op, problem.cpp:6063-6160,
+6337-6437).  The fixtures ``mq_*`` hold FreeFEM's matrix, b and solution of
+-div grad u + c u = 1 for four coefficients (P1 and P2, squares and cubes); the oracle and the
+device (``ffgpu_varf.mass_qp``) reproduce the pattern exactly and the values within 1e-12.
+"""
+import numpy as np
+import pytest
+
+import ffgpu
+import ffo
+from ffgpu import mesh
+from ffgpu.fespace import FESpace
+from golden_cases import load, value_errors
+
+CASES = {
+    "mq_sq_p1": ("P1", lambda x, y: 1 + x * y, (1,)),
+    "mq_sq_p2": ("P2", lambda x, y: np.exp(x + y), (1, 2)),
+    "mq_cube_p1": ("P1", lambda x, y, z: 1 + z * x, (1,)),
+    "mq_cube_p2": ("P2", lambda x, y, z: 2 + np.cos(x) * y, (1,)),
+}
+
+
+def space(name):
+    d, sc = load(name)
+    dim = d["coords"].shape[1]
+    Th = mesh.Mesh(dim, d["coords"], d["elems"], d["belems"], d["blabel"], d["vlabel"])
+    Vh = FESpace(Th, CASES[name][0])
+    assert np.array_equal(Vh.dof, d["dof"])
+    return d, sc, Th, Vh
+
+
+def check(d, sc, rp, cl, v, b, u, it):
+    I = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    assert np.array_equal(I, d["I"]) and np.array_equal(cl, d["J"])
+    assert value_errors(v, d["C"], rp).max() <= 1e-12
+    assert np.abs(b - d["b"]).max() <= 1e-12 * np.abs(d["b"]).max()
+    assert np.linalg.norm(u - d["u"]) <= 1e-9 * np.linalg.norm(d["u"])
+    assert abs(it - int(sc["nit"])) <= 2
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_oracle_mass_function_equals_freefem(name):
+    d, sc, Th, Vh = space(name)
+    _, c, labels = CASES[name]
+    A = ffo.assemble(Th, Vh, mass=c)
+    b = ffo.rhs(Th, Vh, f=1.0)
+    ffo.setbc(A, b, Vh.on(labels))
+    rp, cl, v = A.csr()
+    u, it, _, _ = ffo.cg(A, b, eps=1e-12)
+    check(d, sc, rp, cl, v, b, u, it)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
+def test_device_mass_function_equals_freefem(name):
+    from ffgpu.build import build
+    build()
+    d, sc, Th, Vh = space(name)
+    _, c, labels = CASES[name]
+    a = ffgpu.varf_diffusion(c_mass=c, f=1.0, on=labels)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, eps=1e-12, rhs_out=b)
+    rp, cl, v = A.csr()
+    u = A.solve(b)
+    check(d, sc, rp, cl, v, b, u, A.stats.iterations)
