@@ -152,15 +152,69 @@ struct BoundaryRec {
     std::vector<double> g;       // nbe * ncomp, empty: none
 };
 
+// the volume rule of `di`: size, point q (reference coordinates) and its weight
+static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).n; }
+static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).n; }
+static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R2 &P, double &w) {
+    const QuadratureFormular &FI = di.FIT(s);
+    P = R2(FI[q].x, FI[q].y);
+    w = FI[q].a;
+}
+static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R3 &P, double &w) {
+    const GQuadratureFormular<R3> &FI = di.FIV(s);
+    P = R3(FI[q].x, FI[q].y, FI[q].z);
+    w = FI[q].a;
+}
+static void barycentric(const R2 &P, double *l) { l[0] = 1. - P.x - P.y; l[1] = P.x; l[2] = P.y; }
+static void barycentric(const R3 &P, double *l) { l[0] = 1. - P.x - P.y - P.z; l[1] = P.x; l[2] = P.y; l[3] = P.z; }
+
 struct Recognised {
     int fe = 0, form = FFGPU_FORM_DIFFUSION;
     std::vector<double> kappa;
     double c_mass = 0, lam = 0, mu = 0, tgv = 1e30;
+    // a mass coefficient that depends on the point: its values at the points of the rule
+    int nqp = 0;
+    std::vector<double> lam_q, w_q;   // nqp x (dim+1) barycentric coordinates, weights
+    std::vector<double> mqp;          // nt x nqp
     int comp_mask = -1;   // components constrained by on(...) (-1: no on)
     std::vector<int32_t> labels;
     std::vector<BoundaryRec> bterms;   // Robin terms, in varf order
     std::string why;
 };
+
+// a mass term's coefficient at the points of its rule, per element (Element_Op takes it so,
+// problem.cpp:6063-6160, 6337-6437); every such term must use one rule
+template <class MMesh, class FES>
+static bool mass_at_points(Stack stack, const C_F0 &coef, const MMesh &Th, const FES &Uh,
+                           const CDomainOfIntegration &di, Recognised &r) {
+    typedef typename Dim<MMesh>::Rd Rd;
+    const int d = Dim<MMesh>::d, nt = Th.nt;
+    const int nq = rule_size(stack, di, &Th);
+    std::vector<Rd> P(nq);
+    std::vector<double> lam((size_t)nq * (d + 1)), w(nq);
+    for (int q = 0; q < nq; ++q) {
+        rule_point(stack, di, q, P[q], w[q]);
+        barycentric(P[q], &lam[(size_t)q * (d + 1)]);
+    }
+    if (r.nqp == 0) {
+        if (nq < 1 || nq > 64) { r.why = "quadrature rule size"; return false; }
+        r.nqp = nq;
+        r.lam_q = lam;
+        r.w_q = w;
+        r.mqp.assign((size_t)nt * nq, 0.0);
+    } else if (lam != r.lam_q || w != r.w_q) {
+        r.why = "mass terms with different quadrature rules";
+        return false;
+    }
+    for (int k = 0; k < nt; ++k) {
+        typename FES::FElement FK = Uh[k];
+        for (int q = 0; q < nq; ++q) {
+            MeshPointStack(stack)->set(Th[k](P[q]), P[q], FK);
+            r.mqp[(size_t)k * nq + q] += GetAny<double>(coef.eval(stack));
+        }
+    }
+    return true;
+}
 
 // element type of a space: FFGPU_FE_* or 0
 static int fe_kind(const FESpace &Uh) {
@@ -417,8 +471,14 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
             // degree of the integrand for these two operators (coefficient constant on elements)
             const int order = r.fe == FFGPU_FE_P1 ? 1 : 2;
             const int deg = (pu ? order - 1 : order) + (pv ? order - 1 : order);
-            if (ex < deg) { r.why = "quadrature not exact for the form"; ok = false; break; }
             const bool constant = l->second.LeftValue()->MeshIndependent();
+            if (nc == 1 && pu == 0 && pv == 0 && ju == 0 && jv == 0 && (!constant || ex < deg)) {
+                // a mass coefficient that depends on the point, or a rule that does not integrate
+                // the mass exactly: the coefficient at the rule's points
+                if (!mass_at_points(stack, l->second, Th, Uh, di, r)) { ok = false; break; }
+                continue;
+            }
+            if (ex < deg) { r.why = "quadrature not exact for the form"; ok = false; break; }
             if (nc == 3) {
                 // elasticity: coefficients independent of the mesh point
                 if (!constant) { r.why = "coefficient not constant"; ok = false; break; }
@@ -468,10 +528,12 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
             const double *c = &kx[(size_t)k * (d + 1)];
             for (int a = 1; a < d; ++a)
                 if (c[a] != c[0]) { r.why = "anisotropic diffusion"; return false; }
-            if (c[d] != m0) { r.why = "mass coefficient not constant"; return false; }
+            if (r.nqp)   // constant mass terms join the values at the points
+                for (int q = 0; q < r.nqp; ++q) r.mqp[(size_t)k * r.nqp + q] += c[d];
+            else if (c[d] != m0) { r.why = "mass coefficient not constant"; return false; }
             r.kappa[k] = c[0];
         }
-        r.c_mass = m0;
+        r.c_mass = r.nqp ? 0.0 : m0;
         return true;
     }
     // isotropic elasticity: T[(j,p),(i,q)] = lambda d_jp d_iq + mu (d_ij d_pq + d_jq d_ip)
@@ -554,6 +616,11 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
                   << " ndof " << Uh.NbOfDF;
         if (r.form == FFGPU_FORM_ELASTICITY) std::cout << " lambda " << r.lam << " mu " << r.mu;
         else std::cout << " kappa-check " << std::setprecision(17) << ksum << " mass " << r.c_mass;
+        if (r.nqp) {
+            double ms = 0;
+            for (size_t k = 0; k < r.mqp.size(); ++k) ms += r.mqp[k] * (double)(k % 7 + 1);
+            std::cout << " | mass at " << r.nqp << " points, mq-check " << std::setprecision(17) << ms;
+        }
         std::cout << " tgv " << ds.tgv << " components " << r.comp_mask << " labels";
         for (size_t i = 0; i < r.labels.size(); ++i) std::cout << " " << r.labels[i];
         for (size_t t = 0; t < r.bterms.size(); ++t) {
@@ -584,6 +651,7 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         dump(p + "/belems.bin", BE.data(), BE.size() * sizeof(int32_t));
         dump(p + "/blabel.bin", BL.data(), BL.size() * sizeof(int32_t));
         dump(p + "/kappa.bin", r.kappa.data(), r.kappa.size() * sizeof(double));
+        dump(p + "/mass_qp.bin", r.mqp.data(), r.mqp.size() * sizeof(double));
         for (size_t t = 0; t < r.bterms.size(); ++t)
             dump(p + "/robin" + std::to_string(t) + ".bin", r.bterms[t].robin.data(), r.bterms[t].robin.size() * sizeof(double));
     }
@@ -603,6 +671,12 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         } else {
             v.kappa = r.kappa.data();
             v.c_mass = r.c_mass;
+            if (r.nqp) {
+                v.nqp = r.nqp;
+                v.qp_lambda = r.lam_q.data();
+                v.qp_weight = r.w_q.data();
+                v.mass_qp = r.mqp.data();
+            }
         }
         const std::vector<ffgpu_bterm> bt = c_bterms(r.bterms);
         v.nbterms = (int)bt.size();
@@ -689,22 +763,6 @@ struct RecognisedRhs {
     int comp_mask = -1;
     std::string why;
 };
-
-// the volume rule of `di`: size, point q (reference coordinates) and its weight
-static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh *) { return di.FIT(s).n; }
-static int rule_size(Stack s, const CDomainOfIntegration &di, const Mesh3 *) { return di.FIV(s).n; }
-static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R2 &P, double &w) {
-    const QuadratureFormular &FI = di.FIT(s);
-    P = R2(FI[q].x, FI[q].y);
-    w = FI[q].a;
-}
-static void rule_point(Stack s, const CDomainOfIntegration &di, int q, R3 &P, double &w) {
-    const GQuadratureFormular<R3> &FI = di.FIV(s);
-    P = R3(FI[q].x, FI[q].y, FI[q].z);
-    w = FI[q].a;
-}
-static void barycentric(const R2 &P, double *l) { l[0] = 1. - P.x - P.y; l[1] = P.x; l[2] = P.y; }
-static void barycentric(const R3 &P, double *l) { l[0] = 1. - P.x - P.y - P.z; l[1] = P.x; l[2] = P.y; l[3] = P.z; }
 
 // Every volume source term taken at the points of its rule, as Element_rhs takes it
 // (problem.cpp:7839-7911, 7917-7990), summed per (element, point, component); the terms must
