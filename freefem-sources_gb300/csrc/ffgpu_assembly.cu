@@ -392,6 +392,7 @@ struct FillArgs {
     const double *fP0;        // nt*bs or NULL
     const double *fint;       // element vectors of a source at quadrature points, or NULL
     const double *mloc;       // element mass matrices of a coefficient at quadrature points, or NULL
+    const double *kloc;       // element stiffness matrices of a coefficient at quadrature points, or NULL
     double f0, f1, f2;
     double c_mass;
     double lam, mu;           // elasticity
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     double s = 0;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d) s += __ldg(G + 3 * la + d) * __ldg(G + 3 * lb + d);
-                    double val = kap * meas * s;
+                    double val = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * meas * s;
                     if (has_mass) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
                     if (A.mloc) val += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     v[0] = val;
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     const P2Pair<DIM> P(G, la, lb);
                     const double m = meas * mfac;
                     if (FE == 2) {
-                        v[0] = kap * m * P.trace();
+                        v[0] = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * m * P.trace();
                         if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
                         if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     } else {
@@ -834,10 +835,13 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
     double *fint = nullptr, *mloc = nullptr;
     if (rh.d) FFGPU_TRY(source_prepare(S, v, M->geo, &fint));
+    double *kloc = nullptr;
     int frc = mass_prepare(S, v, M->geo, &mloc);
-    if (frc) { dfree(ctx, fint); return frc; }
+    if (!frc) frc = stiff_prepare(S, v, M->geo, &kloc);
+    if (frc) { dfree(ctx, fint); dfree(ctx, mloc); return frc; }
     fa.fint = fint;
     fa.mloc = mloc;
+    fa.kloc = kloc;
     BoundaryTerms bt;
     frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
     if (!frc) {
@@ -847,6 +851,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     }
     dfree(ctx, fint);
     dfree(ctx, mloc);
+    dfree(ctx, kloc);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish());

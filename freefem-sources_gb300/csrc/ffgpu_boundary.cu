@@ -168,6 +168,68 @@ __global__ void mass_qp_kernel(int nt, int nqp, const double *__restrict__ lam, 
         for (int j = 0; j <= i; ++j, ++p) out[i * NN + j] = out[j * NN + i] = meas * m[p];
 }
 
+// One thread per element: the stiffness matrix of a coefficient given at quadrature points,
+// |K| sum_q w_q k_q grad phi_i . grad phi_j, with grad lambda_i = G_i from the element geometry
+// (P2: grad of l(2l-1) = (4 l - 1) G, of 4 l_a l_b = 4 (l_a G_b + l_b G_a))
+template <int DIM, int NN>
+__global__ void stiff_qp_kernel(int nt, int nqp, const double *__restrict__ lam, const double *__restrict__ w,
+                                const double *__restrict__ kqp, const double *__restrict__ geo,
+                                double *__restrict__ kloc) {
+    constexpr int NV = DIM + 1;
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= nt) return;
+    const double *ge = geo + e * kGeoStride;
+    double G[NV][DIM];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) G[i][d] = ge[4 + 3 * i + d];
+    double m[NN * (NN + 1) / 2];
+#pragma unroll
+    for (int i = 0; i < NN * (NN + 1) / 2; ++i) m[i] = 0.0;
+    for (int q = 0; q < nqp; ++q) {
+        double l[NV], g[NN][DIM];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) l[i] = lam[q * NV + i];
+        if (NN == NV) {
+#pragma unroll
+            for (int i = 0; i < NV; ++i)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) g[i][d] = G[i][d];
+        } else {
+#pragma unroll
+            for (int i = 0; i < NV; ++i)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) g[i][d] = (4. * l[i] - 1.) * G[i][d];
+#pragma unroll
+            for (int k = 0; k < NN - NV; ++k) {
+                const int a = DIM == 2 ? kTriEdge[k][0] : kTetEdge[k][0];
+                const int b = DIM == 2 ? kTriEdge[k][1] : kTetEdge[k][1];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) g[NV + k][d] = 4. * (l[a] * G[b][d] + l[b] * G[a][d]);
+            }
+        }
+        const double wk = w[q] * kqp[e * nqp + q];
+        int p = 0;
+#pragma unroll
+        for (int i = 0; i < NN; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+                double s = 0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) s += g[i][d] * g[j][d];
+                m[p++] += wk * s;
+            }
+    }
+    const double meas = ge[0];
+    double *out = kloc + e * NN * NN;
+    int p = 0;
+#pragma unroll
+    for (int i = 0; i < NN; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j, ++p) out[i * NN + j] = out[j * NN + i] = meas * m[p];
+}
+
 // One thread per boundary element: the element vector and Robin matrix of one term.
 template <int DIM, int NN, int BS>
 __global__ void bterm_kernel(BTermArgs A) {
@@ -472,6 +534,31 @@ int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double 
     k<<<(int)((S->nt + 127) / 128), 128, 0, ctx->stream>>>(S->nt, v->nqp, lam.d, w.d, cq.d, geo, *mloc);
     const int rc = launch_check(ctx, "mass_qp");
     if (rc) { dfree(ctx, *mloc); *mloc = nullptr; }
+    return rc;
+}
+
+int stiff_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **kloc) {
+    *kloc = nullptr;
+    if (!v || !v->stiff_qp) return FFGPU_OK;
+    FFGPU_CHECK(v->form == FFGPU_FORM_DIFFUSION && S->bs == 1, FFGPU_EINVAL,
+                "a stiffness coefficient at quadrature points needs the scalar diffusion form");
+    FFGPU_CHECK(v->nqp > 0 && v->nqp <= 64 && v->qp_lambda && v->qp_weight, FFGPU_EINVAL,
+                "stiffness at quadrature points: 1..64 points with coordinates and weights expected (nqp %d)", v->nqp);
+    ffgpu_ctx *ctx = S->ctx;
+    const int nv = S->dim + 1, nn = S->nn;
+    DevIn<double> lam(v->qp_lambda, (size_t)v->nqp * nv, ctx), w(v->qp_weight, v->nqp, ctx);
+    DevIn<double> kq(v->stiff_qp, (size_t)S->nt * v->nqp, ctx);
+    FFGPU_TRY(lam.err); FFGPU_TRY(w.err); FFGPU_TRY(kq.err);
+    FFGPU_CUDA(dalloc(ctx, (void **)kloc, sizeof(double) * (size_t)S->nt * nn * nn));
+    void (*k)(int, int, const double *, const double *, const double *, const double *, double *) = nullptr;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P1) k = stiff_qp_kernel<2, 3>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P1) k = stiff_qp_kernel<3, 4>;
+    if (S->dim == 2 && S->fe == FFGPU_FE_P2) k = stiff_qp_kernel<2, 6>;
+    if (S->dim == 3 && S->fe == FFGPU_FE_P2) k = stiff_qp_kernel<3, 10>;
+    FFGPU_CHECK(k, FFGPU_EINVAL, "stiffness at quadrature points: unsupported element");
+    k<<<(int)((S->nt + 127) / 128), 128, 0, ctx->stream>>>(S->nt, v->nqp, lam.d, w.d, kq.d, geo, *kloc);
+    const int rc = launch_check(ctx, "stiff_qp");
+    if (rc) { dfree(ctx, *kloc); *kloc = nullptr; }
     return rc;
 }
 

@@ -250,6 +250,9 @@ int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, doubl
 // Element mass matrices of a coefficient given at quadrature points (ffgpu_varf.mass_qp):
 // *mloc = nt * nn * nn values |K| sum_q w_q c_q phi_i phi_j ((e*nn + i)*nn + j), or NULL.
 int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **mloc);
+// Element stiffness matrices of a coefficient given at quadrature points (ffgpu_varf.stiff_qp):
+// *kloc = nt * nn * nn values |K| sum_q w_q k_q grad phi_i . grad phi_j, or NULL.
+int stiff_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **kloc);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 

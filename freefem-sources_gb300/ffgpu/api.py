@@ -154,7 +154,10 @@ class VarForm:
         v.E = self.E
         v.nu = self.nu
         v.kappa = None
-        if self.kappa is not None:
+        v.stiff_qp = None
+        if callable(self.kappa):
+            self._stiff_at_points(v, Vh)
+        elif self.kappa is not None:
             k = self.kappa if hasattr(self.kappa, "data_ptr") else np.ascontiguousarray(self.kappa, np.float64)
             self._keep.append(k)
             v.kappa = _ptr(k).value
@@ -244,6 +247,16 @@ class VarForm:
         self._keep.append(cq)
         v.mass_qp = _ptr(cq).value
 
+    def _stiff_at_points(self, v: Varf, Vh: FESpace) -> None:
+        """c_stiff * kappa(x, y[, z]) of the grad u . grad v term at the quadrature points."""
+        if self.form != _lib.FORM_DIFFUSION:
+            raise ValueError("a stiffness coefficient function needs the diffusion form")
+        lam, xq = self._rule_points(v, Vh)
+        val = self.kappa(*[xq[..., d] for d in range(Vh.Th.dim)])
+        kq = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64) * self.c_stiff, xq.shape[:2]))
+        self._keep.append(kq)
+        v.stiff_qp = _ptr(kq).value
+
     def _source_at_points(self, v: Varf, Vh: FESpace) -> None:
         """f(x, y[, z]) at the quadrature points of every element, as Element_rhs takes it."""
         Th = Vh.Th
@@ -296,8 +309,8 @@ def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tg
                    bterms=(), quad=None) -> VarForm:
     """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v)
     + the boundary terms (BoundaryTerm: robin*u*v + g*v on labelled boundary edges/faces)
-    + on(on, u=g).  f and c_mass may be functions of the coordinates, f(x, y[, z]), taken at
-    the points of `quad`."""
+    + on(on, u=g).  kappa, c_mass and f may be functions of the coordinates, f(x, y[, z]),
+    taken at the points of `quad`."""
     return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
                    c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms), quad=quad)
 

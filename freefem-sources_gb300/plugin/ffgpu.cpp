@@ -176,17 +176,18 @@ struct Recognised {
     int nqp = 0;
     std::vector<double> lam_q, w_q;   // nqp x (dim+1) barycentric coordinates, weights
     std::vector<double> mqp;          // nt x nqp
+    std::vector<double> kqp[3];       // per derivative d: nt x nqp (grad u . grad v at the points)
     int comp_mask = -1;   // components constrained by on(...) (-1: no on)
     std::vector<int32_t> labels;
     std::vector<BoundaryRec> bterms;   // Robin terms, in varf order
     std::string why;
 };
 
-// a mass term's coefficient at the points of its rule, per element (Element_Op takes it so,
-// problem.cpp:6063-6160, 6337-6437); every such term must use one rule
+// a term's coefficient at the points of its rule, per element, added into `out` (Element_Op
+// takes it so, problem.cpp:6063-6160, 6337-6437); every such term must use one rule
 template <class MMesh, class FES>
-static bool mass_at_points(Stack stack, const C_F0 &coef, const MMesh &Th, const FES &Uh,
-                           const CDomainOfIntegration &di, Recognised &r) {
+static bool coef_at_points(Stack stack, const C_F0 &coef, const MMesh &Th, const FES &Uh,
+                           const CDomainOfIntegration &di, Recognised &r, std::vector<double> &out) {
     typedef typename Dim<MMesh>::Rd Rd;
     const int d = Dim<MMesh>::d, nt = Th.nt;
     const int nq = rule_size(stack, di, &Th);
@@ -201,16 +202,16 @@ static bool mass_at_points(Stack stack, const C_F0 &coef, const MMesh &Th, const
         r.nqp = nq;
         r.lam_q = lam;
         r.w_q = w;
-        r.mqp.assign((size_t)nt * nq, 0.0);
     } else if (lam != r.lam_q || w != r.w_q) {
-        r.why = "mass terms with different quadrature rules";
+        r.why = "terms at quadrature points with different rules";
         return false;
     }
+    if (out.empty()) out.assign((size_t)nt * nq, 0.0);
     for (int k = 0; k < nt; ++k) {
         typename FES::FElement FK = Uh[k];
         for (int q = 0; q < nq; ++q) {
             MeshPointStack(stack)->set(Th[k](P[q]), P[q], FK);
-            r.mqp[(size_t)k * nq + q] += GetAny<double>(coef.eval(stack));
+            out[(size_t)k * nq + q] += GetAny<double>(coef.eval(stack));
         }
     }
     return true;
@@ -475,7 +476,7 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
             if (nc == 1 && pu == 0 && pv == 0 && ju == 0 && jv == 0 && (!constant || ex < deg)) {
                 // a mass coefficient that depends on the point, or a rule that does not integrate
                 // the mass exactly: the coefficient at the rule's points
-                if (!mass_at_points(stack, l->second, Th, Uh, di, r)) { ok = false; break; }
+                if (!coef_at_points(stack, l->second, Th, Uh, di, r, r.mqp)) { ok = false; break; }
                 continue;
             }
             if (ex < deg) { r.why = "quadrature not exact for the form"; ok = false; break; }
@@ -500,6 +501,8 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
             // as its average by the form's own quadrature rule (the gradients are constant on
             // the element); other terms need it constant on every element (P0)
             const bool p1_stiff = r.fe == FFGPU_FE_P1 && pu == pv && pu > 0;
+            std::vector<double> cterm(nt);   // the term's value per element, added once all pass
+            bool at_points = false;
             for (int k = 0; k < nt; ++k) {
                 typename FES::FElement FK = Uh[k];
                 MeshPointStack(stack)->set(Th[k](pa), pa, FK);
@@ -508,13 +511,25 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
                 const double cb = GetAny<double>(l->second.eval(stack));
                 if (!(std::fabs(ca - cb) <= 1e-14 * std::max(std::fabs(ca), std::fabs(cb)))) {
                     if (!p1_stiff) {
+                        // a P2 stiffness term dx_d(u) dx_d(v): its coefficient at the rule's points
+                        if (pu == pv && pu > 0 && ju == 0 && jv == 0) { at_points = true; break; }
                         r.why = "coefficient not constant on elements (a P1 stiffness term takes any)"; ok = false; break;
                     }
                     ca = rule_average(stack, l->second, Th[k], FK, di);
                 }
-                if (pu == pv && pu > 0) kx[(size_t)k * (d + 1) + pu - 1] += ca;
-                else if (pu == 0 && pv == 0) kx[(size_t)k * (d + 1) + d] += ca;
-                else if (ca != 0.0) { r.why = "mixed derivative term"; ok = false; break; }
+                if (!(pu == pv && pu > 0) && !(pu == 0 && pv == 0) && ca != 0.0) {
+                    r.why = "mixed derivative term"; ok = false; break;
+                }
+                cterm[k] = ca;
+            }
+            if (!ok) break;
+            if (at_points) {
+                if (!coef_at_points(stack, l->second, Th, Uh, di, r, r.kqp[pu - 1])) { ok = false; break; }
+                continue;
+            }
+            for (int k = 0; k < nt; ++k) {
+                if (pu == pv && pu > 0) kx[(size_t)k * (d + 1) + pu - 1] += cterm[k];
+                else if (pu == 0 && pv == 0) kx[(size_t)k * (d + 1) + d] += cterm[k];
             }
         }
     }
@@ -528,12 +543,25 @@ static bool recognise(Stack stack, const list<C_F0> &largs, const MMesh &Th, con
             const double *c = &kx[(size_t)k * (d + 1)];
             for (int a = 1; a < d; ++a)
                 if (c[a] != c[0]) { r.why = "anisotropic diffusion"; return false; }
-            if (r.nqp)   // constant mass terms join the values at the points
+            if (!r.mqp.empty())   // constant mass terms join the values at the points
                 for (int q = 0; q < r.nqp; ++q) r.mqp[(size_t)k * r.nqp + q] += c[d];
             else if (c[d] != m0) { r.why = "mass coefficient not constant"; return false; }
             r.kappa[k] = c[0];
         }
-        r.c_mass = r.nqp ? 0.0 : m0;
+        r.c_mass = r.mqp.empty() ? m0 : 0.0;
+        bool at = false;
+        for (int a = 0; a < d; ++a) at |= !r.kqp[a].empty();
+        if (at) {
+            // stiffness at the points: the constant / P0 parts join, every derivative alike
+            for (int a = 0; a < d; ++a) {
+                if (r.kqp[a].empty()) r.kqp[a].assign((size_t)nt * r.nqp, 0.0);
+                for (int k = 0; k < nt; ++k)
+                    for (int q = 0; q < r.nqp; ++q) r.kqp[a][(size_t)k * r.nqp + q] += kx[(size_t)k * (d + 1) + a];
+            }
+            for (int a = 1; a < d; ++a)
+                if (r.kqp[a] != r.kqp[0]) { r.why = "anisotropic diffusion"; return false; }
+            for (int k = 0; k < nt; ++k) r.kappa[k] = 1.0;
+        }
         return true;
     }
     // isotropic elasticity: T[(j,p),(i,q)] = lambda d_jp d_iq + mu (d_ij d_pq + d_jq d_ip)
@@ -616,10 +644,15 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
                   << " ndof " << Uh.NbOfDF;
         if (r.form == FFGPU_FORM_ELASTICITY) std::cout << " lambda " << r.lam << " mu " << r.mu;
         else std::cout << " kappa-check " << std::setprecision(17) << ksum << " mass " << r.c_mass;
-        if (r.nqp) {
+        if (!r.mqp.empty()) {
             double ms = 0;
             for (size_t k = 0; k < r.mqp.size(); ++k) ms += r.mqp[k] * (double)(k % 7 + 1);
             std::cout << " | mass at " << r.nqp << " points, mq-check " << std::setprecision(17) << ms;
+        }
+        if (!r.kqp[0].empty()) {
+            double ks = 0;
+            for (size_t k = 0; k < r.kqp[0].size(); ++k) ks += r.kqp[0][k] * (double)(k % 7 + 1);
+            std::cout << " | stiffness at " << r.nqp << " points, kq-check " << std::setprecision(17) << ks;
         }
         std::cout << " tgv " << ds.tgv << " components " << r.comp_mask << " labels";
         for (size_t i = 0; i < r.labels.size(); ++i) std::cout << " " << r.labels[i];
@@ -652,6 +685,7 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         dump(p + "/blabel.bin", BL.data(), BL.size() * sizeof(int32_t));
         dump(p + "/kappa.bin", r.kappa.data(), r.kappa.size() * sizeof(double));
         dump(p + "/mass_qp.bin", r.mqp.data(), r.mqp.size() * sizeof(double));
+        dump(p + "/stiff_qp.bin", r.kqp[0].data(), r.kqp[0].size() * sizeof(double));
         for (size_t t = 0; t < r.bterms.size(); ++t)
             dump(p + "/robin" + std::to_string(t) + ".bin", r.bterms[t].robin.data(), r.bterms[t].robin.size() * sizeof(double));
     }
@@ -675,7 +709,8 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
                 v.nqp = r.nqp;
                 v.qp_lambda = r.lam_q.data();
                 v.qp_weight = r.w_q.data();
-                v.mass_qp = r.mqp.data();
+                v.mass_qp = r.mqp.empty() ? nullptr : r.mqp.data();
+                v.stiff_qp = r.kqp[0].empty() ? nullptr : r.kqp[0].data();
             }
         }
         const std::vector<ffgpu_bterm> bt = c_bterms(r.bterms);

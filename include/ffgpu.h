@@ -85,6 +85,10 @@ typedef struct {
      * |K| sum_q qp_weight[q] c_q phi_i(lambda_q) phi_j(lambda_q) (Element_Op,
      * problem.cpp:6063-6160, 6337-6437). */
     const double *mass_qp;
+    /* stiff_qp: the coefficient of grad u . grad v (diffusion form) at the points of the same
+     * rule, stiff_qp[k*nqp + q]; when non-NULL it replaces kappa and c_stiff: the element matrix
+     * gains |K| sum_q qp_weight[q] k_q grad phi_i(lambda_q) . grad phi_j(lambda_q). */
+    const double *stiff_qp;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or

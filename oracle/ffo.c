@@ -244,6 +244,7 @@ static int basis(int dim, int order, const double *l, double G[4][3], double *w,
  *       1 = linear elasticity lambda div u div v + 2 mu eps(u):eps(v)  (P2 vector, 3D)
  * fe:   1 = P1, 2 = P2 scalar, 3 = [P2,P2,P2] (local DOF = comp*10 + node)
  * coef: P0 coefficient per element or NULL (then c0 = 1 multiplies the stiffness)
+ * kqp:  or the stiffness coefficient at the rule's points, kqp[k*nq + q] (replaces coef)
  * mass: constant coefficient of u*v (0 = none), or mqp: its values at the rule's points,
  *       mqp[k*nq + q] (a coefficient that is any function of the point, as Element_Op takes it)
  */
@@ -254,6 +255,7 @@ typedef struct {
     const double *coef;
     double E, nu, mass;
     const double *mqp;
+    const double *kqp;   /* stiffness coefficient at the rule's points (replaces coef), or NULL */
 } ffo_form;
 
 static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = test */) {
@@ -274,7 +276,7 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
         double coef = mes * W[q];
         int nb = basis(dim, order, l, G, w, dw);
         if (F->form == 0) {
-            double c = F->coef ? F->coef[k] : 1.0;
+            double c = F->kqp ? F->kqp[(int64_t)k * nq + q] : (F->coef ? F->coef[k] : 1.0);
             /* one term per derivative, as the varf lists them: dx(u)*dx(v) + dy(u)*dy(v) [+ dz] */
             for (int d = 0; d < dim; ++d) {
                 double ccc = c * coef;
@@ -327,9 +329,9 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
 /* assemble the bilinear form into the hash matrix, element by element (insertion order) */
 int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, int ndofK,
                  const int *dof, int fe, int form, int quad, const double *coef, double E,
-                 double nu, double mass, const double *mqp) {
+                 double nu, double mass, const double *mqp, const double *kqp) {
     ffo_hm *A = (ffo_hm *)hm;
-    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass, mqp};
+    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass, mqp, kqp};
     double *M = (double *)malloc(sizeof(double) * ndofK * ndofK);
     for (int k = 0; k < nt; ++k) {
         elem_matrix(&F, k, M);
@@ -345,7 +347,7 @@ int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, i
 void ffo_element_matrix(int dim, const double *X, const int *elems, int k, int ndofK, int fe,
                         int form, int quad, const double *coef, double E, double nu,
                         double mass, double *M) {
-    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass, 0};
+    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass, 0, 0};
     elem_matrix(&F, k, M);
 }
 

@@ -50,7 +50,7 @@ def lib():
         L.ffo_hm_csr.argtypes = [C.c_void_p, _ip, _ip, _dp]
         L.ffo_assemble.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
                                    C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double,
-                                   C.c_void_p]
+                                   C.c_void_p, C.c_void_p]
         L.ffo_element_matrix.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp]
         L.ffo_rhs.argtypes = [_dp, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int, C.c_int,
@@ -153,8 +153,9 @@ def points_values(Th, quad, fn):
 
 def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad=None,
              c_stiff=1.0):
-    """matrix A = a(Vh,Vh) of the oracle (no BC).  Returns a HashMatrix.  mass: constant, or a
-    function c(x, y[, z]) taken at the rule's points."""
+    """matrix A = a(Vh,Vh) of the oracle (no BC).  Returns a HashMatrix.  kappa: P0 array or a
+    function k(x, y[, z]); mass: constant or a function c(x, y[, z]); functions are taken at the
+    rule's points."""
     L = lib()
     dim = Th.dim
     if quad is None:
@@ -167,7 +168,11 @@ def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad
     dof = np.ascontiguousarray(Vh.dof, np.int32)
     fe = {"P1": 1, "P2": 2, "P2vec": 3}[Vh.kind]
     coef = None
-    if kappa is not None or c_stiff != 1.0:
+    kqp = None
+    if callable(kappa):
+        val, nq = points_values(Th, quad, kappa)
+        kqp = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64) * c_stiff, (Th.nt, nq)))
+    elif kappa is not None or c_stiff != 1.0:
         coef = np.ascontiguousarray(
             (np.ones(Th.nt) if kappa is None else np.asarray(kappa, np.float64)) * c_stiff)
     mqp = None
@@ -176,8 +181,8 @@ def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad
         mqp = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64), (Th.nt, nq)))
         mass = 0.0
     L.ffo_assemble(A.h, dim, Th.nt, X, el, Vh.ndofK, dof, fe, 1 if form == "elasticity" else 0,
-                   int(quad), _ptr(coef), float(E), float(nu), float(mass), _ptr(mqp))
-    A._keep = (coef, mqp)
+                   int(quad), _ptr(coef), float(E), float(nu), float(mass), _ptr(mqp), _ptr(kqp))
+    A._keep = (coef, mqp, kqp)
     return A
 
 
@@ -372,7 +377,11 @@ def element_contributions(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, m
     X = np.ascontiguousarray(Th.coords, np.float64)
     el = np.ascontiguousarray(Th.elems, np.int32)
     coef = None
-    if kappa is not None or c_stiff != 1.0:
+    kqp = None
+    if callable(kappa):
+        val, nq = points_values(Th, quad, kappa)
+        kqp = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64) * c_stiff, (Th.nt, nq)))
+    elif kappa is not None or c_stiff != 1.0:
         coef = np.ascontiguousarray(
             (np.ones(Th.nt) if kappa is None else np.asarray(kappa, np.float64)) * c_stiff)
     V = np.empty((Th.nt, nd, nd))

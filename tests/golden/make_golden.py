@@ -298,6 +298,33 @@ MASS_CASES = {
 }
 
 
+# stiffness coefficients that are functions of the point
+STIFF_CASES = {
+    "sq_p1": ("mesh Th=square(5,4);", "P1", "int2d(Th)", "1+x*x*y", "1,3"),
+    "sq_p2": ("mesh Th=square(4,3);", "P2", "int2d(Th)", "exp(x-y)", "1,2"),
+    "cube_p2": ("mesh3 Th=cube(2,2,1);", "P2", "int3d(Th)", "1+x*y*z", "1,2"),
+}
+
+
+def case_stiff_function(which):
+    """-div(k grad u) = 1 with k a function of the point: FreeFEM's matrix, b and u."""
+    mesh_line, kind, dom, k, labels = STIFF_CASES[which]
+    three = "mesh3" in mesh_line
+    grad = "dx(u)*dx(v)+dy(u)*dy(v)" + ("+dz(u)*dz(v)" if three else "")
+    body = HEAD + ("load \"msh3\"\n" if three else "") + mesh_line + f"""
+fespace Vh(Th,{kind});
+Vh u,v;
+varf a(u,v)={dom}(({k})*({grad})) + {dom}(1.*v) + on({labels},u=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-12,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u[]=0; u[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + (DUMP_MESH3 if three else DUMP_MESH2) + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u[][k] << endl;\n"
+    return body, {}
+
+
 def case_mass_function(which):
     """-div grad u + c(x) u = 1 with c a function of the point: FreeFEM's matrix, b and u."""
     mesh_line, kind, dom, c, labels = MASS_CASES[which]
@@ -487,6 +514,7 @@ CASES = {
     **{f"p2num_{w}": (lambda w=w: case_p2_numbering(w)) for w in P2NUM_MESHES},
     **{f"src_{w}": (lambda w=w: case_source_function(w)) for w in SOURCE_CASES},
     **{f"mq_{w}": (lambda w=w: case_mass_function(w)) for w in MASS_CASES},
+    **{f"kq_{w}": (lambda w=w: case_stiff_function(w)) for w in STIFF_CASES},
     "p1sq_n6_tgvm1": lambda: case_p1_square_tgv(6, -1, "GMRES"),
     "p1sq_n6_tgvm2": lambda: case_p1_square_tgv(6, -2, "CG"),
     "p1sq_n6_tgvm3": lambda: case_p1_square_tgv(6, -3, "GMRES"),

@@ -1,9 +1,11 @@
-"""Mass coefficients that are functions of the point: int(Th)(c(x,y[,z]) * u * v).
+"""Matrix coefficients that are functions of the point: int(Th)(c(x,y[,z]) * u * v) and
+int(Th)(k(x,y[,z]) * grad u . grad v).
 
-FreeFEM takes c at the points of the form's rule (Element_Op, problem.cpp:6063-6160,
+FreeFEM takes them at the points of the form's rule (Element_Op, problem.cpp:6063-6160,
 6337-6437).  The fixtures ``mq_*`` hold FreeFEM's matrix, b and solution of
--div grad u + c u = 1 for four coefficients (P1 and P2, squares and cubes); the oracle and the
-device (``ffgpu_varf.mass_qp``) reproduce the pattern exactly and the values within 1e-12.
+-div grad u + c u = 1 for four mass coefficients, ``kq_*`` those of -div(k grad u) = 1 for
+three stiffness coefficients (P1 and P2, squares and cubes); the oracle and the device
+(``ffgpu_varf.mass_qp``, ``stiff_qp``) reproduce the pattern exactly and the values within 1e-12.
 """
 import numpy as np
 import pytest
@@ -19,7 +21,15 @@ CASES = {
     "mq_sq_p2": ("P2", lambda x, y: np.exp(x + y), (1, 2)),
     "mq_cube_p1": ("P1", lambda x, y, z: 1 + z * x, (1,)),
     "mq_cube_p2": ("P2", lambda x, y, z: 2 + np.cos(x) * y, (1,)),
+    "kq_sq_p1": ("P1", lambda x, y: 1 + x * x * y, (1, 3)),
+    "kq_sq_p2": ("P2", lambda x, y: np.exp(x - y), (1, 2)),
+    "kq_cube_p2": ("P2", lambda x, y, z: 1 + x * y * z, (1, 2)),
 }
+
+
+def coefs(name, c):
+    """(kappa, mass) keyword values of the case's coefficient function."""
+    return (c, 0.0) if name.startswith("kq_") else (None, c)
 
 
 def space(name):
@@ -41,10 +51,11 @@ def check(d, sc, rp, cl, v, b, u, it):
 
 
 @pytest.mark.parametrize("name", list(CASES))
-def test_oracle_mass_function_equals_freefem(name):
+def test_oracle_coefficient_function_equals_freefem(name):
     d, sc, Th, Vh = space(name)
     _, c, labels = CASES[name]
-    A = ffo.assemble(Th, Vh, mass=c)
+    kappa, mass = coefs(name, c)
+    A = ffo.assemble(Th, Vh, kappa=kappa, mass=mass)
     b = ffo.rhs(Th, Vh, f=1.0)
     ffo.setbc(A, b, Vh.on(labels))
     rp, cl, v = A.csr()
@@ -54,12 +65,13 @@ def test_oracle_mass_function_equals_freefem(name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", list(CASES))
-def test_device_mass_function_equals_freefem(name):
+def test_device_coefficient_function_equals_freefem(name):
     from ffgpu.build import build
     build()
     d, sc, Th, Vh = space(name)
     _, c, labels = CASES[name]
-    a = ffgpu.varf_diffusion(c_mass=c, f=1.0, on=labels)
+    kappa, mass = coefs(name, c)
+    a = ffgpu.varf_diffusion(kappa=kappa, c_mass=mass, f=1.0, on=labels)
     b = np.empty(Vh.ndof)
     A = ffgpu.matrix(a, Vh, eps=1e-12, rhs_out=b)
     rp, cl, v = A.csr()

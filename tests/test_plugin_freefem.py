@@ -146,7 +146,7 @@ fespace Vh(Th,P1);
 Vh u,v;
 fespace Wh(Th,P2);
 Wh w,z;
-varf a(w,z)=int2d(Th)((1+x*y)*(dx(w)*dx(z)+dy(w)*dy(z))) + on(1,2,3,4,w=0);
+varf a(w,z)=int2d(Th)((1+x*y)*dx(w)*dx(z)+(2+x*y)*dy(w)*dy(z)) + on(1,2,3,4,w=0);
 matrix A=a(Wh,Wh);
 cout << "nnzA " << A.nnz << endl;
 varf b(w,z)=int2d(Th,qft=qf1pT)(dx(w)*dx(z)+dy(w)*dy(z)) + on(1,2,3,4,w=0);
@@ -163,8 +163,8 @@ cout << "nnzD " << D.nnz << endl;
 """
     r, out = run_script(plugin, "fb.edp", body)
     assert r.returncode == 0, out[-2000:]
-    for why in ("coefficient not constant on elements (a P1 stiffness term takes any)",
-                "quadrature not exact for the form", "element type", "mixed derivative term"):
+    for why in ("anisotropic diffusion", "quadrature not exact for the form", "element type",
+                "mixed derivative term"):
         assert f"ffgpu: form assembled by FreeFEM ({why})" in out
     nnz = {l.split()[0]: int(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("nnz")}
     # square(6) P1: 7 nv - 8 n - 6 entries
@@ -421,6 +421,35 @@ matrix A=a(Vh,Vh,solver=GPUCG);
     xq = quadrature.points(X, E, lam)
     ref = c(*[xq[..., k] for k in range(dim)])
     assert np.max(np.abs(mq - ref)) <= 1e-14 * np.max(np.abs(ref))
+    if not gpu_present():
+        assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
+
+
+def test_p2_stiffness_function_goes_to_the_device_at_the_rule_points(plugin, tmp_path):
+    """A P2 stiffness coefficient that depends on the point goes to the device by FreeFEM's
+    values at the rule's points; a P0 part of the same form joins them."""
+    body = r"""
+mesh Th=square(5,4);
+fespace Vh(Th,P2);
+fespace Ph(Th,P0);
+Ph k0=1+x;
+Vh u,v;
+varf a(u,v)=int2d(Th)(exp(x-y)*(dx(u)*dx(v)+dy(u)*dy(v))) + int2d(Th)(k0*(dx(u)*dx(v)+dy(u)*dy(v))) + on(1,u=0);
+matrix A=a(Vh,Vh,solver=GPUCG);
+"""
+    d1 = tmp_path / "kq"
+    d1.mkdir()
+    r, out = run_script(plugin, "kq.edp", body, {"FFGPU_PLUGIN_DUMP": str(d1)})
+    assert "stiffness at 7 points, kq-check" in out
+    X = np.fromfile(d1 / "coords.bin", np.float64).reshape(-1, 2)
+    E = np.fromfile(d1 / "elems.bin", np.int32).reshape(-1, 3)
+    kq = np.fromfile(d1 / "stiff_qp.bin", np.float64).reshape(E.shape[0], 7)
+    from ffgpu import quadrature
+    lam, _ = quadrature.rule(None, 2)
+    xq = quadrature.points(X, E, lam)
+    centre = X[E].mean(axis=1)[:, 0]                    # the P0 function 1+x, at the centroid
+    ref = np.exp(xq[..., 0] - xq[..., 1]) + (1 + centre)[:, None]
+    assert np.max(np.abs(kq - ref)) <= 1e-13 * np.max(np.abs(ref))
     if not gpu_present():
         assert r.returncode != 0 and "ffgpu: no usable CUDA device" in out
 
