@@ -150,11 +150,12 @@ class VarForm:
         v.form = self.form
         v.c_stiff = self.c_stiff
         v.c_mass = 0.0 if callable(self.c_mass) else self.c_mass
-        v.mass_qp = None
+        # values at quadrature points (one rule for the varf), set by the helpers below
+        v.nqp = 0
+        v.qp_lambda = v.qp_weight = v.f_qp = v.mass_qp = v.stiff_qp = None
         v.E = self.E
         v.nu = self.nu
         v.kappa = None
-        v.stiff_qp = None
         if callable(self.kappa):
             self._stiff_at_points(v, Vh)
         elif self.kappa is not None:
@@ -162,8 +163,6 @@ class VarForm:
             self._keep.append(k)
             v.kappa = _ptr(k).value
         v.f = None
-        v.nqp = 0
-        v.qp_lambda = v.qp_weight = v.f_qp = None
         if callable(self.c_mass):
             self._mass_at_points(v, Vh)
         if callable(self.f):

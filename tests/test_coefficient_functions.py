@@ -77,3 +77,12 @@ def test_device_coefficient_function_equals_freefem(name):
     rp, cl, v = A.csr()
     u = A.solve(b)
     check(d, sc, rp, cl, v, b, u, A.stats.iterations)
+
+
+def test_varf_carries_every_function_at_one_rule():
+    """The C varf of a form with several functions holds them all, at one rule (host only)."""
+    Vh = FESpace(mesh.square(3), "P2")
+    a = ffgpu.varf_diffusion(kappa=lambda x, y: 1 + x, c_mass=lambda x, y: 2 + y, f=lambda x, y: x * y)
+    v = a.c_varf(Vh)
+    assert v.nqp == 7 and v.stiff_qp and v.mass_qp and v.f_qp and v.qp_lambda and v.qp_weight
+    assert not v.kappa and v.c_mass == 0.0
