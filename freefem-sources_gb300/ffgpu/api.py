@@ -30,6 +30,14 @@ from .mesh import Mesh
 _ctx = {}
 
 
+def _touched_zeros(shape):
+    """A zero host array whose pages are already mapped: np.zeros maps large arrays lazily, and
+    the device-to-host copy of the result into unmapped pages pays a fault per page."""
+    a = np.empty(shape)
+    a.fill(0.0)
+    return a
+
+
 def _ptr(a):
     """Raw pointer of a numpy array or a torch tensor (host or CUDA), None for None."""
     if a is None:
@@ -375,7 +383,7 @@ class Matrix:
                 import torch
                 out = torch.zeros_like(b) if x0 is None else x0.clone()
             else:
-                out = np.zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
+                out = _touched_zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
         elif x0 is not None:
             out[...] = x0
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
@@ -402,7 +410,7 @@ class Matrix:
                 import torch
                 out = torch.zeros_like(b) if x0 is None else x0.clone()
             else:
-                out = np.zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
+                out = _touched_zeros(np.shape(b)) if x0 is None else np.array(x0, np.float64)
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
         p = _lib.IRParams()
         p.eps = self.eps if eps is None else eps
@@ -489,7 +497,7 @@ def rhs(varf: VarForm, Vh, out=None, device=0):
     space = Vh if isinstance(Vh, DeviceSpace) else DeviceSpace(Vh, device)
     V = space.Vh
     if out is None:
-        out = np.empty(V.ndof)
+        out = _touched_zeros(V.ndof)
     v = varf.c_varf(V)
     bc = varf.c_bc(V, device_marking=space.has_boundary)
     check(lib().ffgpu_rhs_assemble(space.h, C.byref(v), C.byref(bc), _ptr(out)))
