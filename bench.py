@@ -732,12 +732,15 @@ def run_batch(args, rank=0, world=1):
         ffo.setbc(A, bo, Vh.on((1, 2, 3, 4)))
         uo, it, r, _ = ffo.cg(A, bo, eps=1e-10)
         errs.append(float(np.linalg.norm(xs[p] - uo) / np.linalg.norm(uo)))
-    # e2e from host arrays
+    # e2e from host arrays: the batch as the C ABI takes it (counts, coordinates, elements,
+    # on() mask, coefficients back to back), copied in and solved every step
+    arrays = batch.batch_arrays(meshes)
+    kap_h = np.concatenate(kappas)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        B2 = batch.Batch(meshes, device=di)
-        B2.assemble(kappas, f=1.0)
+        B2 = batch.Batch(arrays=arrays, device=di)
+        B2.assemble(kap_h, f=1.0)
         xh = B2.solve(eps=cfg["eps"])
         B2.close()
     t_e2e = (time.perf_counter() - t0) * 1e3 / args.steps

@@ -15,23 +15,37 @@ import numpy as np
 
 from . import api
 from ._lib import IRParams, SolverStats, check, lib
-from .fespace import FESpace
 from .mesh import Mesh
 
 
+def batch_arrays(meshes: list[Mesh], on=(1, 2, 3, 4)):
+    """The batch as the C ABI takes it: (nv, nt, coords, elems, onbc) -- vertex and element
+    counts per problem, the problems' coordinates and (local) elements back to back, and the
+    P1 on(labels) mask (the vertices of the boundary edges carrying one of the labels)."""
+    nv = np.array([m.nv for m in meshes], np.int32)
+    nt = np.array([m.nt for m in meshes], np.int32)
+    voff = np.concatenate([[0], np.cumsum(nv)]).astype(np.int64)
+    coords = np.ascontiguousarray(np.concatenate([m.coords for m in meshes]), np.float64)
+    elems = np.ascontiguousarray(np.concatenate([m.elems for m in meshes]), np.int32)
+    be = np.concatenate([m.belems.astype(np.int64) + voff[i] for i, m in enumerate(meshes)])
+    bl = np.concatenate([m.blabel for m in meshes])
+    onbc = np.zeros(int(voff[-1]), np.uint8)
+    onbc[be[np.isin(bl, np.asarray(on))].ravel()] = 1
+    return nv, nt, coords, elems, onbc
+
+
 class Batch:
-    def __init__(self, meshes: list[Mesh], on=(1, 2, 3, 4), device=0):
-        self.meshes = meshes
-        self.nv = np.array([m.nv for m in meshes], np.int32)
-        self.nt = np.array([m.nt for m in meshes], np.int32)
+    def __init__(self, meshes: list[Mesh] | None = None, on=(1, 2, 3, 4), device=0, arrays=None):
+        """A batch of independent P1 problems, from a list of meshes or from the arrays of
+        batch_arrays (host or device)."""
+        nv, nt, coords, elems, onbc = arrays if arrays is not None else batch_arrays(meshes, on)
+        self.nv = np.asarray(nv, np.int32)
+        self.nt = np.asarray(nt, np.int32)
         self.voff = np.concatenate([[0], np.cumsum(self.nv)]).astype(np.int64)
         self.toff = np.concatenate([[0], np.cumsum(self.nt)]).astype(np.int64)
-        coords = np.ascontiguousarray(np.concatenate([m.coords for m in meshes]), np.float64)
-        elems = np.ascontiguousarray(np.concatenate([m.elems for m in meshes]), np.int32)
-        self.onbc = np.ascontiguousarray(
-            np.concatenate([FESpace(m, "P1").on(on) for m in meshes]), np.uint8)
+        self.onbc = onbc
         h = C.c_void_p()
-        check(lib().ffgpu_batch_create(api.context(device), len(meshes), api._ptr(self.nv), api._ptr(self.nt),
+        check(lib().ffgpu_batch_create(api.context(device), self.nv.size, api._ptr(self.nv), api._ptr(self.nt),
                                        api._ptr(coords), api._ptr(elems), C.byref(h)))
         self.h = h
         self.stats = None
@@ -69,7 +83,7 @@ class Batch:
 
     def solve(self, eps=1e-8, eps_inner=1e-4, itmax_inner=0, max_outer=30, out=None):
         if out is None:
-            out = np.zeros(self.ndof)
+            out = api._touched_zeros(self.ndof)
         p = IRParams()
         p.eps = eps
         p.eps_inner = eps_inner
@@ -77,7 +91,7 @@ class Batch:
         p.max_outer = max_outer
         p.tgv = 1e30
         p.unroll = 1
-        it = np.zeros(len(self.meshes), np.int32)
+        it = np.zeros(self.nv.size, np.int32)
         st = SolverStats()
         code = lib().ffgpu_batch_solve(self.h, api._ptr(out), C.byref(p), api._ptr(it), C.byref(st))
         self.stats = st
@@ -86,7 +100,7 @@ class Batch:
         return out
 
     def split(self, x):
-        return [x[self.voff[p]:self.voff[p + 1]] for p in range(len(self.meshes))]
+        return [x[self.voff[p]:self.voff[p + 1]] for p in range(self.nv.size)]
 
     def tuned(self):
         nt, lanes, ms = C.c_int(), C.c_int(), C.c_float()

@@ -94,3 +94,14 @@ def test_batch_reassemble_and_resolve():
     x2 = B.solve(eps=1e-8)
     # kappa scaled by 2 => solution halved
     assert np.linalg.norm(x2 - 0.5 * x1) <= 1e-6 * np.linalg.norm(x1)
+
+
+def test_batch_from_arrays_equals_batch_from_meshes():
+    meshes, kappas, _ = batch.c5_meshes(24, 16, 48, seed=11)
+    B1 = batch.Batch(meshes)
+    B1.assemble(kappas, f=1.0)
+    x1 = B1.solve(eps=1e-8)
+    B2 = batch.Batch(arrays=batch.batch_arrays(meshes))
+    B2.assemble(np.concatenate(kappas), f=1.0)
+    x2 = B2.solve(eps=1e-8)
+    assert np.array_equal(x1, x2)
