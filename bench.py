@@ -24,6 +24,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -172,7 +173,7 @@ def cpu_baseline(cfgname, procs=1, reps=1):
 class ClockSampler:
     def __init__(self):
         self.p = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(tempfile.gettempdir(), "ffgpu_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
