@@ -393,6 +393,7 @@ struct FillArgs {
     const double *fint;       // element vectors of a source at quadrature points, or NULL
     const double *mloc;       // element mass matrices of a coefficient at quadrature points, or NULL
     const double *kloc;       // element stiffness matrices of a coefficient at quadrature points, or NULL
+    const double *lame;       // per-element (lambda, mu) of the elasticity form, or NULL
     double f0, f1, f2;
     double c_mass;
     double lam, mu;           // elasticity
@@ -474,12 +475,14 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                         if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     } else {
                         const double tr = P.trace();
+                        const double lam = A.lame ? __ldg(A.lame + 2 * (int64_t)e) : A.lam;
+                        const double mu = A.lame ? __ldg(A.lame + 2 * (int64_t)e + 1) : A.mu;
 #pragma unroll
                         for (int c = 0; c < 3; ++c)
 #pragma unroll
                             for (int cp = 0; cp < 3; ++cp) {
-                                double x = A.lam * P.g(c, cp) + A.mu * P.g(cp, c);
-                                if (cp == c) x += A.mu * tr;
+                                double x = lam * P.g(c, cp) + mu * P.g(cp, c);
+                                if (cp == c) x += mu * tr;
                                 v[3 * c + cp] = m * x;
                             }
                     }
@@ -833,6 +836,9 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     }
     fa.onbc = mask; fa.g = gv.d; fa.tgv = bc ? bc->tgv : 0.0;
     fa.max_deg = M->max_deg; fa.status = ctx->d_status;
+    DevIn<double> lame(v->form == FFGPU_FORM_ELASTICITY ? v->lame : nullptr, (size_t)S->nt * 2, ctx);
+    FFGPU_TRY(lame.err);
+    fa.lame = lame.d;
     double *fint = nullptr, *mloc = nullptr;
     if (rh.d) FFGPU_TRY(source_prepare(S, v, M->geo, &fint));
     double *kloc = nullptr;

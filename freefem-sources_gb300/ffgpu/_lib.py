@@ -48,7 +48,7 @@ class Varf(C.Structure):
                 ("f", C.c_void_p), ("f_const", C.c_double * 3), ("nbterms", C.c_int),
                 ("bterms", C.c_void_p), ("nqp", C.c_int), ("qp_lambda", C.c_void_p),
                 ("qp_weight", C.c_void_p), ("f_qp", C.c_void_p), ("mass_qp", C.c_void_p),
-                ("stiff_qp", C.c_void_p)]
+                ("stiff_qp", C.c_void_p), ("lame", C.c_void_p)]
 
 
 class BC(C.Structure):

@@ -161,8 +161,17 @@ class VarForm:
         # values at quadrature points (one rule for the varf), set by the helpers below
         v.nqp = 0
         v.qp_lambda = v.qp_weight = v.f_qp = v.mass_qp = v.stiff_qp = None
-        v.E = self.E
-        v.nu = self.nu
+        v.E = self.E if np.ndim(self.E) == 0 else 1.0
+        v.nu = self.nu if np.ndim(self.nu) == 0 else 0.3
+        v.lame = None
+        if self.form == _lib.FORM_ELASTICITY and (np.ndim(self.E) > 0 or np.ndim(self.nu) > 0):
+            # several materials: lambda, mu per element, by the same formulas as for constants
+            nt = Vh.Th.nt
+            Ea = np.broadcast_to(np.asarray(self.E, np.float64), (nt,))
+            na = np.broadcast_to(np.asarray(self.nu, np.float64), (nt,))
+            lame = np.ascontiguousarray(np.stack([Ea * na / ((1 + na) * (1 - 2 * na)), Ea / (2 * (1 + na))], axis=1))
+            self._keep.append(lame)
+            v.lame = _ptr(lame).value
         v.kappa = None
         if callable(self.kappa):
             self._stiff_at_points(v, Vh)
@@ -325,8 +334,9 @@ def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tg
 def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30,
                     bterms=(), quad=None) -> VarForm:
     """varf a([u],[v]) = int(lambda div u div v + 2mu eps(u):eps(v)) + int(f.v)
-    + the boundary terms (tractions g.v, Robin robin*u.v) + on(on, u=0).  f may be a function
-    f(x, y, z) returning three components, taken at the points of `quad`."""
+    + the boundary terms (tractions g.v, Robin robin*u.v) + on(on, u=0).  E and nu may be
+    arrays per element (several materials); f may be a function f(x, y, z) returning three
+    components, taken at the points of `quad`."""
     return VarForm(form=_lib.FORM_ELASTICITY, E=E, nu=nu, f=f, on=tuple(on), components=components,
                    tgv=tgv, bterms=tuple(bterms), quad=quad)
 

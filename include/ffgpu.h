@@ -89,6 +89,9 @@ typedef struct {
      * rule, stiff_qp[k*nqp + q]; when non-NULL it replaces kappa and c_stiff: the element matrix
      * gains |K| sum_q qp_weight[q] k_q grad phi_i(lambda_q) . grad phi_j(lambda_q). */
     const double *stiff_qp;
+    /* lame: per-element Lame coefficients of the elasticity form, lame[2k] = lambda_k,
+     * lame[2k+1] = mu_k (several materials), or NULL (then E and nu). */
+    const double *lame;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or

@@ -256,6 +256,7 @@ typedef struct {
     double E, nu, mass;
     const double *mqp;
     const double *kqp;   /* stiffness coefficient at the rule's points (replaces coef), or NULL */
+    const double *lame;  /* elasticity: per-element (lambda, mu) (replaces E, nu), or NULL */
 } ffo_form;
 
 static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = test */) {
@@ -295,6 +296,7 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
              *   2mu/2 * (dq u_p + dp u_q)(dq v_p + dp v_q)     for p < q     */
             double E = F->E, nu = F->nu;
             double mu = E / (2 * (1 + nu)), lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+            if (F->lame) { lam = F->lame[2 * (int64_t)k]; mu = F->lame[2 * (int64_t)k + 1]; }
             double s2 = sqrt(2.), is2 = 1. / s2;
             double half = 2. * mu * is2 * is2;
             for (int ci = 0; ci < 3; ++ci)      /* test component, derivative ci */
@@ -329,9 +331,9 @@ static void elem_matrix(const ffo_form *F, int k, double *M /* ndofK^2, row = te
 /* assemble the bilinear form into the hash matrix, element by element (insertion order) */
 int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, int ndofK,
                  const int *dof, int fe, int form, int quad, const double *coef, double E,
-                 double nu, double mass, const double *mqp, const double *kqp) {
+                 double nu, double mass, const double *mqp, const double *kqp, const double *lame) {
     ffo_hm *A = (ffo_hm *)hm;
-    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass, mqp, kqp};
+    ffo_form F = {dim, nt, ndofK, fe, form, quad, X, elems, dof, coef, E, nu, mass, mqp, kqp, lame};
     double *M = (double *)malloc(sizeof(double) * ndofK * ndofK);
     for (int k = 0; k < nt; ++k) {
         elem_matrix(&F, k, M);
@@ -347,7 +349,7 @@ int ffo_assemble(void *hm, int dim, int nt, const double *X, const int *elems, i
 void ffo_element_matrix(int dim, const double *X, const int *elems, int k, int ndofK, int fe,
                         int form, int quad, const double *coef, double E, double nu,
                         double mass, double *M) {
-    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass, 0, 0};
+    ffo_form F = {dim, 0, ndofK, fe, form, quad, X, elems, 0, coef, E, nu, mass, 0, 0, 0};
     elem_matrix(&F, k, M);
 }
 

@@ -50,7 +50,7 @@ def lib():
         L.ffo_hm_csr.argtypes = [C.c_void_p, _ip, _ip, _dp]
         L.ffo_assemble.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
                                    C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double,
-                                   C.c_void_p, C.c_void_p]
+                                   C.c_void_p, C.c_void_p, C.c_void_p]
         L.ffo_element_matrix.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, _dp]
         L.ffo_rhs.argtypes = [_dp, C.c_int, C.c_int, _dp, _ip, C.c_int, _ip, C.c_int, C.c_int,
@@ -180,9 +180,15 @@ def assemble(Th, Vh, form="diffusion", kappa=None, E=1.0, nu=0.3, mass=0.0, quad
         val, nq = points_values(Th, quad, mass)
         mqp = np.ascontiguousarray(np.broadcast_to(np.asarray(val, np.float64), (Th.nt, nq)))
         mass = 0.0
+    lame = None
+    if form == "elasticity" and (np.ndim(E) > 0 or np.ndim(nu) > 0):
+        Ea = np.broadcast_to(np.asarray(E, np.float64), (Th.nt,))
+        na = np.broadcast_to(np.asarray(nu, np.float64), (Th.nt,))
+        lame = np.ascontiguousarray(np.stack([Ea * na / ((1 + na) * (1 - 2 * na)), Ea / (2 * (1 + na))], axis=1))
+        E, nu = 1.0, 0.3
     L.ffo_assemble(A.h, dim, Th.nt, X, el, Vh.ndofK, dof, fe, 1 if form == "elasticity" else 0,
-                   int(quad), _ptr(coef), float(E), float(nu), float(mass), _ptr(mqp), _ptr(kqp))
-    A._keep = (coef, mqp, kqp)
+                   int(quad), _ptr(coef), float(E), float(nu), float(mass), _ptr(mqp), _ptr(kqp), _ptr(lame))
+    A._keep = (coef, mqp, kqp, lame)
     return A
 
 

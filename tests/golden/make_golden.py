@@ -174,6 +174,37 @@ cout << "S nit " << nit << endl;
     return body, {}
 
 
+def case_p2_elasticity_materials(nx, ny, nz, seed):
+    """[P2,P2,P2] elasticity with per-element E and nu (two materials, seeded): P0 Lame
+    coefficients mu = E/(2(1+nu)), lambda = E nu/((1+nu)(1-2nu))."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nt = 6 * nx * ny * nz
+    Ea = np.where(rng.random(nt) < 0.5, 1.0, 10.0)
+    na = np.where(rng.random(nt) < 0.5, 0.25, 0.35)
+    files = {"E.txt": Ea, "nu.txt": na}
+    body = HEAD + f"""
+load "msh3"
+mesh3 Th=cube({nx},{ny},{nz});
+fespace Vh(Th,[P2,P2,P2]);
+fespace Ph(Th,P0);
+""" + read_vec_edp("Ea", "E.txt", "Th.nt") + read_vec_edp("na", "nu.txt", "Th.nt") + """
+Ph Ek, nuk; Ek[]=Ea; nuk[]=na;
+Ph mu=Ek/(2*(1+nuk)), lambda=Ek*nuk/((1+nuk)*(1-2*nuk));
+Vh [u1,u2,u3],[v1,v2,v3];
+real s2=sqrt(2.);
+macro epsilon(u1,u2,u3) [dx(u1),dy(u2),dz(u3),(dz(u2)+dy(u3))/s2,(dz(u1)+dx(u3))/s2,(dy(u1)+dx(u2))/s2] // EOM
+macro div(u1,u2,u3) (dx(u1)+dy(u2)+dz(u3)) // EOM
+varf a([u1,u2,u3],[v1,v2,v3])=int3d(Th)(lambda*div(u1,u2,u3)*div(v1,v2,v3)+2.*mu*(epsilon(u1,u2,u3)'*epsilon(v1,v2,v3))) + int3d(Th)(-1.*v3) + on(4,u1=0,u2=0,u3=0);
+int nit=0;
+matrix A=a(Vh,Vh,solver=CG,eps=1e-10,getnbiteration=nit);
+real[int] b=a(0,Vh);
+u1[]=0; u1[]=A^-1*b;
+cout << "S nit " << nit << endl;
+""" + DUMP_MESH3 + DUMP_DOF + DUMP_A + \
+        "for (int k=0;k<b.n;k++) cout << \"b \" << b[k] << \" \" << u1[][k] << endl;\n"
+    return body, files
+
+
 def case_p2_elasticity(nx, ny, nz):
     body = HEAD + f"""
 load "msh3"
@@ -515,6 +546,7 @@ CASES = {
     **{f"src_{w}": (lambda w=w: case_source_function(w)) for w in SOURCE_CASES},
     **{f"mq_{w}": (lambda w=w: case_mass_function(w)) for w in MASS_CASES},
     **{f"kq_{w}": (lambda w=w: case_stiff_function(w)) for w in STIFF_CASES},
+    "p2elmat_2x2x1": lambda: case_p2_elasticity_materials(2, 2, 1, seed=61),
     "p1sq_n6_tgvm1": lambda: case_p1_square_tgv(6, -1, "GMRES"),
     "p1sq_n6_tgvm2": lambda: case_p1_square_tgv(6, -2, "CG"),
     "p1sq_n6_tgvm3": lambda: case_p1_square_tgv(6, -3, "GMRES"),

@@ -86,3 +86,35 @@ def test_varf_carries_every_function_at_one_rule():
     v = a.c_varf(Vh)
     assert v.nqp == 7 and v.stiff_qp and v.mass_qp and v.f_qp and v.qp_lambda and v.qp_weight
     assert not v.kappa and v.c_mass == 0.0
+
+
+def _materials():
+    d, sc = load("p2elmat_2x2x1")
+    Th = mesh.Mesh(3, d["coords"], d["elems"], d["belems"], d["blabel"], d["vlabel"])
+    Vh = FESpace(Th, "P2vec")
+    assert np.array_equal(Vh.dof, d["dof"])
+    return d, sc, Th, Vh, d["in_E"], d["in_nu"]
+
+
+def test_oracle_elasticity_with_materials_equals_freefem():
+    """[P2,P2,P2] elasticity with E and nu per element (two materials, P0 Lame coefficients)."""
+    d, sc, Th, Vh, E, nu = _materials()
+    A = ffo.assemble(Th, Vh, form="elasticity", E=E, nu=nu)
+    b = ffo.rhs(Th, Vh, f=(0.0, 0.0, -1.0))
+    ffo.setbc(A, b, Vh.on((4,)))
+    rp, cl, v = A.csr()
+    u, it, _, _ = ffo.cg(A, b, eps=1e-10)
+    check(d, sc, rp, cl, v, b, u, it)
+
+
+@pytest.mark.gpu
+def test_device_elasticity_with_materials_equals_freefem():
+    from ffgpu.build import build
+    build()
+    d, sc, Th, Vh, E, nu = _materials()
+    a = ffgpu.varf_elasticity(E=E, nu=nu, f=(0.0, 0.0, -1.0), on=(4,))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, eps=1e-10, rhs_out=b)
+    rp, cl, v = A.csr()
+    u = A.solve(b)
+    check(d, sc, rp, cl, v, b, u, A.stats.iterations)
