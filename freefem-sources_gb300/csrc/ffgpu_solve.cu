@@ -848,6 +848,10 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
         FFGPU_CUDA(dalloc(ctx, (void **)&A->wcl, n));
         FFGPU_CUDA(dalloc(ctx, (void **)&A->ks, sizeof(KrylovScalars)));
         FFGPU_CUDA(cudaMemsetAsync(A->ks, 0, sizeof(KrylovScalars), s));
+        // pool memory comes back with an earlier object's contents: the work vectors (and
+        // their padding slots) start from zero, as freshly mapped memory does
+        FFGPU_CUDA(cudaMemsetAsync(A->vec, 0, sizeof(double) * vstride(n) * 8, s));
+        FFGPU_CUDA(cudaMemsetAsync(A->diag_inv, 0, sizeof(double) * vstride(n), s));
     }
     FFGPU_TRY(tune_lanes(A, 0));
     if (A->ntgv >= 0) return FFGPU_OK;
