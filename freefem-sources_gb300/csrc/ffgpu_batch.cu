@@ -372,14 +372,14 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     if (B->tuned < 0)
-        for (int i = 0; i < ctx->nbtuned; ++i)
-            if (ctx->btuned[i].nprob == B->nprob && ctx->btuned[i].n == NV && ctx->btuned[i].nnz == B->A->nnz)
-                B->tuned = ctx->btuned[i].cand;
+        for (const ffgpu_ctx::BatchTuned &t : ctx->btuned)
+            if (t.nprob == B->nprob && t.n == NV && t.nnz == B->A->nnz) B->tuned = t.cand;
     if (B->tuned < 0) {
-        // autotune: time every candidate (CTA size x lanes per row) on this batch; the choice is
-        // kept in the context for later batches of the same shape
-        float best = 1e30f;
-        int bi = 0;
+        // autotune: time every candidate (CTA size x lanes per row) on this batch and keep the
+        // first one within the tuner margin of the fastest; the choice is kept in the context
+        // for later batches of the same shape
+        float tms[64];
+        static_assert(g_ncands <= 64, "batched tuner: too many candidates");
         for (int c = 0; c < g_ncands; ++c) {
             FFGPU_TRY(batch_graph(B, c));
             cudaGraphLaunch(B->exec, s);   // warm
@@ -390,12 +390,13 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             ctx->launches += 4;
-            if (ms < best) { best = ms; bi = c; }
+            tms[c] = ms;
         }
+        const int bi = tuned_pick(tms, g_ncands);
         B->tuned = bi;
-        B->tuned_ms = best;
+        B->tuned_ms = tms[bi];
         changed = true;
-        ctx->btuned[ctx->nbtuned < 8 ? ctx->nbtuned++ : 7] = ffgpu_ctx::BatchTuned{B->nprob, NV, B->A->nnz, bi};
+        ctx->btuned.push_back(ffgpu_ctx::BatchTuned{B->nprob, NV, B->A->nnz, bi});
     }
     if (changed || !B->exec) FFGPU_TRY(batch_graph(B, B->tuned));
     cudaEventRecord(e0, s);

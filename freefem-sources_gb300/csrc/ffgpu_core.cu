@@ -34,6 +34,26 @@ int launch_check(ffgpu_ctx *ctx, const char *what) {
     return FFGPU_OK;
 }
 
+int tuned_layout(const ffgpu_ctx *ctx, const ffgpu_matrix *A, int mode) {
+    for (const ffgpu_ctx::Tuned &t : ctx->tuned)
+        if (t.nb == A->nb && t.nnzb == A->nnzb && t.bs == A->bs && t.mode == mode) return t.lanes;
+    return 0;
+}
+
+void tuned_store(ffgpu_ctx *ctx, const ffgpu_matrix *A, int mode, int code) {
+    for (ffgpu_ctx::Tuned &t : ctx->tuned)
+        if (t.nb == A->nb && t.nnzb == A->nnzb && t.bs == A->bs && t.mode == mode) { t.lanes = code; return; }
+    ctx->tuned.push_back(ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, code, mode});
+}
+
+int tuned_pick(const float *ms, int n) {
+    float best = ms[0];
+    for (int i = 1; i < n; ++i) best = ms[i] < best ? ms[i] : best;
+    for (int i = 0; i < n; ++i)
+        if (ms[i] <= best * (1.0f + kTuneMargin)) return i;
+    return 0;
+}
+
 int check_device_status(ffgpu_ctx *ctx, const char *where) {
     int st = 0;
     FFGPU_CUDA(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -246,8 +266,7 @@ int ffgpu_ctx_create(int device, ffgpu_ctx **out) {
     FFGPU_CUDA(cudaGetDeviceCount(&ndev));
     FFGPU_CHECK(device >= 0 && device < ndev, FFGPU_EINVAL, "ffgpu_ctx_create: no device %d", device);
     FFGPU_CUDA(cudaSetDevice(device));
-    ffgpu_ctx *c = new ffgpu_ctx();
-    memset(c, 0, sizeof(*c));
+    ffgpu_ctx *c = new ffgpu_ctx();   // value-initialised: every plain member starts at zero
     c->device = device;
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;

@@ -73,12 +73,14 @@ struct ffgpu_ctx {
     int *d_status;              // DevStatus word
     unsigned int *d_ticket;     // last-block counters
     int *d_iscratch;            // small integer scratch (max reductions)
-    // SpMV lanes-per-row chosen by timing, per matrix shape (nb, nnzb, bs)
-    struct Tuned { int64_t nb, nnzb; int bs, lanes, mode; } tuned[32];
-    int ntuned;
+    // SpMV layout chosen by timing, per matrix shape (nb, nnzb, bs) and mode, kept for the
+    // context's lifetime: every later matrix of a shape gets the same layout, however many
+    // shapes the context has seen
+    struct Tuned { int64_t nb, nnzb; int bs, lanes, mode; };
+    std::vector<Tuned> tuned;
     // batched solver launch shape chosen by timing, per batch shape (problems, DOFs, nnz)
-    struct BatchTuned { int64_t nprob, n, nnz; int cand; } btuned[8];
-    int nbtuned;
+    struct BatchTuned { int64_t nprob, n, nnz; int cand; };
+    std::vector<BatchTuned> btuned;
 };
 
 struct ffgpu_space {
@@ -255,6 +257,15 @@ int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double 
 int stiff_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **kloc);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
+
+// SpMV layout cache of the context (0: shape not tuned yet)
+int tuned_layout(const ffgpu_ctx *ctx, const ffgpu_matrix *A, int mode);
+void tuned_store(ffgpu_ctx *ctx, const ffgpu_matrix *A, int mode, int code);
+// Tuner rule: the first candidate (in the tuner's fixed order) whose time is within
+// kTuneMargin of the fastest.  Candidates closer than the margin are treated as equal, so
+// timing noise between runs rarely changes the choice (and with it the summation order).
+constexpr float kTuneMargin = 0.03f;
+int tuned_pick(const float *ms, int n);
 
 // Work-vector slot stride: slots start on 512-byte boundaries (16-byte vector accesses).
 inline int64_t vstride(int64_t n) { return (n + 63) & ~(int64_t)63; }

@@ -296,20 +296,17 @@ static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditional
 static int ir_tune(ffgpu_matrix *A, IRState &S) {
     if (A->sell32_kind) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
-    for (int i = 0; i < ctx->ntuned; ++i)
-        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs &&
-            ctx->tuned[i].mode == 2) {
-            A->sell32_kind = ctx->tuned[i].lanes;
-            return FFGPU_OK;
-        }
+    if (const int known = tuned_layout(ctx, A, 2)) {
+        A->sell32_kind = known;
+        return FFGPU_OK;
+    }
     cudaStream_t s = ctx->stream;
     FFGPU_CUDA(cudaMemsetAsync(S.h, 0, sizeof(float) * A->n, s));
     FFGPU_CUDA(cudaMemsetAsync(S.ks, 0, sizeof(InnerScalars), s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    float best = 1e30f;
-    int bestk = kSellCode;
+    float tms[4];
     const int kinds[4] = {kSellCode, kSellCode + 1, kSellCode + 2, kSellCode + 3};
     const char *names[4] = {"ranges", "rotated", "ranges deep", "rotated deep"};
     for (int kk = 0; kk < 4; ++kk) {
@@ -332,12 +329,12 @@ static int ir_tune(ffgpu_matrix *A, IRState &S) {
         if (getenv("FFGPU_VERBOSE"))
             fprintf(stderr, "ffgpu: FP32 SpMV tuner (%d block rows): sell32 %s %.4f ms\n", A->nb, names[kk],
                     ms / 3);
-        if (ms < best) { best = ms; bestk = kinds[kk]; }
+        tms[kk] = ms;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    A->sell32_kind = bestk;
-    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestk, 2};
+    A->sell32_kind = kinds[tuned_pick(tms, 4)];
+    tuned_store(ctx, A, 2, A->sell32_kind);
     return FFGPU_OK;
 }
 

@@ -724,65 +724,82 @@ static int ka_setup(ffgpu_matrix *A, int mode, int trans, int T, const double *h
     return FFGPU_OK;
 }
 
+// Candidate layouts of the K_a kernel, in the tuner's order (the first one wins ties).
+// FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row; double-float:
+// reductions are FP32, so wider lane groups.
+static const int kCands64[] = {kSellCode, kSellCode + 1, kSellCode + 2, kSellCode + 3, kSellCode + 4,
+                               kSellCode + 5, kSellCode + 6, kSellCode + 7, 1, 2, 4, 8};
+static const int kCandsX[] = {kSellCode, kSellCode + 1, kSellCode + 2, kSellCode + 3, 4, 8, 16, 32};
+// matrices with fewer stored entries than this take the first candidate without timing: their
+// K_a is launch-latency bound and the candidates' times differ by noise only
+constexpr int64_t kTuneMinEntries = 1 << 16;
+
+static bool layout_valid(int mode, int code) {
+    const int *c = mode == 1 ? kCandsX : kCands64;
+    const int n = mode == 1 ? 8 : 12;
+    for (int i = 0; i < n; ++i)
+        if (c[i] == code) return true;
+    return false;
+}
+
 // Times the K_a kernel of one mode (0: FP64, 1: double-float) for the SELL-32 layout and for
-// block CSR with each candidate lanes-per-row on this matrix, and keeps the fastest; the
-// choice is cached per matrix shape in the context.  Value arrays of the losing layout are
-// released.
+// block CSR with each candidate lanes-per-row on this matrix, and keeps the first candidate
+// within the tuner margin of the fastest (tuned_pick).  The choice is cached per matrix shape
+// in the context, so every matrix of a shape gets the same layout (and the same summation
+// order) for the context's lifetime.  Value arrays of the losing layout are released.
 static int tune_lanes(ffgpu_matrix *A, int mode) {
     int *slot = mode == 1 ? &A->csr_lanes_x : &A->csr_lanes;
     if (*slot > 0) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
-    for (int i = 0; i < ctx->ntuned; ++i)
-        if (ctx->tuned[i].nb == A->nb && ctx->tuned[i].nnzb == A->nnzb && ctx->tuned[i].bs == A->bs &&
-            ctx->tuned[i].mode == mode) {
-            *slot = ctx->tuned[i].lanes;
-            return FFGPU_OK;
-        }
+    if (const int known = tuned_layout(ctx, A, mode)) {
+        *slot = known;
+        return FFGPU_OK;
+    }
     if (!A->vec) { *slot = kSellCode; return FFGPU_OK; }
-    // FP64 block CSR: reductions across lanes cost FP64 adds, so few lanes per row;
-    // double-float: reductions are FP32, so wider lane groups
-    const int S0 = kSellCode;
-    const int cands64[] = {S0, S0 + 1, S0 + 2, S0 + 3, S0 + 4, S0 + 5, S0 + 6, S0 + 7, 1, 2, 4, 8};
-    const int candsx[] = {S0, S0 + 1, S0 + 2, S0 + 3, 4, 8, 16, 32};
-    const int *cands = mode == 1 ? candsx : cands64;
+    const int *cands = mode == 1 ? kCandsX : kCands64;
     const int ncand = mode == 1 ? 8 : 12;
     const int64_t vs = vstride(A->n);
     double *y = A->vec + 6 * vs, *x = A->vec + 5 * vs;
     cudaStream_t s = ctx->stream;
     if (mode == 1 && !A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vs));
-    FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
-    if (mode == 1) FFGPU_CUDA(cudaMemsetAsync(A->hx, 0, sizeof(float2) * A->n, s));
-    KrylovScalars *ks = A->ks;
-    FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    float best = 1e30f;
-    int bestT = kSellCode;
-    for (int c = 0; c < ncand; ++c) {
-        const int T = cands[c];
-        KaCall k;
-        FFGPU_TRY(ka_setup(A, mode, 0, T, x, y, k));
-        k.launch(s);   // warm
-        cudaEventRecord(e0, s);
-        for (int r = 0; r < 3; ++r) k.launch(s);
-        cudaEventRecord(e1, s);
-        FFGPU_CUDA(cudaEventSynchronize(e1));
-        FFGPU_CUDA(cudaGetLastError());
-        ctx->launches += 4;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
+    int bestT = cands[0];
+    if (A->nnz >= kTuneMinEntries) {
+        FFGPU_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * A->n, s));
+        if (mode == 1) FFGPU_CUDA(cudaMemsetAsync(A->hx, 0, sizeof(float2) * A->n, s));
+        KrylovScalars *ks = A->ks;
+        FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        // two passes over all candidates, each candidate's time the faster of its two
+        float tms[12];
+        for (int c = 0; c < ncand; ++c) tms[c] = 1e30f;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int c = 0; c < ncand; ++c) {
+                KaCall k;
+                FFGPU_TRY(ka_setup(A, mode, 0, cands[c], x, y, k));
+                k.launch(s);   // warm
+                cudaEventRecord(e0, s);
+                for (int r = 0; r < 3; ++r) k.launch(s);
+                cudaEventRecord(e1, s);
+                FFGPU_CUDA(cudaEventSynchronize(e1));
+                FFGPU_CUDA(cudaGetLastError());
+                ctx->launches += 4;
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                tms[c] = fminf(tms[c], ms / 3);
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        bestT = cands[tuned_pick(tms, ncand)];
         if (getenv("FFGPU_VERBOSE"))
-            fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s %.4f ms\n", mode,
-                    A->nb, (long long)A->nnzb,
-                    is_sell(T) ? sell_name(T) : "bsr lanes",
-                    ms / 3);
-        if (ms < best) { best = ms; bestT = T; }
+            for (int c = 0; c < ncand; ++c)
+                fprintf(stderr, "ffgpu: SpMV tuner (mode %d, %d block rows, %lld blocks): %s%s %d %.4f ms\n", mode,
+                        A->nb, (long long)A->nnzb, cands[c] == bestT ? "* " : "",
+                        is_sell(cands[c]) ? sell_name(cands[c]) : "bsr lanes", cands[c], tms[c]);
+        FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
+        FFGPU_CUDA(cudaStreamSynchronize(s));
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    FFGPU_CUDA(cudaMemsetAsync(ks, 0, sizeof(KrylovScalars), s));
-    FFGPU_CUDA(cudaStreamSynchronize(s));
     if (is_sell(bestT)) {
         if (mode == 1) { dfree(ctx, A->valx); A->valx = nullptr; }
     } else if (mode == 1) {
@@ -791,7 +808,31 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
         dfree(ctx, A->sval); A->sval = nullptr;
     }
     *slot = bestT;
-    if (ctx->ntuned < 32) ctx->tuned[ctx->ntuned++] = ffgpu_ctx::Tuned{A->nb, A->nnzb, A->bs, bestT, mode};
+    tuned_store(ctx, A, mode, bestT);
+    return FFGPU_OK;
+}
+
+// A layout fixed by the caller (ffgpu_solver_params.spmv_layout, else the environment variable
+// FFGPU_SPMV_LAYOUT for the FP64 CG) replaces the tuned one for this matrix.
+static int pin_layout(ffgpu_matrix *A, int mode, int code) {
+    if (code == 0) {
+        const char *e = mode == 0 ? getenv("FFGPU_SPMV_LAYOUT") : nullptr;
+        if (!e || !e[0]) return FFGPU_OK;
+        code = atoi(e);
+    }
+    FFGPU_CHECK(layout_valid(mode, code), FFGPU_EINVAL,
+                "spmv_layout %d is not a layout of SpMV mode %d (SELL-32: 64..%d, block CSR lanes: %s)", code, mode,
+                mode == 1 ? 67 : 71, mode == 1 ? "4, 8, 16, 32" : "1, 2, 4, 8");
+    int *slot = mode == 1 ? &A->csr_lanes_x : &A->csr_lanes;
+    if (*slot == code) return FFGPU_OK;
+    *slot = code;
+    if (A->cg_exec) { cudaGraphExecDestroy(A->cg_exec); A->cg_exec = nullptr; }
+    if (!is_sell(code)) {
+        // spmv() takes the SELL copy whenever it exists: drop it so every SpMV uses the pin
+        ffgpu_ctx *ctx = A->ctx;
+        if (mode == 1) { dfree(ctx, A->svalx); dfree(ctx, A->svalx_t); A->svalx = A->svalx_t = nullptr; }
+        else { dfree(ctx, A->sval); dfree(ctx, A->sval_t); A->sval = A->sval_t = nullptr; }
+    }
     return FFGPU_OK;
 }
 
@@ -1228,6 +1269,7 @@ static int solve_many(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     int64_t n = A->n;
+    FFGPU_TRY(pin_layout(A, fn == cg_one && prm->spmv_mode == 1 ? 1 : 0, prm->spmv_layout));
     FFGPU_TRY(matrix_prepare_solver(A));
     if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
     DevIn<double> bd(b, (size_t)n * nrhs, ctx);

@@ -12,8 +12,9 @@
 //     diagonal, the tgv-row mask and the reduction partials: about 17 MB, held by every GPU
 //     that loads libffgpu.so until the process exits);
 //   * the first call on a device (with that device current) looks up the array's device
-//     address with cudaGetSymbolAddress and caches it; make that first call before any stream
-//     capture;
+//     address with cudaGetSymbolAddress and caches it;
+//   * every call synchronises the caller's stream (it polls the convergence flag every 32
+//     iterations and reads the result at the end), so no call can run under stream capture;
 //   * every call shares the one array and leaves its last contents there; each call clears
 //     the counters and scalars it needs before use.  Calls that overlap on the GPU (two host
 //     threads, or two streams) race on the array: serialise them.
@@ -46,8 +47,7 @@ constexpr size_t kOffG = 0;
 constexpr size_t kOffH = kOffG + 8 * kStaticMaxN;
 constexpr size_t kOffQ = kOffH + 8 * kStaticMaxN;
 constexpr size_t kOffD = kOffQ + 8 * kStaticMaxN;
-constexpr size_t kOffX = kOffD + 8 * kStaticMaxN;         // unused slot kept for alignment
-constexpr size_t kOffW = kOffX;                           // tgv mask (bytes)
+constexpr size_t kOffW = kOffD + 8 * kStaticMaxN;         // tgv-row mask (one byte per DOF)
 constexpr size_t kOffP = kOffW + ((kStaticMaxN + 255) / 256) * 256;
 constexpr size_t kOffS = kOffP + 8 * kStPart;
 constexpr size_t kStaticBytes = kOffS + 256;
@@ -140,7 +140,9 @@ __global__ void st_jacobi(int n, const double *b, double *x, double tgv, unsigne
     if (i >= n) return;
     double top = __longlong_as_double((long long)v.ks->maxbits);
     double max1 = __longlong_as_double((long long)v.ks->max1bits);
-    bool has_tgv = !(max1 * 1e6 > top) && v.ks->count > 0;
+    // no positive diagonal at all (top == 0): no tgv rows, as in ffgpu_solve_cg, whose
+    // threshold is then out of reach
+    bool has_tgv = top > 0 && !(max1 * 1e6 > top) && v.ks->count > 0;
     double d = v.dinv[i];
     bool w = has_tgv && d == top;
     v.wcl[i] = w;
@@ -299,10 +301,13 @@ static int static_scratch(unsigned char **out) {
     return FFGPU_OK;
 }
 
-static bool on_device(const void *p) {
+// device memory of the current device `dev`, or managed memory (reachable from every device);
+// device memory of another GPU is refused: the kernels here would read it as peer memory
+static bool on_device(const void *p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 template <int T>
@@ -327,8 +332,12 @@ int ffgpu_solve_cg_csr_noalloc(int n, int64_t nnz, const int32_t *rowptr, const 
                 "ffgpu_solve_cg_csr_noalloc: n = %d exceeds the fixed scratch capacity of %lld DOFs", n,
                 (long long)kStaticMaxN);
     FFGPU_CHECK(rowptr && col && val && b && x, FFGPU_EINVAL, "ffgpu_solve_cg_csr_noalloc: NULL array");
-    FFGPU_CHECK(on_device(rowptr) && on_device(col) && on_device(val) && on_device(b) && on_device(x),
-                FFGPU_EINVAL, "ffgpu_solve_cg_csr_noalloc: every array must be in device memory");
+    int dev = -1;
+    FFGPU_CUDA(cudaGetDevice(&dev));
+    FFGPU_CHECK(on_device(rowptr, dev) && on_device(col, dev) && on_device(val, dev) && on_device(b, dev) &&
+                    on_device(x, dev),
+                FFGPU_EINVAL, "ffgpu_solve_cg_csr_noalloc: every array must be device memory of the current device "
+                "(or managed memory)");
     unsigned char *base = nullptr;
     FFGPU_TRY(static_scratch(&base));
     cudaStream_t s = (cudaStream_t)stream;

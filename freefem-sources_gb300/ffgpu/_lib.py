@@ -58,7 +58,8 @@ class BC(C.Structure):
 
 class SolverParams(C.Structure):
     _fields_ = [("eps", C.c_double), ("itmax", C.c_int), ("dim_krylov", C.c_int),
-                ("tgv", C.c_double), ("verb", C.c_int), ("unroll", C.c_int), ("spmv_mode", C.c_int)]
+                ("tgv", C.c_double), ("verb", C.c_int), ("unroll", C.c_int), ("spmv_mode", C.c_int),
+                ("spmv_layout", C.c_int)]
 
 
 class SolverStats(C.Structure):

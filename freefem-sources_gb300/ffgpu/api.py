@@ -372,9 +372,10 @@ class Matrix:
         except Exception:
             pass
 
-    def params(self, eps=None, itmax=None, unroll=8, spmv_mode=0) -> SolverParams:
+    def params(self, eps=None, itmax=None, unroll=8, spmv_mode=0, spmv_layout=0) -> SolverParams:
         p = SolverParams()
         p.spmv_mode = spmv_mode
+        p.spmv_layout = spmv_layout
         p.eps = self.eps if eps is None else eps
         p.itmax = self.itmax if itmax is None else itmax
         p.dim_krylov = self.dim_krylov
@@ -384,8 +385,9 @@ class Matrix:
         return p
 
     def solve(self, b, x0=None, trans=False, solver=None, eps=None, itmax=None, out=None, unroll=8,
-              spmv_mode=0):
-        """u[] = A^-1*b (A'^-1*b when trans).  x0 is the initial guess (FreeFEM: u[] before)."""
+              spmv_mode=0, spmv_layout=0):
+        """u[] = A^-1*b (A'^-1*b when trans).  x0 is the initial guess (FreeFEM: u[] before).
+        spmv_layout: 0 = tuned per shape; a layout code (see ffgpu_solver_params) fixes it."""
         solver = (solver or self.solver).upper()
         dev_in = hasattr(b, "data_ptr")
         if out is None:
@@ -399,7 +401,7 @@ class Matrix:
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
         nrhs = int(np.prod(np.shape(b))) // self.n
         st = SolverStats()
-        p = self.params(eps, itmax, unroll, spmv_mode)
+        p = self.params(eps, itmax, unroll, spmv_mode, spmv_layout)
         fn = lib().ffgpu_solve_cg if solver == "CG" else lib().ffgpu_solve_gmres
         if solver not in ("CG", "GMRES"):
             raise ValueError(f"solver {solver!r}: the device path provides CG and GMRES")
@@ -447,6 +449,10 @@ class Matrix:
             loop = ["", "-deep", "-batch", "-batch-deep"][(v - 64) >> 1]
             return ("sell32" if (v - 64) % 2 == 0 else "sell32-rot") + loop
         return f"bsr/{v}"
+
+    def layout_code(self, mode=0):
+        """The raw layout code of spmv_layout (the value Matrix.solve(spmv_layout=...) takes)."""
+        return int(lib().ffgpu_matrix_spmv_layout(self.h, int(mode)))
 
     def save(self, path, format="coo"):
         """``ofstream f(path); f << A;``: FreeFEM's text form of the matrix (sorted)."""

@@ -114,7 +114,13 @@ typedef struct {
  * dim_krylov is GMRES's restart (NbSpace).  unroll: CG iterations per CUDA-graph body (>=1).
  * spmv_mode (CG): 0 = SpMV in FP64 arithmetic; 1 = FP64 values and vectors with the products
  * formed exactly on the FP32 pipe and summed as double-float (about 2^-44 relative), every
- * other CG operation in FP64. */
+ * other CG operation in FP64.
+ * spmv_layout: 0 = the layout the tuner picks for the matrix's shape (timed once per shape and
+ * context, then kept); otherwise a fixed layout code as ffgpu_matrix_spmv_layout reports it:
+ * 64..71 SELL-32 variants, or block CSR with 1, 2, 4, 8 lanes per block row (FP64), 64..67 or
+ * 4, 8, 16, 32 lanes (double-float).  The layout fixes the summation order of the SpMV and the
+ * fused dot products, so a fixed code gives bit-identical results from run to run.  With 0, the
+ * environment variable FFGPU_SPMV_LAYOUT, when set, fixes the FP64 layout the same way. */
 typedef struct {
     double eps;
     int itmax;
@@ -123,6 +129,7 @@ typedef struct {
     int verb;
     int unroll;
     int spmv_mode;
+    int spmv_layout;
 } ffgpu_solver_params;
 
 /* Solver report: iterations (FreeFEM's nbitermax / getnbiteration), final C-norm^2 of the
@@ -338,9 +345,12 @@ int ffgpu_batch_destroy(ffgpu_batch *B);
  * memory; x holds the initial guess and receives the solution.  n <= 524288: the work vectors
  * live in a fixed ~17 MB device array that every GPU loading the library keeps until exit.
  * The first call on a device (made with that device current) looks the array up with
- * cudaGetSymbolAddress; make it before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race, so serialise them.  stream: cudaStream_t as void* (NULL =
- * default stream).  iterations and gcg_out[2] = {final gCg, eps2} may be NULL.
+ * cudaGetSymbolAddress.  Every call synchronises `stream` (convergence is polled from the host
+ * every 32 iterations), so it cannot be called while that stream is being captured into a
+ * CUDA graph.  All calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  stream: cudaStream_t as void* (NULL = default stream).  iterations and
+ * gcg_out[2] = {final gCg, eps2} may be NULL.  Arrays must be device memory of the current
+ * device (or managed memory).
  * Returns FFGPU_EINVAL for n above the limit or non-device arrays, FFGPU_ENOCONV at itmax. */
 int ffgpu_solve_cg_csr_noalloc(int n, int64_t nnz, const int32_t *rowptr, const int32_t *col,
                                const double *val, const double *b, double *x, double eps, int itmax,

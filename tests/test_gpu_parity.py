@@ -204,6 +204,48 @@ def test_reassemble_then_solve_uses_new_values():
         assert np.array_equal(ua, ub)
 
 
+def test_reassemble_after_many_tuned_shapes():
+    """The SpMV layout of a shape is chosen once per context: after more shapes than any fixed
+    cache would hold (each large enough to be timed), a fresh matrix of an already-seen shape
+    still gets that shape's layout, so it solves bit for bit like the first one."""
+    mats = []
+    for n in range(100, 140):
+        Vh = FESpace(mesh.square(n), "P1")
+        A = ffgpu.matrix(ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4)), Vh, eps=1e-10)
+        A.solve(np.ones(Vh.ndof))
+        mats.append(A)
+    Vh = FESpace(mesh.square(100), "P1")
+    a = ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4))
+    b = np.empty(Vh.ndof)
+    B = ffgpu.matrix(a, Vh, eps=1e-12, rhs_out=b)
+    ub = B.solve(b)
+    assert B.layout_code() == mats[0].layout_code()
+    u0 = mats[0].solve(b, eps=1e-12)
+    assert np.array_equal(u0, ub)
+    test_reassemble_then_solve_uses_new_values()
+
+
+@pytest.mark.parametrize("name", ["p1sq_n16", "p2el_n2"])
+def test_every_spmv_layout_against_freefem(name):
+    """Each layout the tuner may pick (SELL-32 variants, block CSR lanes) solves FreeFEM's
+    system to the solution bar; the same fixed layout gives the same bits in two matrices."""
+    c = case(name)
+    d = c["d"]
+    Vh = FESpace(c["Th"], c["kind"], c.get("dof"))
+    codes = list(range(64, 72)) + [1, 2, 4, 8]
+    for code in codes:
+        b = np.empty(Vh.ndof)
+        A = ffgpu.matrix(gpu_varf(c), Vh, eps=c["eps"], rhs_out=b)
+        u = A.solve(b, spmv_layout=code)
+        assert A.layout_code() == code
+        assert np.linalg.norm(u - d["u"]) <= SOL_TOL * np.linalg.norm(d["u"]), code
+        B = ffgpu.matrix(gpu_varf(c), A.space, eps=c["eps"])
+        assert np.array_equal(B.solve(b, spmv_layout=code), u), code
+    for code in (5, 63, 72):
+        with pytest.raises(ffgpu.FFGPUError):
+            A.solve(b, spmv_layout=code)
+
+
 def test_wide_band_matrix_against_oracle():
     """Rows and columns randomly permuted (bandwidth above 2^15, so the SpMV keeps 32-bit
     column indices): same solution as the oracle's on the unpermuted matrix."""
