@@ -393,6 +393,7 @@ struct FillArgs {
     const double *fint;       // element vectors of a source at quadrature points, or NULL
     const double *mloc;       // element mass matrices of a coefficient at quadrature points, or NULL
     const double *kloc;       // element stiffness matrices of a coefficient at quadrature points, or NULL
+    const double *tloc;       // element matrices of the general volume terms (ffgpu_varf.terms), or NULL
     const double *lame;       // per-element (lambda, mu) of the elasticity form, or NULL
     double f0, f1, f2;
     double c_mass;
@@ -465,6 +466,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     double val = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * meas * s;
                     if (has_mass) val += A.c_mass * meas * mfac * (la == lb ? 2.0 : 1.0);
                     if (A.mloc) val += A.mloc[((int64_t)e * NN + la) * NN + lb];
+                    if (A.tloc) val += A.tloc[((int64_t)e * NN + la) * NN + lb];
                     v[0] = val;
                 } else {
                     const P2Pair<DIM> P(G, la, lb);
@@ -473,6 +475,7 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                         v[0] = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * m * P.trace();
                         if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
                         if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
+                        if (A.tloc) v[0] += A.tloc[((int64_t)e * NN + la) * NN + lb];
                     } else {
                         const double tr = P.trace();
                         const double lam = A.lame ? __ldg(A.lame + 2 * (int64_t)e) : A.lam;
@@ -841,13 +844,15 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     fa.lame = lame.d;
     double *fint = nullptr, *mloc = nullptr;
     if (rh.d) FFGPU_TRY(source_prepare(S, v, M->geo, &fint));
-    double *kloc = nullptr;
+    double *kloc = nullptr, *tloc = nullptr;
     int frc = mass_prepare(S, v, M->geo, &mloc);
     if (!frc) frc = stiff_prepare(S, v, M->geo, &kloc);
-    if (frc) { dfree(ctx, fint); dfree(ctx, mloc); return frc; }
+    if (!frc) frc = terms_prepare(S, v, M->geo, &tloc);
+    if (frc) { dfree(ctx, fint); dfree(ctx, mloc); dfree(ctx, kloc); return frc; }
     fa.fint = fint;
     fa.mloc = mloc;
     fa.kloc = kloc;
+    fa.tloc = tloc;
     BoundaryTerms bt;
     frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
     if (!frc) {
@@ -858,6 +863,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     dfree(ctx, fint);
     dfree(ctx, mloc);
     dfree(ctx, kloc);
+    dfree(ctx, tloc);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish());

@@ -490,6 +490,7 @@ int boundary_prepare(ffgpu_space *S, const ffgpu_varf *v, bool want_rhs, bool wa
 
 int source_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **fint) {
     *fint = nullptr;
+    if (v && v->f_expr) return source_expr_prepare(S, v, geo, fint);
     if (!v || !v->f_qp) return FFGPU_OK;
     FFGPU_CHECK(v->nqp > 0 && v->nqp <= 64 && v->qp_lambda && v->qp_weight, FFGPU_EINVAL,
                 "source at quadrature points: 1..64 points with coordinates and weights expected (nqp %d)", v->nqp);

@@ -132,6 +132,8 @@ struct ffgpu_matrix {
     // tuning
     int csr_lanes;        // lanes per block row of the FP64 SpMV (tuned)
     int csr_lanes_x;      // lanes per block row of the double-float SpMV (tuned)
+    int layout_pinned;    // the caller fixed the SpMV layout of the current solve
+    int last_cluster;     // the last FP64 CG solve ran in one thread-block cluster
     // SELL-32 copy for the Krylov SpMVs: block rows sliced into chunks of 32 (one row per
     // lane), rows sorted by decreasing degree inside windows of 1024 rows, each chunk padded
     // to its longest row and stored slot-major so that a warp reads 32 consecutive entries.
@@ -255,6 +257,11 @@ int mass_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double 
 // Element stiffness matrices of a coefficient given at quadrature points (ffgpu_varf.stiff_qp):
 // *kloc = nt * nn * nn values |K| sum_q w_q k_q grad phi_i . grad phi_j, or NULL.
 int stiff_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **kloc);
+// General volume terms of a scalar varf (ffgpu_varf.terms, ffgpu_expr.cu): *tloc = nt * nn * nn
+// element matrices |K| sum_q w_q sum_t c_t(x_q) op_i(phi_i) op_j(phi_j), or NULL when none.
+int terms_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **tloc);
+// Element vectors of a source given as expressions (ffgpu_varf.f_expr), as source_prepare.
+int source_expr_prepare(ffgpu_space *S, const ffgpu_varf *v, const double *geo, double **fint);
 // on(labels) DOF mask on the device (onbc: ndof bytes, device)
 int space_bc_mask_device(ffgpu_space *S, int nlabels, const int32_t *labels, int comp_mask, uint8_t *onbc);
 
@@ -300,6 +307,15 @@ int matrix_prepare_solver(ffgpu_matrix *A);
 int matrix_prepare_transpose(ffgpu_matrix *A);
 int matrix_prepare_split(ffgpu_matrix *A, int trans);
 int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t s);
+// The CG iteration loop of a small scalar system in one thread-block cluster (ffgpu_cluster.cu):
+// whether it takes the matrix (a rule on sizes and the device, never on timings), and the run
+// from the state cg_init leaves (x, g, h, Krylov scalars; x receives the solution).
+bool cluster_cg_fits(ffgpu_matrix *A, int trans);
+constexpr int kClusterRefused = 1;   // cluster_cg_run: the launch was refused, nothing ran
+int cluster_cg_run(ffgpu_matrix *A, int trans, double *x, const double *g, const double *h, cudaStream_t s);
+// solver=GMRES for one right-hand side (ffgpu_gmres.cu); b, x device pointers
+int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
+              ffgpu_solver_stats *st);
 
 // -------------------------------------------------------------------- device helpers
 __device__ __forceinline__ double warp_sum(double v) {

@@ -815,6 +815,7 @@ static int tune_lanes(ffgpu_matrix *A, int mode) {
 // A layout fixed by the caller (ffgpu_solver_params.spmv_layout, else the environment variable
 // FFGPU_SPMV_LAYOUT for the FP64 CG) replaces the tuned one for this matrix.
 static int pin_layout(ffgpu_matrix *A, int mode, int code) {
+    A->layout_pinned = 0;
     if (code == 0) {
         const char *e = mode == 0 ? getenv("FFGPU_SPMV_LAYOUT") : nullptr;
         if (!e || !e[0]) return FFGPU_OK;
@@ -823,6 +824,7 @@ static int pin_layout(ffgpu_matrix *A, int mode, int code) {
     FFGPU_CHECK(layout_valid(mode, code), FFGPU_EINVAL,
                 "spmv_layout %d is not a layout of SpMV mode %d (SELL-32: 64..%d, block CSR lanes: %s)", code, mode,
                 mode == 1 ? 67 : 71, mode == 1 ? "4, 8, 16, 32" : "1, 2, 4, 8");
+    A->layout_pinned = 1;
     int *slot = mode == 1 ? &A->csr_lanes_x : &A->csr_lanes;
     if (*slot == code) return FFGPU_OK;
     *slot = code;
@@ -1017,7 +1019,11 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         if (!A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vs));
         FFGPU_TRY(tune_lanes(A, 1));
     }
-    FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
+    // small scalar systems: the whole iteration loop in one thread-block cluster
+    // (ffgpu_cluster.cu), unless a layout is fixed by the caller
+    const bool cluster = mode == 0 && !A->layout_pinned && cluster_cg_fits(A, trans);
+    A->last_cluster = cluster;
+    if (!cluster) FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
     FFGPU_CUDA(cudaMemcpyAsync(x, xu, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -1036,7 +1042,20 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     }
     const char *ge = getenv("FFGPU_CG_GRAPH");
     int bodies_host = -1;
-    if (ge && ge[0] == '0') {
+    bool use_graph = !cluster;
+    if (cluster) {
+        const int rc = cluster_cg_run(A, trans, x, g, h, s);
+        if (rc == kClusterRefused) {
+            // the device refused this cluster shape: the regular path from the same state
+            A->last_cluster = 0;
+            FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
+            use_graph = true;
+        } else {
+            FFGPU_TRY(rc);
+            bodies_host = 0;
+        }
+    }
+    if (use_graph && ge && ge[0] == '0') {
         // Same kernels launched from the host (for profilers that do not trace conditional
         // graph nodes): poll the done flag after every `unroll` iterations.
         KaCall ka;
@@ -1051,7 +1070,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
             FFGPU_CUDA(cudaStreamSynchronize(s));
             if (done) break;
         }
-    } else {
+    } else if (use_graph) {
         FFGPU_CUDA(cudaGraphLaunch(A->cg_exec, s));
     }
     FFGPU_CUDA(cudaMemcpyAsync(xu, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
@@ -1064,7 +1083,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     int bodies = bodies_host >= 0 ? bodies_host : (hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll);
-    ctx->launches += (int64_t)bodies * A->cg_kernels_body;
+    if (use_graph) ctx->launches += (int64_t)bodies * A->cg_kernels_body;
     if (st) {
         st->iterations = hk.iter;
         st->converged = hk.converged != 0;
@@ -1073,186 +1092,6 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         st->elapsed_ms += ms;
     }
     return hk.converged ? FFGPU_OK : FFGPU_ENOCONV;
-}
-
-// ------------------------------------------------------------------ FGMRES kernels
-__global__ void vec_dot_kernel(int n, const double *x, const double *y, double *part, unsigned *ticket,
-                               double *out) {
-    __shared__ double sh[32];
-    double s = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        s = fma(x[i], y[i], s);
-    double tot;
-    double p = block_sum(s, sh);
-    if (last_block_total(p, part, ticket, &tot, sh)) *out = tot;
-}
-
-// y += alpha * x with alpha = sign * (*palpha)
-__global__ void vec_axpy_dev_kernel(int n, const double *palpha, double sign, const double *x, double *y) {
-    double a = sign * *palpha;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        y[i] = fma(a, x[i], y[i]);
-}
-
-// y = x * (1/ *pnorm2 ^ 0.5) ... y = (1/sqrt(*pn2)) * x
-__global__ void vec_scale_inv_sqrt_kernel(int n, const double *pn2, const double *x, double *y) {
-    double a = 1.0 / sqrt(*pn2);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        y[i] = a * x[i];
-}
-
-__global__ void vec_mul_kernel(int n, const double *d, const double *x, double *y) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        y[i] = d[i] * x[i];
-}
-
-// r = b - r ; (r,r)
-__global__ void resid_kernel(int n, const double *b, double *r) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        r[i] = -(r[i] - b[i]);
-}
-
-__global__ void masked_copy_kernel(int n, const double *b, const uint8_t *wcl, int use, double *w) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        w[i] = (use && wcl[i]) ? 0.0 : b[i];
-}
-
-// Givens step of fgmres on column `it` of Hn (device resident, single thread).
-__global__ void givens_kernel(int it, int ld, double *Hn, const double *hnext2, double *rot0, double *rot1,
-                              double *g, double *relres) {
-    Hn[(size_t)(it + 1) * ld + it] = sqrt(*hnext2);
-    for (int i = 0; i < it; i++) {
-        double a = Hn[(size_t)i * ld + it], b = Hn[(size_t)(i + 1) * ld + it];
-        Hn[(size_t)i * ld + it] = rot0[i] * a + rot1[i] * b;
-        Hn[(size_t)(i + 1) * ld + it] = -rot1[i] * a + rot0[i] * b;
-    }
-    double a = Hn[(size_t)it * ld + it], b = Hn[(size_t)(it + 1) * ld + it];
-    double sq = sqrt(a * a + b * b);
-    rot0[it] = a / sq;
-    rot1[it] = b / sq;
-    Hn[(size_t)it * ld + it] = rot0[it] * a + rot1[it] * b;
-    Hn[(size_t)(it + 1) * ld + it] = 0.;
-    g[it + 1] = -rot1[it] * g[it];
-    g[it] = rot0[it] * g[it];
-    *relres = fabs(g[it + 1]);
-}
-
-// back substitution y = Hn^-1 g (upper triangular, it+1 unknowns)
-__global__ void backsolve_kernel(int it, int ld, const double *Hn, const double *g, double *y) {
-    for (int i = it; i >= 0; i--) {
-        double s = g[i];
-        for (int j = i + 1; j < it + 1; j++) s -= Hn[(size_t)i * ld + j] * y[j];
-        y[i] = s / Hn[(size_t)i * ld + i];
-    }
-}
-
-__global__ void gmres_update_kernel(int n, int k, const double *y, const double *Vp, const double *x0, double *x) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double s = 0;
-        for (int j = 0; j < k; ++j) s += y[j] * Vp[(size_t)j * n + i];
-        x[i] = s + x0[i];
-    }
-}
-
-static int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
-                     ffgpu_solver_stats *st) {
-    ffgpu_ctx *ctx = A->ctx;
-    cudaStream_t s = ctx->stream;
-    const int n = A->n;
-    const int m = prm->dim_krylov > 0 ? prm->dim_krylov : 50;
-    const int itmax = prm->itmax > 0 ? prm->itmax : n;
-    const double eps = prm->eps;
-    const double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
-    const int G = kVecBlocks, TB = kVecThreads;
-    double *V = nullptr, *Vp = nullptr, *dev = nullptr;
-    size_t ld = m + 1;
-    FFGPU_CUDA(dalloc(ctx, (void **)&V, sizeof(double) * (size_t)n * (m + 1)));
-    FFGPU_CUDA(dalloc(ctx, (void **)&Vp, sizeof(double) * (size_t)n * (m + 1)));
-    // device scalars: Hn[(m+2) x (m+1)], rot0, rot1, g, y, dotv, relres
-    size_t nsc = (size_t)(m + 2) * ld + 4 * (m + 2) + 8;
-    FFGPU_CUDA(dalloc(ctx, (void **)&dev, sizeof(double) * nsc));
-    FFGPU_CUDA(cudaMemsetAsync(dev, 0, sizeof(double) * nsc, s));
-    double *Hn = dev, *rot0 = Hn + (size_t)(m + 2) * ld, *rot1 = rot0 + (m + 2), *gv = rot1 + (m + 2);
-    double *y = gv + (m + 2), *dotv = y + (m + 2), *relres_d = dotv + 2;
-    double *wi = A->vec, *ri = A->vec + 2 * vstride(n), *x0 = A->vec + 3 * vstride(n);
-    unsigned *tk = ctx->d_ticket;
-    double *part = ctx->d_part;
-    int rc = FFGPU_OK;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, s);
-    if (A->ntgv > 0) cg_x0_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, x, b, A->wcl, tgv);
-    masked_copy_kernel<<<G, TB, 0, s>>>(n, b, A->wcl, A->ntgv > 0, wi);
-    vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, wi, part, tk, dotv);
-    ctx->launches += 3;
-    double hb[2];
-    cudaMemcpyAsync(hb, dotv, sizeof(double), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    double normb = sqrt(hb[0]);
-    int iter = 0;
-    bool noconv = true;
-    double relres = 1e100;
-    while (noconv) {
-        cudaMemcpyAsync(x0, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
-        if ((rc = spmv(A, x, ri, trans, s))) break;
-        resid_kernel<<<G, TB, 0, s>>>(n, b, ri);
-        vec_dot_kernel<<<G, TB, 0, s>>>(n, ri, ri, part, tk, dotv);
-        ctx->launches += 2;
-        cudaMemcpyAsync(hb, dotv, sizeof(double), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        double g0 = sqrt(hb[0]);
-        if (normb < 1.e-20 || eps < 0) normb = 1.;
-        cudaMemcpyAsync(gv, &g0, sizeof(double), cudaMemcpyHostToDevice, s);
-        vec_scale_inv_sqrt_kernel<<<G, TB, 0, s>>>(n, dotv, ri, V);
-        ctx->launches += 1;
-        int it;
-        for (it = 0; it < m; it++, iter++) {
-            double *Vit = V + (size_t)it * n, *Vpit = Vp + (size_t)it * n;
-            vec_mul_kernel<<<G, TB, 0, s>>>(n, A->diag_inv, Vit, Vpit);
-            ctx->launches += 1;
-            if ((rc = spmv(A, Vpit, wi, trans, s))) break;
-            for (int i = 0; i <= it; i++) {   // modified Gram-Schmidt
-                double *hij = Hn + (size_t)i * ld + it;
-                vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, V + (size_t)i * n, part, tk, hij);
-                vec_axpy_dev_kernel<<<G, TB, 0, s>>>(n, hij, -1.0, V + (size_t)i * n, wi);
-                ctx->launches += 2;
-            }
-            vec_dot_kernel<<<G, TB, 0, s>>>(n, wi, wi, part, tk, dotv);
-            vec_scale_inv_sqrt_kernel<<<G, TB, 0, s>>>(n, dotv, wi, V + (size_t)(it + 1) * n);
-            givens_kernel<<<1, 1, 0, s>>>(it, (int)ld, Hn, dotv, rot0, rot1, gv, relres_d);
-            ctx->launches += 3;
-            cudaMemcpyAsync(&relres, relres_d, sizeof(double), cudaMemcpyDeviceToHost, s);
-            if (cudaStreamSynchronize(s) != cudaSuccess) { set_error("gmres: %s", cudaGetErrorString(cudaGetLastError())); rc = FFGPU_ECUDA; break; }
-            if (relres / normb < fabs(eps)) { noconv = false; break; }
-            if (it > itmax) break;
-        }
-        if (rc) break;
-        it = min(it, m - 1);
-        backsolve_kernel<<<1, 1, 0, s>>>(it, (int)ld, Hn, gv, y);
-        gmres_update_kernel<<<G, TB, 0, s>>>(n, it + 1, y, Vp, x0, x);
-        ctx->launches += 2;
-        if (!noconv) break;
-        if (iter > itmax) break;
-    }
-    cudaEventRecord(e1, s);
-    cudaStreamSynchronize(s);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    dfree(ctx, V);
-    dfree(ctx, Vp);
-    dfree(ctx, dev);
-    cudaStreamSynchronize(s);
-    if (rc) return rc;
-    if (st) {
-        st->iterations = iter;
-        st->converged = !noconv;
-        st->residual = relres / normb;
-        st->elapsed_ms += ms;
-    }
-    return noconv ? FFGPU_ENOCONV : FFGPU_OK;
 }
 
 }  // namespace ffgpu
@@ -1317,6 +1156,7 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode) {
     if (!A) return 0;
     if (mode == 3) return A->scol16 != nullptr;
+    if (mode == 5) return A->last_cluster;
     if (mode == 4) return A->nslot > 0 && A->nslot * 32 <= INT32_MAX ? (int)(A->nslot * 32) : (A->nslot ? -1 : 0);
     return mode == 2 ? A->sell32_kind : (mode == 1 ? A->csr_lanes_x : A->csr_lanes);
 }

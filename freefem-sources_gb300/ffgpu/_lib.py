@@ -13,7 +13,7 @@ LIBPATH = os.path.join(HERE, "lib", "libffgpu.so")
 
 FFGPU_OK = 0
 ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOCONV", -4: "EMESH", -5: "ENOMEM"}
-FE_P1, FE_P2, FE_P2VEC3 = 1, 2, 3
+FE_P0, FE_P1, FE_P2, FE_P2VEC3 = 0, 1, 2, 3
 FORM_DIFFUSION, FORM_ELASTICITY = 0, 1
 
 # every symbol include/ffgpu.h declares
@@ -42,13 +42,27 @@ class BTerm(C.Structure):
                 ("robin_const", C.c_double), ("g", C.c_void_p), ("g_const", C.c_double * 3)]
 
 
+class FEFuncC(C.Structure):
+    _fields_ = [("kind", C.c_int), ("values", C.c_void_p), ("dof", C.c_void_p)]
+
+
+class ExprC(C.Structure):
+    _fields_ = [("nops", C.c_int), ("ops", C.c_void_p), ("consts", C.c_void_p), ("nfe", C.c_int),
+                ("fe", C.c_void_p)]
+
+
+class TermC(C.Structure):
+    _fields_ = [("iop", C.c_int), ("jop", C.c_int), ("c", C.c_double), ("expr", C.c_void_p)]
+
+
 class Varf(C.Structure):
     _fields_ = [("form", C.c_int), ("kappa", C.c_void_p), ("c_stiff", C.c_double),
                 ("c_mass", C.c_double), ("E", C.c_double), ("nu", C.c_double),
                 ("f", C.c_void_p), ("f_const", C.c_double * 3), ("nbterms", C.c_int),
                 ("bterms", C.c_void_p), ("nqp", C.c_int), ("qp_lambda", C.c_void_p),
                 ("qp_weight", C.c_void_p), ("f_qp", C.c_void_p), ("mass_qp", C.c_void_p),
-                ("stiff_qp", C.c_void_p), ("lame", C.c_void_p)]
+                ("stiff_qp", C.c_void_p), ("lame", C.c_void_p), ("f_expr", C.c_void_p),
+                ("nterms", C.c_int), ("terms", C.c_void_p)]
 
 
 class BC(C.Structure):

@@ -24,6 +24,7 @@ import numpy as np
 
 from . import _lib, quadrature
 from ._lib import BC, BTerm, SolverParams, SolverStats, Varf, check, lib
+from .expr import Expr, c_expr, const
 from .fespace import FESpace
 from .mesh import Mesh
 
@@ -151,13 +152,16 @@ class VarForm:
     components: tuple | None = None
     tgv: float = 1e30
     bterms: tuple = ()            # BoundaryTerm, in varf order
+    terms: tuple = ()             # general volume terms (iop, jop, coef) of a scalar space:
+                                  # int(coef*op_i(v)*op_j(u)), op "id"/"dx"/"dy"/"dz" (or 0..3),
+                                  # coef a number or an ffgpu.expr expression
     _keep: list = field(default_factory=list)
 
     def c_varf(self, Vh: FESpace) -> Varf:
         v = Varf()
         v.form = self.form
         v.c_stiff = self.c_stiff
-        v.c_mass = 0.0 if callable(self.c_mass) else self.c_mass
+        v.c_mass = 0.0 if (callable(self.c_mass) or isinstance(self.c_mass, Expr)) else self.c_mass
         # values at quadrature points (one rule for the varf), set by the helpers below
         v.nqp = 0
         v.qp_lambda = v.qp_weight = v.f_qp = v.mass_qp = v.stiff_qp = None
@@ -173,16 +177,24 @@ class VarForm:
             self._keep.append(lame)
             v.lame = _ptr(lame).value
         v.kappa = None
-        if callable(self.kappa):
+        v.f_expr = None
+        v.nterms = 0
+        v.terms = None
+        self._expressions(v, Vh)
+        if isinstance(self.kappa, Expr):
+            pass
+        elif callable(self.kappa):
             self._stiff_at_points(v, Vh)
         elif self.kappa is not None:
             k = self.kappa if hasattr(self.kappa, "data_ptr") else np.ascontiguousarray(self.kappa, np.float64)
             self._keep.append(k)
             v.kappa = _ptr(k).value
         v.f = None
-        if callable(self.c_mass):
+        if callable(self.c_mass) and not isinstance(self.c_mass, Expr):
             self._mass_at_points(v, Vh)
-        if callable(self.f):
+        if _is_expr_source(self.f):
+            pass
+        elif callable(self.f):
             self._source_at_points(v, Vh)
         elif np.isscalar(self.f):
             v.f_const[0] = float(self.f)
@@ -240,6 +252,61 @@ class VarForm:
             v.nbterms = len(self.bterms)
             v.bterms = C.cast(arr, C.c_void_p).value
         return v
+
+    def _expressions(self, v: Varf, Vh: FESpace) -> None:
+        """Coefficients and sources given as ffgpu.expr expressions: evaluated on the device at
+        the points of the varf's rule.  kappa -> the terms (dx,dx)+(dy,dy)[+(dz,dz)] with
+        coefficient c_stiff*kappa; c_mass -> the term (id,id); f -> f_expr; plus self.terms."""
+        dim = Vh.Th.dim
+        ops = {"id": 0, "dx": 1, "dy": 2, "dz": 3}
+        terms = []
+        if isinstance(self.kappa, Expr):
+            terms += [(d + 1, d + 1, self.c_stiff, self.kappa) for d in range(dim)]
+            v.c_stiff = 0.0          # the closed-form stiffness then contributes nothing
+        if isinstance(self.c_mass, Expr):
+            terms.append((0, 0, 1.0, self.c_mass))
+            v.c_mass = 0.0
+        for t in self.terms:
+            iop, jop, coef = t
+            iop = ops.get(iop, iop)
+            jop = ops.get(jop, jop)
+            if isinstance(coef, Expr):
+                terms.append((int(iop), int(jop), 1.0, coef))
+            else:
+                terms.append((int(iop), int(jop), float(coef), None))
+        fexpr = _is_expr_source(self.f)
+        if not terms and not fexpr:
+            return
+        if self.form != _lib.FORM_DIFFUSION and terms:
+            raise ValueError("expression coefficients and general terms need the scalar diffusion form")
+        lam, w = quadrature.rule(self.quad, dim)
+        self._keep += [lam, w]
+        v.nqp = lam.shape[0]
+        v.qp_lambda = _ptr(lam).value
+        v.qp_weight = _ptr(w).value
+        if terms:
+            arr = (_lib.TermC * len(terms))()
+            for k, (iop, jop, c, e) in enumerate(terms):
+                arr[k].iop, arr[k].jop, arr[k].c = iop, jop, c
+                if e is None:
+                    arr[k].expr = None
+                else:
+                    ex = c_expr(e, self._keep)
+                    self._keep.append(ex)
+                    arr[k].expr = C.addressof(ex)
+            self._keep.append(arr)
+            v.nterms = len(terms)
+            v.terms = C.cast(arr, C.c_void_p).value
+        if fexpr:
+            nc = 3 if Vh.kind == "P2vec" else 1
+            comps = list(self.f) if isinstance(self.f, (tuple, list)) else [self.f]
+            if len(comps) != nc:
+                raise ValueError(f"the source needs {nc} component(s)")
+            arr = (_lib.ExprC * nc)()
+            for c, e in enumerate(comps):
+                arr[c] = c_expr(e if isinstance(e, Expr) else const(e), self._keep)
+            self._keep.append(arr)
+            v.f_expr = C.cast(arr, C.c_void_p).value
 
     def _rule_points(self, v: Varf, Vh: FESpace):
         """The rule (set once in v) and the physical points of every element."""
@@ -321,14 +388,23 @@ class VarForm:
         return bc
 
 
+def _is_expr_source(f):
+    if isinstance(f, Expr):
+        return True
+    return isinstance(f, (tuple, list)) and any(isinstance(c, Expr) for c in f)
+
+
 def varf_diffusion(kappa=None, f=1.0, on=(), g=None, c_mass=0.0, c_stiff=1.0, tgv=1e30,
-                   bterms=(), quad=None) -> VarForm:
+                   bterms=(), quad=None, terms=()) -> VarForm:
     """varf a(u,v) = int(c_stiff*kappa*grad u.grad v + c_mass*u*v) + int(f*v)
     + the boundary terms (BoundaryTerm: robin*u*v + g*v on labelled boundary edges/faces)
     + on(on, u=g).  kappa, c_mass and f may be functions of the coordinates, f(x, y[, z]),
-    taken at the points of `quad`."""
+    taken at the points of `quad` on the host, or ffgpu.expr expressions (x, y, z, FE functions
+    by their DOF values, their derivatives), evaluated on the device at those points.
+    terms: further volume terms (iop, jop, coef) = int(coef*op_i(v)*op_j(u)) with op "id",
+    "dx", "dy", "dz" -- anisotropic diffusion, advection, reaction."""
     return VarForm(form=_lib.FORM_DIFFUSION, kappa=kappa, f=f, on=tuple(on), g=g, c_mass=c_mass,
-                   c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms), quad=quad)
+                   c_stiff=c_stiff, tgv=tgv, bterms=tuple(bterms), quad=quad, terms=tuple(terms))
 
 
 def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, tgv=1e30,

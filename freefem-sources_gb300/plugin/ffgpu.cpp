@@ -39,6 +39,20 @@ void Expandsetoflab(Stack stack, const CDomainOfIntegration &di, set<int> &setof
 namespace {
 
 ffgpu_ctx *g_ctx = nullptr;
+// ffgpustrict (script variable; or the environment variable FFGPU_STRICT=1): a form the device
+// does not assemble stops the script with ExecError instead of going to FreeFEM's own assembly
+long g_strict = 0;
+
+bool strict() {
+    static const bool env = getenv("FFGPU_STRICT") && getenv("FFGPU_STRICT")[0] == '1';
+    return env || g_strict != 0;
+}
+
+// A form the device does not take: reported at verbosity > 0, an error under ffgpustrict.
+void not_on_device(const char *what, const std::string &why) {
+    if (strict()) ExecError((std::string("ffgpu (ffgpustrict): ") + what + " not assembled on the device: " + why).c_str());
+    if (verbosity > 0) std::cout << "  ffgpu: " << what << " assembled by FreeFEM on the CPU (" << why << ")" << std::endl;
+}
 
 ffgpu_ctx *context() {
     if (!g_ctx) {
@@ -61,6 +75,7 @@ class SolverGpu : public VirtualSolver<int, double> {
     typedef HashMatrix<int, double> HMat;
     HMat &A;
     ffgpu_matrix *M;
+    bool adopted;   // M is the device matrix of `matrix A = a(Vh,Vh)`, equal to A's values
     double eps, tgv;
     long itmax, verb, restart;
     double *veps;
@@ -68,7 +83,7 @@ class SolverGpu : public VirtualSolver<int, double> {
     long cs, cn;
 
     SolverGpu(HMat &AA, const Data_Sparse_Solver &ds, Stack)
-        : A(AA), M(nullptr), eps(ds.epsilon), tgv(ds.tgv), itmax(ds.itmax), verb(ds.verb),
+        : A(AA), M(nullptr), adopted(false), eps(ds.epsilon), tgv(ds.tgv), itmax(ds.itmax), verb(ds.verb),
           restart(ds.NbSpace), veps(ds.veps), getnbiter(ds.getnbiter), cs(0), cn(0) {
         if (ds.precon) ExecError("ffgpu: a script precon= function cannot run on the GPU");
         ffassert(A.n == A.m);
@@ -76,12 +91,27 @@ class SolverGpu : public VirtualSolver<int, double> {
     ~SolverGpu() {
         if (M) ffgpu_matrix_destroy(M);
     }
+    // The device assembly hands over its matrix: the first factorisation uses it instead of
+    // uploading FreeFEM's copy, unless the script changed A in between (HashMatrix's
+    // re_do_numerics / re_do_symbolic flags, HashMatrix.hpp:278-279, read in UpdateState).
+    void adopt(ffgpu_matrix *dm) {
+        if (M) ffgpu_matrix_destroy(M);
+        M = dm;
+        adopted = true;
+    }
     void UpdateState() {
-        if (A.GetReDoNumerics()) cn++;
-        if (A.GetReDoSymbolic()) cs++;
+        const bool num = A.GetReDoNumerics(), sym = A.GetReDoSymbolic();
+        if (num) cn++;
+        if (sym) cs++;
+        if (num || sym) adopted = false;
         this->ChangeCodeState(A.n, cs, cn);
     }
     void fac_numeric() {
+        if (M && adopted) {
+            adopted = false;   // later factorisations follow FreeFEM's matrix
+            if (verb > 1) std::cout << "  ffgpu: solver uses the device-assembled matrix" << std::endl;
+            return;
+        }
         int *IA = nullptr, *JA = nullptr;
         double *AA = nullptr;
         A.CSR(IA, JA, AA);
@@ -627,14 +657,14 @@ static const char *fe_name(int fe) { return fe == FFGPU_FE_P1 ? "P1" : (fe == FF
 // The device assembly of a recognised form into FreeFEM's matrix object; false: not ours.
 template <class MMesh, class FES>
 static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, const Data_Sparse_Solver &ds,
-                          Matrice_Creuse<double> &A) {
+                          Matrice_Creuse<double> &A, ffgpu_matrix **keep) {
     const MMesh &Th = Uh.Th;
     const int d = Dim<MMesh>::d;
     Recognised r;
     if (ds.sym) r.why = "symmetric storage requested";
     else if (!recognise(stack, largs, Th, Uh, r)) {}
     if (!r.why.empty()) {
-        if (verbosity > 1) std::cout << "  ffgpu: form assembled by FreeFEM (" << r.why << ")" << std::endl;
+        not_on_device("form", r.why);
         return false;
     }
     double ksum = 0;
@@ -735,7 +765,9 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
         val.resize(nnz);
         rc = ffgpu_matrix_csr(M, rp.data(), col.data(), val.data());
     }
-    if (M) ffgpu_matrix_destroy(M);
+    // the matrix stays on the device for a GPU solver of A; the space's arrays it needs for
+    // reassembly are not kept (a reassembly comes through this path again)
+    if (rc && M) { ffgpu_matrix_destroy(M); M = nullptr; }
     if (S) ffgpu_space_destroy(S);
     if (rc) ExecError((std::string("ffgpu assembly: ") + ffgpu_last_error()).c_str());
     // FreeFEM's matrix object, as creationBlockOfMatrixToBilinearForm leaves it (problem.hpp:1663-1714)
@@ -744,8 +776,23 @@ static bool device_matrix(Stack stack, const list<C_F0> &largs, const FES &Uh, c
     A.Vh = Uh;
     HashMatrix<int, double> *H = new HashMatrix<int, double>(n, n, 0, 0);
     H->set(n, n, 0, (size_t)nnz, rp.data(), col.data(), val.data(), 0, 1);
+    // H now holds the device matrix's values: clear its change flags, so that a solver can tell
+    // whether the script modified A before the first solve
+    H->GetReDoNumerics();
+    H->GetReDoSymbolic();
     A.A.master(H);
+    *keep = M;
     return true;
+}
+
+// the device matrix to the GPU solver of A, if A has one of ours; otherwise it is freed
+static void hand_over(VirtualMatrix<int, double> &VA, ffgpu_matrix *M) {
+    if (!M) return;
+    VirtualSolver<int, double> *vs = dynamic_cast<VirtualSolver<int, double> *>(VA.vsolver);
+    if (SolverGpu<kCG> *s = dynamic_cast<SolverGpu<kCG> *>(vs)) return s->adopt(M);
+    if (SolverGpu<kGMRES> *s = dynamic_cast<SolverGpu<kGMRES> *>(vs)) return s->adopt(M);
+    if (SolverGpu<kMixed> *s = dynamic_cast<SolverGpu<kMixed> *>(vs)) return s->adopt(M);
+    ffgpu_matrix_destroy(M);
 }
 
 template <class MMesh, class v_fes>
@@ -761,7 +808,10 @@ struct GpuBilinear : public OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> 
             pfes *pUh = GetAny<pfes *>((*b->euh)(stack));
             pfes *pVh = GetAny<pfes *>((*b->evh)(stack));
             const FES *PUh = (FES *)**pUh, *PVh = (FES *)**pVh;
-            if (!PUh || PUh != PVh || isVF(b->largs)) return Base::Op::operator()(stack);
+            if (!PUh || PUh != PVh || isVF(b->largs)) {
+                not_on_device("form", !PUh ? "no space" : (PUh != PVh ? "different test and trial spaces" : "a VF form"));
+                return Base::Op::operator()(stack);
+            }
             Data_Sparse_Solver ds;
             ds.factorize = 0;
             ds.initmat = true;
@@ -769,9 +819,11 @@ struct GpuBilinear : public OpMatrixtoBilinearForm<double, MMesh, v_fes, v_fes> 
             SetEnd_Data_Sparse_Solver<double>(stack, ds, b->nargs, np);
             Matrice_Creuse<double> &A(*GetAny<Matrice_Creuse<double> *>((*this->a)(stack)));
             if (this->init) A.init();
-            if (!device_matrix<MMesh, FES>(stack, b->largs, *PUh, ds, A)) return Base::Op::operator()(stack);
+            ffgpu_matrix *M = nullptr;
+            if (!device_matrix<MMesh, FES>(stack, b->largs, *PUh, ds, A, &M)) return Base::Op::operator()(stack);
             A.pHM()->half = ds.sym;
             SetSolver(stack, false, *A.A, ds);
+            hand_over(*A.A, M);
             return SetAny<Matrice_Creuse<double> *>(&A);
         }
     };
@@ -931,7 +983,7 @@ static bool device_rhs(Stack stack, const list<C_F0> &largs, const FES &Uh, doub
     const int d = Dim<MMesh>::d;
     RecognisedRhs r;
     if (!recognise_rhs(stack, largs, Th, Uh, r)) {
-        if (verbosity > 1) std::cout << "  ffgpu: linear form assembled by FreeFEM (" << r.why << ")" << std::endl;
+        not_on_device("linear form", r.why);
         return false;
     }
     if (verbosity > 1) {
@@ -1056,6 +1108,8 @@ static void Load_Init() {
     Global.New("GPUCG", CConstant<std::string *>(&gpucg));
     Global.New("GPUGMRES", CConstant<std::string *>(&gpugmres));
     Global.New("GPUCGMIXED", CConstant<std::string *>(&gpumixed));
+    // `ffgpustrict = 1;` in a script: forms the device does not assemble are errors
+    Global.New("ffgpustrict", CPValue<long>(g_strict));
     // device assembly behind `matrix A = a(Vh,Vh)` (lgfem.cpp:6669-6673, :6823-6826)
     TheOperators->Add("=", new GpuBilinear<Mesh, v_fes>(0), new GpuBilinear<Mesh3, v_fes3>(0));
     TheOperators->Add("<-", new GpuBilinear<Mesh, v_fes>(1));

@@ -57,6 +57,75 @@ typedef struct {
     double g_const[3];
 } ffgpu_bterm;
 
+/* ------------------------------------------------------------------ coefficient expressions
+ * A coefficient or source of a varf term as an expression of the point, evaluated on the
+ * device at every quadrature point, as FreeFEM's Element_Op / Element_rhs evaluate the term's
+ * expression (optiexpK / the C_F0 of the term) at each point of the rule
+ * (problem.cpp:6117-6132, 6391-6410, 7880-7900).  A postfix program over a stack of doubles
+ * (depth <= 16):
+ *   FFGPU_OP_CONST k     push consts[k]
+ *   FFGPU_OP_X/Y/Z       push the point's coordinate (x = sum_i lambda_i X_i)
+ *   FFGPU_OP_FE k        push FE function fe[k] at the point
+ *   FFGPU_OP_DX/DY/DZ k  push a derivative of FE function fe[k] (P1, P2) at the point
+ *   FFGPU_OP_ADD SUB MUL DIV POW MIN MAX     pop b, pop a, push a op b
+ *   FFGPU_OP_NEG EXP LOG SQRT SIN COS TAN ABS TANH ATAN      pop a, push f(a)
+ * The operand k follows its opcode in ops[].  Functions are CUDA's own (exp, log, ...). */
+#define FFGPU_OP_CONST 1
+#define FFGPU_OP_X 2
+#define FFGPU_OP_Y 3
+#define FFGPU_OP_Z 4
+#define FFGPU_OP_FE 5
+#define FFGPU_OP_DX 6
+#define FFGPU_OP_DY 7
+#define FFGPU_OP_DZ 8
+#define FFGPU_OP_ADD 16
+#define FFGPU_OP_SUB 17
+#define FFGPU_OP_MUL 18
+#define FFGPU_OP_DIV 19
+#define FFGPU_OP_POW 20
+#define FFGPU_OP_MIN 21
+#define FFGPU_OP_MAX 22
+#define FFGPU_OP_NEG 32
+#define FFGPU_OP_EXP 33
+#define FFGPU_OP_LOG 34
+#define FFGPU_OP_SQRT 35
+#define FFGPU_OP_SIN 36
+#define FFGPU_OP_COS 37
+#define FFGPU_OP_TAN 38
+#define FFGPU_OP_ABS 39
+#define FFGPU_OP_TANH 40
+#define FFGPU_OP_ATAN 41
+
+/* an FE function of the mesh by its DOF values (FreeFEM's u[] of a P0/P1/P2 fespace):
+ *   kind 0 (P0): values[element];  FFGPU_FE_P1: values[vertex];
+ *   FFGPU_FE_P2: values[dof[element*nloc + i]] with FreeFEM's local P2 order (vertices, then the
+ *   edges: opposite vertex 0,1,2 in 2D; 01,02,03,12,13,23 in 3D); dof = NULL: the assembled
+ *   space's own DOF table (the space must then be P2). */
+#define FFGPU_FE_P0 0
+typedef struct {
+    int kind;
+    const double *values;
+    const int32_t *dof;
+} ffgpu_fefunc;
+
+typedef struct {
+    int nops;
+    const int32_t *ops;
+    const double *consts;
+    int nfe;
+    const ffgpu_fefunc *fe;
+} ffgpu_expr;
+
+/* A volume term of a scalar (P1/P2) varf: int(Th)(coef * op_i(v) * op_j(u)), op 0 = value,
+ * 1 = d/dx, 2 = d/dy, 3 = d/dz (FreeFEM's term tuple ((icomp,iop),(jcomp,jop)) of a
+ * FormBilinear, problem.cpp:6123-6132, for the scalar component); coef = c * expr(x), expr
+ * NULL meaning 1.  Integrated with the varf's rule (nqp points), added to the form's matrix. */
+typedef struct {
+    int iop, jop;
+    double c;
+    const ffgpu_expr *expr;
+} ffgpu_term;
+
 /* varf description.  kappa: P0 coefficient per element (length nt) or NULL (= 1);
  * the stiffness term is c_stiff*kappa_e, the mass term c_mass (0 = none).
  * Elasticity uses E and nu (mu = E/(2(1+nu)), lambda = E nu/((1+nu)(1-2nu))).
@@ -92,6 +161,14 @@ typedef struct {
     /* lame: per-element Lame coefficients of the elasticity form, lame[2k] = lambda_k,
      * lame[2k+1] = mu_k (several materials), or NULL (then E and nu). */
     const double *lame;
+    /* f_expr: the volume source as expressions evaluated on the device at the points of the
+     * rule (nqp, qp_lambda, qp_weight), one per component (ncomp entries), or NULL.  When
+     * non-NULL it replaces f, f_const and f_qp. */
+    const ffgpu_expr *f_expr;
+    /* terms[0..nterms): general volume terms of a scalar space (diffusion form), evaluated
+     * with the same rule and added to the matrix after kappa/c_mass/mass_qp/stiff_qp. */
+    int nterms;
+    const ffgpu_term *terms;
 } ffgpu_varf;
 
 /* Dirichlet data of `on(labels, u=g)`.  Either onbc[dof] != 0 marks the DOFs directly, or
@@ -247,6 +324,8 @@ int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_si
  * u = 0 unrolled, 1 unrolled deeper, 2 batched, 3 batched deeper (2 and 3: FP64 only); T in
  * {1,..,32} for block CSR with T lanes per block row; 0 before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences;
  * mode 4: block entries the SELL copy stores, padding included (32 per slot; -1 past INT32_MAX).
+ * mode 5: 1 when the last FP64 CG solve ran its whole iteration loop in one thread-block
+ * cluster (small scalar systems, up to 16 x 8192 rows; a fixed layout selects the regular path).
  * No FreeFEM counterpart. */
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
 /* Average device time in ms of `nrep` back-to-back launches of the solver's SpMV kernel (K_a,

@@ -30,7 +30,8 @@ _ref = None
 def build(ref_dir: str | None = None) -> None:
     """Compile the oracle (and oracle/_ref when the FreeFEM sources are reachable)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    src = ref_dir or "/root/reference"
+    from paths import REFERENCE
+    src = ref_dir or REFERENCE
     if os.path.isdir(os.path.join(src, "src", "femlib")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 

@@ -34,8 +34,8 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FF_BIN = os.environ.get("FREEFEM_BIN", "/tmp/ffbuild/src/nw/FreeFem++-nw")
-FF_LOADPATH = os.environ.get("FF_LOADPATH", "/tmp/ffbuild/plugin/seq")
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle"))
+from paths import FF_BIN, FF_LOADPATH   # noqa: E402  (oracle/paths.py)
 
 # ---------------------------------------------------------------- edp fragments
 DUMP_MESH2 = r"""

@@ -1,0 +1,135 @@
+"""solver=GMRES on the device (FreeFEM's fgmres, CG.cpp:348-517) against the oracle's fgmres.
+
+The oracle restates FreeFEM's fgmres step for step (modified Gram-Schmidt, Givens rotations,
+restarts, FreeFEM's stopping tests) and reproduces FreeFEM's GMRES fixture bit for bit.  The
+device forms the same Gram-Schmidt coefficients through one reduction per Arnoldi step
+(low-synchronisation MGS), so its residual estimates differ from the oracle's by rounding:
+solutions agree within 1e-9 relative, iteration counts within max(2, 1 %) (5 % for a restart
+length below 10, whose many restart cycles carry the rounding differences forward).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ffgpu
+import ffo
+from ffgpu import mesh
+from ffgpu.fespace import FESpace
+
+pytestmark = pytest.mark.gpu
+
+SOL_TOL = 1e-9
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_built():
+    from ffgpu.build import build
+    build()
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    ffgpu.context(0)
+    yield
+
+
+def _diffusion(n, seed=1, dim=2):
+    Th = mesh.square(n) if dim == 2 else mesh.cube(n)
+    Vh = FESpace(Th, "P1")
+    kappa = np.exp(np.random.Generator(np.random.PCG64(seed)).standard_normal(Th.nt))
+    on = (1, 2, 3, 4) if dim == 2 else (1, 2, 3, 4, 5, 6)
+    Ao = ffo.assemble(Th, Vh, kappa=kappa)
+    bo = ffo.rhs(Th, Vh, f=1.0)
+    ffo.setbc(Ao, bo, Vh.on(on))
+    return Th, Vh, ffgpu.varf_diffusion(kappa=kappa, f=1.0, on=on), Ao, bo
+
+
+def _close(it, ito, frac=0.01):
+    return abs(it - ito) <= max(2, int(frac * ito))
+
+
+@pytest.mark.parametrize("m", [5, 30, 50, 80])
+def test_gmres_restarts_against_oracle(m):
+    Th, Vh, a, Ao, bo = _diffusion(40)
+    uo, ito, conv, rr = ffo.fgmres(Ao, bo, eps=1e-12, restart=m)
+    assert conv
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-12, dim_krylov=m, rhs_out=b)
+    assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
+    u = A.solve(b)
+    assert A.stats.converged
+    assert A.stats.residual < 1e-12
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    # a short restart (m = 5: 170 restart cycles here) carries rounding differences of the
+    # Gram-Schmidt coefficients from cycle to cycle: 5 % there, 1 % otherwise
+    assert _close(A.stats.iterations, ito, 0.05 if m < 10 else 0.01), (A.stats.iterations, ito)
+
+
+def test_gmres_transpose_against_oracle():
+    Th, Vh, a, Ao, bo = _diffusion(24, seed=5)
+    rng = np.random.Generator(np.random.PCG64(9))
+    c = rng.standard_normal(Vh.ndof)
+    uo, ito, conv, _ = ffo.fgmres(Ao, c, eps=1e-12, restart=40, trans=True)
+    assert conv
+    A = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-12, dim_krylov=40)
+    u = A.solve(c, trans=True)
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    assert _close(A.stats.iterations, ito)
+
+
+def test_gmres_elasticity_against_oracle():
+    Th = mesh.cube(3)
+    Vh = FESpace(Th, "P2vec")
+    Ao = ffo.assemble(Th, Vh, form="elasticity")
+    bo = ffo.rhs(Th, Vh, f=(0.0, 0.0, -1.0))
+    ffo.setbc(Ao, bo, Vh.on((4,)))
+    uo, ito, conv, _ = ffo.fgmres(Ao, bo, eps=1e-12, restart=50)
+    assert conv
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(ffgpu.varf_elasticity(f=(0, 0, -1.0), on=(4,)), Vh, solver="GMRES", eps=1e-12,
+                     dim_krylov=50, rhs_out=b)
+    u = A.solve(b)
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    assert _close(A.stats.iterations, ito)
+
+
+def test_gmres_reproducible_and_host_loop_equal():
+    """Two solves give the same bits, and the host-driven loop (FFGPU_CG_GRAPH=0, the launch
+    sequence profilers see) gives the bits of the graph-driven one."""
+    Th, Vh, a, Ao, bo = _diffusion(32, seed=2)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-10, dim_krylov=25, rhs_out=b)
+    u1 = A.solve(b)
+    u2 = A.solve(b)
+    assert np.array_equal(u1, u2)
+    os.environ["FFGPU_CG_GRAPH"] = "0"
+    try:
+        u3 = A.solve(b)
+    finally:
+        del os.environ["FFGPU_CG_GRAPH"]
+    assert np.array_equal(u1, u3)
+
+
+def test_gmres_nonconvergence_and_exact_guess():
+    Th, Vh, a, Ao, bo = _diffusion(16, seed=3)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-12, dim_krylov=10, itmax=4, rhs_out=b)
+    with pytest.raises(ffgpu.FFGPUError) as ei:
+        A.solve(b)
+    assert ei.value.code == -3
+    # the exact solution as the initial guess: converged at once, nothing changed
+    uo, _, _, _ = ffo.cg(Ao, bo, eps=1e-14)
+    Ab = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-12)
+    u = Ab.solve(b, x0=uo)
+    assert Ab.stats.converged
+    assert np.linalg.norm(u - uo) <= 1e-12 * np.linalg.norm(uo)
+
+
+def test_gmres_multiple_rhs_and_3d():
+    Th, Vh, a, Ao, bo = _diffusion(10, seed=4, dim=3)
+    rng = np.random.Generator(np.random.PCG64(3))
+    B = rng.standard_normal((3, Vh.ndof))
+    A = ffgpu.matrix(a, Vh, solver="GMRES", eps=1e-12, dim_krylov=30)
+    X = A.solve(B.ravel()).reshape(3, -1)
+    for k in range(3):
+        uo, _, conv, _ = ffo.fgmres(Ao, B[k], eps=1e-12, restart=30)
+        assert np.linalg.norm(X[k] - uo) <= SOL_TOL * np.linalg.norm(uo)

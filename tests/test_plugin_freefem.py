@@ -11,9 +11,7 @@ import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-FF_BIN = os.environ.get("FREEFEM_BIN", "/tmp/ffbuild/src/nw/FreeFem++-nw")
-FF_CXX = os.environ.get("FREEFEM_FFCXX", "/tmp/ffbuild/plugin/seq/ff-c++")
-FF_LOADPATH = os.environ.get("FF_LOADPATH", "/tmp/ffbuild/plugin/seq")
+from paths import FF_BIN, FF_CXX, FF_LOADPATH   # oracle/paths.py
 
 pytestmark = pytest.mark.skipif(not (os.path.exists(FF_BIN) and os.path.exists(FF_CXX)),
                                 reason="FreeFEM is not installed here")
@@ -165,10 +163,28 @@ cout << "nnzD " << D.nnz << endl;
     assert r.returncode == 0, out[-2000:]
     for why in ("anisotropic diffusion", "quadrature not exact for the form", "element type",
                 "mixed derivative term"):
-        assert f"ffgpu: form assembled by FreeFEM ({why})" in out
+        assert f"ffgpu: form assembled by FreeFEM on the CPU ({why})" in out
     nnz = {l.split()[0]: int(l.split()[1]) for l in r.stdout.splitlines() if l.startswith("nnz")}
     # square(6) P1: 7 nv - 8 n - 6 entries
     assert nnz["nnzD"] == 7 * 49 - 8 * 6 - 6
+
+
+def test_strict_mode_stops_on_unsupported_form(plugin):
+    """`ffgpustrict = 1;`: a form the device does not assemble is an error, not a silent CPU
+    assembly."""
+    body = r"""
+ffgpustrict = 1;
+mesh Th=square(6,6);
+fespace Vh(Th,P1);
+Vh u,v;
+varf e(u,v)=int2d(Th)(dx(u)*dy(v));
+matrix D=e(Vh,Vh);
+cout << "after " << D.nnz << endl;
+"""
+    r, out = run_script(plugin, "strict.edp", body)
+    assert r.returncode != 0
+    assert "ffgpustrict" in out and "mixed derivative term" in out
+    assert "after " not in r.stdout
 
 
 def test_linear_form_hook(plugin):
@@ -186,7 +202,7 @@ real[int] b2=a2(0,Vh);
 cout << "b2sum " << b2.sum << endl;
 """
     r, out = run_script(plugin, "lf.edp", body)
-    assert "ffgpu: linear form assembled by FreeFEM (operator)" in out
+    assert "ffgpu: linear form assembled by FreeFEM on the CPU (operator)" in out
     assert any(line.startswith("bsum ") for line in r.stdout.splitlines())
     # 72 triangles, f = 2.5: sum_k 2.5 (k % 7 + 1) = 707.5
     assert "ffgpu: device linear form P1 dim 2 f-check 707.5 g 1.5 tgv 1e+30" in out
@@ -245,7 +261,7 @@ real[int] b=a(0,Vh);
 cout << "bsum " << b.sum << endl;
 """
     r, out = run_script(plugin, "fs2.edp", body2)
-    assert "ffgpu: linear form assembled by FreeFEM (volume sources with different quadrature rules)" in out
+    assert "ffgpu: linear form assembled by FreeFEM on the CPU (volume sources with different quadrature rules)" in out
     assert any(line.startswith("bsum ") for line in r.stdout.splitlines())
 
 
@@ -331,7 +347,7 @@ varf a2(u,v)=int2d(Th)(dx(u)*dx(v)+dy(u)*dy(v)) + int2d(Th)(1.*v) + int1d(Th,2)(
 real[int] b2=a2(0,Vh);
 """
     r, out = run_script(plugin, "bt2.edp", body2)
-    assert "ffgpu: linear form assembled by FreeFEM (boundary source not constant on boundary elements)" in out
+    assert "ffgpu: linear form assembled by FreeFEM on the CPU (boundary source not constant on boundary elements)" in out
     # right edges (x = 1): 1 + x = 2; top edges (y = 1): 2 + y = 3
     g2 = np.where(Th.blabel == 2, 2.0, 0.0)
     g3 = np.where(Th.blabel == 3, 3.0, 0.0)
@@ -367,8 +383,8 @@ cout << "nnzA2 " << A2.nnz << endl;
 """
     r, out = run_script(plugin, "bt4.edp", body2)
     assert r.returncode == 0, out[-2000:]
-    assert "ffgpu: form assembled by FreeFEM (boundary term other than c*u*v)" in out
-    assert "ffgpu: form assembled by FreeFEM (boundary quadrature not exact)" in out
+    assert "ffgpu: form assembled by FreeFEM on the CPU (boundary term other than c*u*v)" in out
+    assert "ffgpu: form assembled by FreeFEM on the CPU (boundary quadrature not exact)" in out
 
 
 def test_p2_with_a_mass_term_goes_to_the_device(plugin):

@@ -10,7 +10,7 @@ import pytest
 import ffgpu
 from golden_cases import load
 
-FF_BIN = os.environ.get("FREEFEM_BIN", "/tmp/ffbuild/src/nw/FreeFem++-nw")
+from paths import FF_BIN   # oracle/paths.py
 
 
 def test_read_freefem_coo_text(tmp_path):
