@@ -308,6 +308,32 @@ def flush_l2(dev):
     torch.cuda.synchronize(dev)
 
 
+def pinned(a):
+    """A page-locked host copy of a numpy array (the e2e legs copy from pinned memory)."""
+    import numpy as np
+    import torch
+    a = np.ascontiguousarray(a)
+    t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0] if a.ndim else a.reshape(1)[:0]).dtype,
+                    pin_memory=True)
+    out = t.numpy()           # the array keeps the pinned tensor alive
+    out[...] = a
+    return out
+
+
+def pinned_problem(Th, Vh, a):
+    """The mesh, FE space and varf with every array the e2e leg hands over in pinned memory."""
+    import copy
+    Th_p = dataclasses.replace(Th, coords=pinned(Th.coords), elems=pinned(Th.elems),
+                               belems=pinned(Th.belems), blabel=pinned(Th.blabel))
+    Vh_p = copy.copy(Vh)
+    Vh_p.Th = Th_p
+    Vh_p.dof = Th_p.elems if Vh.kind == "P1" else pinned(Vh.dof)
+    import numpy as np
+    kap = getattr(a, "kappa", None)
+    a_p = dataclasses.replace(a, kappa=pinned(kap)) if isinstance(kap, np.ndarray) else a
+    return Th_p, Vh_p, a_p
+
+
 def peak_hbm():
     try:
         return float(json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]), \
@@ -319,7 +345,8 @@ def peak_hbm():
 # ------------------------------------------------------------------ GPU arm: one problem
 def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
     """Assemble + solve of one problem per rank (C1, C2, C3); `variants` from "doublefloat"
-    (FP64 CG with the double-float SpMV), "mixed" (FP32 inner / FP64 refinement), "gmres"."""
+    (FP64 CG with the double-float SpMV), "mixed" (FP32 inner / FP64 refinement), "gmres",
+    "cholesky" (the direct solver)."""
     import numpy as np
     import torch
     import ffgpu
@@ -441,6 +468,29 @@ def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
                                       "frac": achieved / peak}}
     u_ref = u.clone()
     var = {}
+    elem = None
+    if cfg["kind"] in ("P2", "P2vec"):
+        # the assembly with the element matrices from the tensor cores (the default) and from
+        # the FP64 path inside the row gather, on the same inputs (median of 2 after 1 warm-up)
+        def asm_ms(tc):
+            os.environ["FFGPU_ELEM_TC"] = "1" if tc else "0"
+            try:
+                ts = []
+                for _ in range(3):
+                    S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    A2 = ffgpu.matrix(a, S2, eps=cfg["eps"], itmax=ITMAX, rhs_out=b, device=dev)
+                    e1.record(stream)
+                    e1.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+                    del A2, S2
+                return statistics.median(ts[1:])
+            finally:
+                del os.environ["FFGPU_ELEM_TC"]
+        elem = {"path": "tensor cores: tcgen05.mma kind::f16, features as five exact 11-bit digits",
+                "assemble_ms_tensor_cores": asm_ms(True), "assemble_ms_fp64_elements": asm_ms(False)}
 
     def timed_variant(fn, reps):
         out, ms = None, []
@@ -460,11 +510,11 @@ def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
 
     solve_fp64 = statistics.median(phase["solve"][-steps:])
     if "gmres" in variants:
-        # solver=GMRES (restart 50, FreeFEM's fgmres) on the same system: its own step time,
-        # iterations and time per iteration, error against the FP64 CG solution
+        # solver=GMRES (FreeFEM's fgmres with its default restart, 1000) on the same system: its
+        # own step time, iterations and time per iteration, error against the FP64 CG solution
         def run_gm():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
-            A2 = ffgpu.matrix(a, S2, solver="GMRES", eps=cfg["eps"], itmax=ITMAX, dim_krylov=50, rhs_out=b,
+            A2 = ffgpu.matrix(a, S2, solver="GMRES", eps=cfg["eps"], itmax=ITMAX, dim_krylov=1000, rhs_out=b,
                               device=dev)
             t0 = torch.cuda.Event(enable_timing=True)
             t1 = torch.cuda.Event(enable_timing=True)
@@ -474,11 +524,31 @@ def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
             t1.synchronize()
             return ug, A2.stats.iterations, A2.stats.residual, t0.elapsed_time(t1)
         (ugm, itgm, resgm, solve_gm_ms), msgm = timed_variant(run_gm, 3)
-        var["fp64_gmres_restart50"] = {
+        var["fp64_gmres_restart1000"] = {
             "value": Vh.ndof / (msgm * 1e-3), "ms_per_step": msgm, "iterations": itgm,
             "solve_ms": solve_gm_ms, "ms_per_iteration": solve_gm_ms / max(1, itgm),
             "relative_residual": resgm,
             "rel_err_vs_fp64_cg": float(torch.linalg.norm(ugm - u_ref) / torch.linalg.norm(u_ref))}
+    if "cholesky" in variants:
+        # the direct solver on the same system: ordering + analysis + factorisation + solve in
+        # the first call, then solves alone on the kept factorisation
+        def run_ch():
+            S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
+            A2 = ffgpu.matrix(a, S2, solver="CHOLESKY", rhs_out=b, device=dev)
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            uc = A2.solve(b)
+            t1.record(stream)
+            t1.synchronize()
+            t2 = time.perf_counter()
+            A2.solve(b)
+            return uc, t0.elapsed_time(t1), (time.perf_counter() - t2) * 1e3
+        (uch, first_ms, again_ms), msch = timed_variant(run_ch, 2)
+        var["fp64_direct_cholesky"] = {
+            "value": Vh.ndof / (msch * 1e-3), "ms_per_step": msch,
+            "factor_and_solve_ms": first_ms, "solve_on_kept_factor_ms": again_ms,
+            "rel_err_vs_fp64_cg": float(torch.linalg.norm(uch - u_ref) / torch.linalg.norm(u_ref))}
     if "doublefloat" in variants:
         def run_df():
             S2 = ffgpu.DeviceSpace(Vh, device=dev, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
@@ -510,18 +580,21 @@ def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
             "solve_speedup_vs_fp64": solve_fp64 / solve_ir_ms,
             "rel_err_vs_fp64": float(torch.linalg.norm(uir - u_ref) / torch.linalg.norm(u_ref))}
         del Air
-    # e2e: public API from host arrays (H2D of mesh/DOF table/BC mask, D2H of b and u)
+    # e2e: public API from pinned host arrays (H2D of mesh/DOF table/P0 coefficient, D2H of b
+    # and u; the solve starts from u = 0 as FreeFEM's first solve does)
     e2e_times = []
-    bh = np.zeros(Vh.ndof)
-    bh.fill(0.0)   # pages mapped before the timed region, as a caller's reused buffer is
+    Th_p, Vh_p, a_p = pinned_problem(Th, Vh, a_host)
+    bh = pinned(np.zeros(Vh.ndof))
+    uh = pinned(np.zeros(Vh.ndof))
     w_e2e = max(1, warmup // 3)
     for s in range(w_e2e + steps):
         if small:
             flush_l2(dev)
         barrier()
         t0 = time.perf_counter()
-        Ah = ffgpu.matrix(a_host, Vh, eps=cfg["eps"], itmax=ITMAX, rhs_out=bh, device=dev)
-        uh = Ah.solve(bh)
+        Ah = ffgpu.matrix(a_p, Vh_p, eps=cfg["eps"], itmax=ITMAX, rhs_out=bh, device=dev)
+        uh.fill(0.0)
+        Ah.solve(bh, out=uh)
         t1 = time.perf_counter()
         if s >= w_e2e:
             e2e_times.append((t1 - t0) * 1e3)
@@ -554,7 +627,8 @@ def run_gpu(args, cfgname, steps, warmup, rank, world, variants=(), cpu=True):
                    "spmv_layout": layout,
                    "cg_path": ("one thread-block cluster (whole iteration loop in one kernel)"
                                if cluster else "CUDA graph of K_a, K_b, K_c per iteration"),
-                   "rel_residual": rel_res},
+                   "rel_residual": rel_res,
+                   "element_matrices": elem},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e},
         "gpu_launches": int(launches),
@@ -602,8 +676,8 @@ def assembly_roofline(Th, Vh, cfg, ms, peak):
                     "the scatter formula's bytes are not what it moves"}
 
 
-def profile_case(kind, n, iters, spmv_mode):
-    """Small case for ncu: space + assembly + a fixed number of CG iterations, twice."""
+def profile_case(kind, n, iters, spmv_mode, solver="CG", dim_krylov=1000):
+    """Small case for ncu: space + assembly + a fixed number of CG (or GMRES) iterations, twice."""
     import numpy as np
     import torch
     import ffgpu
@@ -626,7 +700,7 @@ def profile_case(kind, n, iters, spmv_mode):
     b = torch.empty(Vh.ndof, dtype=torch.float64, device=dev)
     for rep in range(2):
         S = ffgpu.DeviceSpace(Vh, coords=X, elems=E, dof=D, belems=BE, blabel=BL)
-        A = ffgpu.matrix(a, S, eps=1e-10, itmax=iters, rhs_out=b)
+        A = ffgpu.matrix(a, S, solver=solver, eps=1e-10, itmax=iters, dim_krylov=dim_krylov, rhs_out=b)
         try:
             if spmv_mode == 2:      # mixed precision: one refinement step of `iters` FP32 iterations
                 A.solve_mixed(b, eps=1e-10, eps_inner=1e-30, itmax_inner=iters, max_outer=1)
@@ -739,12 +813,13 @@ def run_adjoint(args, cfgname, steps, warmup, rank, world, cpu=True):
             hg.append((t2 - t1) * 1e3)
     # e2e: the same gradient from host arrays through the public API
     P2 = adjoint.DiffusionProblem(Vh, on=cfg["on"], eps=cfg["eps"], device=di)
-    uo_h = u_obs.cpu().numpy()
+    uo_h = pinned(u_obs.cpu().numpy())
+    kap_h, f_h = pinned(np.ones(Th.nt)), pinned(np.ones(Th.nt))
     e2e = []
     for k in range(1 + steps):
         flush_l2(di)
         t0 = time.perf_counter()
-        P2.value_and_grad(np.ones(Th.nt), np.ones(Th.nt), uo_h)
+        P2.value_and_grad(kap_h, f_h, uo_h)
         if k >= 1:
             e2e.append((time.perf_counter() - t0) * 1e3)
     t_e2e = statistics.median(e2e)
@@ -848,8 +923,9 @@ def run_batch(args, cfgname, steps, warmup, rank, world, cpu=True):
         errs.append(float(np.linalg.norm(xs[p] - uo) / np.linalg.norm(uo)))
     # e2e from host arrays: the batch as the C ABI takes it (counts, coordinates, elements,
     # on() mask, coefficients back to back), copied in and solved every step
-    arrays = batch.batch_arrays(meshes)
-    kap_h = np.concatenate(kappas)
+    arrays = tuple(pinned(x) for x in batch.batch_arrays(meshes))
+    kap_h = pinned(np.concatenate(kappas))
+    xh = pinned(np.zeros(ndof))
     e2e = []
     for _ in range(steps):
         flush_l2(di)
@@ -857,7 +933,7 @@ def run_batch(args, cfgname, steps, warmup, rank, world, cpu=True):
         t0 = time.perf_counter()
         B2 = batch.Batch(arrays=arrays, device=di)
         B2.assemble(kap_h, f=1.0)
-        xh = B2.solve(eps=cfg["eps"])
+        B2.solve(eps=cfg["eps"], out=xh)   # x is written, not read (each problem starts at 0)
         B2.close()
         e2e.append((time.perf_counter() - t0) * 1e3)
     t_e2e = sum(e2e) / len(e2e)
@@ -891,7 +967,7 @@ def run_batch(args, cfgname, steps, warmup, rank, world, cpu=True):
     return out
 
 
-VARIANTS = {"elasticity_p2_cube64": ("doublefloat", "mixed"), "poisson_p1_square256": ("gmres",),
+VARIANTS = {"elasticity_p2_cube64": ("doublefloat", "mixed"), "poisson_p1_square256": ("gmres", "cholesky"),
             "diffusion_p1_cube160": ("doublefloat", "mixed")}
 
 
@@ -1031,9 +1107,11 @@ def main():
     ap.add_argument("--iters", type=int, default=40)
     ap.add_argument("--spmv-mode", type=int, default=0,
                     help="profile case: 0 FP64 CG, 1 double-float SpMV CG, 2 FP32-inner refinement")
+    ap.add_argument("--solver", default="CG", choices=["CG", "GMRES"], help="profile case: Krylov solver")
+    ap.add_argument("--dim-krylov", type=int, default=1000, help="profile case: GMRES restart length")
     args = ap.parse_args()
     if args.profile_case:
-        profile_case(args.profile_case, args.n, args.iters, args.spmv_mode)
+        profile_case(args.profile_case, args.n, args.iters, args.spmv_mode, args.solver, args.dim_krylov)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -395,6 +395,7 @@ struct FillArgs {
     const double *kloc;       // element stiffness matrices of a coefficient at quadrature points, or NULL
     const double *tloc;       // element matrices of the general volume terms (ffgpu_varf.terms), or NULL
     const double *lame;       // per-element (lambda, mu) of the elasticity form, or NULL
+    const double *eloc;       // [P2]^3 element blocks from the tensor cores (ffgpu_elemtc.cu), or NULL
     double f0, f1, f2;
     double c_mass;
     double lam, mu;           // elasticity
@@ -468,15 +469,20 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
                     if (A.mloc) val += A.mloc[((int64_t)e * NN + la) * NN + lb];
                     if (A.tloc) val += A.tloc[((int64_t)e * NN + la) * NN + lb];
                     v[0] = val;
+                } else if (FE == 2) {
+                    const double m = meas * mfac;
+                    v[0] = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * m * P2Pair<DIM>(G, la, lb).trace();
+                    if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
+                    if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
+                    if (A.tloc) v[0] += A.tloc[((int64_t)e * NN + la) * NN + lb];
+                } else if (A.eloc) {
+                    const double *eb = A.eloc + (((int64_t)e * NN + la) * NN + lb) * BS2;
+#pragma unroll
+                    for (int q = 0; q < BS2; ++q) v[q] = __ldg(eb + q);
                 } else {
                     const P2Pair<DIM> P(G, la, lb);
                     const double m = meas * mfac;
-                    if (FE == 2) {
-                        v[0] = A.kloc ? A.kloc[((int64_t)e * NN + la) * NN + lb] : kap * m * P.trace();
-                        if (has_mass) v[0] += A.c_mass * meas * p2_mass<DIM>(la, lb);
-                        if (A.mloc) v[0] += A.mloc[((int64_t)e * NN + la) * NN + lb];
-                        if (A.tloc) v[0] += A.tloc[((int64_t)e * NN + la) * NN + lb];
-                    } else {
+                    {
                         const double tr = P.trace();
                         const double lam = A.lame ? __ldg(A.lame + 2 * (int64_t)e) : A.lam;
                         const double mu = A.lame ? __ldg(A.lame + 2 * (int64_t)e + 1) : A.mu;
@@ -848,10 +854,16 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     int frc = mass_prepare(S, v, M->geo, &mloc);
     if (!frc) frc = stiff_prepare(S, v, M->geo, &kloc);
     if (!frc) frc = terms_prepare(S, v, M->geo, &tloc);
-    if (frc) { dfree(ctx, fint); dfree(ctx, mloc); dfree(ctx, kloc); return frc; }
+    // P2 stiffness / [P2]^3 elasticity with an element-constant coefficient: the element
+    // matrices from the tensor cores (a coefficient at the rule's points keeps its own path)
+    double *eloc = nullptr;
+    if (!frc && !kloc && (S->fe == FFGPU_FE_P2VEC3 || (S->fe == FFGPU_FE_P2 && v->c_stiff != 0.0)))
+        frc = elem_tc_prepare(S, M->geo, fa.lam, fa.mu, lame.d, &eloc);
+    if (frc) { dfree(ctx, fint); dfree(ctx, mloc); dfree(ctx, kloc); dfree(ctx, tloc); return frc; }
     fa.fint = fint;
     fa.mloc = mloc;
-    fa.kloc = kloc;
+    fa.kloc = S->fe == FFGPU_FE_P2 && eloc ? eloc : kloc;
+    fa.eloc = S->fe == FFGPU_FE_P2VEC3 ? eloc : nullptr;
     fa.tloc = tloc;
     BoundaryTerms bt;
     frc = boundary_prepare(S, v, rh.d != nullptr, true, bt);
@@ -864,6 +876,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     dfree(ctx, mloc);
     dfree(ctx, kloc);
     dfree(ctx, tloc);
+    dfree(ctx, eloc);
     FFGPU_TRY(frc);
     FFGPU_TRY(check_device_status(ctx, "assembly"));
     FFGPU_TRY(rh.finish());
@@ -875,6 +888,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     if (M->valx) { dfree(ctx, M->valx); M->valx = nullptr; }
     if (M->valx_t) { dfree(ctx, M->valx_t); M->valx_t = nullptr; }
     sell_release_values(M);
+    direct_invalidate(M);
     if (M->cg_exec) { cudaGraphExecDestroy(M->cg_exec); M->cg_exec = nullptr; }
     return FFGPU_OK;
 }
@@ -1199,6 +1213,7 @@ int ffgpu_matrix_destroy(ffgpu_matrix *M) {
     if (!M) return FFGPU_OK;
     cudaStreamSynchronize(M->ctx->stream);
     if (M->cg_exec) cudaGraphExecDestroy(M->cg_exec);
+    direct_release(M);
     dfree(M->ctx, M->browptr); dfree(M->ctx, M->bcol); dfree(M->ctx, M->diagpos); dfree(M->ctx, M->rowperm); dfree(M->ctx, M->val);
     dfree(M->ctx, M->geo); dfree(M->ctx, M->bcmask);
     dfree(M->ctx, M->diag_inv); dfree(M->ctx, M->wcl); dfree(M->ctx, M->vec); dfree(M->ctx, M->val_t);

@@ -19,6 +19,13 @@
 // The recurrence is FreeFEM's ConjugueGradient (CG.cpp:196-265) as in ffgpu_solve.cu: the
 // rows sum in the same order as the SELL-32 K_a kernel; only the dot products' order differs.
 // The iteration count is bounded by itmax; every CTA runs the same number of barriers.
+//
+// Measured on GB300 (square(256) P1, 532 iterations): 56 us per iteration against 20 us for the
+// graph of three kernels on the whole GPU.  ncu: the FP64 pipe of the 8 SMs is 68 % busy.  One
+// iteration is ~1 M FP64 operations (SpMV 460 k FMAs, vector updates and dots ~530 k), and
+// GB300's FP64 rate (~2 FMA per clock per SM) makes 8 SMs need ~32 us for them: the FP64 work
+// has to be spread over all 152 SMs, which a single cluster cannot do.  The path is therefore
+// opt-in (FFGPU_CLUSTER_CG=1); the regular path serves every system by default.
 #include <cooperative_groups.h>
 #include <stdlib.h>
 
@@ -188,8 +195,9 @@ static int cluster_rows(int n, int *ncta) {
 // matrix and the device only, never on timings.
 bool cluster_cg_fits(ffgpu_matrix *A, int trans) {
     if (A->bs != 1 || A->n > kClMaxCtas * 1024 * kClMaxPass) return false;
-    if (const char *e = getenv("FFGPU_CLUSTER_CG"))
-        if (e[0] == '0') return false;
+    // opt-in (measured slower than the three-kernel graph on GB300, see the file's header)
+    const char *e = getenv("FFGPU_CLUSTER_CG");
+    if (!e || e[0] != '1') return false;
     int ncta = 0;
     const int R = cluster_rows(A->n, &ncta);
     if (!R) return false;

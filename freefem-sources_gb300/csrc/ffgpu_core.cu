@@ -62,11 +62,12 @@ int check_device_status(ffgpu_ctx *ctx, const char *where) {
         static const char *msg[] = {"ok", "too many candidate neighbours per row (mesh valence)",
                                     "row degree above capacity", "[P2]^3 DOF table is not 3*node+c",
                                     "index out of range in an input table",
-                                    "column missing from a row"};
-        set_error("%s: device reported: %s", where, (st > 0 && st < 6) ? msg[st] : "unknown");
+                                    "column missing from a row", "a bounded wait in a kernel timed out"};
+        set_error("%s: device reported: %s", where, (st > 0 && st < 7) ? msg[st] : "unknown");
         int zero = 0;
         cudaMemcpyAsync(ctx->d_status, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
+        if (st == kDevTimeout) return FFGPU_ECUDA;
         return st == kDevBadDofLayout || st == kDevBadIndex ? FFGPU_EINVAL : FFGPU_EMESH;
     }
     return FFGPU_OK;

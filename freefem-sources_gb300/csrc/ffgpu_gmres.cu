@@ -9,12 +9,21 @@
 //   h_i = s_i - sum_{j<i} h_j G(i,j)
 // (low-synchronisation MGS, Swirydowicz, Langou, Ananthan, Yang & Thomas, Numer. Linear Algebra
 // Appl. 28 (2021)).  The new Gram row G(it, .) = (v_it, v_j) is formed in the same pass as s.
-// One Arnoldi step is four kernels, none with a host round trip:
+// The recurrence is evaluated to first order in the Gram entries, h = s - L s with L the strictly
+// lower Gram triangle: the dropped terms are O(|L|^2 |s|), below the rounding of s itself while
+// the basis is orthonormal to working accuracy, and the coefficients then come from a parallel
+// matrix-vector product instead of a sequential substitution (GB300 runs ~2 FP64 FMAs per clock
+// per SM: O(it^2) sequential work in one block cost more than the whole step at it ~ 500).
+// One Arnoldi step is five kernels, none with a host round trip:
 //   gm_prep    v_it *= 1/||w_prev|| (FreeFEM's Vi[it] = (1/aux) w), vp = C v_it (Jacobi)
 //   SpMV       w = A vp
-//   gm_dots    s = V' w and the Gram row in one pass; last block: h by forward substitution
+//   gm_dots    s = V' w and the Gram row in one pass over V: blocks are (slab of the vectors'
+//              elements) x (group of basis vectors), w and v_it of a slab staged in shared
+//              memory, one warp reduction per vector per 2048 elements; last block: the sums
+//   gm_coef    h = s - L s (a warp per row, all SMs)
 //   gm_update  v_{it+1} = w - V h, ||v_{it+1}||^2; last block: Givens rotations of the new
-//              Hessenberg column, residual estimate |g_{it+1}|, FreeFEM's stopping tests
+//              Hessenberg column (staged in shared memory), residual estimate |g_{it+1}|,
+//              FreeFEM's stopping tests
 // and the Arnoldi loop of one restart cycle is a CUDA-graph `while` node.  The host reads the
 // scalars once per restart cycle.  All reductions sum in a fixed order (warp order inside a
 // block, block order across blocks), so results are reproducible run to run.
@@ -31,8 +40,9 @@ namespace ffgpu {
 
 constexpr int kGmThreads = 256;
 constexpr int kGmWarps = kGmThreads / 32;
-constexpr int kGmE = 8;                      // elements per lane per tile
-constexpr int kGmTile = 32 * kGmE;           // elements per warp per tile
+constexpr int kGmSub = 2048;                 // elements of w and v_it staged per sub-tile of gm_dots
+constexpr int kGmMaxSlabs = 256;             // slabs of gm_dots (partials summed by its last block)
+constexpr int kGmHs = 1024;                  // Hessenberg columns up to this length stay in shared memory
 
 struct GmScal {
     double normb, relres, eps;
@@ -43,6 +53,8 @@ struct GmScal {
 struct GmArgs {
     int n, m;
     int64_t vs;
+    int nslab, ngrp;                         // gm_dots grid: nslab x ngrp blocks
+    int64_t slab_len;                        // elements per slab (a multiple of kGmSub)
     double *V, *Vp, *vpc, *w, *x;
     const double *b, *dinv;
     const uint8_t *wcl;
@@ -160,66 +172,84 @@ __global__ void __launch_bounds__(kGmThreads) gm_prep(GmArgs a) {
 }
 
 // s_i = (w, v_i), i <= it, and the Gram row (v_it, v_j), j < it, in one pass over V.
-// Per warp: tiles of 256 elements, w and v_it of the tile in registers, then every v_i of
-// the tile; per-warp sums accumulate in shared memory (acc[warp][0..2(it+1))).
+// Block (slab, group): the elements [slab * slab_len, +slab_len) of the vectors i = group +
+// ngrp * r; per sub-tile of kGmSub elements w and v_it are staged in shared memory and each warp
+// runs its vectors over the sub-tile (64 elements per lane, then one warp reduction per sum).
+// Partials part[k * nslab + slab], k < 2(it+1); the last block sums them in slab order.
 __global__ void __launch_bounds__(kGmThreads) gm_dots(GmArgs a) {
-    extern __shared__ double acc[];
+    extern __shared__ double smd[];
+    double *wsh = smd, *vsh = smd + kGmSub, *acc = smd + 2 * kGmSub;
     const int it = a.sc->it;
     const int ni = it + 1, K = 2 * ni;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double *my = acc + (int64_t)warp * 2 * (a.m + 1);
-    for (int i = lane; i < K; i += 32) my[i] = 0;
-    __syncwarp();
+    const int slab = blockIdx.x % a.nslab, grp = blockIdx.x / a.nslab;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) acc[k] = 0;
     const double *vit = a.V + it * a.vs;
-    for (int64_t base = ((int64_t)blockIdx.x * kGmWarps + warp) * kGmTile; base < a.n;
-         base += (int64_t)gridDim.x * kGmWarps * kGmTile) {
-        double wv[kGmE], vv[kGmE];
-#pragma unroll
-        for (int e = 0; e < kGmE; ++e) {
-            const int64_t k = base + lane + 32 * e;
-            wv[e] = k < a.n ? a.w[k] : 0.0;
-            vv[e] = k < a.n ? vit[k] : 0.0;
+    const int64_t e0 = (int64_t)slab * a.slab_len;
+    const int64_t e1 = e0 + a.slab_len < a.n ? e0 + a.slab_len : (int64_t)a.n;
+    for (int64_t t0 = e0; t0 < e1; t0 += kGmSub) {
+        const int len = e1 - t0 < kGmSub ? (int)(e1 - t0) : kGmSub;
+        __syncthreads();   // the previous sub-tile's readers are done (and acc is zeroed)
+        for (int e = threadIdx.x; e < len; e += blockDim.x) {
+            wsh[e] = a.w[t0 + e];
+            vsh[e] = vit[t0 + e];
         }
-        for (int i = 0; i < ni; ++i) {
-            const double *vi = a.V + i * a.vs;
+        __syncthreads();
+        for (int i = grp + a.ngrp * warp; i < ni; i += a.ngrp * kGmWarps) {
+            const double *vi = a.V + i * a.vs + t0;
             double ts = 0, tl = 0;
-#pragma unroll
-            for (int e = 0; e < kGmE; ++e) {
-                const int64_t k = base + lane + 32 * e;
-                const double q = k < a.n ? __ldcs(vi + k) : 0.0;
-                ts = fma(q, wv[e], ts);
-                tl = fma(q, vv[e], tl);
+#pragma unroll 8
+            for (int e = lane; e < len; e += 32) {
+                const double q = __ldcs(vi + e);
+                ts = fma(q, wsh[e], ts);
+                tl = fma(q, vsh[e], tl);
             }
             ts = warp_sum(ts);
             tl = warp_sum(tl);
-            if (lane == 0) { my[i] += ts; my[ni + i] += tl; }
+            if (lane == 0) { acc[i] += ts; acc[ni + i] += tl; }   // vector i belongs to this warp
         }
     }
     __syncthreads();
-    // block totals in warp order, kept in warp 0's row
+    for (int i = grp + a.ngrp * warp; i < ni; i += a.ngrp * kGmWarps)
+        if (lane == 0) {
+            a.part[(int64_t)i * a.nslab + slab] = acc[i];
+            a.part[(int64_t)(ni + i) * a.nslab + slab] = acc[ni + i];
+        }
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&a.sc->ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int ld = a.m + 1;
+    // a thread per sum, slabs in order (independent loads in flight, no shuffle chain per sum)
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const double *pk = a.part + (int64_t)k * a.nslab;
         double t = 0;
-        for (int w = 0; w < kGmWarps; ++w) t += acc[(int64_t)w * 2 * (a.m + 1) + k];
-        acc[k] = t;   // row 0 is read only by this thread from here on
+        for (int b = 0; b < a.nslab; ++b) t += __ldcg(pk + b);
+        if (k < ni) a.red[k] = t;                                    // s
+        else if (k - ni < it) a.Gm[(int64_t)it * ld + (k - ni)] = t;   // Gram row of v_it
     }
     __syncthreads();
-    if (!gm_last_block(acc, K, a.part, a.red, &a.sc->ticket)) return;
-    // Gram row of v_it, then modified Gram-Schmidt's coefficients by forward substitution
-    // h_i = s_i - sum_{j<i} h_j G(i,j) (one warp: the dot of each row across the lanes)
-    const int ld = a.m + 1;
-    if (warp == 0) {
-        for (int j = lane; j < it; j += 32) a.Gm[(int64_t)it * ld + j] = a.red[ni + j];
-        __syncwarp();
-        for (int i = 0; i < ni; ++i) {
-            double t = 0;
-            for (int j = lane; j < i; j += 32) t = fma(a.h[j], a.Gm[(int64_t)i * ld + j], t);
-            t = warp_sum(t);
-            if (lane == 0) {
-                const double hi = a.red[i] - t;
-                a.h[i] = hi;
-                a.H[(int64_t)i * ld + it] = hi;
-            }
-            __syncwarp();
+    if (threadIdx.x == 0) a.sc->ticket = 0u;
+}
+
+// modified Gram-Schmidt's coefficients of this step to first order in the Gram entries:
+// h_i = s_i - sum_{j<i} G(i,j) s_j (a warp per row, rows over the whole grid)
+__global__ void __launch_bounds__(kGmThreads) gm_coef(GmArgs a) {
+    const int it = a.sc->it;
+    const int ni = it + 1, ld = a.m + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = blockIdx.x * kGmWarps + warp; i < ni; i += gridDim.x * kGmWarps) {
+        const double *gi = a.Gm + (int64_t)i * ld;
+        double t = 0;
+        for (int j = lane; j < i; j += 32) t = fma(__ldcg(gi + j), __ldcg(a.red + j), t);
+        t = warp_sum(t);
+        if (lane == 0) {
+            const double hi = __ldcg(a.red + i) - t;
+            a.h[i] = hi;
+            a.H[(int64_t)i * ld + it] = hi;
         }
     }
 }
@@ -227,12 +257,12 @@ __global__ void __launch_bounds__(kGmThreads) gm_dots(GmArgs a) {
 // v_{it+1} = w - sum_i h_i v_i (FreeFEM's order: i = 0..it), ||v_{it+1}||^2; last block: the
 // Hessenberg column's Givens rotations and FreeFEM's stopping tests
 __global__ void __launch_bounds__(kGmThreads) gm_update(GmArgs a) {
-    __shared__ double hs[1024];
+    __shared__ double hs[kGmHs], rc[kGmHs], rs[kGmHs];
     __shared__ double sh[kGmWarps + 1];
     const int it = a.sc->it;
     const int ni = it + 1;
     const double *hh = a.h;
-    const bool in_smem = ni <= 1024;
+    const bool in_smem = ni <= kGmHs;
     if (in_smem)
         for (int i = threadIdx.x; i < ni; i += blockDim.x) hs[i] = a.h[i];
     __syncthreads();
@@ -241,50 +271,86 @@ __global__ void __launch_bounds__(kGmThreads) gm_update(GmArgs a) {
     double s = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
         double t = a.w[k];
-        for (int i = 0; i < ni; ++i) t = fma(-hh[i], __ldcs(a.V + i * a.vs + k), t);
+        // FreeFEM's order i = 0..it; the loads of 8 vectors are issued before their products
+        int i = 0;
+        for (; i + 8 <= ni; i += 8) {
+            double q[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) q[u] = __ldcs(a.V + (i + u) * a.vs + k);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) t = fma(-hh[i + u], q[u], t);
+        }
+        for (; i < ni; ++i) t = fma(-hh[i], __ldcs(a.V + i * a.vs + k), t);
         vn[k] = t;
         s = fma(t, t, s);
     }
     const double tot = gm_block_sum(s, sh);
-    if (!gm_last_block(&tot, 1, a.part, a.red, &a.sc->ticket) || threadIdx.x != 0) return;
+    if (!gm_last_block(&tot, 1, a.part, a.red + 2 * (a.m + 1), &a.sc->ticket)) return;
     GmScal *c = a.sc;
     const int ld = a.m + 1;
     double *H = a.H;
-    const double aux = sqrt(a.red[0]);
-    a.vnorm[it + 1] = aux;
-    H[(int64_t)(it + 1) * ld + it] = aux;
-    for (int i = 0; i < it; i++) {
-        const double hi = H[(int64_t)i * ld + it], hi1 = H[(int64_t)(i + 1) * ld + it];
-        const double aa = a.rot0[i] * hi + a.rot1[i] * hi1;
-        const double bb = -a.rot1[i] * hi + a.rot0[i] * hi1;
-        H[(int64_t)i * ld + it] = aa;
-        H[(int64_t)(i + 1) * ld + it] = bb;
+    const double aux = sqrt(a.red[2 * (a.m + 1)]);
+    // the new column's rotations by the earlier ones: a chain through i, staged in shared memory
+    double *col = in_smem ? hs : nullptr;
+    if (in_smem) {
+        for (int i = threadIdx.x; i < it; i += blockDim.x) {
+            rc[i] = a.rot0[i];
+            rs[i] = a.rot1[i];
+        }
+        __syncthreads();
     }
-    const double hd = H[(int64_t)it * ld + it], hs1 = H[(int64_t)(it + 1) * ld + it];
-    const double sq = sqrt(hd * hd + hs1 * hs1);
-    a.rot0[it] = hd / sq;
-    a.rot1[it] = hs1 / sq;
-    H[(int64_t)it * ld + it] = a.rot0[it] * hd + a.rot1[it] * hs1;
-    H[(int64_t)(it + 1) * ld + it] = 0.;
-    a.g[it + 1] = -a.rot1[it] * a.g[it];
-    a.g[it] = a.rot0[it] * a.g[it];
-    const double relres = fabs(a.g[it + 1]);
-    c->relres = relres;
-    c->steps += 1;
-    c->itf = it;
-    bool stop = false;
-    if (relres / c->normb < fabs(c->eps)) {
-        c->conv = 1;
-        stop = true;
-    } else if (it > c->itmax) {
-        stop = true;                       // FreeFEM: `if (it > nbitermx) break;`
-    } else {
-        c->it = it + 1;                    // the loop increment it++, iter++
-        c->iter += 1;
-        if (it + 1 >= a.m) { stop = true; c->itf = a.m - 1; }
+    if (threadIdx.x == 0) {
+        a.vnorm[it + 1] = aux;
+        if (in_smem) {
+            double hi = col[0];
+            for (int i = 0; i < it; i++) {
+                const double hi1 = col[i + 1];
+                const double aa = rc[i] * hi + rs[i] * hi1;
+                const double bb = -rs[i] * hi + rc[i] * hi1;
+                col[i] = aa;
+                hi = bb;
+            }
+            col[it] = hi;
+        } else {
+            for (int i = 0; i < it; i++) {
+                const double hi = H[(int64_t)i * ld + it], hi1 = H[(int64_t)(i + 1) * ld + it];
+                const double aa = a.rot0[i] * hi + a.rot1[i] * hi1;
+                const double bb = -a.rot1[i] * hi + a.rot0[i] * hi1;
+                H[(int64_t)i * ld + it] = aa;
+                H[(int64_t)(i + 1) * ld + it] = bb;
+            }
+        }
+        const double hd = in_smem ? col[it] : H[(int64_t)it * ld + it], hs1 = aux;
+        const double sq = sqrt(hd * hd + hs1 * hs1);
+        a.rot0[it] = hd / sq;
+        a.rot1[it] = hs1 / sq;
+        const double top = a.rot0[it] * hd + a.rot1[it] * hs1;
+        if (in_smem) col[it] = top; else H[(int64_t)it * ld + it] = top;
+        H[(int64_t)(it + 1) * ld + it] = 0.;
+        a.g[it + 1] = -a.rot1[it] * a.g[it];
+        a.g[it] = a.rot0[it] * a.g[it];
+        const double relres = fabs(a.g[it + 1]);
+        c->relres = relres;
+        c->steps += 1;
+        c->itf = it;
+        bool stop = false;
+        if (relres / c->normb < fabs(c->eps)) {
+            c->conv = 1;
+            stop = true;
+        } else if (it > c->itmax) {
+            stop = true;                       // FreeFEM: `if (it > nbitermx) break;`
+        } else {
+            c->it = it + 1;                    // the loop increment it++, iter++
+            c->iter += 1;
+            if (it + 1 >= a.m) { stop = true; c->itf = a.m - 1; }
+        }
+        c->stop = stop;
+        if (stop && a.in_graph) gm_set_cond(a.cond, 0);
     }
-    c->stop = stop;
-    if (stop && a.in_graph) gm_set_cond(a.cond, 0);
+    if (in_smem) {
+        __syncthreads();
+        for (int i = threadIdx.x; i <= it; i += blockDim.x) H[(int64_t)i * ld + it] = col[i];
+    }
 }
 
 // y = H^-1 g on the it+1 leading rows (back substitution, one warp per row dot)
@@ -307,7 +373,15 @@ __global__ void __launch_bounds__(kGmThreads) gm_xupd(GmArgs a) {
     if (it < 0) return;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
         double t = 0;
-        for (int i = 0; i <= it; ++i) t = fma(a.y[i], __ldcs(a.Vp + i * a.vs + k), t);
+        int i = 0;
+        for (; i + 8 <= it + 1; i += 8) {
+            double q[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) q[u] = __ldcs(a.Vp + (i + u) * a.vs + k);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) t = fma(a.y[i + u], q[u], t);
+        }
+        for (; i <= it; ++i) t = fma(a.y[i], __ldcs(a.Vp + i * a.vs + k), t);
         a.x[k] = t + a.x[k];
     }
 }
@@ -319,11 +393,18 @@ __global__ void gm_x0_kernel(int n, double *x, const double *b, const uint8_t *w
 
 // grids: vector kernels resident and capped by the work; the dot kernel by tiles
 static int gm_vec_grid(int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(4 * kNumSM, (n + kGmThreads * 4 - 1) / (kGmThreads * 4)));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(4 * kNumSM, (n + kGmThreads - 1) / kGmThreads));
 }
-static int gm_dot_grid(int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(2 * kNumSM, (n + kGmWarps * kGmTile - 1) / (kGmWarps * kGmTile)));
+// gm_dots: sub-tiles of kGmSub elements grouped into at most kGmMaxSlabs slabs, and enough
+// vector groups for about two blocks per SM
+static void gm_dot_shape(int64_t n, int &nslab, int &ngrp, int64_t &slab_len) {
+    const int64_t nsub = std::max<int64_t>(1, (n + kGmSub - 1) / kGmSub);
+    const int64_t per = (nsub + kGmMaxSlabs - 1) / kGmMaxSlabs;
+    nslab = (int)((nsub + per - 1) / per);
+    slab_len = per * kGmSub;
+    ngrp = std::max(1, (2 * kNumSM + nslab - 1) / nslab);
 }
+static int gm_coef_grid(int m) { return std::max(1, std::min(kNumSM, (m + 1 + kGmWarps - 1) / kGmWarps)); }
 
 // one right-hand side; b, x device pointers of length n (x: initial guess, then solution)
 int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
@@ -331,18 +412,22 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
     const int n = A->n;
-    const int m = prm->dim_krylov > 0 ? prm->dim_krylov : 50;
+    // FreeFEM's default restart (Data_Sparse_Solver::NbSpace, VirtualSolver.hpp:79)
+    const int m = prm->dim_krylov > 0 ? prm->dim_krylov : 1000;
     const int itmax = prm->itmax > 0 ? prm->itmax : n;
     const double tgv = prm->tgv > 0 ? prm->tgv : 1e30;
-    const size_t dsmem = sizeof(double) * 2 * (size_t)(m + 1) * kGmWarps;
-    FFGPU_CHECK(dsmem <= 200 * 1024, FFGPU_EINVAL, "gmres: dim_krylov %d above the supported 1600", m);
+    const size_t dsmem = sizeof(double) * (2 * (size_t)kGmSub + 2 * (size_t)(m + 1));
+    FFGPU_CHECK(dsmem <= 200 * 1024, FFGPU_EINVAL, "gmres: dim_krylov %d above the supported 10000", m);
     const int64_t vs = vstride(n);
-    const int Gv = gm_vec_grid(n), Gd = gm_dot_grid(n);
+    int nslab = 1, ngrp = 1;
+    int64_t slab_len = kGmSub;
+    gm_dot_shape(n, nslab, ngrp, slab_len);
+    const int Gv = gm_vec_grid(n), Gd = nslab * ngrp, Gc = gm_coef_grid(m);
     // workspace: V (m+1 vectors), Vp (m), the SpMV input and output, the small arrays
     // H, rot0 rot1 g y vnorm, Gram, h, red, part, then the scalars (in doubles, rounded up)
     const size_t nscal = (sizeof(GmScal) + sizeof(double) - 1) / sizeof(double);
     const size_t small = (size_t)(m + 2) * (m + 1) + 5 * (size_t)(m + 2) + (size_t)(m + 1) * (m + 1) +
-                         (size_t)(m + 2) + (2 * (size_t)(m + 1) + 2) + 2 * (size_t)(m + 1) * std::max(Gv, Gd) +
+                         (size_t)(m + 2) + (2 * (size_t)(m + 1) + 2) + 2 * (size_t)(m + 1) * std::max(Gv, nslab) +
                          nscal;
     double *ws = nullptr;
     const size_t nvec = (size_t)(2 * m + 3);
@@ -350,6 +435,7 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
     GmArgs a;
     memset(&a, 0, sizeof(a));
     a.n = n; a.m = m; a.vs = vs;
+    a.nslab = nslab; a.ngrp = ngrp; a.slab_len = slab_len;
     a.V = ws; a.Vp = ws + (size_t)(m + 1) * vs; a.vpc = a.Vp + (size_t)m * vs; a.w = a.vpc + vs;
     double *sm = a.w + vs;
     a.H = sm; sm += (size_t)(m + 2) * (m + 1);
@@ -361,7 +447,7 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
     a.Gm = sm; sm += (size_t)(m + 1) * (m + 1);
     a.h = sm; sm += m + 2;
     a.red = sm; sm += 2 * (m + 1) + 2;
-    a.part = sm; sm += 2 * (size_t)(m + 1) * std::max(Gv, Gd);
+    a.part = sm; sm += 2 * (size_t)(m + 1) * std::max(Gv, nslab);
     a.sc = reinterpret_cast<GmScal *>(sm);
     sm += nscal;
     if ((size_t)(sm - ws) != nvec * vs + small) {
@@ -389,7 +475,7 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
     if (!rc) rc = spmv(A, a.vpc, a.w, trans, s);
     const bool host_loop = getenv("FFGPU_CG_GRAPH") && getenv("FFGPU_CG_GRAPH")[0] == '0';
     if (!rc && !host_loop) {
-        // graph of one restart cycle: [A x -> V0, residual, while(!stop){prep, SpMV, dots, update},
+        // graph of one restart cycle: [A x -> V0, residual, while(!stop){prep, SpMV, dots, coef, update},
         // back substitution, x update]
         cudaGraph_t graph = nullptr;
         cudaGraphConditionalHandle cond;
@@ -435,6 +521,7 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
             gm_prep<<<Gv, kGmThreads, 0, s>>>(ag);
             int r2 = spmv(A, a.vpc, a.w, trans, s);
             gm_dots<<<Gd, kGmThreads, dsmem, s>>>(ag);
+            gm_coef<<<Gc, kGmThreads, 0, s>>>(ag);
             gm_update<<<Gv, kGmThreads, 0, s>>>(ag);
             cudaError_t ec = cudaStreamEndCapture(s, &body);
             if (r2 || ec != cudaSuccess) e = ec != cudaSuccess ? ec : cudaErrorUnknown;
@@ -471,8 +558,9 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
                 gm_prep<<<Gv, kGmThreads, 0, s>>>(a);
                 if ((rc = spmv(A, a.vpc, a.w, trans, s))) break;
                 gm_dots<<<Gd, kGmThreads, dsmem, s>>>(a);
+                gm_coef<<<Gc, kGmThreads, 0, s>>>(a);
                 gm_update<<<Gv, kGmThreads, 0, s>>>(a);
-                ctx->launches += 3;
+                ctx->launches += 4;
             }
             if (rc) break;
             gm_back<<<1, 32, 0, s>>>(a);
@@ -489,7 +577,7 @@ int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgp
             break;
         }
         ++cycles;
-        if (!host_loop) ctx->launches += 4 + 4 * (hs.steps - steps_seen);
+        if (!host_loop) ctx->launches += 4 + 5 * (hs.steps - steps_seen);
         steps_seen = hs.steps;
         if (hs.conv) break;
         if (hs.iter > itmax) break;

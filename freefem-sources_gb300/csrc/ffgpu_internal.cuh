@@ -49,6 +49,7 @@ enum DevStatus : int {
     kDevBadDofLayout = 3,   // [P2]^3 DOF table not of the form 3*node+c
     kDevBadIndex = 4,       // index out of range in an input table
     kDevNotFound = 5,       // column missing from a row (pattern inconsistency)
+    kDevTimeout = 6,        // a bounded wait in a kernel ran out (tensor-core element kernel)
 };
 
 // Scalars of a running Krylov solve, kept in device memory so the iteration loop runs
@@ -134,6 +135,7 @@ struct ffgpu_matrix {
     int csr_lanes_x;      // lanes per block row of the double-float SpMV (tuned)
     int layout_pinned;    // the caller fixed the SpMV layout of the current solve
     int last_cluster;     // the last FP64 CG solve ran in one thread-block cluster
+    void *direct;         // sparse Cholesky state of the direct solver (ffgpu_direct.cu), or NULL
     // SELL-32 copy for the Krylov SpMVs: block rows sliced into chunks of 32 (one row per
     // lane), rows sorted by decreasing degree inside windows of 1024 rows, each chunk padded
     // to its longest row and stored slot-major so that a warp reads 32 consecutive entries.
@@ -313,6 +315,12 @@ int spmv(ffgpu_matrix *A, const double *x, double *y, int trans, cudaStream_t s)
 bool cluster_cg_fits(ffgpu_matrix *A, int trans);
 constexpr int kClusterRefused = 1;   // cluster_cg_run: the launch was refused, nothing ran
 int cluster_cg_run(ffgpu_matrix *A, int trans, double *x, const double *g, const double *h, cudaStream_t s);
+// the direct solver's factorisation: stale after a numeric change (the ordering and the
+// symbolic analysis stay), freed with the matrix (ffgpu_direct.cu)
+// P2 element matrices on the tensor cores (ffgpu_elemtc.cu): NULL *out when not applicable
+int elem_tc_prepare(ffgpu_space *S, const double *geo, double lam, double mu, const double *lame, double **out);
+void direct_invalidate(ffgpu_matrix *A);
+void direct_release(ffgpu_matrix *A);
 // solver=GMRES for one right-hand side (ffgpu_gmres.cu); b, x device pointers
 int gmres_one(ffgpu_matrix *A, const double *b, double *x, int trans, const ffgpu_solver_params *prm,
               ffgpu_solver_stats *st);

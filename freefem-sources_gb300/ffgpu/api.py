@@ -185,8 +185,12 @@ class VarForm:
             pass
         elif callable(self.kappa):
             self._stiff_at_points(v, Vh)
+        elif self.kappa is not None and np.ndim(self.kappa) == 0 and not hasattr(self.kappa, "data_ptr"):
+            v.c_stiff = float(v.c_stiff) * float(self.kappa)   # a constant kappa: part of c_stiff
         elif self.kappa is not None:
             k = self.kappa if hasattr(self.kappa, "data_ptr") else np.ascontiguousarray(self.kappa, np.float64)
+            if int(np.prod(np.shape(k))) != Vh.Th.nt:
+                raise ValueError(f"kappa: one value per element expected ({Vh.Th.nt}), got shape {np.shape(k)}")
             self._keep.append(k)
             v.kappa = _ptr(k).value
         v.f = None
@@ -421,7 +425,7 @@ class Matrix:
     """``matrix A = a(Vh,Vh, solver=..., eps=..., ...)`` with a device-resident pattern/values."""
 
     def __init__(self, h, space: DeviceSpace | None, solver="CG", eps=1e-6, itmax=0,
-                 dim_krylov=50, tgv=1e30, device=0):
+                 dim_krylov=1000, tgv=1e30, device=0):
         self.h = h
         self.space = space
         self.solver = solver
@@ -477,10 +481,16 @@ class Matrix:
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
         nrhs = int(np.prod(np.shape(b))) // self.n
         st = SolverStats()
+        if solver in ("CHOLESKY", "CHOLMOD", "SPARSESOLVER"):
+            # direct: the factorisation is kept for later solves of this numeric state (A' = A)
+            code = lib().ffgpu_solve_direct(self.h, _ptr(bb), _ptr(out), nrhs, C.byref(st))
+            self.stats = st
+            check(code)
+            return out
         p = self.params(eps, itmax, unroll, spmv_mode, spmv_layout)
         fn = lib().ffgpu_solve_cg if solver == "CG" else lib().ffgpu_solve_gmres
         if solver not in ("CG", "GMRES"):
-            raise ValueError(f"solver {solver!r}: the device path provides CG and GMRES")
+            raise ValueError(f"solver {solver!r}: the device path provides CG, GMRES and CHOLESKY")
         code = fn(self.h, _ptr(bb), _ptr(out), nrhs, int(trans), C.byref(p), C.byref(st))
         self.stats = st
         check(code)
@@ -570,7 +580,7 @@ class Matrix:
         return rhs_out
 
 
-def matrix(varf: VarForm, Vh, solver="CG", eps=1e-6, itmax=0, dim_krylov=50, rhs_out=None,
+def matrix(varf: VarForm, Vh, solver="CG", eps=1e-6, itmax=0, dim_krylov=1000, rhs_out=None,
            device=0) -> Matrix:
     """matrix A = a(Vh,Vh, solver=..., eps=...).  Vh: FESpace or DeviceSpace.  If rhs_out is
     given the linear form a(0,Vh) is assembled into it in the same device pass."""

@@ -12,10 +12,13 @@
 //                                             (src/femlib/VirtualSolverCG.hpp:113-192)
 //   GPUGMRES    right-preconditioned FGMRES -- as SolverGMRES (VirtualSolverCG.hpp:195-257)
 //   GPUCGMIXED  FP32 inner PCG + FP64 refinement, same stopping rule on the true residual
+//   GPUCHOLESKY sparse Cholesky on the device, factored once per numeric state (the role of
+//               FreeFEM's CHOLMOD / MUMPS plugins); symmetric positive definite matrices
 // The matrix FreeFEM assembled is uploaded once per numeric state (fac_numeric, in sorted CSR
 // via HashMatrix::CSR, HashMatrix.cpp:859-867) and stays on the device with the solver object,
 // which the matrix owns (VirtualMatrix.hpp:71-94).  Errors become ExecError / ffassert as in
 // FreeFEM's own solvers; there is no CPU fallback.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -65,7 +68,40 @@ ffgpu_ctx *context() {
     return g_ctx;
 }
 
-enum Kind { kCG = 0, kGMRES = 1, kMixed = 2 };
+enum Kind { kCG = 0, kGMRES = 1, kMixed = 2, kCholesky = 3 };
+
+// FreeFEM's matrix in full sorted CSR: A.CSR (HashMatrix.cpp:859-867), the other triangle added
+// when FreeFEM stores half of a symmetric matrix (HashMatrix::half)
+static void full_csr(HashMatrix<int, double> &A, std::vector<int32_t> &rp, std::vector<int32_t> &col,
+                     std::vector<double> &val) {
+    int *IA = nullptr, *JA = nullptr;
+    double *AA = nullptr;
+    A.CSR(IA, JA, AA);
+    const int n = A.n;
+    if (!A.half) {
+        rp.assign(IA, IA + n + 1);
+        col.assign(JA, JA + IA[n]);
+        val.assign(AA, AA + IA[n]);
+        return;
+    }
+    std::vector<std::vector<std::pair<int, double> > > rows(n);
+    for (int i = 0; i < n; ++i)
+        for (int k = IA[i]; k < IA[i + 1]; ++k) {
+            rows[i].push_back(std::make_pair(JA[k], AA[k]));
+            if (JA[k] != i) rows[JA[k]].push_back(std::make_pair(i, AA[k]));
+        }
+    rp.assign(n + 1, 0);
+    col.clear();
+    val.clear();
+    for (int i = 0; i < n; ++i) {
+        std::sort(rows[i].begin(), rows[i].end());
+        for (size_t k = 0; k < rows[i].size(); ++k) {
+            col.push_back(rows[i][k].first);
+            val.push_back(rows[i][k].second);
+        }
+        rp[i + 1] = (int32_t)col.size();
+    }
+}
 
 template <int KIND>
 class SolverGpu : public VirtualSolver<int, double> {
@@ -110,17 +146,25 @@ class SolverGpu : public VirtualSolver<int, double> {
         if (M && adopted) {
             adopted = false;   // later factorisations follow FreeFEM's matrix
             if (verb > 1) std::cout << "  ffgpu: solver uses the device-assembled matrix" << std::endl;
+            factor();
             return;
         }
-        int *IA = nullptr, *JA = nullptr;
-        double *AA = nullptr;
-        A.CSR(IA, JA, AA);
+        std::vector<int32_t> rp, col;
+        std::vector<double> val;
+        full_csr(A, rp, col, val);
         if (M) {
             ffgpu_matrix_destroy(M);
             M = nullptr;
         }
-        int r = ffgpu_matrix_from_csr(context(), A.n, (int64_t)A.nnz, IA, JA, AA, &M);
+        int r = ffgpu_matrix_from_csr(context(), A.n, (int64_t)col.size(), rp.data(), col.data(), val.data(), &M);
         if (r != FFGPU_OK) ExecError((std::string("ffgpu upload: ") + ffgpu_last_error()).c_str());
+        factor();
+    }
+    // the direct solver factors here, once per numeric state (VirtualSolver::factorize)
+    void factor() {
+        if (KIND != kCholesky) return;
+        const int r = ffgpu_direct_factor(M);
+        if (r != FFGPU_OK) ExecError((std::string("ffgpu Cholesky: ") + ffgpu_last_error()).c_str());
     }
     void dosolver(double *x, double *b, int N, int trans) {
         ffgpu_solver_stats st;
@@ -130,6 +174,8 @@ class SolverGpu : public VirtualSolver<int, double> {
             r = FFGPU_OK;
             for (int k = 0; k < N && r == FFGPU_OK; ++k)
                 r = ffgpu_solve_ir(M, b + (size_t)k * A.n, x + (size_t)k * A.n, &p, &st);
+        } else if (KIND == kCholesky) {
+            r = ffgpu_solve_direct(M, b, x, N, &st);   // A' = A
         } else {
             ffgpu_solver_params p = {eps, (int)itmax, (int)restart, tgv, (int)verb, 8};
             r = KIND == kCG ? ffgpu_solve_cg(M, b, x, N, trans, &p, &st)
@@ -149,6 +195,7 @@ class SolverGpu : public VirtualSolver<int, double> {
 template <> const int SolverGpu<kCG>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 template <> const int SolverGpu<kGMRES>::orTypeSol = 1 | 2 | 4 | 8 | 16 | 32;
 template <> const int SolverGpu<kMixed>::orTypeSol = 1 | 2 | 4 | 8 | 32;
+template <> const int SolverGpu<kCholesky>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 
 // ------------------------------------------------------------------ device assembly
 // `matrix A = a(Vh, Vh, ...)` is routed here (an OpMatrixtoBilinearForm with a higher
@@ -792,6 +839,7 @@ static void hand_over(VirtualMatrix<int, double> &VA, ffgpu_matrix *M) {
     if (SolverGpu<kCG> *s = dynamic_cast<SolverGpu<kCG> *>(vs)) return s->adopt(M);
     if (SolverGpu<kGMRES> *s = dynamic_cast<SolverGpu<kGMRES> *>(vs)) return s->adopt(M);
     if (SolverGpu<kMixed> *s = dynamic_cast<SolverGpu<kMixed> *>(vs)) return s->adopt(M);
+    if (SolverGpu<kCholesky> *s = dynamic_cast<SolverGpu<kCholesky> *>(vs)) return s->adopt(M);
     ffgpu_matrix_destroy(M);
 }
 
@@ -1103,11 +1151,13 @@ static void Load_Init() {
     addsolver<SolverGpu<kCG> >("GPUCG", 20);
     addsolver<SolverGpu<kGMRES> >("GPUGMRES", 20);
     addsolver<SolverGpu<kMixed> >("GPUCGMIXED", 20);
+    addsolver<SolverGpu<kCholesky> >("GPUCHOLESKY", 20);
     // script constants, as lgfem.cpp:6380-6395 declares CG, GMRES, ...: solver=GPUCG
-    static std::string gpucg = "GPUCG", gpugmres = "GPUGMRES", gpumixed = "GPUCGMIXED";
+    static std::string gpucg = "GPUCG", gpugmres = "GPUGMRES", gpumixed = "GPUCGMIXED", gpuchol = "GPUCHOLESKY";
     Global.New("GPUCG", CConstant<std::string *>(&gpucg));
     Global.New("GPUGMRES", CConstant<std::string *>(&gpugmres));
     Global.New("GPUCGMIXED", CConstant<std::string *>(&gpumixed));
+    Global.New("GPUCHOLESKY", CConstant<std::string *>(&gpuchol));
     // `ffgpustrict = 1;` in a script: forms the device does not assemble are errors
     Global.New("ffgpustrict", CPValue<long>(g_strict));
     // device assembly behind `matrix A = a(Vh,Vh)` (lgfem.cpp:6669-6673, :6823-6826)
@@ -1119,7 +1169,7 @@ static void Load_Init() {
                       new GpuLinear<Mesh3, v_fes3>(atype<KN_<double> >(), false, false));
     TheOperators->Add("<-", new GpuLinear<Mesh, v_fes>(atype<KN<double> *>(), true, true),
                       new GpuLinear<Mesh3, v_fes3>(atype<KN<double> *>(), true, true));
-    if (verbosity > 1) std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED)" << std::endl;
+    if (verbosity > 1) std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED, GPUCHOLESKY)" << std::endl;
 }
 
 LOADFUNC(Load_Init)

@@ -188,7 +188,8 @@ typedef struct {
 
 /* Krylov parameters, named as in FreeFEM's Data_Sparse_Solver (VirtualSolver.hpp:30-96).
  * eps > 0 relative, eps < 0 absolute (CG.cpp:226); itmax <= 0 means n (VirtualSolverCG.hpp:135);
- * dim_krylov is GMRES's restart (NbSpace).  unroll: CG iterations per CUDA-graph body (>=1).
+ * dim_krylov is GMRES's restart (NbSpace; <= 0: FreeFEM's default, 1000).  unroll: CG iterations
+ * per CUDA-graph body (>=1).
  * spmv_mode (CG): 0 = SpMV in FP64 arithmetic; 1 = FP64 values and vectors with the products
  * formed exactly on the FP32 pipe and summed as double-float (about 2^-44 relative), every
  * other CG operation in FP64.
@@ -325,7 +326,8 @@ int ffgpu_matrix_info(const ffgpu_matrix *A, int *n, int64_t *nnz, int *block_si
  * {1,..,32} for block CSR with T lanes per block row; 0 before the first solve.  mode 3: 1 when the SELL copy stores 16-bit column differences;
  * mode 4: block entries the SELL copy stores, padding included (32 per slot; -1 past INT32_MAX).
  * mode 5: 1 when the last FP64 CG solve ran its whole iteration loop in one thread-block
- * cluster (small scalar systems, up to 16 x 8192 rows; a fixed layout selects the regular path).
+ * cluster (opt-in with FFGPU_CLUSTER_CG=1: scalar systems of up to 8 x 9216 rows; a fixed
+ * layout selects the regular path).
  * No FreeFEM counterpart. */
 int ffgpu_matrix_spmv_layout(const ffgpu_matrix *A, int mode);
 /* Average device time in ms of `nrep` back-to-back launches of the solver's SpMV kernel (K_a,
@@ -351,6 +353,20 @@ int ffgpu_solve_cg(ffgpu_matrix *A, const double *b, double *x, int nrhs, int tr
  * CG.cpp:348-517): right Jacobi preconditioning, modified Gram-Schmidt, Givens rotations. */
 int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
                       const ffgpu_solver_params *prm, ffgpu_solver_stats *stats);
+
+/* ------------------------------------------------------------------ direct solver
+ * Sparse Cholesky on the device for a symmetric positive definite matrix (tgv > 0 and
+ * tgv = -2 rows keep it so): the direct solver behind addsolver, in the role FreeFEM's
+ * CHOLMOD / MUMPS plugins play (VirtualSolverSparseSuite.hpp:305, plugin/seq/MUMPS_seq.cpp:
+ * 260-300), driven as FreeFEM drives them (VirtualSolver::factorize: symbolic once per pattern,
+ * numeric once per numeric state, then the solves, VirtualSolver.hpp:226-239).
+ * ffgpu_direct_factor: fill-reducing ordering (nested dissection; approximate minimum degree as
+ * the fallback), symbolic analysis, numeric factorisation (cuSOLVER's sparse Cholesky); a
+ * reassembly keeps the ordering and analysis and refactors at the next solve.  FFGPU_EINVAL
+ * for a nonsymmetric or not positive definite matrix, or when cuSOLVER is not installed.
+ * ffgpu_solve_direct: x = A^-1 b for nrhs right-hand sides (A' = A), factoring first if needed. */
+int ffgpu_direct_factor(ffgpu_matrix *A);
+int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ffgpu_solver_stats *stats);
 
 /* ------------------------------------------------------------------ mixed precision
  * FP32 inner Jacobi-PCG (FP32 values, vectors, SpMV and dot products) inside an FP64

@@ -88,6 +88,18 @@ def test_varf_carries_every_function_at_one_rule():
     assert not v.kappa and v.c_mass == 0.0
 
 
+def test_constant_kappa_and_kappa_shape():
+    """A constant kappa is part of c_stiff (no per-element array crosses); a P0 array must
+    have one value per element (host only)."""
+    Vh = FESpace(mesh.square(3), "P1")
+    v = ffgpu.varf_diffusion(kappa=2.5, c_stiff=2.0).c_varf(Vh)
+    assert not v.kappa and v.c_stiff == 5.0
+    v = ffgpu.varf_diffusion(kappa=np.full(Vh.Th.nt, 2.5)).c_varf(Vh)
+    assert v.kappa and v.c_stiff == 1.0
+    with pytest.raises(ValueError):
+        ffgpu.varf_diffusion(kappa=np.ones(5)).c_varf(Vh)
+
+
 def _materials():
     d, sc = load("p2elmat_2x2x1")
     Th = mesh.Mesh(3, d["coords"], d["elems"], d["belems"], d["blabel"], d["vlabel"])

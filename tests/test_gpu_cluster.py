@@ -1,7 +1,8 @@
 """The CG loop of small scalar systems in one thread-block cluster (ffgpu_cluster.cu).
 
-Systems of up to 8 x 9216 rows take this path by default (a rule on the sizes, not on
-timings).  Same bars as the other CG tests: solution within 1e-9 of the oracle (FreeFEM's
+The path is opt-in (FFGPU_CLUSTER_CG=1: on GB300 the FP64 work of an iteration needs more SMs
+than one cluster has, so the three-kernel graph is faster); with it, systems of up to
+8 x 9216 rows take it (a rule on the sizes, not on timings).  Same bars as the other CG tests: solution within 1e-9 of the oracle (FreeFEM's
 ConjugueGradient restated), iteration counts within 2; against the regular three-kernel
 path (a fixed SpMV layout selects it) the rows sum in the same order, so only the dot
 products' order differs: solutions within 1e-12, iterations within 1.
@@ -26,7 +27,9 @@ def _lib_built():
     import torch
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
     ffgpu.context(0)
+    os.environ["FFGPU_CLUSTER_CG"] = "1"
     yield
+    del os.environ["FFGPU_CLUSTER_CG"]
 
 
 def _problem(Th, kind="P1", seed=1):
@@ -95,6 +98,6 @@ def test_cluster_cg_can_be_switched_off():
         A.solve(b)
         u2, l2 = _solve_counting(A, b)
     finally:
-        del os.environ["FFGPU_CLUSTER_CG"]
+        os.environ["FFGPU_CLUSTER_CG"] = "1"
     assert l1 < 8 < l2
     assert np.linalg.norm(u1 - u2) <= 1e-12 * np.linalg.norm(u2)

@@ -1,0 +1,88 @@
+"""The direct solver (sparse Cholesky on the device, ffgpu_solve_direct) against the oracle.
+
+FreeFEM's direct solvers (UMFPACK, CHOLMOD) are not in this image, so the reference is the
+oracle's CG driven to eps = 1e-14, whose solution is exact to ~1e-12 on these systems, and
+numpy's dense solve on small ones.  Bars: solution within 1e-9 relative (the benchmark spec's
+solution bar); one factorisation serves every right-hand side; a reassembly refactors; a
+nonsymmetric matrix (tgv = -1 rows) is refused.
+"""
+import numpy as np
+import pytest
+
+import ffgpu
+import ffo
+from ffgpu import mesh
+from ffgpu.fespace import FESpace
+
+pytestmark = pytest.mark.gpu
+
+SOL_TOL = 1e-9
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_built():
+    from ffgpu.build import build
+    build()
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    ffgpu.context(0)
+    yield
+
+
+@pytest.mark.parametrize("case", ["square64_p1", "square24_p2", "cube8_p1", "cube3_el"])
+def test_cholesky_against_oracle(case):
+    rng = np.random.Generator(np.random.PCG64(7))
+    if case == "cube3_el":
+        Th = mesh.cube(3)
+        Vh = FESpace(Th, "P2vec")
+        a = ffgpu.varf_elasticity(f=(0.0, 0.0, -1.0), on=(4,))
+        Ao = ffo.assemble(Th, Vh, form="elasticity")
+        bo = ffo.rhs(Th, Vh, f=(0.0, 0.0, -1.0))
+        on = Vh.on((4,))
+    else:
+        Th = {"square64_p1": mesh.square(64), "square24_p2": mesh.square(24), "cube8_p1": mesh.cube(8)}[case]
+        kind = "P2" if case.endswith("p2") else "P1"
+        Vh = FESpace(Th, kind)
+        kappa = np.exp(rng.standard_normal(Th.nt))
+        labels = (1, 2, 3, 4) if Th.dim == 2 else (1, 2, 3, 4, 5, 6)
+        a = ffgpu.varf_diffusion(kappa=kappa, f=1.0, on=labels)
+        Ao = ffo.assemble(Th, Vh, kappa=kappa)
+        bo = ffo.rhs(Th, Vh, f=1.0)
+        on = Vh.on(labels)
+    ffo.setbc(Ao, bo, on)
+    uo, _, _, _ = ffo.cg(Ao, bo, eps=1e-14)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver="CHOLESKY", rhs_out=b)
+    u = A.solve(b)
+    assert A.stats.converged
+    assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
+    # several right-hand sides on the one factorisation, against numpy where small
+    B = rng.standard_normal((3, Vh.ndof))
+    X = A.solve(B.ravel()).reshape(3, -1)
+    if Vh.ndof <= 3000:
+        rp, cl, v = A.csr()
+        M = np.zeros((Vh.ndof, Vh.ndof))
+        M[np.repeat(np.arange(Vh.ndof), np.diff(rp)), cl] = v
+        R = np.linalg.solve(M, B.T).T
+        for k in range(3):
+            assert np.linalg.norm(X[k] - R[k]) <= SOL_TOL * np.linalg.norm(R[k])
+    for k in range(3):
+        ok, _, _, _ = ffo.cg(Ao, B[k], eps=1e-14)
+        assert np.linalg.norm(X[k] - ok) <= SOL_TOL * np.linalg.norm(ok)
+
+
+def test_cholesky_refactors_after_reassembly_and_refuses_nonsymmetric():
+    Th = mesh.square(20)
+    Vh = FESpace(Th, "P1")
+    k1 = np.ones(Th.nt)
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(ffgpu.varf_diffusion(kappa=k1, f=1.0, on=(1, 2, 3, 4)), Vh, solver="CHOLESKY", rhs_out=b)
+    u1 = A.solve(b)
+    A.reassemble(ffgpu.varf_diffusion(kappa=2.0 * k1, f=1.0, on=(1, 2, 3, 4)), rhs_out=b)
+    u2 = A.solve(b)
+    assert np.linalg.norm(u2 - 0.5 * u1) <= 1e-12 * np.linalg.norm(u1)
+    # tgv = -1: the Dirichlet rows become unit rows, the columns stay: not symmetric
+    N = ffgpu.matrix(ffgpu.varf_diffusion(f=1.0, on=(1, 2, 3, 4), tgv=-1.0), Vh, solver="CHOLESKY", rhs_out=b)
+    with pytest.raises(ffgpu.FFGPUError) as ei:
+        N.solve(b)
+    assert ei.value.code == -1 and b"symmetric" in ffgpu.lib().ffgpu_last_error()

@@ -5,7 +5,9 @@ restarts, FreeFEM's stopping tests) and reproduces FreeFEM's GMRES fixture bit f
 device forms the same Gram-Schmidt coefficients through one reduction per Arnoldi step
 (low-synchronisation MGS), so its residual estimates differ from the oracle's by rounding:
 solutions agree within 1e-9 relative, iteration counts within max(2, 1 %) (5 % for a restart
-length below 10, whose many restart cycles carry the rounding differences forward).
+length below 10, whose many restart cycles carry the rounding differences forward).  The
+coefficients are the first-order form of that recurrence (h = s - L s, L the strictly lower
+Gram triangle), which differs from modified Gram-Schmidt by O(|L|^2) terms below rounding.
 """
 import os
 
@@ -49,7 +51,10 @@ def _close(it, ito, frac=0.01):
 
 @pytest.mark.parametrize("m", [5, 30, 50, 80])
 def test_gmres_restarts_against_oracle(m):
-    Th, Vh, a, Ao, bo = _diffusion(40)
+    # square(40) with a restart of 5 is chaotic in the last bits: the oracle itself takes 946
+    # iterations compiled without fused multiply-adds and 1038 with them; square(24) is not
+    # (360 / 357), so the short restart runs there
+    Th, Vh, a, Ao, bo = _diffusion(24 if m < 10 else 40)
     uo, ito, conv, rr = ffo.fgmres(Ao, bo, eps=1e-12, restart=m)
     assert conv
     b = np.empty(Vh.ndof)
@@ -59,7 +64,7 @@ def test_gmres_restarts_against_oracle(m):
     assert A.stats.converged
     assert A.stats.residual < 1e-12
     assert np.linalg.norm(u - uo) <= SOL_TOL * np.linalg.norm(uo)
-    # a short restart (m = 5: 170 restart cycles here) carries rounding differences of the
+    # a short restart (m = 5: 72 restart cycles here) carries rounding differences of the
     # Gram-Schmidt coefficients from cycle to cycle: 5 % there, 1 % otherwise
     assert _close(A.stats.iterations, ito, 0.05 if m < 10 else 0.01), (A.stats.iterations, ito)
 
