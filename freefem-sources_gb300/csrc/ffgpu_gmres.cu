@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kGmThreads) gm_prep(GmArgs a) {
 // runs its vectors over the sub-tile (64 elements per lane, then one warp reduction per sum).
 // Partials part[k * nslab + slab], k < 2(it+1); the last block sums them in slab order.
 __global__ void __launch_bounds__(kGmThreads) gm_dots(GmArgs a) {
-    extern __shared__ double smd[];
+    extern __shared__ __align__(16) double smd[];
     double *wsh = smd, *vsh = smd + kGmSub, *acc = smd + 2 * kGmSub;
     const int it = a.sc->it;
     const int ni = it + 1, K = 2 * ni;
@@ -195,14 +195,24 @@ __global__ void __launch_bounds__(kGmThreads) gm_dots(GmArgs a) {
             vsh[e] = vit[t0 + e];
         }
         __syncthreads();
+        const int len2 = len & ~1;   // pairs of elements as 16-byte loads; an odd last element apart
         for (int i = grp + a.ngrp * warp; i < ni; i += a.ngrp * kGmWarps) {
-            const double *vi = a.V + i * a.vs + t0;
+            const double *vi = a.V + i * a.vs + t0;   // 16-byte aligned: vs and t0 are even
             double ts = 0, tl = 0;
 #pragma unroll 8
-            for (int e = lane; e < len; e += 32) {
-                const double q = __ldcs(vi + e);
-                ts = fma(q, wsh[e], ts);
-                tl = fma(q, vsh[e], tl);
+            for (int e = 2 * lane; e < len2; e += 64) {
+                const double2 q = __ldcs(reinterpret_cast<const double2 *>(vi + e));
+                const double2 w2 = *reinterpret_cast<const double2 *>(wsh + e);
+                const double2 v2 = *reinterpret_cast<const double2 *>(vsh + e);
+                ts = fma(q.x, w2.x, ts);
+                tl = fma(q.x, v2.x, tl);
+                ts = fma(q.y, w2.y, ts);
+                tl = fma(q.y, v2.y, tl);
+            }
+            if (len2 < len && lane == 0) {
+                const double q = __ldcs(vi + len2);
+                ts = fma(q, wsh[len2], ts);
+                tl = fma(q, vsh[len2], tl);
             }
             ts = warp_sum(ts);
             tl = warp_sum(tl);
@@ -271,14 +281,14 @@ __global__ void __launch_bounds__(kGmThreads) gm_update(GmArgs a) {
     double s = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
         double t = a.w[k];
-        // FreeFEM's order i = 0..it; the loads of 8 vectors are issued before their products
+        // FreeFEM's order i = 0..it; the loads of 16 vectors are issued before their products
         int i = 0;
-        for (; i + 8 <= ni; i += 8) {
-            double q[8];
+        for (; i + 16 <= ni; i += 16) {
+            double q[16];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) q[u] = __ldcs(a.V + (i + u) * a.vs + k);
+            for (int u = 0; u < 16; ++u) q[u] = __ldcs(a.V + (i + u) * a.vs + k);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) t = fma(-hh[i + u], q[u], t);
+            for (int u = 0; u < 16; ++u) t = fma(-hh[i + u], q[u], t);
         }
         for (; i < ni; ++i) t = fma(-hh[i], __ldcs(a.V + i * a.vs + k), t);
         vn[k] = t;
@@ -374,12 +384,12 @@ __global__ void __launch_bounds__(kGmThreads) gm_xupd(GmArgs a) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
         double t = 0;
         int i = 0;
-        for (; i + 8 <= it + 1; i += 8) {
-            double q[8];
+        for (; i + 16 <= it + 1; i += 16) {
+            double q[16];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) q[u] = __ldcs(a.Vp + (i + u) * a.vs + k);
+            for (int u = 0; u < 16; ++u) q[u] = __ldcs(a.Vp + (i + u) * a.vs + k);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) t = fma(a.y[i + u], q[u], t);
+            for (int u = 0; u < 16; ++u) t = fma(a.y[i + u], q[u], t);
         }
         for (; i <= it; ++i) t = fma(a.y[i], __ldcs(a.Vp + i * a.vs + k), t);
         a.x[k] = t + a.x[k];
