@@ -801,10 +801,12 @@ def run_adjoint(args, cfgname, steps, warmup, rank, world, cpu=True):
     hf, hg = [], []
     for k in range(1 + max(1, steps // 3)):
         torch.cuda.synchronize()
+        H.iterations_state = 0
         t0 = time.perf_counter()
         H.forward(kappa, 1.0, keep_checkpoints=False)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
+        heat_fwd_its = H.iterations_state
         H.value_and_grad(kappa, 1.0, h_obs)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
@@ -840,7 +842,10 @@ def run_adjoint(args, cfgname, steps, warmup, rank, world, cpu=True):
                                "checkpoint": cfg["heat_checkpoint"], "forward_ms": statistics.median(hf),
                                "gradient_ms": statistics.median(hg),
                                "gradient_over_forward": statistics.median(hg) / statistics.median(hf),
-                               "solves_gradient": H.solves},
+                               "solves_gradient": H.solves,
+                               "cg_iterations_forward": heat_fwd_its,
+                               "cg_iterations_gradient_state_solves": H.iterations_state,
+                               "cg_iterations_gradient_adjoint_solves": H.iterations_adjoint},
                       "l2": "working set below L2: L2 flushed (256 MB written) before every timed step"},
            "e2e": {"value": world * Vh.ndof / (t_e2e * 1e-3), "unit": UNIT,
                    "h2d_bytes_per_step": int(2 * Th.nt * 8 + Vh.ndof * 8),

@@ -1,6 +1,7 @@
-// ffgpu_direct.cu -- a sparse direct solver on the device behind addsolver: Cholesky
-// factorisation of a symmetric positive definite matrix (tgv rows included), factored once per
-// numeric state and reused by every solve, as FreeFEM's direct solvers are driven
+// ffgpu_direct.cu -- sparse direct solvers on the device behind addsolver: Cholesky
+// factorisation of a symmetric positive definite matrix (tgv rows included) and QR of any
+// nonsingular one (the UMFPACK role), factored once per numeric state and reused by every
+// solve, as FreeFEM's direct solvers are driven
 // (VirtualSolver::factorize: fac_symbolic / fac_numeric, then dosolver, VirtualSolver.hpp:226-239;
 // the CHOLMOD / MUMPS plugins, VirtualSolverSparseSuite.hpp:305, plugin/seq/MUMPS_seq.cpp:260-300).
 //
@@ -8,8 +9,12 @@
 //     (nested dissection, METIS through cuSOLVER; approximate minimum degree if that fails),
 //     P A P' built on the host, cuSOLVER's symbolic Cholesky analysis on the device;
 //   numeric (once per numeric state): the permuted values gathered on the device, the numeric
-//     factorisation, a zero-pivot check (not positive definite: an error, as CHOLMOD reports);
-//   solve: b permuted on the device, the two triangular solves, x unpermuted.
+//     factorisation, a zero-pivot check (not positive definite / singular: an error, as CHOLMOD
+//     and UMFPACK report);
+//   solve: b permuted on the device, the two triangular solves (QR: Q' b, then R), x unpermuted.
+// QR is not invariant under row scaling: a tgv row (1e30 on its diagonal) would dominate the
+// Householder reflections, so every row of P A P' is divided by its largest magnitude first
+// (D P A P', with D P b on the right-hand side).
 // The factorisation itself is cuSOLVER's (a library routine, like a GEMM from cuBLAS); the
 // ordering, permutation and the plumbing around it are this file's.  cuSOLVER's sparse routines
 // are opened when the direct solver is first used: a machine without them still loads
@@ -46,6 +51,16 @@ struct SolverLib {
     decltype(&cusolverSpDcsrcholFactor) Factor;
     decltype(&cusolverSpDcsrcholZeroPivot) ZeroPivot;
     decltype(&cusolverSpDcsrcholSolve) Solve;
+    // sparse QR (the nonsymmetric case); optional: without it only Cholesky is offered
+    bool qr_ok = false;
+    decltype(&cusolverSpCreateCsrqrInfo) QrCreateInfo;
+    decltype(&cusolverSpDestroyCsrqrInfo) QrDestroyInfo;
+    decltype(&cusolverSpXcsrqrAnalysis) QrAnalysis;
+    decltype(&cusolverSpDcsrqrBufferInfo) QrBufferInfo;
+    decltype(&cusolverSpDcsrqrSetup) QrSetup;
+    decltype(&cusolverSpDcsrqrFactor) QrFactor;
+    decltype(&cusolverSpDcsrqrZeroPivot) QrZeroPivot;
+    decltype(&cusolverSpDcsrqrSolve) QrSolve;
     decltype(&cusparseCreateMatDescr) CreateDescr;
     decltype(&cusparseDestroyMatDescr) DestroyDescr;
     decltype(&cusparseSetMatType) SetType;
@@ -89,14 +104,29 @@ static const SolverLib &solver_lib() {
         get(hp, "cusparseSetMatType", L.SetType);
         get(hp, "cusparseSetMatIndexBase", L.SetBase);
         L.ok = ok;
+        const std::string why = L.why;
+        get(hs, "cusolverSpCreateCsrqrInfo", L.QrCreateInfo);
+        get(hs, "cusolverSpDestroyCsrqrInfo", L.QrDestroyInfo);
+        get(hs, "cusolverSpXcsrqrAnalysis", L.QrAnalysis);
+        get(hs, "cusolverSpDcsrqrBufferInfo", L.QrBufferInfo);
+        get(hs, "cusolverSpDcsrqrSetup", L.QrSetup);
+        get(hs, "cusolverSpDcsrqrFactor", L.QrFactor);
+        get(hs, "cusolverSpDcsrqrZeroPivot", L.QrZeroPivot);
+        get(hs, "cusolverSpDcsrqrSolve", L.QrSolve);
+        L.qr_ok = L.ok && ok;
+        if (L.ok) L.why = L.qr_ok ? why : "sparse QR symbols missing: " + L.why;
     });
     return L;
 }
 
 struct DirectState {
+    int method = FFGPU_DIRECT_CHOLESKY;      // the factorisation in use (Cholesky or QR)
     cusolverSpHandle_t h = nullptr;
     cusparseMatDescr_t descr = nullptr;
     csrcholInfo_t info = nullptr;
+    csrqrInfo_t qinfo = nullptr;
+    double *rscale = nullptr;                // QR: 1 / largest magnitude of each row of P A P' (device)
+    bool qr_factored = false;                // qinfo holds a factorisation (a refactor re-analyses)
     int n = 0;
     int64_t nnz = 0;
     int32_t *rp = nullptr, *col = nullptr;   // P A P' pattern (device)
@@ -149,6 +179,22 @@ __global__ void symmetry_kernel(int nb, int bs, const int32_t *__restrict__ brow
     }
 }
 
+// QR's row equilibration: rs[k] = 1 / max_j |a_kj| of the permuted matrix, then a_kj *= rs[k]
+__global__ void row_scale_kernel(int n, const int32_t *__restrict__ rp, double *__restrict__ val,
+                                 double *__restrict__ rs) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double m = 0.0;
+    for (int j = rp[k]; j < rp[k + 1]; ++j) m = fmax(m, fabs(val[j]));
+    const double r = m > 0.0 ? 1.0 / m : 1.0;
+    rs[k] = r;
+    for (int j = rp[k]; j < rp[k + 1]; ++j) val[j] *= r;
+}
+__global__ void scale_kernel(int64_t n, const double *__restrict__ rs, double *__restrict__ v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] *= rs[i];
+}
+
 static int grid_of(int64_t n) { return (int)((n + 255) / 256); }
 
 void direct_invalidate(ffgpu_matrix *A) {
@@ -162,10 +208,12 @@ void direct_release(ffgpu_matrix *A) {
     ffgpu_ctx *ctx = A->ctx;
     cudaStreamSynchronize(ctx->stream);
     if (d->info) L.DestroyInfo(d->info);
+    if (d->qinfo) L.QrDestroyInfo(d->qinfo);
     if (d->descr) L.DestroyDescr(d->descr);
     if (d->h) L.Destroy(d->h);
     dfree(ctx, d->rp); dfree(ctx, d->col); dfree(ctx, d->src); dfree(ctx, d->perm);
     dfree(ctx, d->val); dfree(ctx, d->exported); dfree(ctx, d->t1); dfree(ctx, d->t2);
+    dfree(ctx, d->rscale);
     if (d->buf) cudaFree(d->buf);
     delete d;
     A->direct = nullptr;
@@ -224,6 +272,12 @@ static int direct_symbolic(ffgpu_matrix *A, DirectState *d) {
     FFGPU_CUDA(cudaMemcpyAsync(d->src, src.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s));
     FFGPU_CUDA(cudaMemcpyAsync(d->perm, p.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
     FFGPU_CUDA(cudaStreamSynchronize(s));   // the host vectors die here
+    if (d->method == FFGPU_DIRECT_QR) {
+        FFGPU_CUDA(dalloc(ctx, (void **)&d->rscale, sizeof(double) * n));
+        FFGPU_SOLVER(L.QrCreateInfo(&d->qinfo));
+        FFGPU_SOLVER(L.QrAnalysis(d->h, n, n, (int)nnz, d->descr, d->rp, d->col, d->qinfo));
+        return FFGPU_OK;
+    }
     FFGPU_SOLVER(L.CreateInfo(&d->info));
     FFGPU_SOLVER(L.Analysis(d->h, n, (int)nnz, d->descr, d->rp, d->col, d->info));
     return FFGPU_OK;
@@ -242,6 +296,33 @@ static int direct_numeric(ffgpu_matrix *A, DirectState *d) {
     gather_kernel<<<grid_of(nnz), 256, 0, s>>>(nnz, d->src, d->exported, d->val);
     FFGPU_TRY(launch_check(ctx, "direct gather"));
     size_t internal = 0, work = 0;
+    if (d->method == FFGPU_DIRECT_QR) {
+        if (d->qr_factored) {
+            // a factored csrqr info takes no second setup: a new numeric state starts from a new
+            // analysis of the same pattern
+            L.QrDestroyInfo(d->qinfo);
+            d->qinfo = nullptr;
+            FFGPU_SOLVER(L.QrCreateInfo(&d->qinfo));
+            FFGPU_SOLVER(L.QrAnalysis(d->h, n, n, (int)nnz, d->descr, d->rp, d->col, d->qinfo));
+        }
+        row_scale_kernel<<<grid_of(n), 256, 0, s>>>(n, d->rp, d->val, d->rscale);
+        FFGPU_TRY(launch_check(ctx, "direct row scale"));
+        FFGPU_SOLVER(L.QrBufferInfo(d->h, n, n, (int)nnz, d->descr, d->val, d->rp, d->col, d->qinfo, &internal,
+                                    &work));
+        if (d->buf) { cudaFree(d->buf); d->buf = nullptr; }
+        FFGPU_CUDA(cudaMalloc(&d->buf, std::max<size_t>(work, 256)));
+        FFGPU_SOLVER(L.QrSetup(d->h, n, n, (int)nnz, d->descr, d->val, d->rp, d->col, 0.0, d->qinfo));
+        // the factorisation also solves one system: a zero right-hand side on the scratch vectors
+        FFGPU_CUDA(cudaMemsetAsync(d->t1, 0, sizeof(double) * n, s));
+        FFGPU_SOLVER(L.QrFactor(d->h, n, n, (int)nnz, d->t1, d->t2, d->qinfo, d->buf));
+        int pos = -1;
+        FFGPU_SOLVER(L.QrZeroPivot(d->h, d->qinfo, 0.0, &pos));
+        d->qr_factored = true;
+        FFGPU_CHECK(pos < 0, FFGPU_EINVAL, "direct solver: the matrix is singular (zero pivot of R at column %d)",
+                    pos);
+        d->factored = true;
+        return FFGPU_OK;
+    }
     FFGPU_SOLVER(L.BufferInfo(d->h, n, (int)nnz, d->descr, d->val, d->rp, d->col, d->info, &internal, &work));
     if (d->buf) { cudaFree(d->buf); d->buf = nullptr; }
     FFGPU_CUDA(cudaMalloc(&d->buf, std::max<size_t>(work, 256)));
@@ -261,17 +342,25 @@ static int direct_prepare(ffgpu_matrix *A) {
     ffgpu_ctx *ctx = A->ctx;
     if (!d) {
         // Cholesky needs a symmetric matrix (tgv > 0 and tgv = -2 keep it so; -1 and -3 do not)
-        FFGPU_TRY(matrix_prepare_transpose(A));
-        int *flag = ctx->d_iscratch + 8;
-        FFGPU_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
-        symmetry_kernel<<<grid_of(A->nb), 256, 0, ctx->stream>>>(A->nb, A->bs, A->browptr, A->bcol, A->diagpos,
-                                                                A->val, A->val_t, flag);
-        FFGPU_TRY(launch_check(ctx, "symmetry"));
-        int hf = 0;
-        FFGPU_CUDA(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        FFGPU_CUDA(cudaStreamSynchronize(ctx->stream));
-        FFGPU_CHECK(!hf, FFGPU_EINVAL, "direct solver: Cholesky needs a symmetric matrix");
+        int method = A->direct_method;
+        if (method != FFGPU_DIRECT_QR) {
+            FFGPU_TRY(matrix_prepare_transpose(A));
+            int *flag = ctx->d_iscratch + 8;
+            FFGPU_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+            symmetry_kernel<<<grid_of(A->nb), 256, 0, ctx->stream>>>(A->nb, A->bs, A->browptr, A->bcol,
+                                                                    A->diagpos, A->val, A->val_t, flag);
+            FFGPU_TRY(launch_check(ctx, "symmetry"));
+            int hf = 0;
+            FFGPU_CUDA(cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            FFGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+            FFGPU_CHECK(!hf || method == FFGPU_DIRECT_AUTO, FFGPU_EINVAL,
+                        "direct solver: Cholesky needs a symmetric matrix");
+            method = hf ? FFGPU_DIRECT_QR : FFGPU_DIRECT_CHOLESKY;
+        }
+        FFGPU_CHECK(method != FFGPU_DIRECT_QR || solver_lib().qr_ok, FFGPU_EINVAL,
+                    "direct solver: sparse QR unavailable: %s", solver_lib().why.c_str());
         d = new DirectState();
+        d->method = method;
         A->direct = d;
         const int rc = direct_symbolic(A, d);
         if (rc) { direct_release(A); return rc; }
@@ -286,6 +375,18 @@ static int direct_prepare(ffgpu_matrix *A) {
 using namespace ffgpu;
 
 extern "C" {
+
+int ffgpu_direct_method(ffgpu_matrix *A, int method) {
+    FFGPU_CHECK(A, FFGPU_EINVAL, "ffgpu_direct_method: NULL matrix");
+    FFGPU_CHECK(method == FFGPU_DIRECT_AUTO || method == FFGPU_DIRECT_CHOLESKY || method == FFGPU_DIRECT_QR,
+                FFGPU_EINVAL, "ffgpu_direct_method: unknown method %d", method);
+    if (A->direct_method != method) {
+        FFGPU_CUDA(cudaSetDevice(A->ctx->device));
+        direct_release(A);
+        A->direct_method = method;
+    }
+    return FFGPU_OK;
+}
 
 int ffgpu_direct_factor(ffgpu_matrix *A) {
     FFGPU_CHECK(A, FFGPU_EINVAL, "ffgpu_direct_factor: NULL matrix");
@@ -313,7 +414,13 @@ int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ff
     for (int k = 0; k < nrhs; ++k) {
         gather_kernel<<<grid_of(n), 256, 0, s>>>(n, d->perm, bd.d + k * n, d->t1);
         FFGPU_TRY(launch_check(ctx, "direct permute"));
-        FFGPU_SOLVER(L.Solve(d->h, (int)n, d->t1, d->t2, d->info, d->buf));
+        if (d->method == FFGPU_DIRECT_QR) {
+            scale_kernel<<<grid_of(n), 256, 0, s>>>(n, d->rscale, d->t1);
+            FFGPU_TRY(launch_check(ctx, "direct scale"));
+            FFGPU_SOLVER(L.QrSolve(d->h, (int)n, (int)n, d->t1, d->t2, d->qinfo, d->buf));
+        } else {
+            FFGPU_SOLVER(L.Solve(d->h, (int)n, d->t1, d->t2, d->info, d->buf));
+        }
         scatter_kernel<<<grid_of(n), 256, 0, s>>>(n, d->perm, d->t2, xd.d + k * n);
         FFGPU_TRY(launch_check(ctx, "direct unpermute"));
     }

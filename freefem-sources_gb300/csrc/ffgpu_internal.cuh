@@ -135,7 +135,8 @@ struct ffgpu_matrix {
     int csr_lanes_x;      // lanes per block row of the double-float SpMV (tuned)
     int layout_pinned;    // the caller fixed the SpMV layout of the current solve
     int last_cluster;     // the last FP64 CG solve ran in one thread-block cluster
-    void *direct;         // sparse Cholesky state of the direct solver (ffgpu_direct.cu), or NULL
+    void *direct;         // factorisation state of the direct solver (ffgpu_direct.cu), or NULL
+    int direct_method;    // FFGPU_DIRECT_AUTO / _CHOLESKY / _QR
     // SELL-32 copy for the Krylov SpMVs: block rows sliced into chunks of 32 (one row per
     // lane), rows sorted by decreasing degree inside windows of 1024 rows, each chunk padded
     // to its longest row and stored slot-major so that a warp reads 32 consecutive entries.

@@ -9,9 +9,11 @@
 //   K_a  AH = A H (SpMV) with (H,AH) -> rho                     [last block]
 //   K_b  x += rho H, G += rho AH, (G, C G) -> gamma, stop test  [last block]
 //   K_c  H = gamma H - C G with (G,H)                            [last block]
-// CG = C G is recomputed where it is used instead of being stored.  The iteration loop is
-// a CUDA graph `while` node whose condition K_b clears on convergence or at itmax, so a
-// whole solve is one graph launch with no host round trip.
+// CG = C G is recomputed where it is used instead of being stored.  Small scalar systems (the
+// matrix in L2, an iteration bound by kernel boundaries) run two kernels per iteration: K_b
+// stores C G and the next K_a forms H = gamma H - C G at every column it gathers (cg_kca_sell).
+// The iteration loop is a CUDA graph `while` node whose condition K_b clears on convergence or
+// at itmax, so a whole solve is one graph launch with no host round trip.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -153,11 +155,14 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
 
 // The vector kernels run on a resident grid and read/write two elements per access (all
 // work vectors are 16-byte aligned); an odd last element is done by thread 0 of block 0.
-// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence
+// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence; with STORE also C G into cgv
+// (read by the fused direction update of cg_kca_sell)
+template <bool STORE>
 __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
                                                      const double *__restrict__ h, const double *__restrict__ q,
-                                                     const double *__restrict__ dinv, KrylovScalars *ks,
-                                                     double *part, cudaGraphConditionalHandle cond, int in_graph) {
+                                                     const double *__restrict__ dinv, double *__restrict__ cgv,
+                                                     KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond,
+                                                     int in_graph) {
     __shared__ double sh[32];
     if (ks->done) {
         if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) graph_stop(cond);
@@ -176,15 +181,19 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         gv.x = fma(rho, qv.x, gv.x); gv.y = fma(rho, qv.y, gv.y);
         x2[i] = xv;
         g2[i] = gv;
-        s = fma(gv.x, dv.x * gv.x, s);
-        s = fma(gv.y, dv.y * gv.y, s);
+        const double c0 = __dmul_rn(dv.x, gv.x), c1 = __dmul_rn(dv.y, gv.y);
+        if (STORE) reinterpret_cast<double2 *>(cgv)[i] = make_double2(c0, c1);
+        s = fma(gv.x, c0, s);
+        s = fma(gv.y, c1, s);
     }
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const int i = n - 1;
         x[i] = fma(rho, h[i], x[i]);
         const double gi = fma(rho, q[i], g[i]);
         g[i] = gi;
-        s = fma(gi, dinv[i] * gi, s);
+        const double ci = __dmul_rn(dinv[i], gi);
+        if (STORE) cgv[i] = ci;
+        s = fma(gi, ci, s);
     }
     double tot;
     double p = block_sum(s, sh);
@@ -216,8 +225,9 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__re
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
         const double2 gv = g2[i], dv = d2[i];
         double2 hv = h2[i];
-        hv.x = gamma * hv.x - dv.x * gv.x;
-        hv.y = gamma * hv.y - dv.y * gv.y;
+        // the roundings spelled out: the fused update of cg_kca_sell forms the same bits
+        hv.x = fma(gamma, hv.x, -__dmul_rn(dv.x, gv.x));
+        hv.y = fma(gamma, hv.y, -__dmul_rn(dv.y, gv.y));
         h2[i] = hv;
         if (SPLIT) {
             const float2 a = split_f64(hv.x), b = split_f64(hv.y);
@@ -229,7 +239,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__re
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const int i = n - 1;
         const double gi = g[i];
-        const double hi = gamma * h[i] - dinv[i] * gi;
+        const double hi = fma(gamma, h[i], -__dmul_rn(dinv[i], gi));
         h[i] = hi;
         if (SPLIT) hx[i] = split_f64(hi);
         s = fma(gi, hi, s);
@@ -380,6 +390,131 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
         ks->s_hq = tot;
         ks->rho = -ks->s_gh / tot;
     }
+}
+
+// Fused direction update and SpMV for small scalar systems (two kernels per CG iteration
+// instead of three): H' = gamma H - C G is formed where it is used -- at every gathered column
+// and for the lane's own row, which is written to the other H buffer -- and AH' = A H',
+// (G, H') and (H', AH') -> rho come out of one pass.  C G was stored by K_b.  Each gathered
+// entry costs one FP64 FMA more, so this runs only where the iteration is latency-bound.
+__device__ __forceinline__ bool last_block_sum2(double p1, double p2, double *part, unsigned *ticket, double *t1,
+                                                double *t2, double *sh) {
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = p1;
+        part[gridDim.x + blockIdx.x] = p2;
+        __threadfence();
+        s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double a = 0, c = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        a += __ldcg(part + i);
+        c += __ldcg(part + gridDim.x + i);
+    }
+    a = block_sum_t(a, sh);
+    c = block_sum_t(c, sh);
+    if (threadIdx.x == 0) {
+        *t1 = a;
+        *t2 = c;
+        *ticket = 0u;
+        return true;
+    }
+    return false;
+}
+
+template <bool C16, int ASSIGN>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_sell(SellArgs S, const double *__restrict__ val,
+                                                               const double *__restrict__ hold,
+                                                               const double *__restrict__ cgv,
+                                                               const double *__restrict__ g,
+                                                               double *__restrict__ hnew, double *__restrict__ q,
+                                                               KrylovScalars *ks, double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const double gamma = ks->gamma;
+    const int lane = threadIdx.x & 31;
+    double hq = 0, gh = 0;
+    sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
+        const int ar = a < 0 ? 0 : a;
+        const int64_t ce = sr * 32 + lane;
+        const double *v = val + sr * 32 + lane;
+        double y = 0;
+#pragma unroll 8
+        for (int j = 0; j < L; ++j) {
+            const int col = sell_col<C16>(S, ce + (int64_t)j * 32, ar);
+            const double hc = fma(gamma, __ldg(hold + col), -__ldg(cgv + col));
+            y = fma(__ldcs(v + (int64_t)j * 32), hc, y);
+        }
+        if (a >= 0) {
+            const double ha = fma(gamma, hold[a], -cgv[a]);
+            hnew[a] = ha;
+            q[a] = y;
+            hq = fma(ha, y, hq);
+            gh = fma(g[a], ha, gh);
+        }
+    });
+    const double pgh = block_sum(gh, sh);
+    const double phq = block_sum(hq, sh);
+    double tgh, thq;
+    if (last_block_sum2(pgh, phq, part, &ks->ticket, &tgh, &thq, sh)) {
+        ks->s_gh = tgh;
+        ks->s_hq = thq;
+        ks->rho = -tgh / thq;
+    }
+}
+
+// the same with block CSR rows (T lanes per row, rows in the degree order of rowperm)
+template <int T>
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_csr(SpmvArgs A, const double *__restrict__ hold,
+                                                              const double *__restrict__ cgv,
+                                                              const double *__restrict__ g,
+                                                              double *__restrict__ hnew, double *__restrict__ q,
+                                                              KrylovScalars *ks, double *part) {
+    __shared__ double sh[32];
+    if (ks->done) return;
+    const double gamma = ks->gamma;
+    const int lane = threadIdx.x & 31;
+    const int gsub = lane / T, sub = lane % T;
+    const int groups = (blockDim.x / 32) * (32 / T);
+    const int gi = blockIdx.x * groups + (threadIdx.x / 32) * (32 / T) + gsub;
+    double hq = 0, gh = 0;
+    for (int base = 0; base < A.nb; base += gridDim.x * groups) {
+        const int slot = base + gi;
+        const bool ok = slot < A.nb;
+        const int a = ok ? __ldg(A.perm + slot) : 0;
+        const int b0 = __ldg(A.rp + a), e0 = __ldg(A.rp + a + 1);
+        double y = 0;
+        for (int k = b0 + (ok ? sub : T); k < e0; k += T) {
+            const int col = __ldg(A.col + k);
+            y = fma(__ldg(A.val + k), fma(gamma, __ldg(hold + col), -__ldg(cgv + col)), y);
+        }
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+        if (ok && sub == 0) {
+            const double ha = fma(gamma, hold[a], -cgv[a]);
+            hnew[a] = ha;
+            q[a] = y;
+            hq = fma(ha, y, hq);
+            gh = fma(g[a], ha, gh);
+        }
+    }
+    const double pgh = block_sum(gh, sh);
+    const double phq = block_sum(hq, sh);
+    double tgh, thq;
+    if (last_block_sum2(pgh, phq, part, &ks->ticket, &tgh, &thq, sh)) {
+        ks->s_gh = tgh;
+        ks->s_hq = thq;
+        ks->rho = -tgh / thq;
+    }
+}
+
+// the fused loop starts from H = -C G (cg_init) with gamma = 1 and C G = 0, so that its first
+// update reproduces that H
+__global__ void cg_fuse_start(KrylovScalars *ks) {
+    if (threadIdx.x == 0) ks->gamma = 1.0;
 }
 
 // double-float: AH = A H from the split H, (H, AH) in FP64
@@ -929,7 +1064,8 @@ int matrix_prepare_solver(ffgpu_matrix *A) {
 // grids of K_b / K_c: resident, at most 4096 blocks, no more than the n/2 double2 pairs need
 static int vec_grid_kb(int n) {
     static int g = 0;
-    if (!g) g = min(4096, resident_grid((const void *)cg_kb, kVecThreads));
+    if (!g) g = min(4096, min(resident_grid((const void *)cg_kb<false>, kVecThreads),
+                              resident_grid((const void *)cg_kb<true>, kVecThreads)));
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, ((int64_t)n / 2 + kVecThreads - 1) / kVecThreads));
 }
 static int vec_grid_kc(int n) {
@@ -944,21 +1080,98 @@ static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h
                     float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
                     cudaStream_t s) {
     ka.launch(s);
-    cg_kb<<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, ks, part, cond, in_graph);
+    cg_kb<false><<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, nullptr, ks, part, cond, in_graph);
     if (mode == 1)
         cg_kc_t<true><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
     else
         cg_kc_t<false><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, nullptr, dinv, ks, part);
 }
 
-// Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }].
-static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x, double *g, double *h, double *q) {
-    if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans && A->cg_mode == mode) return FFGPU_OK;
+// ------------------------------------------------------------------ fused two-kernel iteration
+// Scalar FP64 systems in the SELL-32 layout whose matrix is small enough that an iteration is
+// bound by kernel boundaries (the matrix and vectors stay in L2): K_ca (direction update + SpMV
+// + both dots, cg_kca_sell) and K_b (storing C G).  H alternates between two buffers.
+constexpr int64_t kFuseMaxEntries = 1 << 20;
+
+struct KcaCall {
+    void *fn = nullptr;
+    int grid = 0;
+    SellArgs sl;
+    SpmvArgs sa;
+    const double *v64 = nullptr, *hold = nullptr, *cgv = nullptr, *g = nullptr;
+    double *hnew = nullptr, *q = nullptr;
+    KrylovScalars *ks = nullptr;
+    double *part = nullptr;
+    void *args[9];
+    cudaError_t launch(cudaStream_t s) { return cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, s); }
+};
+
+static bool cg_fused_fits(const ffgpu_matrix *A, int mode) {
+    const char *e = getenv("FFGPU_CG_FUSE");
+    if (e && e[0] == '0') return false;
+    return mode == 0 && A->bs == 1 && A->nnz <= kFuseMaxEntries;
+}
+
+static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hnew, const double *cgv,
+                     const double *g, double *q, KcaCall &k) {
+    k.hold = hold; k.hnew = hnew; k.cgv = cgv; k.g = g; k.q = q;
+    k.ks = A->ks; k.part = A->ctx->d_part;
+    if (!is_sell(A->csr_lanes)) {
+        // block CSR with the tuned lanes per row
+        if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
+        const int T = pick_lanes(A);
+        k.sa = spmv_args(A, trans);
+        k.fn = T == 1 ? (void *)cg_kca_csr<1> : T == 2 ? (void *)cg_kca_csr<2> : T == 4 ? (void *)cg_kca_csr<4>
+                                                                                     : (void *)cg_kca_csr<8>;
+        k.grid = spmv_grid(A, T);
+        FFGPU_CHECK(2 * k.grid <= 4 * kRedBlocks, FFGPU_EINVAL, "fused CG: grid %d above the reduction buffer",
+                    k.grid);
+        k.args[0] = &k.sa; k.args[1] = &k.hold; k.args[2] = &k.cgv; k.args[3] = &k.g; k.args[4] = &k.hnew;
+        k.args[5] = &k.q; k.args[6] = &k.ks; k.args[7] = &k.part;
+        return FFGPU_OK;
+    }
+    FFGPU_TRY(sell_values(A, trans ? kSell64T : kSell64));
+    const bool c16 = A->scol16 != nullptr;
+    const int assign = sell_assign(A->csr_lanes);
+    k.fn = c16 ? (assign ? (void *)cg_kca_sell<true, 1> : (void *)cg_kca_sell<true, 0>)
+               : (assign ? (void *)cg_kca_sell<false, 1> : (void *)cg_kca_sell<false, 0>);
+    k.sl = sell_args(A);
+    k.grid = sized_grid(k.fn, kSpmvWarps * 32, ((int64_t)A->nchunk + kSpmvWarps - 1) / kSpmvWarps);
+    // two partial slots per block in the reduction buffer
+    FFGPU_CHECK(2 * k.grid <= 4 * kRedBlocks, FFGPU_EINVAL, "fused CG: grid %d above the reduction buffer", k.grid);
+    if (assign == kSellRanges) FFGPU_TRY(sell_partition(A, k.grid * kSpmvWarps, &k.sl.part));
+    k.v64 = trans ? A->sval_t : A->sval;
+    k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.hold; k.args[3] = &k.cgv; k.args[4] = &k.g;
+    k.args[5] = &k.hnew; k.args[6] = &k.q; k.args[7] = &k.ks; k.args[8] = &k.part;
+    return FFGPU_OK;
+}
+
+// iteration u of a body: K_ca from H buffer u % 2 into the other one, then K_b on the new H
+static void cg_body_fused(KcaCall (&kc)[2], int u, int n, double *x, double *g, double *const h[2], double *q,
+                          const double *dinv, double *cgv, KrylovScalars *ks, double *part,
+                          cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s) {
+    kc[u & 1].launch(s);
+    cg_kb<true><<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h[(u + 1) & 1], q, dinv, cgv, ks, part, cond,
+                                                         in_graph);
+}
+
+// Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }] (fused: (K_ca K_b) x unroll).
+static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x, double *g, double *h, double *q,
+                    bool fused, double *h2, double *cgv) {
+    const int gmode = mode + (fused ? 2 : 0);
+    if (A->cg_exec && A->cg_unroll == unroll && A->cg_trans == trans && A->cg_mode == gmode) return FFGPU_OK;
     if (A->cg_exec) { cudaGraphExecDestroy(A->cg_exec); A->cg_exec = nullptr; }
     ffgpu_ctx *ctx = A->ctx;
     cudaStream_t s = ctx->stream;
     KaCall ka;
-    FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
+    KcaCall kc[2];
+    double *const hb[2] = {h, h2};
+    if (fused) {
+        FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, kc[0]));
+        FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, kc[1]));
+    } else {
+        FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
+    }
     vec_grid_kb(A->n);
     vec_grid_kc(A->n);
     cudaGraph_t graph, body;
@@ -977,8 +1190,12 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
     body = cp->conditional.phGraph_out[0];
     FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    for (int u = 0; u < unroll; ++u)
-        cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s);
+    for (int u = 0; u < unroll; ++u) {
+        if (fused)
+            cg_body_fused(kc, u, A->n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, cond, 1, s);
+        else
+            cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s);
+    }
     cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e != cudaSuccess) {
         set_error("CG graph capture failed: %s", cudaGetErrorString(e));
@@ -994,8 +1211,8 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     }
     A->cg_unroll = unroll;
     A->cg_trans = trans;
-    A->cg_mode = mode;
-    A->cg_kernels_body = 3 * unroll;
+    A->cg_mode = gmode;
+    A->cg_kernels_body = (fused ? 2 : 3) * unroll;
     return FFGPU_OK;
 }
 
@@ -1015,6 +1232,8 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     int itmax = prm->itmax > 0 ? prm->itmax : n;
     int unroll = prm->unroll > 0 ? prm->unroll : 8;
     const int mode = prm->spmv_mode == 1 ? 1 : 0;
+    // the second H buffer and C G of the fused iteration
+    double *h2 = A->vec + 7 * vs, *cgv = A->vec + 3 * vs;
     if (mode == 1) {
         if (!A->hx) FFGPU_CUDA(dalloc(ctx, (void **)&A->hx, sizeof(float2) * vs));
         FFGPU_TRY(tune_lanes(A, 1));
@@ -1023,7 +1242,9 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     // (ffgpu_cluster.cu), unless a layout is fixed by the caller
     const bool cluster = mode == 0 && !A->layout_pinned && cluster_cg_fits(A, trans);
     A->last_cluster = cluster;
-    if (!cluster) FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
+    const bool fused = !cluster && cg_fused_fits(A, mode);
+    if (fused) unroll += unroll & 1;   // the H buffers alternate: an even number of iterations per body
+    if (!cluster) FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q, fused, h2, cgv));
     FFGPU_CUDA(cudaMemcpyAsync(x, xu, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -1040,6 +1261,11 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         split_vec_kernel<<<kVecBlocks, kVecThreads, 0, s>>>(n, h, A->hx);
         FFGPU_TRY(launch_check(ctx, "split_vec"));
     }
+    if (fused) {
+        FFGPU_CUDA(cudaMemsetAsync(cgv, 0, sizeof(double) * n, s));
+        cg_fuse_start<<<1, 32, 0, s>>>(A->ks);
+        FFGPU_TRY(launch_check(ctx, "cg_fuse_start"));
+    }
     const char *ge = getenv("FFGPU_CG_GRAPH");
     int bodies_host = -1;
     bool use_graph = !cluster;
@@ -1048,7 +1274,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         if (rc == kClusterRefused) {
             // the device refused this cluster shape: the regular path from the same state
             A->last_cluster = 0;
-            FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q));
+            FFGPU_TRY(cg_graph(A, trans, unroll, mode, x, g, h, q, false, h2, cgv));
             use_graph = true;
         } else {
             FFGPU_TRY(rc);
@@ -1059,11 +1285,22 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         // Same kernels launched from the host (for profilers that do not trace conditional
         // graph nodes): poll the done flag after every `unroll` iterations.
         KaCall ka;
-        FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
+        KcaCall kc[2];
+        double *const hb[2] = {h, h2};
+        if (fused) {
+            FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, kc[0]));
+            FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, kc[1]));
+        } else {
+            FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
+        }
         bodies_host = 0;
         for (int it = 0; it <= itmax; it += unroll) {
-            for (int u = 0; u < unroll; ++u)
-                cg_body(ka, mode, n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, 0, 0, s);
+            for (int u = 0; u < unroll; ++u) {
+                if (fused)
+                    cg_body_fused(kc, u, n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, 0, 0, s);
+                else
+                    cg_body(ka, mode, n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, 0, 0, s);
+            }
             ++bodies_host;
             int done = 0;
             FFGPU_CUDA(cudaMemcpyAsync(&done, &A->ks->done, sizeof(int), cudaMemcpyDeviceToHost, s));

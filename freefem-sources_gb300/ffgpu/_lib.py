@@ -31,7 +31,7 @@ EXPORTS = [
     "ffgpu_number_p2", "ffgpu_number_p2_2d", "ffgpu_gibbs_renumber",
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
-    "ffgpu_solve_cg_csr_noalloc", "ffgpu_direct_factor", "ffgpu_solve_direct",
+    "ffgpu_solve_cg_csr_noalloc", "ffgpu_direct_method", "ffgpu_direct_factor", "ffgpu_solve_direct",
     "ffgpu_batch_create", "ffgpu_batch_assemble", "ffgpu_batch_solve", "ffgpu_batch_rhs",
     "ffgpu_batch_matrix", "ffgpu_batch_info", "ffgpu_batch_destroy",
 ]
@@ -136,6 +136,7 @@ def lib():
         "ffgpu_solve_cg": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),
         "ffgpu_solve_gmres": (i32, [vp, vp, vp, i32, i32, P(SolverParams), P(SolverStats)]),
         "ffgpu_matrix_to_f32": (i32, [vp]),
+        "ffgpu_direct_method": (i32, [vp, i32]),
         "ffgpu_direct_factor": (i32, [vp]),
         "ffgpu_solve_direct": (i32, [vp, vp, vp, i32, P(SolverStats)]),
         "ffgpu_solve_ir": (i32, [vp, vp, vp, P(IRParams), P(SolverStats)]),

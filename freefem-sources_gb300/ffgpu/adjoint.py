@@ -183,6 +183,8 @@ class HeatProblem:
         self.mdt = api.matrix(api.varf_diffusion(c_stiff=0.0, c_mass=1.0 / dt), self.space)
         self.A = None
         self.solves = 0
+        self.iterations_state = 0      # CG iterations of the state solves (forward and recomputed)
+        self.iterations_adjoint = 0    # CG iterations of the transpose solves
 
     def assemble(self, kappa, f):
         if _on_device(kappa):
@@ -201,7 +203,9 @@ class HeatProblem:
 
     def step(self, u_prev):
         self.solves += 1
-        return self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev)
+        u = self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev)
+        self.iterations_state += self.A.stats.iterations
+        return u
 
     def forward(self, kappa, f, keep_checkpoints=True):
         """u^N and the checkpoints: every `checkpoint`-th state, plus the states of the last
@@ -224,6 +228,8 @@ class HeatProblem:
     def value_and_grad(self, kappa, f, u_obs):
         """Forward with checkpoints, backward with recomputation of each segment."""
         self.solves = 0
+        self.iterations_state = 0
+        self.iterations_adjoint = 0
         uN, ck = self.forward(kappa, f)
         forward_solves = self.solves
         r = uN - u_obs
@@ -246,6 +252,7 @@ class HeatProblem:
                 rhs = rhs_adj if n == N else self.mdt.mult(lam_next, trans=True)
                 lam = self.A.solve(rhs, trans=True, x0=lam_next)
                 self.solves += 1
+                self.iterations_adjoint += self.A.stats.iterations
                 g1, g2 = sensitivity(self.A, states[n], lam)
                 gk += g1
                 gf += g2

@@ -421,6 +421,10 @@ def varf_elasticity(E=1.0, nu=0.3, f=(0.0, 0.0, -1.0), on=(), components=None, t
                    tgv=tgv, bterms=tuple(bterms), quad=quad)
 
 
+# direct solver names -> ffgpu_direct_method (FFGPU_DIRECT_AUTO / _CHOLESKY / _QR)
+DIRECT_METHODS = {"SPARSESOLVER": 0, "UMFPACK": 0, "LU": 0, "CHOLESKY": 1, "CHOLMOD": 1, "QR": 2}
+
+
 class Matrix:
     """``matrix A = a(Vh,Vh, solver=..., eps=..., ...)`` with a device-resident pattern/values."""
 
@@ -481,8 +485,13 @@ class Matrix:
         bb = b if dev_in else np.ascontiguousarray(b, np.float64)
         nrhs = int(np.prod(np.shape(b))) // self.n
         st = SolverStats()
-        if solver in ("CHOLESKY", "CHOLMOD", "SPARSESOLVER"):
-            # direct: the factorisation is kept for later solves of this numeric state (A' = A)
+        if solver in DIRECT_METHODS:
+            # direct: the factorisation is kept for later solves of this numeric state; Cholesky
+            # (symmetric positive definite), QR (any nonsingular matrix) or the choice between
+            # them by symmetry (SPARSESOLVER, FreeFEM's default direct solver name)
+            if trans:
+                raise ValueError("the direct solvers solve A x = b; use CG or GMRES for A' x = b")
+            check(lib().ffgpu_direct_method(self.h, DIRECT_METHODS[solver]))
             code = lib().ffgpu_solve_direct(self.h, _ptr(bb), _ptr(out), nrhs, C.byref(st))
             self.stats = st
             check(code)
@@ -490,7 +499,8 @@ class Matrix:
         p = self.params(eps, itmax, unroll, spmv_mode, spmv_layout)
         fn = lib().ffgpu_solve_cg if solver == "CG" else lib().ffgpu_solve_gmres
         if solver not in ("CG", "GMRES"):
-            raise ValueError(f"solver {solver!r}: the device path provides CG, GMRES and CHOLESKY")
+            raise ValueError(f"solver {solver!r}: the device path provides CG, GMRES and the direct solvers "
+                             f"{', '.join(DIRECT_METHODS)}")
         code = fn(self.h, _ptr(bb), _ptr(out), nrhs, int(trans), C.byref(p), C.byref(st))
         self.stats = st
         check(code)

@@ -14,6 +14,8 @@
 //   GPUCGMIXED  FP32 inner PCG + FP64 refinement, same stopping rule on the true residual
 //   GPUCHOLESKY sparse Cholesky on the device, factored once per numeric state (the role of
 //               FreeFEM's CHOLMOD / MUMPS plugins); symmetric positive definite matrices
+//   GPUSPARSESOLVER  the direct solver of any nonsingular matrix (the role of UMFPACK, FreeFEM's
+//               `sparsesolver`): Cholesky when the matrix is symmetric, else sparse QR
 // The matrix FreeFEM assembled is uploaded once per numeric state (fac_numeric, in sorted CSR
 // via HashMatrix::CSR, HashMatrix.cpp:859-867) and stays on the device with the solver object,
 // which the matrix owns (VirtualMatrix.hpp:71-94).  Errors become ExecError / ffassert as in
@@ -68,7 +70,7 @@ ffgpu_ctx *context() {
     return g_ctx;
 }
 
-enum Kind { kCG = 0, kGMRES = 1, kMixed = 2, kCholesky = 3 };
+enum Kind { kCG = 0, kGMRES = 1, kMixed = 2, kCholesky = 3, kSparse = 4 };
 
 // FreeFEM's matrix in full sorted CSR: A.CSR (HashMatrix.cpp:859-867), the other triangle added
 // when FreeFEM stores half of a symmetric matrix (HashMatrix::half)
@@ -162,9 +164,10 @@ class SolverGpu : public VirtualSolver<int, double> {
     }
     // the direct solver factors here, once per numeric state (VirtualSolver::factorize)
     void factor() {
-        if (KIND != kCholesky) return;
-        const int r = ffgpu_direct_factor(M);
-        if (r != FFGPU_OK) ExecError((std::string("ffgpu Cholesky: ") + ffgpu_last_error()).c_str());
+        if (KIND != kCholesky && KIND != kSparse) return;
+        int r = ffgpu_direct_method(M, KIND == kCholesky ? FFGPU_DIRECT_CHOLESKY : FFGPU_DIRECT_AUTO);
+        if (r == FFGPU_OK) r = ffgpu_direct_factor(M);
+        if (r != FFGPU_OK) ExecError((std::string("ffgpu direct solver: ") + ffgpu_last_error()).c_str());
     }
     void dosolver(double *x, double *b, int N, int trans) {
         ffgpu_solver_stats st;
@@ -174,8 +177,11 @@ class SolverGpu : public VirtualSolver<int, double> {
             r = FFGPU_OK;
             for (int k = 0; k < N && r == FFGPU_OK; ++k)
                 r = ffgpu_solve_ir(M, b + (size_t)k * A.n, x + (size_t)k * A.n, &p, &st);
-        } else if (KIND == kCholesky) {
-            r = ffgpu_solve_direct(M, b, x, N, &st);   // A' = A
+        } else if (KIND == kCholesky || KIND == kSparse) {
+            // Cholesky: A' = A; the QR of a nonsymmetric matrix solves A x = b only
+            if (trans && KIND == kSparse)
+                ExecError("ffgpu: A'^-1 with GPUSPARSESOLVER is not provided (use GPUGMRES for A'^-1)");
+            r = ffgpu_solve_direct(M, b, x, N, &st);
         } else {
             ffgpu_solver_params p = {eps, (int)itmax, (int)restart, tgv, (int)verb, 8};
             r = KIND == kCG ? ffgpu_solve_cg(M, b, x, N, trans, &p, &st)
@@ -196,6 +202,7 @@ template <> const int SolverGpu<kCG>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 template <> const int SolverGpu<kGMRES>::orTypeSol = 1 | 2 | 4 | 8 | 16 | 32;
 template <> const int SolverGpu<kMixed>::orTypeSol = 1 | 2 | 4 | 8 | 32;
 template <> const int SolverGpu<kCholesky>::orTypeSol = 1 | 2 | 4 | 8 | 32;
+template <> const int SolverGpu<kSparse>::orTypeSol = 1 | 2 | 4 | 8 | 16 | 32;
 
 // ------------------------------------------------------------------ device assembly
 // `matrix A = a(Vh, Vh, ...)` is routed here (an OpMatrixtoBilinearForm with a higher
@@ -840,6 +847,7 @@ static void hand_over(VirtualMatrix<int, double> &VA, ffgpu_matrix *M) {
     if (SolverGpu<kGMRES> *s = dynamic_cast<SolverGpu<kGMRES> *>(vs)) return s->adopt(M);
     if (SolverGpu<kMixed> *s = dynamic_cast<SolverGpu<kMixed> *>(vs)) return s->adopt(M);
     if (SolverGpu<kCholesky> *s = dynamic_cast<SolverGpu<kCholesky> *>(vs)) return s->adopt(M);
+    if (SolverGpu<kSparse> *s = dynamic_cast<SolverGpu<kSparse> *>(vs)) return s->adopt(M);
     ffgpu_matrix_destroy(M);
 }
 
@@ -1152,12 +1160,15 @@ static void Load_Init() {
     addsolver<SolverGpu<kGMRES> >("GPUGMRES", 20);
     addsolver<SolverGpu<kMixed> >("GPUCGMIXED", 20);
     addsolver<SolverGpu<kCholesky> >("GPUCHOLESKY", 20);
+    addsolver<SolverGpu<kSparse> >("GPUSPARSESOLVER", 20);
     // script constants, as lgfem.cpp:6380-6395 declares CG, GMRES, ...: solver=GPUCG
-    static std::string gpucg = "GPUCG", gpugmres = "GPUGMRES", gpumixed = "GPUCGMIXED", gpuchol = "GPUCHOLESKY";
+    static std::string gpucg = "GPUCG", gpugmres = "GPUGMRES", gpumixed = "GPUCGMIXED", gpuchol = "GPUCHOLESKY",
+                       gpusparse = "GPUSPARSESOLVER";
     Global.New("GPUCG", CConstant<std::string *>(&gpucg));
     Global.New("GPUGMRES", CConstant<std::string *>(&gpugmres));
     Global.New("GPUCGMIXED", CConstant<std::string *>(&gpumixed));
     Global.New("GPUCHOLESKY", CConstant<std::string *>(&gpuchol));
+    Global.New("GPUSPARSESOLVER", CConstant<std::string *>(&gpusparse));
     // `ffgpustrict = 1;` in a script: forms the device does not assemble are errors
     Global.New("ffgpustrict", CPValue<long>(g_strict));
     // device assembly behind `matrix A = a(Vh,Vh)` (lgfem.cpp:6669-6673, :6823-6826)
@@ -1169,7 +1180,8 @@ static void Load_Init() {
                       new GpuLinear<Mesh3, v_fes3>(atype<KN_<double> >(), false, false));
     TheOperators->Add("<-", new GpuLinear<Mesh, v_fes>(atype<KN<double> *>(), true, true),
                       new GpuLinear<Mesh3, v_fes3>(atype<KN<double> *>(), true, true));
-    if (verbosity > 1) std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED, GPUCHOLESKY)" << std::endl;
+    if (verbosity > 1)
+        std::cout << " load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED, GPUCHOLESKY, GPUSPARSESOLVER)" << std::endl;
 }
 
 LOADFUNC(Load_Init)

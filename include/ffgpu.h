@@ -355,16 +355,25 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
                       const ffgpu_solver_params *prm, ffgpu_solver_stats *stats);
 
 /* ------------------------------------------------------------------ direct solver
- * Sparse Cholesky on the device for a symmetric positive definite matrix (tgv > 0 and
- * tgv = -2 rows keep it so): the direct solver behind addsolver, in the role FreeFEM's
- * CHOLMOD / MUMPS plugins play (VirtualSolverSparseSuite.hpp:305, plugin/seq/MUMPS_seq.cpp:
- * 260-300), driven as FreeFEM drives them (VirtualSolver::factorize: symbolic once per pattern,
- * numeric once per numeric state, then the solves, VirtualSolver.hpp:226-239).
+ * Sparse direct solves on the device, the direct solvers behind addsolver in the roles FreeFEM's
+ * CHOLMOD / UMFPACK / MUMPS play (VirtualSolverSparseSuite.hpp:305, SparseLinearSolver.hpp:116,
+ * plugin/seq/MUMPS_seq.cpp:260-300), driven as FreeFEM drives them (VirtualSolver::factorize:
+ * symbolic once per pattern, numeric once per numeric state, then the solves,
+ * VirtualSolver.hpp:226-239).
+ * ffgpu_direct_method: FFGPU_DIRECT_AUTO (default: Cholesky when the matrix is symmetric,
+ * else QR), FFGPU_DIRECT_CHOLESKY (symmetric positive definite: tgv > 0 and tgv = -2 rows keep
+ * it so; FFGPU_EINVAL otherwise) or FFGPU_DIRECT_QR (any nonsingular matrix: rows scaled by
+ * their largest entry, then sparse QR); a change drops the current factorisation.
  * ffgpu_direct_factor: fill-reducing ordering (nested dissection; approximate minimum degree as
- * the fallback), symbolic analysis, numeric factorisation (cuSOLVER's sparse Cholesky); a
- * reassembly keeps the ordering and analysis and refactors at the next solve.  FFGPU_EINVAL
- * for a nonsymmetric or not positive definite matrix, or when cuSOLVER is not installed.
- * ffgpu_solve_direct: x = A^-1 b for nrhs right-hand sides (A' = A), factoring first if needed. */
+ * the fallback), symbolic analysis, numeric factorisation (cuSOLVER's sparse Cholesky or QR);
+ * a reassembly keeps the ordering and analysis and refactors at the next solve.  FFGPU_EINVAL
+ * for a matrix the method cannot factor (not positive definite, singular), or when cuSOLVER is
+ * not installed.
+ * ffgpu_solve_direct: x = A^-1 b for nrhs right-hand sides, factoring first if needed. */
+#define FFGPU_DIRECT_AUTO 0
+#define FFGPU_DIRECT_CHOLESKY 1
+#define FFGPU_DIRECT_QR 2
+int ffgpu_direct_method(ffgpu_matrix *A, int method);
 int ffgpu_direct_factor(ffgpu_matrix *A);
 int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ffgpu_solver_stats *stats);
 

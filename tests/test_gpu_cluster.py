@@ -66,7 +66,7 @@ def test_cluster_cg_against_oracle(case):
     A.solve(b, spmv_layout=64)
     ur, launches_r = _solve_counting(A, b, spmv_layout=64)
     assert ffgpu.lib().ffgpu_matrix_spmv_layout(A.h, 5) == 0
-    assert launches_r > 3 * A.stats.iterations
+    assert launches_r >= 2 * A.stats.iterations   # two kernels per iteration (fused direction update)
     assert np.linalg.norm(u - ur) <= 1e-12 * np.linalg.norm(ur)
     # reproducible
     u2 = A.solve(b)

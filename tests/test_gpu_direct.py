@@ -86,3 +86,58 @@ def test_cholesky_refactors_after_reassembly_and_refuses_nonsymmetric():
     with pytest.raises(ffgpu.FFGPUError) as ei:
         N.solve(b)
     assert ei.value.code == -1 and b"symmetric" in ffgpu.lib().ffgpu_last_error()
+
+
+def _dense(A, n):
+    rp, cl, v = A.csr()
+    M = np.zeros((n, n))
+    M[np.repeat(np.arange(n), np.diff(rp)), cl] = v
+    return M
+
+
+@pytest.mark.parametrize("case", ["tgv_minus1", "advection", "advection_p2"])
+def test_sparsesolver_nonsymmetric_against_dense(case):
+    """SPARSESOLVER (FreeFEM's direct solver name) on nonsymmetric systems takes the QR path:
+    tgv = -1 rows (unit rows, columns kept) and a convection-diffusion operator."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    if case == "tgv_minus1":
+        Th = mesh.square(20)
+        Vh = FESpace(Th, "P1")
+        a = ffgpu.varf_diffusion(kappa=np.exp(rng.standard_normal(Th.nt)), f=1.0, on=(1, 2, 3, 4), tgv=-1.0)
+    else:
+        Th = mesh.square(24 if case == "advection" else 12)
+        Vh = FESpace(Th, "P2" if case.endswith("p2") else "P1")
+        a = ffgpu.varf_diffusion(kappa=0.05, f=1.0, on=(1, 2, 3, 4),
+                                 terms=(("id", "dx", 1.0), ("id", "dy", 0.5)))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(a, Vh, solver="SPARSESOLVER", rhs_out=b)
+    M = _dense(A, Vh.ndof)
+    assert np.abs(M - M.T).max() > 1e-3 * np.abs(M[np.abs(M) < 1e29]).max()   # really nonsymmetric
+    u = A.solve(b)
+    ref = np.linalg.solve(M, b)
+    assert np.linalg.norm(u - ref) <= SOL_TOL * np.linalg.norm(ref)
+    B = rng.standard_normal((2, Vh.ndof))
+    X = A.solve(B.ravel()).reshape(2, -1)
+    R = np.linalg.solve(M, B.T).T
+    for k in range(2):
+        assert np.linalg.norm(X[k] - R[k]) <= SOL_TOL * np.linalg.norm(R[k])
+    with pytest.raises(ValueError):
+        A.solve(b, trans=True)
+    with pytest.raises(ffgpu.FFGPUError):
+        A.solve(b, solver="CHOLESKY")
+
+
+def test_qr_on_symmetric_matrix_and_refactor():
+    """QR forced on a symmetric positive definite matrix agrees with Cholesky; a reassembly
+    refactors."""
+    Th = mesh.square(24)
+    Vh = FESpace(Th, "P1")
+    k1 = np.exp(np.random.Generator(np.random.PCG64(4)).standard_normal(Th.nt))
+    b = np.empty(Vh.ndof)
+    A = ffgpu.matrix(ffgpu.varf_diffusion(kappa=k1, f=1.0, on=(1, 2, 3, 4)), Vh, rhs_out=b)
+    uc = A.solve(b, solver="CHOLESKY")
+    uq = A.solve(b, solver="QR")
+    assert np.linalg.norm(uq - uc) <= SOL_TOL * np.linalg.norm(uc)
+    A.reassemble(ffgpu.varf_diffusion(kappa=3.0 * k1, f=1.0, on=(1, 2, 3, 4)), rhs_out=b)
+    uq3 = A.solve(b, solver="QR")
+    assert np.linalg.norm(3.0 * uq3 - uc) <= SOL_TOL * np.linalg.norm(uc)

@@ -59,7 +59,7 @@ def gpu_present():
 
 def test_plugin_registers_solvers_and_refuses_cpu_fallback(plugin):
     r, out = run_script(plugin, "t.edp", SCRIPT.split("\n", 2)[2])
-    assert "load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED, GPUCHOLESKY)" in out
+    assert "load: ffgpu (GPUCG, GPUGMRES, GPUCGMIXED, GPUCHOLESKY, GPUSPARSESOLVER)" in out
     assert "ffgpu: device assembly P1 dim 2" in out
     if gpu_present():
         assert r.returncode == 0 and "umax 0.07" in out, out[-2000:]
