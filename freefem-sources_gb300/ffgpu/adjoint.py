@@ -15,6 +15,8 @@ from __future__ import annotations
 
 import ctypes as C
 
+import math
+
 import numpy as np
 
 from . import api
@@ -201,25 +203,41 @@ class HeatProblem:
         self.F = F
         return F
 
-    def step(self, u_prev):
+    def step(self, u_prev, x0=None, eps=None):
+        """u^n from u^{n-1}: FreeFEM's u[] = A^-1*b with u[] = u^{n-1} as the initial guess, or
+        from x0 with the stopping tolerance eps (eps < 0: absolute, FreeFEM's convention)."""
         self.solves += 1
-        u = self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev)
+        u = self.A.solve(self.mdt.mult(u_prev) + self.F, x0=u_prev if x0 is None else x0, eps=eps)
         self.iterations_state += self.A.stats.iterations
+        self.last_gcg = self.A.stats.gcg
         return u
 
     def forward(self, kappa, f, keep_checkpoints=True):
         """u^N and the checkpoints: every `checkpoint`-th state, plus the states of the last
-        segment, which the backward pass needs first and would otherwise recompute."""
+        segment, which the backward pass needs first and would otherwise recompute.  Also
+        keeps the final (g, Cg) of every step's solve (the accuracy a recomputation matches)."""
         F = self.assemble(kappa, f)
         u = _zeros(self.Vh.ndof, F)
         ck = {0: _copy(u)}
+        self.gcg = [0.0] * (self.nsteps + 1)
         N, c = self.nsteps, self.checkpoint
         last0 = ((N - 1) // c) * c
         for n in range(1, N + 1):
             u = self.step(u)
+            self.gcg[n] = self.last_gcg
             if keep_checkpoints and (n % c == 0 or n > last0):
                 ck[n] = _copy(u)
         return u, ck
+
+    def recompute(self, n, u_prev, u_prev2):
+        """u^n again, from u^{n-1} and (when there is one) u^{n-2}: the same system, started
+        from the linear extrapolation 2 u^{n-1} - u^{n-2} and stopped at the residual the
+        forward solve of step n reached, (g, Cg) <= its final value (absolute tolerance).  The
+        state agrees with the forward's to the solver's accuracy, in fewer iterations."""
+        g = self.gcg[n]
+        if u_prev2 is None or not g > 0.0:
+            return self.step(u_prev)
+        return self.step(u_prev, x0=2.0 * u_prev - u_prev2, eps=-math.sqrt(g))
 
     def loss(self, uN, u_obs):
         r = uN - u_obs
@@ -245,9 +263,11 @@ class HeatProblem:
             s1 = min(s0 + c, N)
             # recompute u^{s0+1..s1} from the checkpoint u^{s0}
             states = {s0: ck[s0]}
-            u = ck[s0]
+            u, up = ck[s0], None
             for n in range(s0 + 1, s1 + 1):
-                u = states[n] = self.step(u) if n not in ck or n == s0 else ck[n]
+                un = self.recompute(n, u, up) if n not in ck or n == s0 else ck[n]
+                states[n] = un
+                u, up = un, u
             for n in range(s1, s0, -1):
                 rhs = rhs_adj if n == N else self.mdt.mult(lam_next, trans=True)
                 lam = self.A.solve(rhs, trans=True, x0=lam_next)
