@@ -229,6 +229,21 @@ class HeatProblem:
                 ck[n] = _copy(u)
         return u, ck
 
+    def _jacobi(self, like):
+        """C = 1/A_ii of the current matrix (1 where |A_ii|^2 < 1e-60), the CG's Jacobi
+        preconditioner, on the side (host / device) of `like`."""
+        rp, cl, v = self.A.csr()
+        n = rp.size - 1
+        row = np.repeat(np.arange(n), np.diff(rp))
+        on = row == cl
+        d = np.zeros(n)
+        d[row[on]] = v[on]
+        cj = np.where(d * d < 1e-60, 1.0, 1.0 / np.where(d == 0.0, 1.0, d))
+        if _on_device(like):
+            import torch
+            return torch.from_numpy(cj).to(like.device)
+        return cj
+
     def recompute(self, n, u_prev, u_prev2):
         """u^n again, from u^{n-1} and (when there is one) u^{n-2}: the same system, started
         from the linear extrapolation 2 u^{n-1} - u^{n-2} and stopped at the residual the
@@ -256,7 +271,8 @@ class HeatProblem:
         gk = _zeros(nt, uN)
         gf = _zeros(nt, uN)
         rhs_adj = self.mass.mult(r)          # dL/du^N
-        lam_next = None
+        lam_next = lam_next2 = None
+        cj = self._jacobi(uN)
         N, c = self.nsteps, self.checkpoint
         seg_starts = sorted(k for k in ck if k < N and k % c == 0)
         for s0 in reversed(seg_starts):
@@ -270,13 +286,21 @@ class HeatProblem:
                 u, up = un, u
             for n in range(s1, s0, -1):
                 rhs = rhs_adj if n == N else self.mdt.mult(lam_next, trans=True)
-                lam = self.A.solve(rhs, trans=True, x0=lam_next)
+                # the adjoint solve starts from the extrapolation of the two later adjoint states
+                # and stops where a solve from zero would (FreeFEM's test for x0 = 0:
+                # (g, Cg) < eps^2 (b, Cb)), as an absolute tolerance
+                x0, eps_adj = lam_next, None
+                if lam_next2 is not None:
+                    x0 = 2.0 * lam_next - lam_next2
+                    bcb = float((rhs * cj * rhs).sum())
+                    eps_adj = -self.eps * math.sqrt(bcb) if bcb > 0.0 else None
+                lam = self.A.solve(rhs, trans=True, x0=x0, eps=eps_adj)
                 self.solves += 1
                 self.iterations_adjoint += self.A.stats.iterations
                 g1, g2 = sensitivity(self.A, states[n], lam)
                 gk += g1
                 gf += g2
-                lam_next = lam
+                lam_next, lam_next2 = lam, lam_next
         self.forward_solves = forward_solves
         return L, gk, gf
 
