@@ -43,7 +43,6 @@ struct BatchArgs {
     double eps, tgv;
     float eps_in;
     int itmax_in, max_outer;
-    int smem_cap;              // rows whose FP32 vectors fit in the CTA's shared memory
 };
 
 template <int NT>
@@ -96,8 +95,6 @@ __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, c
     }
 }
 
-// FP32 y = A x and (x, y) over the problem's rows; x and y are indexed from the problem's first
-// row r0 (shared memory or the global vectors offset by r0)
 template <int NT, int T>
 __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *x, float *y) {
     const int sub = threadIdx.x % T;
@@ -107,10 +104,10 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
         int ii = i < r1 ? i : r0;
         int kb = B.rp[ii], ke = B.rp[ii + 1];
         float s = 0;
-        for (int k = kb + sub; k < ke; k += T) s = fmaf(B.val32[k], x[B.col[k] - r0], s);
+        for (int k = kb + sub; k < ke; k += T) s = fmaf(B.val32[k], x[B.col[k]], s);
 #pragma unroll
         for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (i < r1 && sub == 0) { y[i - r0] = s; dot = fmaf(x[i - r0], s, dot); }
+        if (i < r1 && sub == 0) { y[i] = s; dot = fmaf(x[i], s, dot); }
     }
     return dot;
 }
@@ -120,9 +117,6 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
     __shared__ double sh[33];
     __shared__ float shf[33];
     __shared__ int s_p;
-    // the FP32 inner solve's vectors g, h, q, d and C (Jacobi) of a problem of at most smem_cap
-    // rows live in shared memory; larger problems use their slices of the global vectors
-    extern __shared__ float svec[];
     for (;;) {
         if (threadIdx.x == 0) s_p = atomicAdd(B.queue, 1);
         __syncthreads();
@@ -131,16 +125,6 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
         if (slot >= B.nprob) return;
         const int p = B.order[slot];
         const int r0 = B.voff[p], r1 = B.voff[p + 1];
-        const int nl = r1 - r0;
-        const bool in_smem = nl <= B.smem_cap;
-        const int cap = B.smem_cap;
-        float *g = in_smem ? svec : B.g + r0;
-        float *h = in_smem ? svec + cap : B.h + r0;
-        float *q = in_smem ? svec + 2 * cap : B.q + r0;
-        float *d = in_smem ? svec + 3 * cap : B.d + r0;
-        float *di = in_smem ? svec + 4 * cap : const_cast<float *>(B.dinv32) + r0;
-        if (in_smem)
-            for (int l = threadIdx.x; l < nl; l += NT) di[l] = B.dinv32[r0 + l];
         // x0 = b / tgv on tgv rows (SolverCG::dosolver), x = 0 elsewhere
         for (int i = r0 + threadIdx.x; i < r1; i += NT) B.x[i] = B.wcl[i] ? B.b[i] / B.tgv : 0.0;
         __syncthreads();
@@ -151,12 +135,11 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
             __syncthreads();
             double s64 = 0;
             float sa = 0, sb = 0;
-            for (int l = threadIdx.x; l < nl; l += NT) {
-                const int i = r0 + l;
+            for (int i = r0 + threadIdx.x; i < r1; i += NT) {
                 double ri = B.b[i] - B.r[i];
                 s64 = fma(ri, B.dinv[i] * ri, s64);
-                float gi = -(float)ri, zi = di[l] * gi;
-                g[l] = gi; h[l] = -zi; d[l] = 0.0f;
+                float gi = -(float)ri, zi = B.dinv32[i] * gi;
+                B.g[i] = gi; B.h[i] = -zi; B.d[i] = 0.0f;
                 sa = fmaf(gi, zi, sa);
                 sb = fmaf(gi, -zi, sb);
             }
@@ -172,31 +155,31 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
             float s_gh = cta_sum_f<NT>(sb, shf);
             const float ieps2 = B.eps_in * B.eps_in * ig;
             for (int it = 0; it < B.itmax_in && ig >= 1e-30f && ig >= ieps2; ++it) {
-                float hq = cta_spmv32_dot<NT, T>(B, r0, r1, h, q);
+                float hq = cta_spmv32_dot<NT, T>(B, r0, r1, B.h, B.q);
                 hq = cta_sum_f<NT>(hq, shf);
                 const float rho = -s_gh / hq;
                 float sg = 0;
-                for (int l = threadIdx.x; l < nl; l += NT) {
-                    d[l] = fmaf(rho, h[l], d[l]);
-                    float gi = fmaf(rho, q[l], g[l]);
-                    g[l] = gi;
-                    sg = fmaf(gi, di[l] * gi, sg);
+                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+                    B.d[i] = fmaf(rho, B.h[i], B.d[i]);
+                    float gi = fmaf(rho, B.q[i], B.g[i]);
+                    B.g[i] = gi;
+                    sg = fmaf(gi, B.dinv32[i] * gi, sg);
                 }
                 float ign = cta_sum_f<NT>(sg, shf);
                 const float gamma = ign / ig;
                 ig = ign;
                 float sgh = 0;
-                for (int l = threadIdx.x; l < nl; l += NT) {
-                    float gi = g[l];
-                    float hi = gamma * h[l] - di[l] * gi;
-                    h[l] = hi;
+                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+                    float gi = B.g[i];
+                    float hi = gamma * B.h[i] - B.dinv32[i] * gi;
+                    B.h[i] = hi;
                     sgh = fmaf(gi, hi, sgh);
                 }
                 s_gh = cta_sum_f<NT>(sgh, shf);
                 ++inner;
                 if (!(ig == ig)) break;
             }
-            for (int l = threadIdx.x; l < nl; l += NT) B.x[r0 + l] += (double)d[l];
+            for (int i = r0 + threadIdx.x; i < r1; i += NT) B.x[i] += (double)B.d[i];
             __syncthreads();
         }
         if (threadIdx.x == 0) {
@@ -222,12 +205,6 @@ struct Candidate {
     BatchKernel k;
     int nt, lanes, per_sm;
 };
-
-// shared memory of a batch CTA for its problem's FP32 vectors (5 per row): the SM's 228 KB
-// shared by the candidate's CTAs per SM, less each CTA's reserved 1 KB and static buffers
-static int batch_smem_bytes(int per_sm) {
-    return (228 * 1024 / per_sm - 2048) & ~255;
-}
 
 }  // namespace ffgpu
 
@@ -266,14 +243,11 @@ static int batch_graph(ffgpu_batch *B, int cand) {
     if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
     const Candidate &c = g_cands[cand];
     int grid = kNumSM * c.per_sm;
-    const int smem = batch_smem_bytes(c.per_sm);
-    FFGPU_CUDA(cudaFuncSetAttribute((const void *)c.k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    B->args.smem_cap = smem / (5 * (int)sizeof(float));
     cudaGraph_t g;
     FFGPU_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     reset_queue_kernel<<<1, 1, 0, s>>>(B->queue);
     void *args[] = {&B->args};
-    cudaLaunchKernel((void *)c.k, grid, c.nt, args, smem, s);
+    cudaLaunchKernel((void *)c.k, grid, c.nt, args, 0, s);
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&B->exec, g, 0);
     if (e == cudaSuccess) cudaGraphDestroy(g);
@@ -370,7 +344,7 @@ int ffgpu_batch_assemble(ffgpu_batch *B, const double *kappa, double f, const ui
     size_t NV = A->n;
     B->args = BatchArgs{B->nprob, B->order, B->voff, A->browptr, A->bcol, A->val, A->val32, A->diag_inv,
                         B->dinv32, A->wcl, B->b, nullptr, w, w + NV, w + 2 * NV, w + 3 * NV, B->r, B->queue,
-                        B->iters, B->outers, B->conv, B->resid, 1e-8, tgv > 0 ? tgv : 1e30, 1e-4f, 0, 30, 0};
+                        B->iters, B->outers, B->conv, B->resid, 1e-8, tgv > 0 ? tgv : 1e30, 1e-4f, 0, 30};
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
 }
