@@ -364,13 +364,11 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
 // ------------------------------------------------------------------ SELL-32 K_a
 // One block row per lane, one chunk of 32 rows per warp (resident grid, chunks strided over
 // warps).  FP64: AH = A H and (H, AH) -> rho; padding lanes (a < 0) write nothing.
-// The unrolled row loops (LOOP 0, 1) fit in 40 registers without spilling: six blocks per SM
-// (48 warps) hide more of the gather latency of the FP64-bound [P2]^3 rows than four at 64
-// registers; the batched loops (LOOP 2, 3) keep their registers.
-constexpr int ka_sell_min_blocks(int loop) { return loop < 2 ? 6 : 1; }
-
+// (Six blocks per SM at 40 registers -- the unrolled loops fit without spilling -- measured
+// slower than the compiler's 64 registers at four: [P2]^3 K_a 1.110 against 1.055 ms, P1
+// cube(160) 0.185 against 0.146 ms; fewer loads in flight per thread.)
 template <int BS, bool C16, int ASSIGN, int LOOP>
-__global__ void __launch_bounds__(kSpmvWarps * 32, ka_sell_min_blocks(LOOP)) cg_ka_sell(SellArgs S, const double *__restrict__ val,
+__global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const double *__restrict__ val,
                                                               const double *__restrict__ h, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
