@@ -338,6 +338,10 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// Programmatic dependent launch: wait until the grids this one depends on have completed and
+// their writes are visible.  A no-op for a kernel launched without the programmatic attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ void dev_fail(int *status, int code) {
     atomicCAS(status, 0, code);
 }

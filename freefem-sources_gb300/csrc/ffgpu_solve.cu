@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
                                                          double *__restrict__ q, KrylovScalars *ks,
                                                          double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     const int gsub = lane / T, sub = lane % T;
@@ -164,6 +165,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
                                                      KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond,
                                                      int in_graph) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) {
         if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) graph_stop(cond);
         return;
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__re
                                                        float2 *__restrict__ hx, const double *__restrict__ dinv,
                                                        KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const double gamma = ks->gamma;
     double s = 0;
@@ -322,6 +325,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_x(SpmvArgsX A, const fl
                                                            const double *__restrict__ h, double *__restrict__ q,
                                                            KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     const int gsub = lane / T, sub = lane % T;
@@ -372,6 +376,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
                                                               const double *__restrict__ h, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     double hq = 0;
@@ -436,6 +441,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_sell(SellArgs S, const
                                                                double *__restrict__ hnew, double *__restrict__ q,
                                                                KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const double gamma = ks->gamma;
     const int lane = threadIdx.x & 31;
@@ -477,6 +483,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_csr(SpmvArgs A, const 
                                                               double *__restrict__ hnew, double *__restrict__ q,
                                                               KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const double gamma = ks->gamma;
     const int lane = threadIdx.x & 31;
@@ -527,6 +534,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kax_sell(SellArgs S, const
                                                                const double *__restrict__ h, double *__restrict__ q,
                                                                KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
+    griddep_wait();
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     double hq = 0;
@@ -804,6 +812,31 @@ static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
     return s;
 }
 
+// Launch with programmatic dependent launch allowed (pdl): the kernel may be scheduled while
+// the previous kernel on the stream drains, and waits in griddep_wait() for its results; every
+// kernel launched this way calls griddep_wait() before it reads anything.
+static cudaError_t launch_ex(const void *fn, int grid, int block, void **args, size_t smem, cudaStream_t s,
+                             bool pdl) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+// programmatic dependent launch between the CG kernels (FFGPU_PDL=0 turns it off)
+static bool pdl_default() {
+    const char *e = getenv("FFGPU_PDL");
+    return !(e && e[0] == '0');
+}
+
 // One K_a launch of the CG loop, with its argument storage.
 struct KaCall {
     void *fn = nullptr;
@@ -819,7 +852,9 @@ struct KaCall {
     KrylovScalars *ks = nullptr;
     double *part = nullptr;
     void *args[7];
-    cudaError_t launch(cudaStream_t s) { return cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, s); }
+    cudaError_t launch(cudaStream_t s, bool pdl = false) {
+        return launch_ex(fn, grid, kSpmvWarps * 32, args, 0, s, pdl);
+    }
 };
 
 // K_a for mode (0 FP64, 1 double-float) and layout choice T (SELL-32 codes or BSR lanes)
@@ -1078,16 +1113,28 @@ static int vec_grid_kc(int n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, ((int64_t)n / 2 + kVecThreads - 1) / kVecThreads));
 }
 
+// K_b and K_c launches (optionally with programmatic dependent launch)
+static void launch_kb(bool store, int n, double *x, double *g, const double *h, const double *q,
+                      const double *dinv, double *cgv, KrylovScalars *ks, double *part,
+                      cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s, bool pdl) {
+    void *args[] = {&n, &x, &g, &h, &q, &dinv, &cgv, &ks, &part, &cond, &in_graph};
+    launch_ex(store ? (const void *)cg_kb<true> : (const void *)cg_kb<false>, vec_grid_kb(n), kVecThreads, args, 0,
+              s, pdl);
+}
+static void launch_kc(bool split, int n, const double *g, double *h, float2 *hx, const double *dinv,
+                      KrylovScalars *ks, double *part, cudaStream_t s, bool pdl) {
+    void *args[] = {&n, &g, &h, &hx, &dinv, &ks, &part};
+    launch_ex(split ? (const void *)cg_kc_t<true> : (const void *)cg_kc_t<false>, vec_grid_kc(n), kVecThreads, args,
+              0, s, pdl);
+}
+
 // One CG iteration (K_a K_b K_c) on stream s.
 static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h, double *q, const double *dinv,
                     float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
-                    cudaStream_t s) {
-    ka.launch(s);
-    cg_kb<false><<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h, q, dinv, nullptr, ks, part, cond, in_graph);
-    if (mode == 1)
-        cg_kc_t<true><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, hx, dinv, ks, part);
-    else
-        cg_kc_t<false><<<vec_grid_kc(n), kVecThreads, 0, s>>>(n, g, h, nullptr, dinv, ks, part);
+                    cudaStream_t s, bool pdl = false) {
+    ka.launch(s, pdl);
+    launch_kb(false, n, x, g, h, q, dinv, nullptr, ks, part, cond, in_graph, s, pdl);
+    launch_kc(mode == 1, n, g, h, mode == 1 ? hx : nullptr, dinv, ks, part, s, pdl);
 }
 
 // ------------------------------------------------------------------ fused two-kernel iteration
@@ -1106,7 +1153,9 @@ struct KcaCall {
     KrylovScalars *ks = nullptr;
     double *part = nullptr;
     void *args[9];
-    cudaError_t launch(cudaStream_t s) { return cudaLaunchKernel(fn, grid, kSpmvWarps * 32, args, 0, s); }
+    cudaError_t launch(cudaStream_t s, bool pdl = false) {
+        return launch_ex(fn, grid, kSpmvWarps * 32, args, 0, s, pdl);
+    }
 };
 
 static bool cg_fused_fits(const ffgpu_matrix *A, int mode) {
@@ -1152,10 +1201,9 @@ static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hne
 // iteration u of a body: K_ca from H buffer u % 2 into the other one, then K_b on the new H
 static void cg_body_fused(KcaCall (&kc)[2], int u, int n, double *x, double *g, double *const h[2], double *q,
                           const double *dinv, double *cgv, KrylovScalars *ks, double *part,
-                          cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s) {
-    kc[u & 1].launch(s);
-    cg_kb<true><<<vec_grid_kb(n), kVecThreads, 0, s>>>(n, x, g, h[(u + 1) & 1], q, dinv, cgv, ks, part, cond,
-                                                         in_graph);
+                          cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s, bool pdl = false) {
+    kc[u & 1].launch(s, pdl);
+    launch_kb(true, n, x, g, h[(u + 1) & 1], q, dinv, cgv, ks, part, cond, in_graph, s, pdl);
 }
 
 // Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }] (fused: (K_ca K_b) x unroll).
@@ -1177,39 +1225,47 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     }
     vec_grid_kb(A->n);
     vec_grid_kc(A->n);
-    cudaGraph_t graph, body;
-    FFGPU_CUDA(cudaGraphCreate(&graph, 0));
-    cudaGraphConditionalHandle cond;
-    FFGPU_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
-    // cudaGraphNodeParams has no usable default constructor: build it in zeroed storage
-    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
-    memset(cp_buf, 0, sizeof(cp_buf));
-    cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
-    cp->type = cudaGraphNodeTypeConditional;
-    cp->conditional.handle = cond;
-    cp->conditional.type = cudaGraphCondTypeWhile;
-    cp->conditional.size = 1;
-    cudaGraphNode_t node;
-    FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
-    body = cp->conditional.phGraph_out[0];
-    FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    for (int u = 0; u < unroll; ++u) {
-        if (fused)
-            cg_body_fused(kc, u, A->n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, cond, 1, s);
-        else
-            cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s);
+    // with programmatic dependent launch between the body's kernels first; a device or driver
+    // that refuses the programmatic edges in a conditional body gets the plain graph
+    cudaError_t e = cudaErrorUnknown;
+    for (int attempt = 0; attempt < 2 && e != cudaSuccess; ++attempt) {
+        const bool pdl = attempt == 0 && pdl_default();
+        if (attempt == 1 && !pdl_default()) break;
+        cudaGraph_t graph = nullptr, body = nullptr;
+        FFGPU_CUDA(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle cond;
+        FFGPU_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+        // cudaGraphNodeParams has no usable default constructor: build it in zeroed storage
+        alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+        memset(cp_buf, 0, sizeof(cp_buf));
+        cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
+        cp->type = cudaGraphNodeTypeConditional;
+        cp->conditional.handle = cond;
+        cp->conditional.type = cudaGraphCondTypeWhile;
+        cp->conditional.size = 1;
+        cudaGraphNode_t node;
+        FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
+        body = cp->conditional.phGraph_out[0];
+        FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        for (int u = 0; u < unroll; ++u) {
+            if (fused)
+                cg_body_fused(kc, u, A->n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, cond, 1, s, pdl);
+            else
+                cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s, pdl);
+        }
+        e = cudaStreamEndCapture(s, &body);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&A->cg_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            A->cg_exec = nullptr;
+            cudaGetLastError();
+            if (getenv("FFGPU_VERBOSE"))
+                fprintf(stderr, "ffgpu: CG graph %s programmatic launch failed: %s\n", pdl ? "with" : "without",
+                        cudaGetErrorString(e));
+        }
     }
-    cudaError_t e = cudaStreamEndCapture(s, &body);
     if (e != cudaSuccess) {
         set_error("CG graph capture failed: %s", cudaGetErrorString(e));
-        cudaGraphDestroy(graph);
-        return FFGPU_ECUDA;
-    }
-    e = cudaGraphInstantiate(&A->cg_exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        set_error("CG graph instantiate failed: %s", cudaGetErrorString(e));
-        A->cg_exec = nullptr;
         return FFGPU_ECUDA;
     }
     A->cg_unroll = unroll;
