@@ -1,10 +1,12 @@
-"""The direct solver (sparse Cholesky on the device, ffgpu_solve_direct) against the oracle.
+"""The direct solvers (sparse Cholesky and row-equilibrated sparse QR on the device,
+ffgpu_solve_direct) against the oracle and dense solves.
 
 FreeFEM's direct solvers (UMFPACK, CHOLMOD) are not in this image, so the reference is the
 oracle's CG driven to eps = 1e-14, whose solution is exact to ~1e-12 on these systems, and
-numpy's dense solve on small ones.  Bars: solution within 1e-9 relative (the benchmark spec's
-solution bar); one factorisation serves every right-hand side; a reassembly refactors; a
-nonsymmetric matrix (tgv = -1 rows) is refused.
+numpy's dense solve on small ones.  Bars: solution within 1e-9 relative (the solution bar of
+the FP64 path); one factorisation serves every right-hand side; a reassembly refactors; a
+nonsymmetric matrix (tgv = -1 rows, convection) is refused by CHOLESKY and solved by QR under
+SPARSESOLVER, FreeFEM's name for its default direct solver.
 """
 import numpy as np
 import pytest

@@ -1,6 +1,6 @@
 """CUDA path vs the oracle and FreeFEM's golden outputs, through the C ABI.
 
-Bars (the benchmark spec): pattern and DOF numbering bit-exact; matrix values within 1e-12 relative
+Bars: pattern and DOF numbering bit-exact; matrix values within 1e-12 relative
 per entry (floor 1e-3 x the row's largest non-tgv entry, see golden_cases.value_errors);
 solution within 1e-9 relative in the L2 norm; CG/GMRES iteration counts equal to FreeFEM's
 within 2 (device reductions sum in a different order than the reference's serial loops).
