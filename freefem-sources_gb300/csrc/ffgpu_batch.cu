@@ -95,19 +95,46 @@ __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, c
     }
 }
 
+// FP32 y = A x and (x, y) over the problem's rows [r0, r1), T lanes per row.  A lane group
+// takes four rows at a time (rows base + u G, G = NT / T) and issues their row bounds, columns,
+// values and gathers together: the rows' dependent load chains (row pointer -> column ->
+// x) overlap instead of running one after another.  Each row sums its entries in the order of
+// the one-row loop (lane-strided, then the shuffle tree) and a thread meets its rows in the same
+// order, so y and the dot product are those of the one-row loop bit for bit.
 template <int NT, int T>
 __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *x, float *y) {
+    constexpr int G = NT / T;
+    constexpr int U = 4;
     const int sub = threadIdx.x % T;
     float dot = 0;
-    for (int base = r0; base < r1; base += NT / T) {
-        int i = base + threadIdx.x / T;
-        int ii = i < r1 ? i : r0;
-        int kb = B.rp[ii], ke = B.rp[ii + 1];
-        float s = 0;
-        for (int k = kb + sub; k < ke; k += T) s = fmaf(B.val32[k], x[B.col[k]], s);
+    for (int base = r0; base < r1; base += G * U) {
+        int kb[U], ke[U];
+        float sacc[U];
+        int len = 0;
 #pragma unroll
-        for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (i < r1 && sub == 0) { y[i] = s; dot = fmaf(x[i], s, dot); }
+        for (int u = 0; u < U; ++u) {
+            const int i = base + u * G + threadIdx.x / T;
+            const int ii = i < r1 ? i : r0;
+            kb[u] = B.rp[ii];
+            ke[u] = i < r1 ? B.rp[ii + 1] : kb[u];
+            sacc[u] = 0.f;
+            len = max(len, ke[u] - kb[u]);
+        }
+        for (int t = sub; t < len; t += T) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int k = kb[u] + t;
+                if (k < ke[u]) sacc[u] = fmaf(B.val32[k], x[B.col[k]], sacc[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            float sv = sacc[u];
+#pragma unroll
+            for (int o = T / 2; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+            const int i = base + u * G + threadIdx.x / T;
+            if (i < r1 && sub == 0) { y[i] = sv; dot = fmaf(x[i], sv, dot); }
+        }
     }
     return dot;
 }
