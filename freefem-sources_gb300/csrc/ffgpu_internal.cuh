@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
 #include <string>
 #include <vector>
 
@@ -341,6 +343,31 @@ __device__ __forceinline__ float warp_sum(float v) {
 // Programmatic dependent launch: wait until the grids this one depends on have completed and
 // their writes are visible.  A no-op for a kernel launched without the programmatic attribute.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch with programmatic dependent launch allowed (pdl): the kernel may be scheduled while
+// the previous kernel on the stream drains, and waits in griddep_wait() for its results; every
+// kernel launched this way calls griddep_wait() before it reads anything.
+static inline cudaError_t launch_ex(const void *fn, int grid, int block, void **args, size_t smem,
+                                    cudaStream_t s, bool pdl) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+// programmatic dependent launch between the Krylov loop kernels (FFGPU_PDL=0 turns it off)
+static inline bool pdl_default() {
+    const char *e = getenv("FFGPU_PDL");
+    return !(e && e[0] == '0');
+}
 
 __device__ __forceinline__ void dev_fail(int *status, int code) {
     atomicCAS(status, 0, code);

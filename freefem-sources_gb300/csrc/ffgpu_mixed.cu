@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(kMxWarps * 32) ir_ka(SellArgs S, const float *
                                                        const float *__restrict__ h, float *__restrict__ q,
                                                        InnerScalars *ks, float *part) {
     __shared__ float sh[32];
+    griddep_wait();
     if (ks->done) return;
     const int lane = threadIdx.x & 31;
     float hq = 0;
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_kb(int n, float *__restrict__ x
                                                     const float *__restrict__ dinv, InnerScalars *ks, float *part,
                                                     cudaGraphConditionalHandle cond, int in_graph) {
     __shared__ float sh[32];
+    griddep_wait();
     if (ks->done) {
         if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) ir_graph_stop(cond);
         return;
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(kMxThreads) ir_kb(int n, float *__restrict__ x
 __global__ void __launch_bounds__(kMxThreads) ir_kc(int n, const float *__restrict__ g, float *__restrict__ h,
                                                     const float *__restrict__ dinv, InnerScalars *ks, float *part) {
     __shared__ float sh[32];
+    griddep_wait();
     if (ks->done) return;
     const float gamma = ks->gamma;
     float s = 0;
@@ -271,9 +274,10 @@ static bool ir_ranges(const ffgpu_matrix *A) {
     return !A->sell32_kind || ((A->sell32_kind - kSellCode) & 1) == kSellRanges;
 }
 
-// `unroll` inner iterations (K_a K_b K_c) on stream s
+// `unroll` inner iterations (K_a K_b K_c) on stream s, each kernel with a programmatic
+// dependency on the one before it when pdl is set
 static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditionalHandle cond, int in_graph,
-                   cudaStream_t s) {
+                   cudaStream_t s, bool pdl) {
     SellArgs sa = sell_args(A);
     const float *sv = A->sval32;
     void *ka = ir_ka_fn(A, A->sell32_kind);
@@ -285,9 +289,11 @@ static int ir_body(ffgpu_matrix *A, IRState &S, int unroll, cudaGraphConditional
     int n = A->n;
     for (int u = 0; u < unroll; ++u) {
         void *aa[] = {&sa, &sv, &S.h, &S.q, &S.ks, &part};
-        cudaLaunchKernel(ka, gka, kMxWarps * 32, aa, 0, s);
-        ir_kb<<<gkb, kMxThreads, 0, s>>>(n, S.d, S.g, S.h, S.q, S.dinv, S.ks, part, cond, in_graph);
-        ir_kc<<<gkc, kMxThreads, 0, s>>>(n, S.g, S.h, S.dinv, S.ks, part);
+        void *ab[] = {&n, &S.d, &S.g, &S.h, &S.q, &S.dinv, &S.ks, &part, &cond, &in_graph};
+        void *ac[] = {&n, &S.g, &S.h, &S.dinv, &S.ks, &part};
+        launch_ex(ka, gka, kMxWarps * 32, aa, 0, s, pdl);
+        launch_ex((const void *)ir_kb, gkb, kMxThreads, ab, 0, s, pdl);
+        launch_ex((const void *)ir_kc, gkc, kMxThreads, ac, 0, s, pdl);
     }
     return FFGPU_OK;
 }
@@ -391,28 +397,40 @@ static int ir_build_graph(ffgpu_matrix *A, IRState &S, int unroll) {
         const int32_t *part = nullptr;
         FFGPU_TRY(sell_partition(A, ir_ka_grid(A, ir_ka_fn(A, A->sell32_kind)) * kMxWarps, &part));
     }
-    cudaGraph_t graph, body;
-    FFGPU_CUDA(cudaGraphCreate(&graph, 0));
-    cudaGraphConditionalHandle cond;
-    FFGPU_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
-    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
-    memset(cp_buf, 0, sizeof(cp_buf));
-    cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
-    cp->type = cudaGraphNodeTypeConditional;
-    cp->conditional.handle = cond;
-    cp->conditional.type = cudaGraphCondTypeWhile;
-    cp->conditional.size = 1;
-    cudaGraphNode_t node;
-    FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
-    body = cp->conditional.phGraph_out[0];
-    FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    ir_body(A, S, unroll, cond, 1, s);
-    cudaError_t e = cudaStreamEndCapture(s, &body);
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&S.exec, graph, 0);
-    cudaGraphDestroy(graph);
+    // with programmatic dependent launch between the body's kernels first, else the plain graph
+    cudaError_t e = cudaErrorUnknown;
+    for (int attempt = 0; attempt < 2 && e != cudaSuccess; ++attempt) {
+        const bool pdl = attempt == 0 && pdl_default();
+        if (attempt == 1 && !pdl_default()) break;
+        cudaGraph_t graph = nullptr, body = nullptr;
+        FFGPU_CUDA(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle cond;
+        FFGPU_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+        alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+        memset(cp_buf, 0, sizeof(cp_buf));
+        cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
+        cp->type = cudaGraphNodeTypeConditional;
+        cp->conditional.handle = cond;
+        cp->conditional.type = cudaGraphCondTypeWhile;
+        cp->conditional.size = 1;
+        cudaGraphNode_t node;
+        FFGPU_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, cp));
+        body = cp->conditional.phGraph_out[0];
+        FFGPU_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        ir_body(A, S, unroll, cond, 1, s, pdl);
+        e = cudaStreamEndCapture(s, &body);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&S.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            S.exec = nullptr;
+            cudaGetLastError();
+            if (getenv("FFGPU_VERBOSE"))
+                fprintf(stderr, "ffgpu: mixed-precision graph %s programmatic launch failed: %s\n",
+                        pdl ? "with" : "without", cudaGetErrorString(e));
+        }
+    }
     if (e != cudaSuccess) {
         set_error("mixed-precision graph: %s", cudaGetErrorString(e));
-        S.exec = nullptr;
         return FFGPU_ECUDA;
     }
     S.unroll = unroll;
@@ -532,7 +550,7 @@ int ffgpu_solve_ir(ffgpu_matrix *A, const double *b, double *x, const ffgpu_ir_p
             // the same kernels launched from the host (profilers that do not trace conditional
             // graph nodes); the done flag is polled after every `unroll` iterations
             for (int it = 0; it <= itmax_in; it += unroll) {
-                if ((rc = ir_body(A, S, unroll, 0, 0, s))) break;
+                if ((rc = ir_body(A, S, unroll, 0, 0, s, pdl_default()))) break;
                 int done = 0;
                 cudaMemcpyAsync(&done, &S.ks->done, sizeof(int), cudaMemcpyDeviceToHost, s);
                 if (cudaStreamSynchronize(s) != cudaSuccess || done) break;

@@ -715,7 +715,6 @@ constexpr int kSellCode = 64;
 // (FP64 kernels only): batched row loop (plain, deep)
 static bool is_sell(int T) { return T >= kSellCode && T < kSellCode + 8; }
 static int sell_assign(int T) { return (T - kSellCode) & 1; }
-static int sell_loop(int T) { return (T - kSellCode) >> 1; }
 static const char *sell_name(int T) {
     static const char *names[8] = {"sell32 ranges", "sell32 rotated", "sell32 ranges deep", "sell32 rotated deep",
                                    "sell32 ranges batch", "sell32 rotated batch", "sell32 ranges batch deep",
@@ -810,31 +809,6 @@ static SpmvArgs spmv_args(const ffgpu_matrix *A, int trans) {
     s.val = trans ? A->val_t : A->val;
     s.perm = A->rowperm;
     return s;
-}
-
-// Launch with programmatic dependent launch allowed (pdl): the kernel may be scheduled while
-// the previous kernel on the stream drains, and waits in griddep_wait() for its results; every
-// kernel launched this way calls griddep_wait() before it reads anything.
-static cudaError_t launch_ex(const void *fn, int grid, int block, void **args, size_t smem, cudaStream_t s,
-                             bool pdl) {
-    cudaLaunchConfig_t cfg;
-    memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = pdl ? attr : nullptr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelExC(&cfg, fn, args);
-}
-
-// programmatic dependent launch between the CG kernels (FFGPU_PDL=0 turns it off)
-static bool pdl_default() {
-    const char *e = getenv("FFGPU_PDL");
-    return !(e && e[0] == '0');
 }
 
 // One K_a launch of the CG loop, with its argument storage.
@@ -1402,7 +1376,6 @@ static int solve_many(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
     FFGPU_CHECK(A && b && x && prm && nrhs >= 1, FFGPU_EINVAL, "solve: bad argument");
     ffgpu_ctx *ctx = A->ctx;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = ctx->stream;
     int64_t n = A->n;
     FFGPU_TRY(pin_layout(A, fn == cg_one && prm->spmv_mode == 1 ? 1 : 0, prm->spmv_layout));
     FFGPU_TRY(matrix_prepare_solver(A));
