@@ -135,6 +135,8 @@ struct DirectState {
     double *val = nullptr, *exported = nullptr, *t1 = nullptr, *t2 = nullptr;
     void *buf = nullptr;
     bool factored = false;
+    bool trans = false;                      // this state factors A' (its values gathered transposed)
+    DirectState *tr = nullptr;               // QR of A' for transpose solves, built on demand
 };
 
 #define FFGPU_SOLVER(call)                                                                          \
@@ -198,15 +200,16 @@ __global__ void scale_kernel(int64_t n, const double *__restrict__ rs, double *_
 static int grid_of(int64_t n) { return (int)((n + 255) / 256); }
 
 void direct_invalidate(ffgpu_matrix *A) {
-    if (A->direct) static_cast<DirectState *>(A->direct)->factored = false;
+    if (DirectState *d = static_cast<DirectState *>(A->direct)) {
+        d->factored = false;
+        if (d->tr) d->tr->factored = false;
+    }
 }
 
-void direct_release(ffgpu_matrix *A) {
-    DirectState *d = static_cast<DirectState *>(A->direct);
+static void free_state(ffgpu_ctx *ctx, DirectState *d) {
     if (!d) return;
+    free_state(ctx, d->tr);
     const SolverLib &L = solver_lib();
-    ffgpu_ctx *ctx = A->ctx;
-    cudaStreamSynchronize(ctx->stream);
     if (d->info) L.DestroyInfo(d->info);
     if (d->qinfo) L.QrDestroyInfo(d->qinfo);
     if (d->descr) L.DestroyDescr(d->descr);
@@ -216,7 +219,30 @@ void direct_release(ffgpu_matrix *A) {
     dfree(ctx, d->rscale);
     if (d->buf) cudaFree(d->buf);
     delete d;
+}
+
+void direct_release(ffgpu_matrix *A) {
+    DirectState *d = static_cast<DirectState *>(A->direct);
+    if (!d) return;
+    cudaStreamSynchronize(A->ctx->stream);
+    free_state(A->ctx, d);
     A->direct = nullptr;
+}
+
+// position of the transposed entry of each exported entry: entry j at (r, c) -> the entry at
+// (c, r); false when the pattern is not structurally symmetric
+static bool transpose_map(int n, const std::vector<int32_t> &rp, const std::vector<int32_t> &col,
+                          std::vector<int32_t> &tmap) {
+    tmap.resize(col.size());
+    for (int r = 0; r < n; ++r)
+        for (int j = rp[r]; j < rp[r + 1]; ++j) {
+            const int c = col[j];
+            const int32_t *b = col.data() + rp[c], *e = col.data() + rp[c + 1];
+            const int32_t *f = std::lower_bound(b, e, r);
+            if (f == e || *f != r) return false;
+            tmap[j] = (int32_t)(f - col.data());
+        }
+    return true;
 }
 
 // symbolic phase: ordering, permuted pattern, cuSOLVER analysis
@@ -246,6 +272,11 @@ static int direct_symbolic(ffgpu_matrix *A, DirectState *d) {
         FFGPU_SOLVER(L.SymAmd(d->h, n, (int)nnz, d->descr, rp.data(), col.data(), p.data()));
     std::vector<int32_t> inv(n);
     for (int k = 0; k < n; ++k) inv[p[k]] = k;
+    // A' has A's pattern (FreeFEM's patterns are structurally symmetric): the same permuted
+    // pattern, each value taken from the transposed position
+    std::vector<int32_t> tmap;
+    FFGPU_CHECK(!d->trans || transpose_map(n, rp, col, tmap), FFGPU_EINVAL,
+                "direct solver: a transpose solve needs a structurally symmetric pattern");
     // P A P': row k is old row p[k] with its columns renamed and sorted; src maps to the export
     std::vector<int32_t> brp(n + 1), bcol(nnz), src(nnz);
     brp[0] = 0;
@@ -253,7 +284,7 @@ static int direct_symbolic(ffgpu_matrix *A, DirectState *d) {
     for (int k = 0; k < n; ++k) {
         const int r = p[k];
         row.clear();
-        for (int j = rp[r]; j < rp[r + 1]; ++j) row.emplace_back(inv[col[j]], j);
+        for (int j = rp[r]; j < rp[r + 1]; ++j) row.emplace_back(inv[col[j]], d->trans ? tmap[j] : j);
         std::sort(row.begin(), row.end());
         int64_t o = brp[k];
         for (const auto &e : row) { bcol[o] = e.first; src[o] = e.second; ++o; }
@@ -335,10 +366,10 @@ static int direct_numeric(ffgpu_matrix *A, DirectState *d) {
     return FFGPU_OK;
 }
 
-static int direct_prepare(ffgpu_matrix *A) {
-    FFGPU_CHECK(solver_lib().ok, FFGPU_EINVAL, "direct solver unavailable: %s", solver_lib().why.c_str());
+// the factorisation of A itself: the method is chosen at the first call (a symmetry test for
+// AUTO), the symbolic phase runs once per pattern, the numeric phase once per numeric state
+static int direct_prepare_own(ffgpu_matrix *A) {
     DirectState *d = static_cast<DirectState *>(A->direct);
-    if (d && d->factored) return FFGPU_OK;
     ffgpu_ctx *ctx = A->ctx;
     if (!d) {
         // Cholesky needs a symmetric matrix (tgv > 0 and tgv = -2 keep it so; -1 and -3 do not)
@@ -370,6 +401,44 @@ static int direct_prepare(ffgpu_matrix *A) {
     return rc;
 }
 
+// the factorisation of A (trans 0) or A' (trans 1) behind the next solve; a symmetric matrix
+// (Cholesky) answers both
+static int direct_prepare(ffgpu_matrix *A, int trans, DirectState **out) {
+    FFGPU_CHECK(solver_lib().ok, FFGPU_EINVAL, "direct solver unavailable: %s", solver_lib().why.c_str());
+    DirectState *d = static_cast<DirectState *>(A->direct);
+    if (!d || !d->factored) FFGPU_TRY(direct_prepare_own(A));
+    d = static_cast<DirectState *>(A->direct);
+    *out = d;
+    if (!trans || d->method == FFGPU_DIRECT_CHOLESKY) return FFGPU_OK;
+    DirectState *t = d->tr;
+    if (t && t->factored) {
+        *out = t;
+        return FFGPU_OK;
+    }
+    if (!t) {
+        t = new DirectState();
+        t->method = FFGPU_DIRECT_QR;
+        t->trans = true;
+        d->tr = t;
+        const int rc = direct_symbolic(A, t);
+        if (rc) {
+            d->tr = nullptr;
+            cudaStreamSynchronize(A->ctx->stream);
+            free_state(A->ctx, t);
+            return rc;
+        }
+    }
+    const int rc = direct_numeric(A, t);
+    if (rc) {
+        d->tr = nullptr;
+        cudaStreamSynchronize(A->ctx->stream);
+        free_state(A->ctx, t);
+        return rc;
+    }
+    *out = t;
+    return FFGPU_OK;
+}
+
 }  // namespace ffgpu
 
 using namespace ffgpu;
@@ -391,20 +460,22 @@ int ffgpu_direct_method(ffgpu_matrix *A, int method) {
 int ffgpu_direct_factor(ffgpu_matrix *A) {
     FFGPU_CHECK(A, FFGPU_EINVAL, "ffgpu_direct_factor: NULL matrix");
     FFGPU_CUDA(cudaSetDevice(A->ctx->device));
-    return direct_prepare(A);
+    DirectState *d = nullptr;
+    return direct_prepare(A, 0, &d);
 }
 
-int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ffgpu_solver_stats *stats) {
+int ffgpu_solve_direct_trans(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                             ffgpu_solver_stats *stats) {
     FFGPU_CHECK(A && b && x && nrhs >= 1, FFGPU_EINVAL, "ffgpu_solve_direct: bad argument");
     ffgpu_ctx *ctx = A->ctx;
     FFGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    FFGPU_TRY(direct_prepare(A));
+    DirectState *d = nullptr;
+    FFGPU_TRY(direct_prepare(A, trans ? 1 : 0, &d));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    DirectState *d = static_cast<DirectState *>(A->direct);
     const SolverLib &L = solver_lib();
     const int64_t n = A->n;
     DevIn<double> bd(b, (size_t)n * nrhs, ctx);
@@ -437,6 +508,10 @@ int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ff
         stats->elapsed_ms = ms;
     }
     return FFGPU_OK;
+}
+
+int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ffgpu_solver_stats *stats) {
+    return ffgpu_solve_direct_trans(A, b, x, nrhs, 0, stats);
 }
 
 }  // extern "C"

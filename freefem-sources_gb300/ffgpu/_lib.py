@@ -32,6 +32,7 @@ EXPORTS = [
     "ffgpu_matrix_csr", "ffgpu_matrix_mult", "ffgpu_solve_cg", "ffgpu_solve_gmres",
     "ffgpu_matrix_to_f32", "ffgpu_solve_ir", "ffgpu_diffusion_sensitivity",
     "ffgpu_solve_cg_csr_noalloc", "ffgpu_direct_method", "ffgpu_direct_factor", "ffgpu_solve_direct",
+    "ffgpu_solve_direct_trans",
     "ffgpu_batch_create", "ffgpu_batch_assemble", "ffgpu_batch_solve", "ffgpu_batch_rhs",
     "ffgpu_batch_matrix", "ffgpu_batch_info", "ffgpu_batch_destroy",
 ]
@@ -139,6 +140,7 @@ def lib():
         "ffgpu_direct_method": (i32, [vp, i32]),
         "ffgpu_direct_factor": (i32, [vp]),
         "ffgpu_solve_direct": (i32, [vp, vp, vp, i32, P(SolverStats)]),
+        "ffgpu_solve_direct_trans": (i32, [vp, vp, vp, i32, i32, P(SolverStats)]),
         "ffgpu_solve_ir": (i32, [vp, vp, vp, P(IRParams), P(SolverStats)]),
         "ffgpu_diffusion_sensitivity": (i32, [vp, vp, vp, dbl, vp, vp]),
         "ffgpu_solve_cg_csr_noalloc": (i32, [i32, i64, vp, vp, vp, vp, vp, dbl, i32, dbl, vp,

@@ -488,11 +488,10 @@ class Matrix:
         if solver in DIRECT_METHODS:
             # direct: the factorisation is kept for later solves of this numeric state; Cholesky
             # (symmetric positive definite), QR (any nonsingular matrix) or the choice between
-            # them by symmetry (SPARSESOLVER, FreeFEM's default direct solver name)
-            if trans:
-                raise ValueError("the direct solvers solve A x = b; use CG or GMRES for A' x = b")
+            # them by symmetry (SPARSESOLVER, FreeFEM's default direct solver name); trans solves
+            # A' x = b (a symmetric matrix from its own factors, a nonsymmetric one from a QR of A')
             check(lib().ffgpu_direct_method(self.h, DIRECT_METHODS[solver]))
-            code = lib().ffgpu_solve_direct(self.h, _ptr(bb), _ptr(out), nrhs, C.byref(st))
+            code = lib().ffgpu_solve_direct_trans(self.h, _ptr(bb), _ptr(out), nrhs, int(trans), C.byref(st))
             self.stats = st
             check(code)
             return out

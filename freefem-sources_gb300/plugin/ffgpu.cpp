@@ -178,10 +178,8 @@ class SolverGpu : public VirtualSolver<int, double> {
             for (int k = 0; k < N && r == FFGPU_OK; ++k)
                 r = ffgpu_solve_ir(M, b + (size_t)k * A.n, x + (size_t)k * A.n, &p, &st);
         } else if (KIND == kCholesky || KIND == kSparse) {
-            // Cholesky: A' = A; the QR of a nonsymmetric matrix solves A x = b only
-            if (trans && KIND == kSparse)
-                ExecError("ffgpu: A'^-1 with GPUSPARSESOLVER is not provided (use GPUGMRES for A'^-1)");
-            r = ffgpu_solve_direct(M, b, x, N, &st);
+            // Cholesky: A' = A; a nonsymmetric matrix solves A' x = b with a QR of A'
+            r = ffgpu_solve_direct_trans(M, b, x, N, trans, &st);
         } else {
             ffgpu_solver_params p = {eps, (int)itmax, (int)restart, tgv, (int)verb, 8};
             r = KIND == kCG ? ffgpu_solve_cg(M, b, x, N, trans, &p, &st)

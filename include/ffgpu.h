@@ -369,13 +369,21 @@ int ffgpu_solve_gmres(ffgpu_matrix *A, const double *b, double *x, int nrhs, int
  * a reassembly keeps the ordering and analysis and refactors at the next solve.  FFGPU_EINVAL
  * for a matrix the method cannot factor (not positive definite, singular), or when cuSOLVER is
  * not installed.
- * ffgpu_solve_direct: x = A^-1 b for nrhs right-hand sides, factoring first if needed. */
+ * ffgpu_solve_direct: x = A^-1 b for nrhs right-hand sides, factoring first if needed.
+ * ffgpu_solve_direct_trans: x = A^-1 b (trans 0) or A'^-1 b (trans 1), the direct side of
+ * VirtualSolver::solve(x, b, N, trans) (VirtualSolver.hpp:235-239; UMFPACK solves A' x = b
+ * with the factors of A, UMFPACK_At in VirtualSolverSparseSuite.hpp:169).  A symmetric matrix answers A' from
+ * its Cholesky factors; a nonsymmetric one gets a second QR, of A' (same pattern, values read
+ * transposed), at its first transpose solve, refactored with A after a reassembly.  FFGPU_EINVAL
+ * when the pattern is not structurally symmetric. */
 #define FFGPU_DIRECT_AUTO 0
 #define FFGPU_DIRECT_CHOLESKY 1
 #define FFGPU_DIRECT_QR 2
 int ffgpu_direct_method(ffgpu_matrix *A, int method);
 int ffgpu_direct_factor(ffgpu_matrix *A);
 int ffgpu_solve_direct(ffgpu_matrix *A, const double *b, double *x, int nrhs, ffgpu_solver_stats *stats);
+int ffgpu_solve_direct_trans(ffgpu_matrix *A, const double *b, double *x, int nrhs, int trans,
+                             ffgpu_solver_stats *stats);
 
 /* ------------------------------------------------------------------ mixed precision
  * FP32 inner Jacobi-PCG (FP32 values, vectors, SpMV and dot products) inside an FP64

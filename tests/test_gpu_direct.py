@@ -6,7 +6,8 @@ oracle's CG driven to eps = 1e-14, whose solution is exact to ~1e-12 on these sy
 numpy's dense solve on small ones.  Bars: solution within 1e-9 relative (the solution bar of
 the FP64 path); one factorisation serves every right-hand side; a reassembly refactors; a
 nonsymmetric matrix (tgv = -1 rows, convection) is refused by CHOLESKY and solved by QR under
-SPARSESOLVER, FreeFEM's name for its default direct solver.
+SPARSESOLVER, FreeFEM's name for its default direct solver; A' x = b (FreeFEM's A'^-1) is solved
+from the Cholesky factors of a symmetric matrix and from a QR of A' otherwise, to the same bar.
 """
 import numpy as np
 import pytest
@@ -123,8 +124,16 @@ def test_sparsesolver_nonsymmetric_against_dense(case):
     R = np.linalg.solve(M, B.T).T
     for k in range(2):
         assert np.linalg.norm(X[k] - R[k]) <= SOL_TOL * np.linalg.norm(R[k])
-    with pytest.raises(ValueError):
-        A.solve(b, trans=True)
+    # A' x = b from a QR of A' (UMFPACK_At in FreeFEM), one and several right-hand sides
+    ut = A.solve(b, trans=True)
+    rt = np.linalg.solve(M.T, b)
+    assert np.linalg.norm(ut - rt) <= SOL_TOL * np.linalg.norm(rt)
+    Xt = A.solve(B.ravel(), trans=True).reshape(2, -1)
+    Rt = np.linalg.solve(M.T, B.T).T
+    for k in range(2):
+        assert np.linalg.norm(Xt[k] - Rt[k]) <= SOL_TOL * np.linalg.norm(Rt[k])
+    # the factorisation of A is still the one A x = b uses
+    assert np.linalg.norm(A.solve(b) - ref) <= SOL_TOL * np.linalg.norm(ref)
     with pytest.raises(ffgpu.FFGPUError):
         A.solve(b, solver="CHOLESKY")
 
@@ -140,6 +149,31 @@ def test_qr_on_symmetric_matrix_and_refactor():
     uc = A.solve(b, solver="CHOLESKY")
     uq = A.solve(b, solver="QR")
     assert np.linalg.norm(uq - uc) <= SOL_TOL * np.linalg.norm(uc)
+    # A' = A: Cholesky answers the transpose solve from its own factors, QR from a QR of A'
+    assert np.array_equal(A.solve(b, solver="CHOLESKY", trans=True), uc)
+    uqt = A.solve(b, solver="QR", trans=True)
+    assert np.linalg.norm(uqt - uc) <= SOL_TOL * np.linalg.norm(uc)
     A.reassemble(ffgpu.varf_diffusion(kappa=3.0 * k1, f=1.0, on=(1, 2, 3, 4)), rhs_out=b)
     uq3 = A.solve(b, solver="QR")
     assert np.linalg.norm(3.0 * uq3 - uc) <= SOL_TOL * np.linalg.norm(uc)
+    uq3t = A.solve(b, solver="QR", trans=True)      # both factorisations refactor
+    assert np.linalg.norm(3.0 * uq3t - uc) <= SOL_TOL * np.linalg.norm(uc)
+
+
+def test_transpose_solve_after_reassembly_nonsymmetric():
+    """A' x = b on a convection-diffusion matrix, before and after a reassembly with other
+    coefficients: the QR of A' refactors with A."""
+    Th = mesh.square(16)
+    Vh = FESpace(Th, "P1")
+    b = np.empty(Vh.ndof)
+    a1 = ffgpu.varf_diffusion(kappa=0.05, f=1.0, on=(1, 2, 3, 4), terms=(("id", "dx", 1.0), ("id", "dy", 0.5)))
+    a2 = ffgpu.varf_diffusion(kappa=0.1, f=1.0, on=(1, 2, 3, 4), terms=(("id", "dx", -0.5), ("id", "dy", 2.0)))
+    A = ffgpu.matrix(a1, Vh, solver="SPARSESOLVER", rhs_out=b)
+    c = np.random.Generator(np.random.PCG64(8)).standard_normal(Vh.ndof)
+    for a in (a1, a2):
+        A.reassemble(a, rhs_out=b)
+        M = _dense(A, Vh.ndof)
+        rt = np.linalg.solve(M.T, c)
+        assert np.linalg.norm(A.solve(c, trans=True) - rt) <= SOL_TOL * np.linalg.norm(rt)
+        r = np.linalg.solve(M, c)
+        assert np.linalg.norm(A.solve(c) - r) <= SOL_TOL * np.linalg.norm(r)
