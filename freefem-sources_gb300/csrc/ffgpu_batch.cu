@@ -139,6 +139,9 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
     return dot;
 }
 
+// elements per thread whose loads the vector passes issue together
+constexpr int kVb = 4;
+
 template <int NT, int T>
 __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
     __shared__ double sh[33];
@@ -185,22 +188,48 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
                 float hq = cta_spmv32_dot<NT, T>(B, r0, r1, B.h, B.q);
                 hq = cta_sum_f<NT>(hq, shf);
                 const float rho = -s_gh / hq;
+                // a thread's elements i, i + NT, ... are taken kVb at a time, their loads issued
+                // before the first store (the stores could alias the next loads otherwise); the
+                // sums keep the element order
                 float sg = 0;
-                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-                    B.d[i] = fmaf(rho, B.h[i], B.d[i]);
-                    float gi = fmaf(rho, B.q[i], B.g[i]);
-                    B.g[i] = gi;
-                    sg = fmaf(gi, B.dinv32[i] * gi, sg);
+                for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += kVb * NT) {
+                    float hv[kVb], qv[kVb], dv[kVb], gv[kVb], cv[kVb];
+#pragma unroll
+                    for (int u = 0; u < kVb; ++u) {
+                        const int i = i0 + u * NT;
+                        if (i < r1) { hv[u] = B.h[i]; qv[u] = B.q[i]; dv[u] = B.d[i]; gv[u] = B.g[i]; cv[u] = B.dinv32[i]; }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kVb; ++u) {
+                        const int i = i0 + u * NT;
+                        if (i < r1) {
+                            B.d[i] = fmaf(rho, hv[u], dv[u]);
+                            float gi = fmaf(rho, qv[u], gv[u]);
+                            B.g[i] = gi;
+                            sg = fmaf(gi, cv[u] * gi, sg);
+                        }
+                    }
                 }
                 float ign = cta_sum_f<NT>(sg, shf);
                 const float gamma = ign / ig;
                 ig = ign;
                 float sgh = 0;
-                for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-                    float gi = B.g[i];
-                    float hi = gamma * B.h[i] - B.dinv32[i] * gi;
-                    B.h[i] = hi;
-                    sgh = fmaf(gi, hi, sgh);
+                for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += kVb * NT) {
+                    float gv[kVb], hv[kVb], cv[kVb];
+#pragma unroll
+                    for (int u = 0; u < kVb; ++u) {
+                        const int i = i0 + u * NT;
+                        if (i < r1) { gv[u] = B.g[i]; hv[u] = B.h[i]; cv[u] = B.dinv32[i]; }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kVb; ++u) {
+                        const int i = i0 + u * NT;
+                        if (i < r1) {
+                            float hi = gamma * hv[u] - cv[u] * gv[u];
+                            B.h[i] = hi;
+                            sgh = fmaf(gv[u], hi, sgh);
+                        }
+                    }
                 }
                 s_gh = cta_sum_f<NT>(sgh, shf);
                 ++inner;
