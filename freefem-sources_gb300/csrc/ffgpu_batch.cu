@@ -28,6 +28,8 @@ struct BatchArgs {
     const int32_t *order;      // problems sorted by decreasing size
     const int32_t *voff;       // nprob+1 DOF offsets
     const int32_t *rp, *col;   // CSR of the union (global column numbers)
+    const uint16_t *col16;     // the same columns numbered within their problem (every problem
+                               // below 65 536 DOFs): 2 bytes per entry instead of 4
     const double *val;
     const float *val32;
     const double *dinv;
@@ -79,8 +81,14 @@ __device__ __forceinline__ float cta_sum_f(float v, float *sh) {
     return sh[32];
 }
 
+// column of entry k of a row of the problem starting at DOF r0
+template <bool C16>
+__device__ __forceinline__ int batch_col(const BatchArgs &B, int r0, int k) {
+    return C16 ? r0 + (int)B.col16[k] : B.col[k];
+}
+
 // rows [r0, r1) with T lanes per row: y = A x in FP64
-template <int NT, int T>
+template <int NT, int T, bool C16>
 __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, const double *x, double *y) {
     const int sub = threadIdx.x % T;
     for (int base = r0; base < r1; base += NT / T) {
@@ -88,7 +96,7 @@ __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, c
         int ii = i < r1 ? i : r0;
         int kb = B.rp[ii], ke = B.rp[ii + 1];
         double s = 0;
-        for (int k = kb + sub; k < ke; k += T) s = fma(B.val[k], x[B.col[k]], s);
+        for (int k = kb + sub; k < ke; k += T) s = fma(B.val[k], x[batch_col<C16>(B, r0, k)], s);
 #pragma unroll
         for (int o = T / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (i < r1 && sub == 0) y[i] = s;
@@ -101,7 +109,7 @@ __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, c
 // x) overlap instead of running one after another.  Each row sums its entries in the order of
 // the one-row loop (lane-strided, then the shuffle tree) and a thread meets its rows in the same
 // order, so y and the dot product are those of the one-row loop bit for bit.
-template <int NT, int T>
+template <int NT, int T, bool C16>
 __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *x, float *y) {
     constexpr int G = NT / T;
     constexpr int U = 4;
@@ -124,7 +132,7 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int k = kb[u] + t;
-                if (k < ke[u]) sacc[u] = fmaf(B.val32[k], x[B.col[k]], sacc[u]);
+                if (k < ke[u]) sacc[u] = fmaf(B.val32[k], x[batch_col<C16>(B, r0, k)], sacc[u]);
             }
         }
 #pragma unroll
@@ -142,7 +150,7 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
 // elements per thread whose loads the vector passes issue together
 constexpr int kVb = 4;
 
-template <int NT, int T>
+template <int NT, int T, bool C16>
 __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
     __shared__ double sh[33];
     __shared__ float shf[33];
@@ -161,7 +169,7 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
         double eps2 = 0, gcg = 0, gcg0 = 0;
         int outer = 0, inner = 0, conv = 0;
         for (outer = 0; outer <= B.max_outer; ++outer) {
-            cta_spmv64<NT, T>(B, r0, r1, B.x, B.r);
+            cta_spmv64<NT, T, C16>(B, r0, r1, B.x, B.r);
             __syncthreads();
             double s64 = 0;
             float sa = 0, sb = 0;
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
             float s_gh = cta_sum_f<NT>(sb, shf);
             const float ieps2 = B.eps_in * B.eps_in * ig;
             for (int it = 0; it < B.itmax_in && ig >= 1e-30f && ig >= ieps2; ++it) {
-                float hq = cta_spmv32_dot<NT, T>(B, r0, r1, B.h, B.q);
+                float hq = cta_spmv32_dot<NT, T, C16>(B, r0, r1, B.h, B.q);
                 hq = cta_sum_f<NT>(hq, shf);
                 const float rho = -s_gh / hq;
                 // a thread's elements i, i + NT, ... are taken kVb at a time, their loads issued
@@ -255,6 +263,21 @@ __global__ void f32_copy_kernel(int64_t n, const double *a, float *b) {
 
 __global__ void reset_queue_kernel(int *q) { *q = 0; }
 
+// problem-local column numbers: row i belongs to the problem p with voff[p] <= i < voff[p + 1]
+__global__ void local_col_kernel(int n, int nprob, const int32_t *__restrict__ voff,
+                                 const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                                 uint16_t *__restrict__ col16) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int lo = 0, hi = nprob;   // voff[lo] <= i < voff[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (voff[mid] <= i) lo = mid; else hi = mid;
+        }
+        const int r0 = voff[lo];
+        for (int k = rp[i]; k < rp[i + 1]; ++k) col16[k] = (uint16_t)(col[k] - r0);
+    }
+}
+
 typedef void (*BatchKernel)(BatchArgs);
 
 struct Candidate {
@@ -279,19 +302,25 @@ struct ffgpu_batch {
     float *dinv32;
     int *queue, *iters, *outers, *conv;
     double *resid;
+    uint16_t *col16;    // problem-local columns (null when a problem has 65 536 DOFs or more)
+    bool local16;       // every problem below 65 536 DOFs: the 16-bit column kernels
     int tuned;          // index of the chosen candidate, -1 before tuning
     cudaGraphExec_t exec;
     BatchArgs args;
     float tuned_ms;
 };
 
-static Candidate g_cands[] = {
-    {batch_ir_kernel<256, 2>, 256, 2, 4}, {batch_ir_kernel<256, 4>, 256, 4, 4},
-    {batch_ir_kernel<512, 2>, 512, 2, 2}, {batch_ir_kernel<512, 4>, 512, 4, 2},
-    {batch_ir_kernel<1024, 2>, 1024, 2, 1}, {batch_ir_kernel<1024, 4>, 1024, 4, 1},
-    {batch_ir_kernel<128, 2>, 128, 2, 8},
-};
-static const int g_ncands = sizeof(g_cands) / sizeof(g_cands[0]);
+// tuner candidates: the first kBatchSet with 32-bit global columns, the next kBatchSet with
+// 16-bit problem-local columns (the same shapes)
+#define FFGPU_BATCH_SET(C16)                                                                          \
+    {batch_ir_kernel<256, 2, C16>, 256, 2, 4}, {batch_ir_kernel<256, 4, C16>, 256, 4, 4},             \
+        {batch_ir_kernel<512, 2, C16>, 512, 2, 2}, {batch_ir_kernel<512, 4, C16>, 512, 4, 2},         \
+        {batch_ir_kernel<1024, 2, C16>, 1024, 2, 1}, {batch_ir_kernel<1024, 4, C16>, 1024, 4, 1},     \
+        {batch_ir_kernel<128, 2, C16>, 128, 2, 8}
+static Candidate g_cands[] = {FFGPU_BATCH_SET(false), FFGPU_BATCH_SET(true)};
+#undef FFGPU_BATCH_SET
+constexpr int kBatchSet = 7;
+static_assert(sizeof(g_cands) / sizeof(g_cands[0]) == 2 * kBatchSet, "batched tuner: candidate sets");
 
 static int batch_graph(ffgpu_batch *B, int cand) {
     ffgpu_ctx *ctx = B->ctx;
@@ -352,6 +381,8 @@ static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int3
     ffgpu_batch *B = new ffgpu_batch();
     B->ctx = ctx; B->nprob = nprob; B->voff_h = voff; B->space = nullptr; B->A = nullptr; B->tuned = -1;
     B->exec = nullptr; B->b = nullptr; B->work32 = nullptr; B->r = nullptr; B->dinv32 = nullptr;
+    B->col16 = nullptr;
+    B->local16 = *std::max_element(nv, nv + nprob) < 65536;
     int rc = ffgpu_space_create(ctx, 2, NV, coords, NT, el.data(), FFGPU_FE_P1, 3, el.data(), NV, &B->space);
     if (rc) { delete B; return rc; }
     std::vector<int32_t> order(nprob);
@@ -394,11 +425,17 @@ int ffgpu_batch_assemble(ffgpu_batch *B, const double *kappa, double f, const ui
     FFGPU_TRY(matrix_prepare_solver(A));
     FFGPU_TRY(ffgpu_matrix_to_f32(A));
     cudaStream_t s = B->ctx->stream;
+    if (B->local16 && !B->col16) {
+        // the pattern is fixed by the first assembly: number its columns within their problems
+        FFGPU_CUDA(dalloc(B->ctx, (void **)&B->col16, sizeof(uint16_t) * std::max<int64_t>(A->nnz, 1)));
+        local_col_kernel<<<4 * kNumSM, 256, 0, s>>>(A->n, B->nprob, B->voff, A->browptr, A->bcol, B->col16);
+        FFGPU_TRY(launch_check(B->ctx, "local_col"));
+    }
     f32_copy_kernel<<<4 * kNumSM, 256, 0, s>>>(A->n, A->diag_inv, B->dinv32);
     FFGPU_TRY(launch_check(B->ctx, "f32_copy"));
     float *w = B->work32;
     size_t NV = A->n;
-    B->args = BatchArgs{B->nprob, B->order, B->voff, A->browptr, A->bcol, A->val, A->val32, A->diag_inv,
+    B->args = BatchArgs{B->nprob, B->order, B->voff, A->browptr, A->bcol, B->col16, A->val, A->val32, A->diag_inv,
                         B->dinv32, A->wcl, B->b, nullptr, w, w + NV, w + 2 * NV, w + 3 * NV, B->r, B->queue,
                         B->iters, B->outers, B->conv, B->resid, 1e-8, tgv > 0 ? tgv : 1e30, 1e-4f, 0, 30};
     FFGPU_CUDA(cudaStreamSynchronize(s));
@@ -429,15 +466,16 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
     cudaEventCreate(&e1);
     if (B->tuned < 0)
         for (const ffgpu_ctx::BatchTuned &t : ctx->btuned)
-            if (t.nprob == B->nprob && t.n == NV && t.nnz == B->A->nnz) B->tuned = t.cand;
+            if (t.nprob == B->nprob && t.n == NV && t.nnz == B->A->nnz && (t.cand >= kBatchSet) == B->local16)
+                B->tuned = t.cand;
     if (B->tuned < 0) {
         // autotune: time every candidate (CTA size x lanes per row) on this batch and keep the
         // first one within the tuner margin of the fastest; the choice is kept in the context
         // for later batches of the same shape
-        float tms[64];
-        static_assert(g_ncands <= 64, "batched tuner: too many candidates");
-        for (int c = 0; c < g_ncands; ++c) {
-            FFGPU_TRY(batch_graph(B, c));
+        const int base = B->local16 ? kBatchSet : 0;
+        float tms[kBatchSet];
+        for (int c = 0; c < kBatchSet; ++c) {
+            FFGPU_TRY(batch_graph(B, base + c));
             cudaGraphLaunch(B->exec, s);   // warm
             cudaEventRecord(e0, s);
             cudaGraphLaunch(B->exec, s);
@@ -448,9 +486,9 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
             ctx->launches += 4;
             tms[c] = ms;
         }
-        const int bi = tuned_pick(tms, g_ncands);
+        const int bi = base + tuned_pick(tms, kBatchSet);
         B->tuned = bi;
-        B->tuned_ms = tms[bi];
+        B->tuned_ms = tms[bi - base];
         changed = true;
         ctx->btuned.push_back(ffgpu_ctx::BatchTuned{B->nprob, NV, B->A->nnz, bi});
     }
@@ -513,6 +551,7 @@ int ffgpu_batch_destroy(ffgpu_batch *B) {
     ffgpu_space_destroy(B->space);
     cudaFree(B->voff); cudaFree(B->order); cudaFree(B->queue); cudaFree(B->iters); cudaFree(B->outers);
     cudaFree(B->conv); cudaFree(B->resid); cudaFree(B->b); cudaFree(B->r); cudaFree(B->work32);
+    dfree(B->ctx, B->col16);
     delete B;
     return FFGPU_OK;
 }

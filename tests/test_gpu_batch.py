@@ -105,3 +105,27 @@ def test_batch_from_arrays_equals_batch_from_meshes():
     B2.assemble(np.concatenate(kappas), f=1.0)
     x2 = B2.solve(eps=1e-8)
     assert np.array_equal(x1, x2)
+
+
+def test_batch_with_a_problem_of_more_than_65536_dofs():
+    """A problem of 66 049 DOFs (square(256)) among small ones: the solver keeps 32-bit global
+    columns (problem-local 16-bit columns need every problem below 65 536 DOFs); the same bar
+    against the FP64 oracle, for the small problems alone too (16-bit columns)."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    small, ks, _ = batch.c5_meshes(nprob=5, nmin=8, nmax=24, seed=13)
+    big = mesh.square(256)
+    kb = np.exp(rng.standard_normal(big.nt))
+    meshes, kappas = [small[0], big] + small[1:], [ks[0], kb] + ks[1:]
+    B = batch.Batch(meshes)
+    B.assemble(kappas, f=1.0)
+    xs = B.split(B.solve(eps=1e-8).copy())
+    assert B.stats.converged
+    for p, (Th, k) in enumerate(zip(meshes, kappas)):
+        _, _, uo = oracle_problem(Th, k)
+        err = np.linalg.norm(xs[p] - uo) / np.linalg.norm(uo)
+        assert err <= BATCH_TOL, (p, err)
+    S = batch.Batch(small)
+    S.assemble(ks, f=1.0)
+    ys = S.split(S.solve(eps=1e-8))
+    for q, p in enumerate([0, 2, 3, 4, 5]):
+        assert np.linalg.norm(ys[q] - xs[p]) <= 2 * BATCH_TOL * np.linalg.norm(xs[p]), p
