@@ -5,7 +5,11 @@
 // are offset by voff[p]; its pattern and values are those of a lone assembly).  The solve is
 // one persistent kernel: every CTA takes problems from a queue (largest first) and runs the
 // whole mixed-precision solve of a problem -- FP64 outer refinement r = b - A x, FP32 inner
-// Jacobi-PCG on A d = r -- with CTA barriers only (no grid-wide waits).  The launch sequence
+// Jacobi-PCG on A d = r -- with CTA barriers only (no grid-wide waits).  An inner iteration
+// is two passes over the problem's rows and two CTA reductions: the SpMV forms the direction
+// h = gamma h_old - C g where it reads it (two direction buffers alternate), and the update
+// pass sums (g, Cg) and (g, h), from which (g, h_next) = gamma (g, h) - (g, Cg) follows.
+// The launch sequence
 // (FP32 values, Jacobi, queue reset, persistent solve) is captured in a CUDA graph.  The CTA
 // size and lanes per SpMV row are picked by timing the candidates on the batch (autotune).
 #include <math.h>
@@ -38,6 +42,7 @@ struct BatchArgs {
     const double *b;
     double *x;
     float *g, *h, *q, *d;      // FP32 work vectors (union length)
+    float *h2;                 // second direction buffer (directions alternate between h and h2)
     double *r;                 // FP64 residual
     int *queue;
     int *iters, *outers, *conv;
@@ -87,6 +92,25 @@ __device__ __forceinline__ int batch_col(const BatchArgs &B, int r0, int k) {
     return C16 ? r0 + (int)B.col16[k] : B.col[k];
 }
 
+// two CTA-wide sums with the barriers of one (each summed as cta_sum_f sums it)
+template <int NT>
+__device__ __forceinline__ float2 cta_sum2_f(float a, float b, float *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    __syncthreads();
+    if (lane == 0) { sh[w] = a; sh[32 + w] = b; }
+    __syncthreads();
+    if (w == 0) {
+        float ta = lane < NT / 32 ? sh[lane] : 0.0f, tb = lane < NT / 32 ? sh[32 + lane] : 0.0f;
+        ta = warp_sum(ta);
+        tb = warp_sum(tb);
+        if (lane == 0) { sh[64] = ta; sh[65] = tb; }
+    }
+    __syncthreads();
+    return make_float2(sh[64], sh[65]);
+}
+
 // rows [r0, r1) with T lanes per row: y = A x in FP64
 template <int NT, int T, bool C16>
 __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, const double *x, double *y) {
@@ -103,14 +127,20 @@ __device__ __forceinline__ void cta_spmv64(const BatchArgs &B, int r0, int r1, c
     }
 }
 
-// FP32 y = A x and (x, y) over the problem's rows [r0, r1), T lanes per row.  A lane group
-// takes four rows at a time (rows base + u G, G = NT / T) and issues their row bounds, columns,
-// values and gathers together: the rows' dependent load chains (row pointer -> column ->
-// x) overlap instead of running one after another.  Each row sums its entries in the order of
-// the one-row loop (lane-strided, then the shuffle tree) and a thread meets its rows in the same
-// order, so y and the dot product are those of the one-row loop bit for bit.
+// The direction of this iteration, h = gamma h_old - C g, formed where it is read (the
+// previous iteration's direction update folded into this SpMV); every reader rounds it the same
+// way.
+__device__ __forceinline__ float batch_dir(const BatchArgs &B, const float *hold, float gamma, int j) {
+    return fmaf(gamma, hold[j], -(B.dinv32[j] * B.g[j]));
+}
+
+// FP32 q = A h and (h, q) over the problem's rows [r0, r1), T lanes per row, with h formed from
+// h_old, g and C at every gather (batch_dir) and written to hnew by each row's first lane.  A
+// lane group takes four rows at a time (rows base + u G, G = NT / T) and issues their row
+// bounds, columns, values and gathers together.
 template <int NT, int T, bool C16>
-__device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *x, float *y) {
+__device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int r1, const float *hold,
+                                                float gamma, float *hnew, float *y) {
     constexpr int G = NT / T;
     constexpr int U = 4;
     const int sub = threadIdx.x % T;
@@ -132,7 +162,7 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int k = kb[u] + t;
-                if (k < ke[u]) sacc[u] = fmaf(B.val32[k], x[batch_col<C16>(B, r0, k)], sacc[u]);
+                if (k < ke[u]) sacc[u] = fmaf(B.val32[k], batch_dir(B, hold, gamma, batch_col<C16>(B, r0, k)), sacc[u]);
             }
         }
 #pragma unroll
@@ -141,7 +171,12 @@ __device__ __forceinline__ float cta_spmv32_dot(const BatchArgs &B, int r0, int 
 #pragma unroll
             for (int o = T / 2; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
             const int i = base + u * G + threadIdx.x / T;
-            if (i < r1 && sub == 0) { y[i] = sv; dot = fmaf(x[i], sv, dot); }
+            if (i < r1 && sub == 0) {
+                const float hi = batch_dir(B, hold, gamma, i);
+                hnew[i] = hi;
+                y[i] = sv;
+                dot = fmaf(hi, sv, dot);
+            }
         }
     }
     return dot;
@@ -153,7 +188,7 @@ constexpr int kVb = 4;
 template <int NT, int T, bool C16>
 __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
     __shared__ double sh[33];
-    __shared__ float shf[33];
+    __shared__ float shf[66];
     __shared__ int s_p;
     for (;;) {
         if (threadIdx.x == 0) s_p = atomicAdd(B.queue, 1);
@@ -172,14 +207,13 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
             cta_spmv64<NT, T, C16>(B, r0, r1, B.x, B.r);
             __syncthreads();
             double s64 = 0;
-            float sa = 0, sb = 0;
+            float sa = 0;
             for (int i = r0 + threadIdx.x; i < r1; i += NT) {
                 double ri = B.b[i] - B.r[i];
                 s64 = fma(ri, B.dinv[i] * ri, s64);
                 float gi = -(float)ri, zi = B.dinv32[i] * gi;
-                B.g[i] = gi; B.h[i] = -zi; B.d[i] = 0.0f;
+                B.g[i] = gi; B.h[i] = 0.0f; B.d[i] = 0.0f;   // first direction -C g: gamma 0
                 sa = fmaf(gi, zi, sa);
-                sb = fmaf(gi, -zi, sb);
             }
             gcg = cta_sum<NT>(s64, sh);
             if (outer == 0) {
@@ -190,22 +224,23 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
             if (gcg < eps2) { conv = 1; break; }
             if (outer == B.max_outer) break;
             float ig = cta_sum_f<NT>(sa, shf);
-            float s_gh = cta_sum_f<NT>(sb, shf);
+            float s_gh = -ig, gamma = 0.0f;
+            float *hold = B.h, *hnew = B.h2;
             const float ieps2 = B.eps_in * B.eps_in * ig;
             for (int it = 0; it < B.itmax_in && ig >= 1e-30f && ig >= ieps2; ++it) {
-                float hq = cta_spmv32_dot<NT, T, C16>(B, r0, r1, B.h, B.q);
+                float hq = cta_spmv32_dot<NT, T, C16>(B, r0, r1, hold, gamma, hnew, B.q);
                 hq = cta_sum_f<NT>(hq, shf);
                 const float rho = -s_gh / hq;
                 // a thread's elements i, i + NT, ... are taken kVb at a time, their loads issued
                 // before the first store (the stores could alias the next loads otherwise); the
                 // sums keep the element order
-                float sg = 0;
+                float sg = 0, sgh = 0;
                 for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += kVb * NT) {
                     float hv[kVb], qv[kVb], dv[kVb], gv[kVb], cv[kVb];
 #pragma unroll
                     for (int u = 0; u < kVb; ++u) {
                         const int i = i0 + u * NT;
-                        if (i < r1) { hv[u] = B.h[i]; qv[u] = B.q[i]; dv[u] = B.d[i]; gv[u] = B.g[i]; cv[u] = B.dinv32[i]; }
+                        if (i < r1) { hv[u] = hnew[i]; qv[u] = B.q[i]; dv[u] = B.d[i]; gv[u] = B.g[i]; cv[u] = B.dinv32[i]; }
                     }
 #pragma unroll
                     for (int u = 0; u < kVb; ++u) {
@@ -215,31 +250,16 @@ __global__ void __launch_bounds__(NT) batch_ir_kernel(BatchArgs B) {
                             float gi = fmaf(rho, qv[u], gv[u]);
                             B.g[i] = gi;
                             sg = fmaf(gi, cv[u] * gi, sg);
+                            sgh = fmaf(gi, hv[u], sgh);
                         }
                     }
                 }
-                float ign = cta_sum_f<NT>(sg, shf);
-                const float gamma = ign / ig;
-                ig = ign;
-                float sgh = 0;
-                for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += kVb * NT) {
-                    float gv[kVb], hv[kVb], cv[kVb];
-#pragma unroll
-                    for (int u = 0; u < kVb; ++u) {
-                        const int i = i0 + u * NT;
-                        if (i < r1) { gv[u] = B.g[i]; hv[u] = B.h[i]; cv[u] = B.dinv32[i]; }
-                    }
-#pragma unroll
-                    for (int u = 0; u < kVb; ++u) {
-                        const int i = i0 + u * NT;
-                        if (i < r1) {
-                            float hi = gamma * hv[u] - cv[u] * gv[u];
-                            B.h[i] = hi;
-                            sgh = fmaf(gv[u], hi, sgh);
-                        }
-                    }
-                }
-                s_gh = cta_sum_f<NT>(sgh, shf);
+                // (g, Cg) and (g, h): the next direction's (g, gamma h - Cg) follows from them
+                const float2 t = cta_sum2_f<NT>(sg, sgh, shf);
+                gamma = t.x / ig;
+                ig = t.x;
+                s_gh = fmaf(gamma, t.y, -t.x);
+                float *tmp = hold; hold = hnew; hnew = tmp;
                 ++inner;
                 if (!(ig == ig)) break;
             }
@@ -394,7 +414,7 @@ static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int3
         cudaMalloc((void **)&B->iters, sizeof(int) * nprob) || cudaMalloc((void **)&B->outers, sizeof(int) * nprob) ||
         cudaMalloc((void **)&B->conv, sizeof(int) * nprob) || cudaMalloc((void **)&B->resid, sizeof(double) * nprob) ||
         cudaMalloc((void **)&B->b, sizeof(double) * NV) || cudaMalloc((void **)&B->r, sizeof(double) * NV) ||
-        cudaMalloc((void **)&B->work32, sizeof(float) * (size_t)NV * 5)) {
+        cudaMalloc((void **)&B->work32, sizeof(float) * (size_t)NV * 6)) {
         set_error("ffgpu_batch_create: device allocation failed");
         ffgpu_space_destroy(B->space);
         delete B;
@@ -436,7 +456,7 @@ int ffgpu_batch_assemble(ffgpu_batch *B, const double *kappa, double f, const ui
     float *w = B->work32;
     size_t NV = A->n;
     B->args = BatchArgs{B->nprob, B->order, B->voff, A->browptr, A->bcol, B->col16, A->val, A->val32, A->diag_inv,
-                        B->dinv32, A->wcl, B->b, nullptr, w, w + NV, w + 2 * NV, w + 3 * NV, B->r, B->queue,
+                        B->dinv32, A->wcl, B->b, nullptr, w, w + NV, w + 2 * NV, w + 3 * NV, w + 5 * NV, B->r, B->queue,
                         B->iters, B->outers, B->conv, B->resid, 1e-8, tgv > 0 ? tgv : 1e30, 1e-4f, 0, 30};
     FFGPU_CUDA(cudaStreamSynchronize(s));
     return FFGPU_OK;
