@@ -505,6 +505,9 @@ int ffgpu_batch_solve(ffgpu_batch *B, double *x, const ffgpu_ir_params *prm, int
             cudaEventElapsedTime(&ms, e0, e1);
             ctx->launches += 4;
             tms[c] = ms;
+            if (getenv("FFGPU_VERBOSE"))
+                fprintf(stderr, "ffgpu: batch tuner <%d threads, %d lanes, %d CTAs>: %.3f ms\n", g_cands[base + c].nt,
+                        g_cands[base + c].lanes, kNumSM * g_cands[base + c].per_sm, ms);
         }
         const int bi = base + tuned_pick(tms, kBatchSet);
         B->tuned = bi;
