@@ -386,6 +386,7 @@ struct FillArgs {
     const double *geo;
     const int32_t *browptr;
     int32_t *bcol;            // NULL: numeric only (pattern already built)
+    const int32_t *pcol;      // numeric only: the stored pattern, read instead of re-gathering rows
     int32_t *diagpos;         // block index of the diagonal block, written with the pattern
     double *val;              // NULL: no matrix (linear form only)
     double *rhs;              // NULL: no linear form
@@ -431,7 +432,17 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
     const bool has_mass = A.c_mass != 0.0 && !A.mloc;
 
     for (int a = blockIdx.x * warps + w; a < A.nnodes; a += gridDim.x * warps) {
-        int deg = gather_row(a, A.inc_ptr, A.inc_elem, A.nodes, NN, cols, A.status);
+        int deg;
+        if (A.pcol) {
+            // the row's sorted columns as the pattern pass stored them
+            const int64_t r0 = A.browptr[a];
+            deg = (int)(A.browptr[a + 1] - r0);
+            if (deg > kCandMax) { if (lane == 0) dev_fail(A.status, kDevCandOverflow); continue; }
+            for (int r = lane; r < deg; r += 32) cols[r] = A.pcol[r0 + r];
+            __syncwarp();
+        } else {
+            deg = gather_row(a, A.inc_ptr, A.inc_elem, A.nodes, NN, cols, A.status);
+        }
         if (deg < 0) continue;
         if (deg > A.max_deg) { if (lane == 0) dev_fail(A.status, kDevDegOverflow); continue; }
         const int64_t rb = A.browptr[a];
@@ -835,6 +846,7 @@ static int numeric_pass(ffgpu_matrix *M, const ffgpu_varf *v, const ffgpu_bc *bc
     fa.inc_ptr = S->inc_ptr; fa.inc_elem = S->inc_elem; fa.inc_loc = S->inc_loc;
     fa.nodes = S->nodes; fa.geo = M->geo; fa.browptr = M->browptr;
     fa.bcol = build_cols ? M->bcol : nullptr;
+    fa.pcol = build_cols ? nullptr : M->bcol;
     fa.diagpos = M->diagpos;
     fa.val = M->val; fa.rhs = rh.d; fa.fP0 = fP0.d;
     fa.f0 = v->f_const[0]; fa.f1 = v->f_const[1]; fa.f2 = v->f_const[2];
