@@ -527,15 +527,17 @@ __global__ void __launch_bounds__(128) row_fill_kernel(FillArgs A) {
             }
             __syncwarp();
         }
-        // ---- sum the slot copies (slot order)
+        // ---- sum the slot copies (slot order); slots no element reached hold zeros and are
+        // skipped (a row with ie - ib < SLOTS incident elements fills only that many)
+        const int nsl = min(SLOTS, ie - ib);
         for (int q = lane; q < span; q += 32) {
             double t = acc[q];
-            for (int sl = 1; sl < SLOTS; ++sl) t += acc[sl * span + q];
+            for (int sl = 1; sl < nsl; ++sl) t += acc[sl * span + q];
             acc[q] = t;
         }
         {
             double r = 0.0;
-            for (int sl = 0; sl < SLOTS; ++sl) {
+            for (int sl = 0; sl < max(nsl, 1); ++sl) {
                 const double p = __shfl_sync(0xffffffffu, racc, sl * NN + (lane < BS ? lane : 0));
                 r = sl == 0 ? p : r + p;
             }
