@@ -283,6 +283,26 @@ __global__ void f32_copy_kernel(int64_t n, const double *a, float *b) {
 
 __global__ void reset_queue_kernel(int *q) { *q = 0; }
 
+// union mesh: element k of problem p (toff[p] <= k < toff[p + 1]) gets its vertex numbers
+// offset by voff[p]; a vertex number outside [0, nv_p) records the lowest such problem in *bad
+__global__ void union_elems_kernel(int nt, int nprob, const int32_t *__restrict__ toff,
+                                   const int32_t *__restrict__ voff, int32_t *__restrict__ el, int *bad) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+        int lo = 0, hi = nprob;   // toff[lo] <= k < toff[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (toff[mid] <= k) lo = mid; else hi = mid;
+        }
+        const int v0 = voff[lo], nvp = voff[lo + 1] - v0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int v = el[3 * (int64_t)k + c];
+            if (v < 0 || v >= nvp) atomicMin(bad, lo);
+            el[3 * (int64_t)k + c] = v + v0;
+        }
+    }
+}
+
 // problem-local column numbers: row i belongs to the problem p with voff[p] <= i < voff[p + 1]
 __global__ void local_col_kernel(int n, int nprob, const int32_t *__restrict__ voff,
                                  const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
@@ -384,7 +404,7 @@ static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int3
     FFGPU_CHECK(ctx && out && nv && nt && coords && elems && nprob > 0, FFGPU_EINVAL,
                 "ffgpu_batch_create: bad argument");
     FFGPU_CUDA(cudaSetDevice(ctx->device));
-    // union mesh: offset vertex numbers on the host (these are small int arrays)
+    // per-problem first vertex and first element of the union (nprob + 1 entries each)
     std::vector<int32_t> voff(nprob + 1, 0), toff(nprob + 1, 0);
     for (int p = 0; p < nprob; ++p) {
         FFGPU_CHECK(nv[p] > 0 && nt[p] > 0, FFGPU_EINVAL, "problem %d is empty", p);
@@ -392,18 +412,49 @@ static int batch_create(ffgpu_ctx *ctx, int nprob, const int32_t *nv, const int3
         toff[p + 1] = toff[p] + nt[p];
     }
     const int NV = voff[nprob], NT = toff[nprob];
-    std::vector<int32_t> el(elems, elems + (size_t)3 * NT);
-    for (int p = 0; p < nprob; ++p)
-        for (int64_t k = (int64_t)3 * toff[p]; k < (int64_t)3 * toff[p + 1]; ++k) {
-            FFGPU_CHECK(el[k] >= 0 && el[k] < nv[p], FFGPU_EINVAL, "problem %d: vertex index out of range", p);
-            el[k] += voff[p];
+    // the union's element array on the device: the caller's elements (host or device) copied in,
+    // then every vertex number offset by its problem's first vertex and range-checked there
+    cudaStream_t s = ctx->stream;
+    int32_t *d_el = nullptr, *d_off = nullptr;
+    FFGPU_CUDA(dalloc(ctx, (void **)&d_el, sizeof(int32_t) * (size_t)3 * NT));
+    if (dalloc(ctx, (void **)&d_off, sizeof(int32_t) * (2 * (size_t)(nprob + 1) + 1))) {
+        dfree(ctx, d_el);
+        set_error("ffgpu_batch_create: device allocation failed");
+        return FFGPU_ENOMEM;
+    }
+    int32_t *d_toff = d_off, *d_voff = d_off + nprob + 1, *d_bad = d_off + 2 * (nprob + 1);
+    const int nobad = nprob;
+    int bad = nprob;
+    cudaError_t ce = cudaMemcpyAsync(d_el, elems, sizeof(int32_t) * (size_t)3 * NT, cudaMemcpyDefault, s);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(d_toff, toff.data(), sizeof(int32_t) * (nprob + 1), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(d_voff, voff.data(), sizeof(int32_t) * (nprob + 1), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_bad, &nobad, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (ce == cudaSuccess) {
+        union_elems_kernel<<<4 * kNumSM, 256, 0, s>>>(NT, nprob, d_toff, d_voff, d_el, d_bad);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    dfree(ctx, d_off);
+    if (ce != cudaSuccess || bad < nprob) {
+        dfree(ctx, d_el);
+        if (ce != cudaSuccess) {
+            set_error("ffgpu_batch_create: %s", cudaGetErrorString(ce));
+            return FFGPU_ECUDA;
         }
+        set_error("problem %d: vertex index out of range", bad);
+        return FFGPU_EINVAL;
+    }
     ffgpu_batch *B = new ffgpu_batch();
     B->ctx = ctx; B->nprob = nprob; B->voff_h = voff; B->space = nullptr; B->A = nullptr; B->tuned = -1;
     B->exec = nullptr; B->b = nullptr; B->work32 = nullptr; B->r = nullptr; B->dinv32 = nullptr;
     B->col16 = nullptr;
     B->local16 = *std::max_element(nv, nv + nprob) < 65536;
-    int rc = ffgpu_space_create(ctx, 2, NV, coords, NT, el.data(), FFGPU_FE_P1, 3, el.data(), NV, &B->space);
+    // P1: the DOFs are the vertices (no DOF table)
+    int rc = ffgpu_space_create(ctx, 2, NV, coords, NT, d_el, FFGPU_FE_P1, 3, nullptr, NV, &B->space);
+    dfree(ctx, d_el);
     if (rc) { delete B; return rc; }
     std::vector<int32_t> order(nprob);
     std::iota(order.begin(), order.end(), 0);

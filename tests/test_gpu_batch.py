@@ -129,3 +129,25 @@ def test_batch_with_a_problem_of_more_than_65536_dofs():
     ys = S.split(S.solve(eps=1e-8))
     for q, p in enumerate([0, 2, 3, 4, 5]):
         assert np.linalg.norm(ys[q] - xs[p]) <= 2 * BATCH_TOL * np.linalg.norm(xs[p]), p
+
+
+def test_batch_create_rejects_a_vertex_out_of_range():
+    """A problem whose element names a vertex outside its own mesh is refused with
+    FFGPU_EINVAL naming the first such problem (checked on the device, no fault)."""
+    meshes, _, _ = batch.c5_meshes(nprob=5, nmin=4, nmax=8, seed=3)
+    nv, nt, coords, elems, onbc = batch.batch_arrays(meshes)
+    toff = np.concatenate([[0], np.cumsum(nt)])
+    bad = elems.copy()
+    bad[toff[2] + 1, 2] = nv[2]          # one past problem 2's last vertex
+    with pytest.raises(ffgpu.FFGPUError) as ei:
+        batch.Batch(arrays=(nv, nt, coords, bad, onbc))
+    assert ei.value.code == -1 and b"problem 2" in ffgpu.lib().ffgpu_last_error()
+    neg = elems.copy()
+    neg[toff[4], 0] = -1
+    with pytest.raises(ffgpu.FFGPUError):
+        batch.Batch(arrays=(nv, nt, coords, neg, onbc))
+    # the context stays usable
+    B = batch.Batch(arrays=(nv, nt, coords, elems, onbc))
+    B.assemble([np.ones(m.nt) for m in meshes])
+    B.solve(eps=1e-8)
+    assert B.stats.converged
