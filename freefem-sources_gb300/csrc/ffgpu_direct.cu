@@ -11,7 +11,10 @@
 //   numeric (once per numeric state): the permuted values gathered on the device, the numeric
 //     factorisation, a zero-pivot check (not positive definite / singular: an error, as CHOLMOD
 //     and UMFPACK report);
-//   solve: b permuted on the device, the two triangular solves (QR: Q' b, then R), x unpermuted.
+//   solve: b permuted on the device, the two triangular solves (QR: Q' b, then R), x unpermuted;
+//   a transpose solve A' x = b (UMFPACK_At) uses the Cholesky factors of a symmetric matrix, and
+//   for a nonsymmetric one a second QR, of P A' P' (same pattern, values gathered transposed),
+//   built at the first transpose solve and refactored with A.
 // QR is not invariant under row scaling: a tgv row (1e30 on its diagonal) would dominate the
 // Householder reflections, so every row of P A P' is divided by its largest magnitude first
 // (D P A P', with D P b on the right-hand side).
