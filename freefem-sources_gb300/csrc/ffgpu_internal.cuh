@@ -62,6 +62,12 @@ struct KrylovScalars {
     int iter, itmax, done, converged;
     unsigned int ticket;   // last-block counter of the fused reductions
     int pad;
+    // the two-kernel iteration's (G, C G) and iteration count, one slot per parity of its K_ca
+    // launches: a launch reads the other slot and its block 0 writes its own
+    struct FusedSlot {
+        double gcg;
+        int iter, first;
+    } fs[2];
 };
 
 struct ffgpu_ctx_impl;

@@ -33,6 +33,22 @@ constexpr int kVecThreads = 256;
 
 // ------------------------------------------------------------------ reductions
 __device__ __forceinline__ double block_sum(double v, double *sh) { return block_sum_t(v, sh); }
+
+// The two-kernel iteration leaves no last block behind: each kernel writes its blocks' partials
+// and every block of the next kernel sums them itself, in the order the last block of the
+// writing kernel would have used (thread-strided over the partials, then block_sum_t, with the
+// same block size), so every block gets the bits that last block would have.
+__device__ __forceinline__ double partials_total(const double *part, int n, double *sh, double *bc) {
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(part + i);
+    s = block_sum_t(s, sh);
+    if (threadIdx.x == 0) *bc = s;
+    __syncthreads();
+    s = *bc;
+    __syncthreads();
+    return s;
+}
+
 __device__ __forceinline__ bool last_block_total(double partial, double *part, unsigned *ticket,
                                                   double *tot, double *sh) {
     return last_block_sum(partial, part, ticket, tot, sh);
@@ -156,21 +172,32 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
 
 // The vector kernels run on a resident grid and read/write two elements per access (all
 // work vectors are 16-byte aligned); an odd last element is done by thread 0 of block 0.
-// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence; with STORE also C G into cgv
-// (read by the fused direction update of cg_kca_sell)
+// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence.  With STORE (the two-kernel
+// iteration) also C G into cgv, read by the fused direction update of cg_kca_sell; there rho
+// comes from K_ca's nba pairs of partials at part (summed here by every block) and (G, C G)
+// leaves as partials at part + 2 nba, summed by the next K_ca (fused_prologue).
 template <bool STORE>
 __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
                                                      const double *__restrict__ h, const double *__restrict__ q,
                                                      const double *__restrict__ dinv, double *__restrict__ cgv,
-                                                     KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond,
-                                                     int in_graph) {
+                                                     KrylovScalars *ks, double *part, int nba,
+                                                     cudaGraphConditionalHandle cond, int in_graph) {
     __shared__ double sh[32];
+    __shared__ double bc;
     griddep_wait();
     if (ks->done) {
         if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) graph_stop(cond);
         return;
     }
-    const double rho = ks->rho;
+    double rho;
+    if (STORE) {
+        const double tgh = partials_total(part, nba, sh, &bc);
+        const double thq = partials_total(part + nba, nba, sh, &bc);
+        rho = -tgh / thq;
+        if (blockIdx.x == 0 && threadIdx.x == 0) { ks->s_gh = tgh; ks->s_hq = thq; ks->rho = rho; }
+    } else {
+        rho = ks->rho;
+    }
     double s = 0;
     const int n2 = n >> 1;
     double2 *x2 = reinterpret_cast<double2 *>(x), *g2 = reinterpret_cast<double2 *>(g);
@@ -199,6 +226,10 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
     }
     double tot;
     double p = block_sum(s, sh);
+    if (STORE) {
+        if (threadIdx.x == 0) part[2 * nba + blockIdx.x] = p;
+        return;
+    }
     if (last_block_total(p, part, &ks->ticket, &tot, sh)) {
         ks->gcgp = ks->gcg;
         ks->gcg = tot;
@@ -405,32 +436,39 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka_sell(SellArgs S, const 
 // and for the lane's own row, which is written to the other H buffer -- and AH' = A H',
 // (G, H') and (H', AH') -> rho come out of one pass.  C G was stored by K_b.  Each gathered
 // entry costs one FP64 FMA more, so this runs only where the iteration is latency-bound.
-__device__ __forceinline__ bool last_block_sum2(double p1, double p2, double *part, unsigned *ticket, double *t1,
-                                                double *t2, double *sh) {
-    __shared__ bool s_last;
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = p1;
-        part[gridDim.x + blockIdx.x] = p2;
-        __threadfence();
-        s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double a = 0, c = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-        a += __ldcg(part + i);
-        c += __ldcg(part + gridDim.x + i);
-    }
-    a = block_sum_t(a, sh);
-    c = block_sum_t(c, sh);
-    if (threadIdx.x == 0) {
-        *t1 = a;
-        *t2 = c;
-        *ticket = 0u;
+// Prologue of K_ca (parity p of its launch): the previous K_b's (G, C G) from its partials,
+// then what that K_b's last block did in the three-kernel loop -- gamma, the iteration count,
+// FreeFEM's stopping test.  Every block takes the same decision; block 0 records it.  The first
+// K_ca after cg_init takes gamma = 1 (cg_fuse_start).  Returns false when the solve is over.
+__device__ __forceinline__ bool fused_prologue(KrylovScalars *ks, const double *partb, int nbb, int p,
+                                               cudaGraphConditionalHandle cond, int in_graph, double *sh,
+                                               double *bc, double *gamma) {
+    const double pg = ks->fs[p ^ 1].gcg;
+    const int pit = ks->fs[p ^ 1].iter, first = ks->fs[p ^ 1].first;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    if (first) {
+        *gamma = 1.0;
+        if (lead) { ks->fs[p].gcg = pg; ks->fs[p].iter = pit; ks->fs[p].first = 0; }
         return true;
     }
-    return false;
+    const double tot = partials_total(partb, nbb, sh, bc);
+    const int iter = pit + 1;
+    const bool conv = tot < ks->eps2;
+    const bool done = conv || iter >= ks->itmax;
+    *gamma = tot / pg;
+    if (lead) {
+        ks->gcgp = pg;
+        ks->gcg = tot;
+        ks->gamma = *gamma;
+        ks->iter = iter;
+        ks->fs[p].gcg = tot; ks->fs[p].iter = iter; ks->fs[p].first = 0;
+        if (conv) ks->converged = 1;
+        if (done) {
+            ks->done = 1;
+            if (in_graph) graph_stop(cond);
+        }
+    }
+    return !done;
 }
 
 template <bool C16, int ASSIGN>
@@ -439,11 +477,15 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_sell(SellArgs S, const
                                                                const double *__restrict__ cgv,
                                                                const double *__restrict__ g,
                                                                double *__restrict__ hnew, double *__restrict__ q,
-                                                               KrylovScalars *ks, double *part) {
+                                                               KrylovScalars *ks, double *part, const double *partb,
+                                                               int nbb, int parity, cudaGraphConditionalHandle cond,
+                                                               int in_graph) {
     __shared__ double sh[32];
+    __shared__ double bc;
     griddep_wait();
     if (ks->done) return;
-    const double gamma = ks->gamma;
+    double gamma;
+    if (!fused_prologue(ks, partb, nbb, parity, cond, in_graph, sh, &bc, &gamma)) return;
     const int lane = threadIdx.x & 31;
     double hq = 0, gh = 0;
     sell_for_chunks<ASSIGN>(S, [&](int c, int a, int L, int64_t sr) {
@@ -467,11 +509,10 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_sell(SellArgs S, const
     });
     const double pgh = block_sum(gh, sh);
     const double phq = block_sum(hq, sh);
-    double tgh, thq;
-    if (last_block_sum2(pgh, phq, part, &ks->ticket, &tgh, &thq, sh)) {
-        ks->s_gh = tgh;
-        ks->s_hq = thq;
-        ks->rho = -tgh / thq;
+    // the partials only: K_b sums them (partials_total)
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = pgh;
+        part[gridDim.x + blockIdx.x] = phq;
     }
 }
 
@@ -481,11 +522,15 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_csr(SpmvArgs A, const 
                                                               const double *__restrict__ cgv,
                                                               const double *__restrict__ g,
                                                               double *__restrict__ hnew, double *__restrict__ q,
-                                                              KrylovScalars *ks, double *part) {
+                                                              KrylovScalars *ks, double *part, const double *partb,
+                                                              int nbb, int parity, cudaGraphConditionalHandle cond,
+                                                              int in_graph) {
     __shared__ double sh[32];
+    __shared__ double bc;
     griddep_wait();
     if (ks->done) return;
-    const double gamma = ks->gamma;
+    double gamma;
+    if (!fused_prologue(ks, partb, nbb, parity, cond, in_graph, sh, &bc, &gamma)) return;
     const int lane = threadIdx.x & 31;
     const int gsub = lane / T, sub = lane % T;
     const int groups = (blockDim.x / 32) * (32 / T);
@@ -513,18 +558,22 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_kca_csr(SpmvArgs A, const 
     }
     const double pgh = block_sum(gh, sh);
     const double phq = block_sum(hq, sh);
-    double tgh, thq;
-    if (last_block_sum2(pgh, phq, part, &ks->ticket, &tgh, &thq, sh)) {
-        ks->s_gh = tgh;
-        ks->s_hq = thq;
-        ks->rho = -tgh / thq;
+    // the partials only: K_b sums them (partials_total)
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = pgh;
+        part[gridDim.x + blockIdx.x] = phq;
     }
 }
 
 // the fused loop starts from H = -C G (cg_init) with gamma = 1 and C G = 0, so that its first
-// update reproduces that H
+// update reproduces that H; the first K_ca (parity 0) reads slot 1
 __global__ void cg_fuse_start(KrylovScalars *ks) {
-    if (threadIdx.x == 0) ks->gamma = 1.0;
+    if (threadIdx.x == 0) {
+        ks->gamma = 1.0;
+        ks->fs[1].gcg = ks->gcg;
+        ks->fs[1].iter = ks->iter;
+        ks->fs[1].first = 1;
+    }
 }
 
 // double-float: AH = A H from the split H, (H, AH) in FP64
@@ -1089,9 +1138,9 @@ static int vec_grid_kc(int n) {
 
 // K_b and K_c launches (optionally with programmatic dependent launch)
 static void launch_kb(bool store, int n, double *x, double *g, const double *h, const double *q,
-                      const double *dinv, double *cgv, KrylovScalars *ks, double *part,
+                      const double *dinv, double *cgv, KrylovScalars *ks, double *part, int nba,
                       cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s, bool pdl) {
-    void *args[] = {&n, &x, &g, &h, &q, &dinv, &cgv, &ks, &part, &cond, &in_graph};
+    void *args[] = {&n, &x, &g, &h, &q, &dinv, &cgv, &ks, &part, &nba, &cond, &in_graph};
     launch_ex(store ? (const void *)cg_kb<true> : (const void *)cg_kb<false>, vec_grid_kb(n), kVecThreads, args, 0,
               s, pdl);
 }
@@ -1107,7 +1156,7 @@ static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h
                     float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
                     cudaStream_t s, bool pdl = false) {
     ka.launch(s, pdl);
-    launch_kb(false, n, x, g, h, q, dinv, nullptr, ks, part, cond, in_graph, s, pdl);
+    launch_kb(false, n, x, g, h, q, dinv, nullptr, ks, part, 0, cond, in_graph, s, pdl);
     launch_kc(mode == 1, n, g, h, mode == 1 ? hx : nullptr, dinv, ks, part, s, pdl);
 }
 
@@ -1125,8 +1174,12 @@ struct KcaCall {
     const double *v64 = nullptr, *hold = nullptr, *cgv = nullptr, *g = nullptr;
     double *hnew = nullptr, *q = nullptr;
     KrylovScalars *ks = nullptr;
-    double *part = nullptr;
-    void *args[9];
+    double *part = nullptr;           // this kernel's partial pairs (grid of them)
+    const double *partb = nullptr;    // K_b's partials (nbb of them), after this kernel's
+    int nbb = 0, parity = 0;
+    cudaGraphConditionalHandle cond = 0;
+    int in_graph = 0;
+    void *args[14];
     cudaError_t launch(cudaStream_t s, bool pdl = false) {
         return launch_ex(fn, grid, kSpmvWarps * 32, args, 0, s, pdl);
     }
@@ -1139,9 +1192,11 @@ static bool cg_fused_fits(const ffgpu_matrix *A, int mode) {
 }
 
 static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hnew, const double *cgv,
-                     const double *g, double *q, KcaCall &k) {
+                     const double *g, double *q, int parity, KcaCall &k) {
     k.hold = hold; k.hnew = hnew; k.cgv = cgv; k.g = g; k.q = q;
     k.ks = A->ks; k.part = A->ctx->d_part;
+    k.nbb = vec_grid_kb(A->n);
+    k.parity = parity;
     if (!is_sell(A->csr_lanes)) {
         // block CSR with the tuned lanes per row
         if (trans) FFGPU_TRY(matrix_prepare_transpose(A));
@@ -1150,10 +1205,12 @@ static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hne
         k.fn = T == 1 ? (void *)cg_kca_csr<1> : T == 2 ? (void *)cg_kca_csr<2> : T == 4 ? (void *)cg_kca_csr<4>
                                                                                      : (void *)cg_kca_csr<8>;
         k.grid = spmv_grid(A, T);
-        FFGPU_CHECK(2 * k.grid <= 4 * kRedBlocks, FFGPU_EINVAL, "fused CG: grid %d above the reduction buffer",
-                    k.grid);
+        FFGPU_CHECK(2 * k.grid + k.nbb <= 4 * kRedBlocks, FFGPU_EINVAL,
+                    "fused CG: grid %d above the reduction buffer", k.grid);
+        k.partb = k.part + 2 * k.grid;
         k.args[0] = &k.sa; k.args[1] = &k.hold; k.args[2] = &k.cgv; k.args[3] = &k.g; k.args[4] = &k.hnew;
-        k.args[5] = &k.q; k.args[6] = &k.ks; k.args[7] = &k.part;
+        k.args[5] = &k.q; k.args[6] = &k.ks; k.args[7] = &k.part; k.args[8] = &k.partb; k.args[9] = &k.nbb;
+        k.args[10] = &k.parity; k.args[11] = &k.cond; k.args[12] = &k.in_graph;
         return FFGPU_OK;
     }
     FFGPU_TRY(sell_values(A, trans ? kSell64T : kSell64));
@@ -1163,12 +1220,15 @@ static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hne
                : (assign ? (void *)cg_kca_sell<false, 1> : (void *)cg_kca_sell<false, 0>);
     k.sl = sell_args(A);
     k.grid = sized_grid(k.fn, kSpmvWarps * 32, ((int64_t)A->nchunk + kSpmvWarps - 1) / kSpmvWarps);
-    // two partial slots per block in the reduction buffer
-    FFGPU_CHECK(2 * k.grid <= 4 * kRedBlocks, FFGPU_EINVAL, "fused CG: grid %d above the reduction buffer", k.grid);
+    // two partial slots per block in the reduction buffer, then K_b's partials
+    FFGPU_CHECK(2 * k.grid + k.nbb <= 4 * kRedBlocks, FFGPU_EINVAL, "fused CG: grid %d above the reduction buffer",
+                k.grid);
+    k.partb = k.part + 2 * k.grid;
     if (assign == kSellRanges) FFGPU_TRY(sell_partition(A, k.grid * kSpmvWarps, &k.sl.part));
     k.v64 = trans ? A->sval_t : A->sval;
     k.args[0] = &k.sl; k.args[1] = &k.v64; k.args[2] = &k.hold; k.args[3] = &k.cgv; k.args[4] = &k.g;
-    k.args[5] = &k.hnew; k.args[6] = &k.q; k.args[7] = &k.ks; k.args[8] = &k.part;
+    k.args[5] = &k.hnew; k.args[6] = &k.q; k.args[7] = &k.ks; k.args[8] = &k.part; k.args[9] = &k.partb;
+    k.args[10] = &k.nbb; k.args[11] = &k.parity; k.args[12] = &k.cond; k.args[13] = &k.in_graph;
     return FFGPU_OK;
 }
 
@@ -1176,8 +1236,11 @@ static int kca_setup(ffgpu_matrix *A, int trans, const double *hold, double *hne
 static void cg_body_fused(KcaCall (&kc)[2], int u, int n, double *x, double *g, double *const h[2], double *q,
                           const double *dinv, double *cgv, KrylovScalars *ks, double *part,
                           cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s, bool pdl = false) {
-    kc[u & 1].launch(s, pdl);
-    launch_kb(true, n, x, g, h[(u + 1) & 1], q, dinv, cgv, ks, part, cond, in_graph, s, pdl);
+    KcaCall &k = kc[u & 1];
+    k.cond = cond;
+    k.in_graph = in_graph;
+    k.launch(s, pdl);
+    launch_kb(true, n, x, g, h[(u + 1) & 1], q, dinv, cgv, ks, part, k.grid, cond, in_graph, s, pdl);
 }
 
 // Builds (or reuses) the graph [while(cond){ (K_a K_b K_c) x unroll }] (fused: (K_ca K_b) x unroll).
@@ -1192,8 +1255,8 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
     KcaCall kc[2];
     double *const hb[2] = {h, h2};
     if (fused) {
-        FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, kc[0]));
-        FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, kc[1]));
+        FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, 0, kc[0]));
+        FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, 1, kc[1]));
     } else {
         FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
     }
@@ -1321,8 +1384,8 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
         KcaCall kc[2];
         double *const hb[2] = {h, h2};
         if (fused) {
-            FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, kc[0]));
-            FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, kc[1]));
+            FFGPU_TRY(kca_setup(A, trans, h, h2, cgv, g, q, 0, kc[0]));
+            FFGPU_TRY(kca_setup(A, trans, h2, h, cgv, g, q, 1, kc[1]));
         } else {
             FFGPU_TRY(ka_setup(A, mode, trans, mode == 1 ? A->csr_lanes_x : A->csr_lanes, h, q, ka));
         }
@@ -1352,7 +1415,10 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int bodies = bodies_host >= 0 ? bodies_host : (hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll);
+    // graph bodies run: the three-kernel loop stops in the body of its last K_b; the fused one
+    // in the body of the K_ca after it (K_ca number iter counted from 0)
+    int bodies = bodies_host >= 0 ? bodies_host
+                                  : (fused ? hk.iter / unroll + 1 : (hk.iter == 0 ? 1 : (hk.iter + unroll - 1) / unroll));
     if (use_graph) ctx->launches += (int64_t)bodies * A->cg_kernels_body;
     if (st) {
         st->iterations = hk.iter;
