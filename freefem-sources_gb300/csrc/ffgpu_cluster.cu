@@ -245,11 +245,19 @@ int cluster_cg_run(ffgpu_matrix *A, int trans, double *x, const double *g, const
     a.h = h;
     a.dinv = A->diag_inv;
     a.ks = A->ks;
+    // the SELL columns may have been built just now (sell_values), after cluster_cg_fits looked
+    // at them: the variant launched here gets its shared-memory size set here
     void *fn = A->scol16 ? (void *)cg_cluster<true> : (void *)cg_cluster<false>;
+    const size_t smem = sizeof(double) * 3 * (size_t)R;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cluster CG: %zu bytes of shared memory refused", smem);
+        return kClusterRefused;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(ncta);
     cfg.blockDim = dim3(kClThreads);
-    cfg.dynamicSmemBytes = sizeof(double) * 3 * (size_t)R;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;

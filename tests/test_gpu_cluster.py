@@ -57,7 +57,7 @@ def test_cluster_cg_against_oracle(case):
     b = np.empty(Vh.ndof)
     A = ffgpu.matrix(a, Vh, eps=1e-10, rhs_out=b)
     A.solve(b)                              # first solve: solver setup and SpMV tuning
-    assert ffgpu.lib().ffgpu_matrix_spmv_layout(A.h, 5) == 1
+    assert ffgpu.lib().ffgpu_matrix_spmv_layout(A.h, 5) == 1, ffgpu.lib().ffgpu_last_error()
     u, launches = _solve_counting(A, b)
     assert launches < 8, launches           # one kernel for the whole iteration loop
     assert np.linalg.norm(u - uo) <= 1e-9 * np.linalg.norm(uo)
