@@ -429,7 +429,8 @@ int ffgpu_diffusion_sensitivity(ffgpu_matrix *A, const double *u, const double *
  * (pattern, values, stopping rule of SolverCG applied to the true residual); FreeFEM has no
  * batched path, it runs one script per problem.
  * create: nprob meshes, nv[p] vertices and nt[p] triangles each; coords (sum nv) x 2, elems
- *         (sum nt) x 3 with per-problem vertex numbers.
+ *         (sum nt) x 3 with per-problem vertex numbers (host or device arrays).  A vertex
+ *         number outside [0, nv[p]) gives FFGPU_EINVAL naming the first such problem.
  * assemble: kappa (sum nt) P0 values, constant source f, onbc (sum nv) Dirichlet mask, tgv.
  * solve: x (sum nv) receives all solutions; iterations[p] (may be NULL) the inner iterations.
  *        prm->eps is each problem's outer tolerance.  The first solve autotunes the CTA size
