@@ -151,3 +151,21 @@ def test_batch_create_rejects_a_vertex_out_of_range():
     B.assemble([np.ones(m.nt) for m in meshes])
     B.solve(eps=1e-8)
     assert B.stats.converged
+
+
+def test_batch_from_device_arrays_equals_host_arrays():
+    """The mesh arrays may live on the device (torch CUDA tensors): the same batch, the same
+    bits as from host arrays."""
+    import torch
+    meshes, kappas, _ = batch.c5_meshes(12, 16, 40, seed=17)
+    nv, nt, coords, elems, onbc = batch.batch_arrays(meshes)
+    B1 = batch.Batch(arrays=(nv, nt, coords, elems, onbc))
+    B1.assemble(np.concatenate(kappas), f=1.0)
+    x1 = B1.solve(eps=1e-8).copy()
+    dev = torch.device("cuda", 0)
+    B2 = batch.Batch(arrays=(nv, nt, torch.from_numpy(coords).to(dev), torch.from_numpy(elems).to(dev),
+                             torch.from_numpy(onbc).to(dev)))
+    B2.assemble(torch.from_numpy(np.concatenate(kappas)).to(dev), f=1.0)
+    x2 = B2.solve(eps=1e-8)
+    assert np.array_equal(x1, x2)
+    assert np.array_equal(B1.rhs(), B2.rhs())
