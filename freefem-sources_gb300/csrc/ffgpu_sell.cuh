@@ -48,7 +48,7 @@ __device__ __forceinline__ bool last_block_sum(T partial, T *part, unsigned *tic
 }
 
 // ------------------------------------------------------------------ double-float arithmetic
-// FP64 values and vectors split exactly into FP32 pairs v = hi + lo (48 of the 53 bits); a
+// FP64 values and vectors split into FP32 pairs v ~ hi + lo (48 of the 53 bits kept); a
 // product hi*hi is formed exactly as p + e (e = fma(a, x, -p)), the cross terms are added in
 // FP32, and sums are kept as an unevaluated pair (S, C) with Knuth's TwoSum.  The row result
 // (double)S + (double)C is accurate to about 2^-44 relative.
