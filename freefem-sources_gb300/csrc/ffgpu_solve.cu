@@ -172,11 +172,11 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) cg_ka(SpmvArgs A, const doubl
 
 // The vector kernels run on a resident grid and read/write two elements per access (all
 // work vectors are 16-byte aligned); an odd last element is done by thread 0 of block 0.
-// K_b: x += rho H; G += rho AH; (G, C G) -> gamma, convergence.  With STORE (the two-kernel
-// iteration) also C G into cgv, read by the fused direction update of cg_kca_sell; there rho
+// K_b: x += rho H; G += rho AH; C G into cgv (read by K_c's direction update, or by the fused
+// one of cg_kca_sell); (G, C G) -> gamma, convergence.  In the two-kernel iteration (FUSED) rho
 // comes from K_ca's nba pairs of partials at part (summed here by every block) and (G, C G)
 // leaves as partials at part + 2 nba, summed by the next K_ca (fused_prologue).
-template <bool STORE>
+template <bool FUSED>
 __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__ x, double *__restrict__ g,
                                                      const double *__restrict__ h, const double *__restrict__ q,
                                                      const double *__restrict__ dinv, double *__restrict__ cgv,
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         return;
     }
     double rho;
-    if (STORE) {
+    if (FUSED) {
         const double tgh = partials_total(part, nba, sh, &bc);
         const double thq = partials_total(part + nba, nba, sh, &bc);
         rho = -tgh / thq;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         x2[i] = xv;
         g2[i] = gv;
         const double c0 = __dmul_rn(dv.x, gv.x), c1 = __dmul_rn(dv.y, gv.y);
-        if (STORE) reinterpret_cast<double2 *>(cgv)[i] = make_double2(c0, c1);
+        reinterpret_cast<double2 *>(cgv)[i] = make_double2(c0, c1);
         s = fma(gv.x, c0, s);
         s = fma(gv.y, c1, s);
     }
@@ -221,12 +221,12 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
         const double gi = fma(rho, q[i], g[i]);
         g[i] = gi;
         const double ci = __dmul_rn(dinv[i], gi);
-        if (STORE) cgv[i] = ci;
+        cgv[i] = ci;
         s = fma(gi, ci, s);
     }
     double tot;
     double p = block_sum(s, sh);
-    if (STORE) {
+    if (FUSED) {
         if (threadIdx.x == 0) part[2 * nba + blockIdx.x] = p;
         return;
     }
@@ -241,11 +241,11 @@ __global__ void __launch_bounds__(kVecThreads) cg_kb(int n, double *__restrict__
     }
 }
 
-// K_c: H = gamma H - C G and (G, H); with hx != NULL also the split copy of H for the next
-// double-float SpMV
+// K_c: H = gamma H - C G (C G as K_b stored it) and (G, H); with hx != NULL also the split
+// copy of H for the next double-float SpMV
 template <bool SPLIT>
 __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__restrict__ g, double *__restrict__ h,
-                                                       float2 *__restrict__ hx, const double *__restrict__ dinv,
+                                                       float2 *__restrict__ hx, const double *__restrict__ cgv,
                                                        KrylovScalars *ks, double *part) {
     __shared__ double sh[32];
     griddep_wait();
@@ -254,14 +254,14 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__re
     double s = 0;
     const int n2 = n >> 1;
     double2 *h2 = reinterpret_cast<double2 *>(h);
-    const double2 *g2 = reinterpret_cast<const double2 *>(g), *d2 = reinterpret_cast<const double2 *>(dinv);
+    const double2 *g2 = reinterpret_cast<const double2 *>(g), *c2 = reinterpret_cast<const double2 *>(cgv);
     float4 *hx2 = reinterpret_cast<float4 *>(hx);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) {
-        const double2 gv = g2[i], dv = d2[i];
+        const double2 gv = g2[i], cv = c2[i];
         double2 hv = h2[i];
-        // the roundings spelled out: the fused update of cg_kca_sell forms the same bits
-        hv.x = fma(gamma, hv.x, -__dmul_rn(dv.x, gv.x));
-        hv.y = fma(gamma, hv.y, -__dmul_rn(dv.y, gv.y));
+        // C G rounded once (__dmul_rn in K_b): the fused update of cg_kca_sell forms the same bits
+        hv.x = fma(gamma, hv.x, -cv.x);
+        hv.y = fma(gamma, hv.y, -cv.y);
         h2[i] = hv;
         if (SPLIT) {
             const float2 a = split_f64(hv.x), b = split_f64(hv.y);
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kVecThreads) cg_kc_t(int n, const double *__re
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const int i = n - 1;
         const double gi = g[i];
-        const double hi = fma(gamma, h[i], -__dmul_rn(dinv[i], gi));
+        const double hi = fma(gamma, h[i], -cgv[i]);
         h[i] = hi;
         if (SPLIT) hx[i] = split_f64(hi);
         s = fma(gi, hi, s);
@@ -1137,27 +1137,27 @@ static int vec_grid_kc(int n) {
 }
 
 // K_b and K_c launches (optionally with programmatic dependent launch)
-static void launch_kb(bool store, int n, double *x, double *g, const double *h, const double *q,
+static void launch_kb(bool fused, int n, double *x, double *g, const double *h, const double *q,
                       const double *dinv, double *cgv, KrylovScalars *ks, double *part, int nba,
                       cudaGraphConditionalHandle cond, int in_graph, cudaStream_t s, bool pdl) {
     void *args[] = {&n, &x, &g, &h, &q, &dinv, &cgv, &ks, &part, &nba, &cond, &in_graph};
-    launch_ex(store ? (const void *)cg_kb<true> : (const void *)cg_kb<false>, vec_grid_kb(n), kVecThreads, args, 0,
+    launch_ex(fused ? (const void *)cg_kb<true> : (const void *)cg_kb<false>, vec_grid_kb(n), kVecThreads, args, 0,
               s, pdl);
 }
-static void launch_kc(bool split, int n, const double *g, double *h, float2 *hx, const double *dinv,
+static void launch_kc(bool split, int n, const double *g, double *h, float2 *hx, const double *cgv,
                       KrylovScalars *ks, double *part, cudaStream_t s, bool pdl) {
-    void *args[] = {&n, &g, &h, &hx, &dinv, &ks, &part};
+    void *args[] = {&n, &g, &h, &hx, &cgv, &ks, &part};
     launch_ex(split ? (const void *)cg_kc_t<true> : (const void *)cg_kc_t<false>, vec_grid_kc(n), kVecThreads, args,
               0, s, pdl);
 }
 
 // One CG iteration (K_a K_b K_c) on stream s.
 static void cg_body(KaCall &ka, int mode, int n, double *x, double *g, double *h, double *q, const double *dinv,
-                    float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond, int in_graph,
-                    cudaStream_t s, bool pdl = false) {
+                    double *cgv, float2 *hx, KrylovScalars *ks, double *part, cudaGraphConditionalHandle cond,
+                    int in_graph, cudaStream_t s, bool pdl = false) {
     ka.launch(s, pdl);
-    launch_kb(false, n, x, g, h, q, dinv, nullptr, ks, part, 0, cond, in_graph, s, pdl);
-    launch_kc(mode == 1, n, g, h, mode == 1 ? hx : nullptr, dinv, ks, part, s, pdl);
+    launch_kb(false, n, x, g, h, q, dinv, cgv, ks, part, 0, cond, in_graph, s, pdl);
+    launch_kc(mode == 1, n, g, h, mode == 1 ? hx : nullptr, cgv, ks, part, s, pdl);
 }
 
 // ------------------------------------------------------------------ fused two-kernel iteration
@@ -1288,7 +1288,7 @@ static int cg_graph(ffgpu_matrix *A, int trans, int unroll, int mode, double *x,
             if (fused)
                 cg_body_fused(kc, u, A->n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, cond, 1, s, pdl);
             else
-                cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, cond, 1, s, pdl);
+                cg_body(ka, mode, A->n, x, g, h, q, A->diag_inv, cgv, A->hx, A->ks, ctx->d_part, cond, 1, s, pdl);
         }
         e = cudaStreamEndCapture(s, &body);
         if (e == cudaSuccess) e = cudaGraphInstantiate(&A->cg_exec, graph, 0);
@@ -1395,7 +1395,7 @@ static int cg_one(ffgpu_matrix *A, const double *b, double *x, int trans, const 
                 if (fused)
                     cg_body_fused(kc, u, n, x, g, hb, q, A->diag_inv, cgv, A->ks, ctx->d_part, 0, 0, s);
                 else
-                    cg_body(ka, mode, n, x, g, h, q, A->diag_inv, A->hx, A->ks, ctx->d_part, 0, 0, s);
+                    cg_body(ka, mode, n, x, g, h, q, A->diag_inv, cgv, A->hx, A->ks, ctx->d_part, 0, 0, s);
             }
             ++bodies_host;
             int done = 0;
