@@ -281,14 +281,24 @@ __global__ void __launch_bounds__(kGmThreads) gm_update(GmArgs a) {
     double s = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n; k += (int64_t)gridDim.x * blockDim.x) {
         double t = a.w[k];
-        // FreeFEM's order i = 0..it; the loads of 16 vectors are issued before their products
+        // FreeFEM's order i = 0..it; the loads of 16 vectors are issued before their products,
+        // and the next 16 before the products of these (two batches in flight)
         int i = 0;
-        for (; i + 16 <= ni; i += 16) {
-            double q[16];
+        if (ni >= 16) {
+            double q[16], r[16];
 #pragma unroll
             for (int u = 0; u < 16; ++u) q[u] = __ldcs(a.V + (i + u) * a.vs + k);
+            for (; i + 32 <= ni; i += 16) {
+#pragma unroll
+                for (int u = 0; u < 16; ++u) r[u] = __ldcs(a.V + (i + 16 + u) * a.vs + k);
+#pragma unroll
+                for (int u = 0; u < 16; ++u) t = fma(-hh[i + u], q[u], t);
+#pragma unroll
+                for (int u = 0; u < 16; ++u) q[u] = r[u];
+            }
 #pragma unroll
             for (int u = 0; u < 16; ++u) t = fma(-hh[i + u], q[u], t);
+            i += 16;
         }
         for (; i < ni; ++i) t = fma(-hh[i], __ldcs(a.V + i * a.vs + k), t);
         vn[k] = t;
@@ -412,7 +422,9 @@ static void gm_dot_shape(int64_t n, int &nslab, int &ngrp, int64_t &slab_len) {
     const int64_t per = (nsub + kGmMaxSlabs - 1) / kGmMaxSlabs;
     nslab = (int)((nsub + per - 1) / per);
     slab_len = per * kGmSub;
-    ngrp = std::max(1, (2 * kNumSM + nslab - 1) / nslab);
+    // at most two blocks per SM (a block is 8 warps and ~49 KB of shared memory): a third block on
+    // some SMs sets the kernel's time while most SMs idle
+    ngrp = std::max(1, (2 * kNumSM) / nslab);
 }
 static int gm_coef_grid(int m) { return std::max(1, std::min(kNumSM, (m + 1 + kGmWarps - 1) / kGmWarps)); }
 
